@@ -1,0 +1,281 @@
+"""Synthetic surface meshes and boundary data for the FMM-BEM solve.
+
+The meshes are quadrilateral Q1 surface meshes with shared vertices (no double
+nodes), cells given as 4 node ids in deal.II lexicographic vertex order
+(v0=(0,0), v1=(1,0), v2=(0,1), v3=(1,1) of the unit cell), oriented so that the
+cell normal d x/d xi x d x/d eta points out of the body -- the convention the
+reference's collocation operator assumes (source/bem_problem.cc:478-950).
+
+Workloads:
+  * unit cube-sphere, 6 x n x n cells (6 n^2 + 2 nodes), Dirichlet data from a
+    point source outside the sphere (interior problem);
+  * the same cube-sphere scaled to a prolate spheroid (3,1,1), mixed
+    Dirichlet (cells with centroid z > 0) / Neumann (z <= 0) data from seeded
+    point sources inside the body (exterior problem);
+  * a Wigley-type hull closed by a lid, mixed data from point sources inside;
+  * perturbed spheres r = 1 + 0.1 * sum_{l<=4} c_lm Y_lm.
+All seeds use numpy.random.Generator(PCG64(seed)).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+__all__ = [
+    "Mesh",
+    "cube_sphere",
+    "spheroid",
+    "perturbed_sphere",
+    "wigley_hull",
+    "point_source_field",
+    "mixed_bc_by_cell_centroid",
+    "sphere_dirichlet_case",
+    "spheroid_mixed_case",
+]
+
+
+class Mesh:
+    """Nodes (N,3) float64, cells (C,4) int32, analytic outward normals (N,3)."""
+
+    def __init__(self, xyz, cells, normals):
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.cells = np.ascontiguousarray(cells, dtype=np.int32)
+        self.normals = np.ascontiguousarray(normals, dtype=np.float64)
+
+    @property
+    def n_nodes(self):
+        return self.xyz.shape[0]
+
+    @property
+    def n_cells(self):
+        return self.cells.shape[0]
+
+
+def _cube_surface(n: int):
+    """Equiangular cube-sphere connectivity on the unit cube surface.
+
+    Returns unit-sphere node positions and cells; vertices on cube edges are
+    shared between faces (6 n^2 + 2 nodes)."""
+    ticks = np.tan(np.pi / 4 * np.linspace(-1.0, 1.0, n + 1))
+    index = {}
+    pts = []
+
+    def node(ijk):
+        key = tuple(int(v) for v in ijk)
+        k = index.get(key)
+        if k is None:
+            k = len(pts)
+            index[key] = k
+            pts.append([ticks[key[0]], ticks[key[1]], ticks[key[2]]])
+        return k
+
+    cells = []
+    for a in range(3):
+        b, c = (a + 1) % 3, (a + 2) % 3
+        for sign in (1, -1):
+            s_ax, t_ax = (b, c) if sign > 0 else (c, b)
+            fixed = n if sign > 0 else 0
+            for j in range(n):
+                for i in range(n):
+                    quad = []
+                    for dj in (0, 1):
+                        for di in (0, 1):
+                            ijk = [0, 0, 0]
+                            ijk[a] = fixed
+                            ijk[s_ax] = i + di
+                            ijk[t_ax] = j + dj
+                            quad.append(node(ijk))
+                    cells.append(quad)
+    p = np.asarray(pts, dtype=np.float64)
+    p /= np.linalg.norm(p, axis=1, keepdims=True)
+    return p, np.asarray(cells, dtype=np.int32)
+
+
+def cube_sphere(n: int, radius: float = 1.0) -> Mesh:
+    p, cells = _cube_surface(n)
+    return Mesh(radius * p, cells, p.copy())
+
+
+def spheroid(n: int, axes=(3.0, 1.0, 1.0)) -> Mesh:
+    p, cells = _cube_surface(n)
+    ax = np.asarray(axes, dtype=np.float64)
+    xyz = p * ax
+    nrm = xyz / ax**2
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    return Mesh(xyz, cells, nrm)
+
+
+def _real_sph_harm(l, m, theta, phi):
+    """Real spherical harmonics (unnormalised beyond the Legendre factor)."""
+    from scipy.special import lpmv
+
+    x = np.cos(theta)
+    P = lpmv(abs(m), l, x)
+    if m > 0:
+        return P * np.cos(m * phi)
+    if m < 0:
+        return P * np.sin(-m * phi)
+    return P
+
+
+def perturbed_sphere(n: int, seed: int, amp: float = 0.1, lmax: int = 4) -> Mesh:
+    p, cells = _cube_surface(n)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    theta = np.arccos(np.clip(p[:, 2], -1, 1))
+    phi = np.arctan2(p[:, 1], p[:, 0])
+    s = np.zeros(len(p))
+    for l in range(lmax + 1):
+        for m in range(-l, l + 1):
+            s += rng.normal() * _real_sph_harm(l, m, theta, phi)
+    s /= max(np.abs(s).max(), 1e-300)
+    r = 1.0 + amp * s
+    xyz = p * r[:, None]
+    # normals from the mesh itself: average of adjacent cell normals
+    nrm = _nodal_normals(xyz, cells)
+    return Mesh(xyz, cells, nrm)
+
+
+def _nodal_normals(xyz, cells):
+    v = xyz[cells]
+    t1 = (v[:, 1] - v[:, 0]) + (v[:, 3] - v[:, 2])
+    t2 = (v[:, 2] - v[:, 0]) + (v[:, 3] - v[:, 1])
+    cn = np.cross(t1, t2)
+    out = np.zeros_like(xyz)
+    for j in range(4):
+        np.add.at(out, cells[:, j], cn)
+    out /= np.linalg.norm(out, axis=1, keepdims=True)
+    return out
+
+
+def wigley_hull(nx: int, nz: int, ny_lid: int, L=1.0, B=0.1, T=0.0625) -> Mesh:
+    """Closed Wigley-type hull y = +-(B/2)(1-(2x/L)^2)(1-(z/T)^2), z in [-T,0],
+    closed by the lid z = 0.  Port and starboard sides are nx x nz grids, the lid
+    an nx x ny_lid grid; the keel (z=-T, y=0) and the bow/stern lines (y=0) are
+    single shared node rows.  Outward cell orientation."""
+    xs = np.linspace(-L / 2, L / 2, nx + 1)
+    zs = np.linspace(-T, 0.0, nz + 1)
+    index = {}
+    pts = []
+
+    def half_beam(x, z):
+        return 0.5 * B * (1 - (2 * x / L) ** 2) * (1 - (z / T) ** 2)
+
+    def node(key, xyz):
+        k = index.get(key)
+        if k is None:
+            k = len(pts)
+            index[key] = k
+            pts.append(xyz)
+        return k
+
+    def side_node(i, j, s):
+        x, z = xs[i], zs[j]
+        y = s * half_beam(x, z)
+        if i == 0 or i == nx or j == 0:  # y == 0 lines shared by both sides
+            return node(("c", i, j), [x, 0.0, z])
+        if j == nz:
+            return node(("lid", i, s * ny_lid // 2 + ny_lid // 2), [x, y, z])
+        return node(("s", i, j, s), [x, y, z])
+
+    cells = []
+    for s in (1, -1):
+        for j in range(nz):
+            for i in range(nx):
+                q = [side_node(i, j, s), side_node(i + 1, j, s), side_node(i, j + 1, s),
+                     side_node(i + 1, j + 1, s)]
+                # starboard (y>0): d/dx x d/dz points -y; flip ordering for outward
+                if s > 0:
+                    q = [q[0], q[2], q[1], q[3]]
+                cells.append(q)
+    # lid: z = 0, grid over x and eta in [-1,1] with y = eta * half_beam(x, 0)
+    for j in range(ny_lid):
+        for i in range(nx):
+            quad = []
+            for dj in (0, 1):
+                for di in (0, 1):
+                    ii, jj = i + di, j + dj
+                    x = xs[ii]
+                    eta = -1.0 + 2.0 * jj / ny_lid
+                    y = eta * half_beam(x, 0.0)
+                    if ii == 0 or ii == nx:
+                        k = node(("c", ii, nz), [x, 0.0, 0.0])
+                    elif jj == 0:
+                        k = side_node(ii, nz, -1)
+                    elif jj == ny_lid:
+                        k = side_node(ii, nz, 1)
+                    else:
+                        k = node(("lid", ii, jj), [x, y, 0.0])
+                    quad.append(k)
+            cells.append(quad)  # d/dx x d/deta = +z (outward for the lid)
+    xyz = np.asarray(pts, dtype=np.float64)
+    cells = np.asarray(cells, dtype=np.int32)
+    # drop degenerate cells (bow/stern collapse all four vertices onto y=0 lines)
+    keep = np.array([len(set(c)) == 4 for c in cells.tolist()])
+    cells = cells[keep]
+    used = np.unique(cells)
+    remap = -np.ones(len(xyz), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    xyz = xyz[used]
+    cells = remap[cells].astype(np.int32)
+    return Mesh(xyz, cells, _nodal_normals(xyz, cells))
+
+
+def point_source_field(sources, strengths):
+    """phi(x) = sum_k q_k / |x - s_k| and its gradient."""
+    S = np.asarray(sources, dtype=np.float64).reshape(-1, 3)
+    q = np.asarray(strengths, dtype=np.float64).reshape(-1)
+
+    def phi(x):
+        d = x[:, None, :] - S[None, :, :]
+        r = np.linalg.norm(d, axis=2)
+        return (q[None, :] / r).sum(axis=1)
+
+    def grad(x):
+        d = x[:, None, :] - S[None, :, :]
+        r = np.linalg.norm(d, axis=2)
+        return -(q[None, :, None] * d / r[:, :, None] ** 3).sum(axis=1)
+
+    return phi, grad
+
+
+def mixed_bc_by_cell_centroid(mesh: Mesh, z_split: float = 0.0):
+    """Dirichlet mask: nodes of cells whose centroid has z > z_split (interface
+    nodes are Dirichlet); the rest Neumann."""
+    cz = mesh.xyz[mesh.cells][:, :, 2].mean(axis=1)
+    mask = np.zeros(mesh.n_nodes, dtype=np.uint8)
+    mask[np.unique(mesh.cells[cz > z_split])] = 1
+    return mask
+
+
+def sphere_dirichlet_case(n: int = 16, x0=(2.0, 0.5, 0.3)):
+    """Unit cube-sphere, pure Dirichlet phi = 1/|x-x0| (interior problem).
+
+    Returns mesh, dirichlet mask, tmp_rhs (phi at all nodes) and the analytic
+    dphi/dn at the nodes."""
+    mesh = cube_sphere(n)
+    phi, grad = point_source_field([x0], [1.0])
+    mask = np.ones(mesh.n_nodes, dtype=np.uint8)
+    tmp = phi(mesh.xyz)
+    exact_dn = (grad(mesh.xyz) * mesh.normals).sum(axis=1)
+    return mesh, mask, tmp, exact_dn
+
+
+def spheroid_mixed_case(n: int, seed: int, n_sources: int = 8, axes=(3.0, 1.0, 1.0),
+                        mesh: Mesh | None = None):
+    """Spheroid with mixed data from n_sources point sources of strength U(-1,1)
+    uniformly inside |s| < 0.5 (exterior problem).
+
+    Returns mesh, dirichlet mask, tmp_rhs, exact phi, exact dphi/dn."""
+    if mesh is None:
+        mesh = spheroid(n, axes)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    q = rng.uniform(-1.0, 1.0, n_sources)
+    dirs = rng.normal(size=(n_sources, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rad = 0.5 * rng.uniform(0.0, 1.0, n_sources) ** (1.0 / 3.0)
+    S = dirs * rad[:, None]
+    phi, grad = point_source_field(S, q)
+    mask = mixed_bc_by_cell_centroid(mesh)
+    ph = phi(mesh.xyz)
+    dn = (grad(mesh.xyz) * mesh.normals).sum(axis=1)
+    tmp = np.where(mask == 1, ph, dn)
+    return mesh, mask, tmp, ph, dn
