@@ -1,0 +1,161 @@
+/* pibem_gpu.h -- C ABI of the GB300 FMM-accelerated collocation BEM operator
+ * (3-D Laplace, Q1 surface meshes) and the GMRES solve around it.
+ *
+ * It is the drop-in replacement for pi-BEM's BEMFMA<3> accelerator and for the
+ * FMA branch of BEMProblem<3>:
+ *   include/bem_fma.h:94-202         BEMFMA public interface
+ *   source/bem_problem.cc:1139-1374  compute_alpha / vmult / compute_rhs /
+ *                                    solve_system / solve (FMA branches)
+ * Every entry point returns an int32 status (PIBEM_OK = 0); no C++ exception
+ * crosses this boundary.  The message of the last failure of a handle is
+ * available from pibem_last_error().
+ *
+ * Threading: a handle is used by one host thread at a time; several handles may
+ * share the GPU.  Host arrays are owned by the caller and are read or written
+ * only inside the call.  Device-pointer variants (suffix _device) are ordered
+ * on the handle's stream (pibem_set_stream) and return before the work ends.
+ */
+#ifndef PIBEM_GPU_H
+#define PIBEM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIBEM_OK 0
+#define PIBEM_EINVAL 1      /* bad argument or call order */
+#define PIBEM_ENOMEM_HBM 2  /* device allocation failed or HBM budget exceeded */
+#define PIBEM_ENOCONV 3     /* GMRES did not reach the tolerance within max steps */
+#define PIBEM_ETIMEDOUT 4   /* a bounded device wait gave up */
+#define PIBEM_ECUDA 5       /* CUDA runtime error */
+
+/* Arithmetic of the solve. */
+#define PIBEM_PRECISION_FP64 0  /* plain path: every matvec in FP64 */
+#define PIBEM_PRECISION_MIXED 1 /* FP32 operator inside GMRES + FP64 refinement residual */
+
+typedef struct pibem_handle pibem_handle;
+
+/* Parameter-file knobs of the reference (same names and defaults):
+ *   BEMFMA<3>/Octree Params/Number of Octree Levels                      (10)
+ *   BEMFMA<3>/Octree Params/Maximum Number of Collocation Points per
+ *             Childless Block                                            (20)
+ *   BEMFMA<3>/FMA Params/FMA Truncation Order                            (6)
+ *   BEMProblem<3>/Quadrature rules/Quadrature order                      (4)
+ *   BEMProblem<3>/Quadrature rules/Singular quadrature order             (5)
+ *   BEMProblem<3>/Solver/Max steps, Tolerance
+ *   BEMProblem<3>/Is external flow
+ * (source/bem_fma.cc:65-103, source/bem_problem.cc:247-312), plus the keys of
+ * the added subsection "GB300 Params". */
+typedef struct pibem_params
+{
+  int32_t fma_truncation_order;          /* p, 1..10 */
+  int32_t num_octree_levels;             /* 1..20 */
+  int32_t max_nodes_per_childless_block; /* leaf size */
+  int32_t quadrature_order;              /* QGauss order per direction, 1..8 */
+  int32_t singular_quadrature_order;     /* Telles order per direction, 1..12 */
+  int32_t solver_max_steps;              /* total GMRES iterations */
+  double  solver_tolerance;              /* relative true residual ||b-Ax||/||b|| */
+  int32_t gmres_restart;                 /* Krylov dimension (reference: 100) */
+  int32_t is_external_flow;              /* 0 interior (alpha=-N1), 1 exterior (alpha=-1-N1) */
+  int32_t precision_mode;                /* PIBEM_PRECISION_* */
+  int32_t preconditioner;                /* 0 none, 1 leaf-block Jacobi (right) */
+  int32_t device;                        /* CUDA device ordinal */
+  double  inner_tolerance;               /* mixed mode: inner FP32 GMRES tolerance */
+  double  hbm_budget_gb;                 /* 0 = unlimited */
+} pibem_params;
+
+typedef struct pibem_solve_stats
+{
+  int32_t iterations;        /* GMRES iterations (inner iterations in mixed mode) */
+  int32_t refinement_steps;  /* outer FP64 residual evaluations (mixed mode) */
+  int32_t fp64_matvecs;      /* FP64 operator applications */
+  int32_t fp32_matvecs;      /* FP32 operator applications */
+  double  relative_residual; /* final ||b - A x|| / ||b||, FP64 operator */
+  double  seconds;           /* wall time of the call */
+} pibem_solve_stats;
+
+typedef struct pibem_tree_info
+{
+  int32_t n_boxes, n_levels, n_leaves;
+  int64_t n_m2l_pairs, n_m2p_pairs, near_nnz, p2m_rows, n_quad_points;
+  int32_t n_m2l_offsets;
+  double  setup_seconds;
+} pibem_tree_info;
+
+/* Defaults of the reference parameter file. */
+int pibem_params_default(pibem_params *params);
+/* Parse the knobs above from the text of a deal.II .prm file
+ * (subsection / set / end); unknown keys are ignored. */
+int pibem_params_from_prm(pibem_params *params, const char *prm_text);
+
+int         pibem_create(const pibem_params *params, pibem_handle **out);
+int         pibem_destroy(pibem_handle *h);
+const char *pibem_last_error(const pibem_handle *h);
+/* cudaStream_t passed as void*; NULL selects the handle's own stream. */
+int         pibem_set_stream(pibem_handle *h, void *stream);
+
+/* Mesh: replaces BEMFMA::init_fma + generate_octree_blocking + direct_integrals
+ * + multipole_integrals (bem_fma.cc:42-62, 3615, 108, 1609).
+ *   xyz[3*n_nodes]        support points (DoF k at vertex k)
+ *   cell_nodes[4*n_cells] Q1 cells, deal.II lexicographic vertex order
+ *   double_offsets[n_nodes+1], double_ids: CSR of the double-node sets (each
+ *                         set includes the node itself), both NULL if the mesh
+ *                         has no double nodes. */
+int pibem_set_mesh(pibem_handle *h, int64_t n_nodes, const double *xyz, int64_t n_cells,
+                   const int32_t *cell_nodes, const int32_t *double_offsets,
+                   const int32_t *double_ids);
+
+/* Dirichlet mask (1 = Dirichlet node, 0 = Neumann node), the reference's
+ * dirichlet_nodes vector (bem_problem.cc:315-411).  Computes alpha. */
+int pibem_set_bc(pibem_handle *h, const uint8_t *dirichlet_mask);
+
+/* BEMFMA::generate_multipole_expansions + multipole_matr_vect_products
+ * (bem_fma.cc:1971, 2391): outN = N phi, outD = D dphi_dn, near field plus far
+ * field, FP64.  nrhs vectors stored one after another (length n_nodes each). */
+int pibem_fmm_matvec(pibem_handle *h, int32_t nrhs, const double *phi, const double *dphi_dn,
+                     double *outN, double *outD);
+
+/* BEMProblem::compute_alpha (bem_problem.cc:1139). */
+int pibem_compute_alpha(pibem_handle *h, double *alpha);
+
+/* BEMProblem::vmult (bem_problem.cc:1165): y = N(x.neu) - D(x.dir) + alpha.x.neu. */
+int pibem_system_matvec(pibem_handle *h, int32_t nrhs, const double *x, double *y);
+
+/* BEMProblem::compute_rhs (bem_problem.cc:1220). */
+int pibem_compute_rhs(pibem_handle *h, int32_t nrhs, const double *tmp_rhs, double *rhs);
+
+/* BEMProblem::solve_system (bem_problem.cc:1267): rhs, GMRES from x0 = rhs,
+ * scatter phi(i) = sol(i) on Neumann nodes, dphi_dn(i) = sol(i) on Dirichlet
+ * nodes; the other entries of phi / dphi_dn are left as given. */
+int pibem_solve(pibem_handle *h, int32_t nrhs, double *phi, double *dphi_dn,
+                const double *tmp_rhs, pibem_solve_stats *stats);
+
+/* Same as pibem_solve with device pointers, stream-ordered. */
+int pibem_solve_device(pibem_handle *h, int32_t nrhs, double *d_phi, double *d_dphi_dn,
+                       const double *d_tmp_rhs, pibem_solve_stats *stats);
+
+/* Introspection for parity tests and logging. */
+int pibem_tree_info_get(pibem_handle *h, pibem_tree_info *info);
+/* Box table: level, parent, number of children, pmin[3], delta, nodes, quad points. */
+int pibem_tree_boxes(pibem_handle *h, int32_t *level, int32_t *parent, int32_t *nchild,
+                     double *pmin, double *delta, int32_t *n_nodes, int32_t *n_quads);
+/* List of a box: kind 0 nearNeigh, 1 intList, 2 nonIntList at sublevel sub.
+ * Returns the size (copies at most cap ids), -1 on error. */
+int pibem_tree_list(pibem_handle *h, int32_t kind, int32_t box, int32_t sub, int32_t *out,
+                    int32_t cap);
+int pibem_tree_list_sublevels(pibem_handle *h, int32_t box);
+/* Near-field matrices as COO (rows, cols) sorted by row then column. */
+int64_t pibem_near_nnz(pibem_handle *h);
+int     pibem_near_export(pibem_handle *h, int32_t *rows, int32_t *cols, double *N, double *D);
+/* Quadrature points of the mesh, cell-major (n_cells * nq points). */
+int pibem_quad_points(pibem_handle *h, double *pts);
+/* Phase timings of the last operator application, milliseconds, in the order
+ * near, p2m, m2m, m2l, l2l, m2p, l2p (7 values). */
+int pibem_last_phase_ms(pibem_handle *h, double *ms7);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1445 @@
+// Handle and C ABI (include/pibem_gpu.h): mesh set-up, boundary conditions,
+// FMM operator applications and the GMRES solve, all on one GPU.
+//
+//   pibem_set_mesh       BEMFMA::init_fma + generate_octree_blocking +
+//                        direct_integrals + multipole_integrals (bem_fma.cc:42,3615,108,1609)
+//   pibem_fmm_matvec     generate_multipole_expansions + multipole_matr_vect_products
+//   pibem_compute_alpha  BEMProblem::compute_alpha   (bem_problem.cc:1139)
+//   pibem_system_matvec  BEMProblem::vmult           (bem_problem.cc:1165)
+//   pibem_compute_rhs    BEMProblem::compute_rhs     (bem_problem.cc:1220)
+//   pibem_solve          BEMProblem::solve_system    (bem_problem.cc:1267)
+#include <omp.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "krylov.h"
+#include "pibem_internal.h"
+
+using namespace pibem;
+
+namespace
+{
+  __global__ void diag_block_gather_kernel(int64_t n_rows, const int32_t *__restrict__ row_leaf,
+                                           const int64_t *__restrict__ row_ptr,
+                                           const int64_t *__restrict__ col_ptr,
+                                           const int64_t *__restrict__ val_ptr,
+                                           const int64_t *__restrict__ blk_ptr,
+                                           const int32_t *__restrict__ diag_col,
+                                           const double *__restrict__ S, double *__restrict__ B)
+  {
+    int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (row >= n_rows)
+      return;
+    int     leaf = row_leaf[row];
+    int64_t r0 = row_ptr[leaf], nr = row_ptr[leaf + 1] - r0, r = row - r0;
+    int64_t nc = col_ptr[leaf + 1] - col_ptr[leaf];
+    for (int64_t c = 0; c < nr; ++c)
+      B[blk_ptr[leaf] + r * nr + c] = S[val_ptr[leaf] + r * nc + diag_col[r0 + c]];
+  }
+
+  // Gauss-Jordan inverse with partial pivoting (host, small dense blocks).
+  bool invert(int n, double *a, double *inv)
+  {
+    std::vector<double> m(a, a + size_t(n) * n);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        inv[size_t(i) * n + j] = i == j ? 1.0 : 0.0;
+    for (int c = 0; c < n; ++c)
+      {
+        int    piv = c;
+        double best = std::fabs(m[size_t(c) * n + c]);
+        for (int r = c + 1; r < n; ++r)
+          if (std::fabs(m[size_t(r) * n + c]) > best)
+            {
+              best = std::fabs(m[size_t(r) * n + c]);
+              piv  = r;
+            }
+        if (!(best > 0))
+          return false;
+        if (piv != c)
+          for (int j = 0; j < n; ++j)
+            {
+              std::swap(m[size_t(c) * n + j], m[size_t(piv) * n + j]);
+              std::swap(inv[size_t(c) * n + j], inv[size_t(piv) * n + j]);
+            }
+        double d = 1.0 / m[size_t(c) * n + c];
+        for (int j = 0; j < n; ++j)
+          {
+            m[size_t(c) * n + j] *= d;
+            inv[size_t(c) * n + j] *= d;
+          }
+        for (int r = 0; r < n; ++r)
+          if (r != c)
+            {
+              double f = m[size_t(r) * n + c];
+              if (f != 0)
+                for (int j = 0; j < n; ++j)
+                  {
+                    m[size_t(r) * n + j] -= f * m[size_t(c) * n + j];
+                    inv[size_t(r) * n + j] -= f * inv[size_t(c) * n + j];
+                  }
+            }
+      }
+    return true;
+  }
+
+  template <typename T>
+  void transpose_ops(const std::vector<double> &src, int nops, int K, std::vector<T> &dst)
+  {
+    dst.resize(size_t(nops) * K * K);
+    for (int o = 0; o < nops; ++o)
+      for (int i = 0; i < K; ++i)
+        for (int j = 0; j < K; ++j)
+          dst[size_t(o) * K * K + size_t(j) * K + i] = T(src[size_t(o) * K * K + size_t(i) * K + j]);
+  }
+} // namespace
+
+struct pibem_handle
+{
+  pibem_params prm;
+  std::string  err;
+  cudaStream_t stream = nullptr, own = nullptr;
+  bool         mesh_ok = false, bc_ok = false;
+  MeshHost     mesh;
+  int          nq = 0, n_tel = 0;
+  std::vector<double> gpts, gw, tpts[4], tw[4];
+  Tree         tree;
+  Plan         plan;
+  double       setup_seconds = 0;
+  size_t       bytes_resident = 0;
+  // mesh
+  DBuf<double>  d_xyz, d_qpts, d_qnrm, d_qjxw, d_qshape, d_gpts, d_gw;
+  DBuf<int32_t> d_cells, d_dbl_off, d_dbl_ids;
+  // tree
+  DBuf<int32_t> d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted;
+  DBuf<double>  d_center, d_delta;
+  // plan
+  DBuf<int64_t> d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr,
+    d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr;
+  DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
+    d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
+    d_parents, d_diag_col;
+  DBuf<NearEntry> d_entries;
+  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_m2m, d_l2l, d_m2l, d_Pinv;
+  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_m2mf, d_l2lf, d_m2lf;
+  std::vector<int64_t> blk_ptr;
+  OperatorDev<double> op64;
+  OperatorDev<float>  op32;
+  TreeDev             td;
+  // boundary conditions
+  std::vector<uint8_t> dir;
+  DBuf<uint8_t>        d_dir, d_modes;
+  DBuf<double>         d_alpha;
+  bool                 have_dirichlet = true;
+  // work
+  DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4;
+  DBuf<float>  d_M32, d_L32, d_x32, d_y32;
+  DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
+  // timing
+  bool        timing = false;
+  cudaEvent_t ev[8] = {};
+  double      phase_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+  int         cnt64 = 0, cnt32 = 0;
+
+  int64_t N() const { return mesh.n_nodes; }
+};
+
+namespace
+{
+  int fail(pibem_handle *h, const Error &e)
+  {
+    if (h)
+      h->err = e.what();
+    return e.code;
+  }
+
+  template <typename F>
+  int guarded(pibem_handle *h, F &&f)
+  {
+    if (!h)
+      return PIBEM_EINVAL;
+    try
+      {
+        PIBEM_CUDA(cudaSetDevice(h->prm.device));
+        f();
+        return PIBEM_OK;
+      }
+    catch (const Error &e)
+      {
+        return fail(h, e);
+      }
+    catch (const std::bad_alloc &)
+      {
+        h->err = "host allocation failed";
+        return PIBEM_ENOMEM_HBM;
+      }
+    catch (const std::exception &e)
+      {
+        h->err = e.what();
+        return PIBEM_EINVAL;
+      }
+  }
+
+  void record(pibem_handle *h, int i)
+  {
+    if (h->timing)
+      PIBEM_CUDA(cudaEventRecord(h->ev[i], h->stream));
+  }
+
+  // ---------------------------------------------------------------------
+  // Far field (P2M ... L2P) added to y for R columns.
+  // ---------------------------------------------------------------------
+  template <typename T>
+  void far_field(pibem_handle *h, const OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, int R,
+                 const uint8_t *modes, const T *x, T *y)
+  {
+    const int    N = int(h->N());
+    const size_t need = size_t(h->tree.nb) * R * op.K;
+    if (M.n < need)
+      {
+        M.alloc(need);
+        Lx.alloc(need);
+      }
+    cudaStream_t s = h->stream;
+    PIBEM_CUDA(cudaMemsetAsync(Lx.p, 0, need * sizeof(T), s));
+    PIBEM_CUDA(cudaMemsetAsync(M.p, 0, need * sizeof(T), s));
+    launch_p2m_apply<T>(op, R, N, h->d_dir.p, modes, x, M.p, s);
+    record(h, 2);
+    for (int pl = h->tree.L - 1; pl >= 0; --pl)
+      launch_m2m_level<T>(op, h->td, R, pl, M.p, s);
+    record(h, 3);
+    for (int l = 1; l <= h->tree.L; ++l)
+      {
+        launch_l2l_level<T>(op, h->td, R, l, Lx.p, s);
+        launch_m2l_level<T>(op, R, l, M.p, Lx.p, s);
+      }
+    record(h, 4);
+    record(h, 5);
+    launch_m2p<T>(op, h->td, R, N, M.p, y, s);
+    record(h, 6);
+    launch_l2p<T>(op, R, N, Lx.p, y, s);
+    record(h, 7);
+  }
+
+  void finish_timing(pibem_handle *h)
+  {
+    if (!h->timing)
+      return;
+    PIBEM_CUDA(cudaEventSynchronize(h->ev[7]));
+    for (int i = 0; i < 7; ++i)
+      {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]);
+        h->phase_ms[i] = ms;
+      }
+  }
+
+  // [phi_0..phi_{R-1}, dphi_0..dphi_{R-1}] -> [outN..., outD...]  (FP64)
+  void fmm_apply64(pibem_handle *h, int R, const double *phi, const double *dphi, double *oN,
+                   double *oD)
+  {
+    const int64_t N = h->N();
+    cudaStream_t  s = h->stream;
+    h->d_x64.alloc(size_t(2 * R) * N);
+    h->d_y64.alloc(size_t(2 * R) * N);
+    PIBEM_CUDA(cudaMemcpyAsync(h->d_x64.p, phi, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+    PIBEM_CUDA(cudaMemcpyAsync(h->d_x64.p + R * N, dphi, sizeof(double) * R * N,
+                               cudaMemcpyDeviceToDevice, s));
+    std::vector<uint8_t> modes(2 * R);
+    for (int r = 0; r < R; ++r)
+      {
+        modes[r]     = MODE_KER1;
+        modes[R + r] = MODE_KER2;
+      }
+    h->d_modes.upload(modes, s);
+    record(h, 0);
+    launch_near_spmv<double>(h->op64, R, int(N), h->d_N.p, h->d_x64.p, h->d_y64.p, false, s);
+    launch_near_spmv<double>(h->op64, R, int(N), h->d_D.p, h->d_x64.p + R * N,
+                             h->d_y64.p + R * N, false, s);
+    record(h, 1);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, 2 * R, h->d_modes.p, h->d_x64.p,
+                      h->d_y64.p);
+    PIBEM_CUDA(cudaMemcpyAsync(oN, h->d_y64.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+    PIBEM_CUDA(cudaMemcpyAsync(oD, h->d_y64.p + R * N, sizeof(double) * R * N,
+                               cudaMemcpyDeviceToDevice, s));
+    h->cnt64 += R;
+  }
+
+  // Near-field N only with the double-layer far field (alpha needs N*1 only).
+  void ker1_apply64(pibem_handle *h, const double *x, double *y)
+  {
+    const int64_t        N = h->N();
+    std::vector<uint8_t> modes(1, MODE_KER1);
+    h->d_modes.upload(modes, h->stream);
+    launch_near_spmv<double>(h->op64, 1, int(N), h->d_N.p, x, y, false, h->stream);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, 1, h->d_modes.p, x, y);
+  }
+
+  void set_modes(pibem_handle *h, int R, uint8_t mode)
+  {
+    std::vector<uint8_t> modes(R, mode);
+    h->d_modes.upload(modes, h->stream);
+  }
+
+  // Pure-Neumann shift of bem_problem.cc:1169-1172 / 1214-1215: v -= ||v||_2.
+  void shift_by_norm(pibem_handle *h, int R, double *v)
+  {
+    const int64_t N    = h->N();
+    const int     nblk = 64;
+    h->g_partial.alloc(size_t(R) * nblk * 4);
+    h->g_nrm.alloc(R);
+    launch_dots(N, R, 1, N, N, v, v, h->g_partial.p, nblk, h->g_nrm.p, h->stream);
+    std::vector<double> nr(R);
+    h->g_nrm.download(nr.data(), R, h->stream);
+    PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &x : nr)
+      x = -std::sqrt(x);
+    h->g_u.upload(nr, h->stream);
+    launch_add_scalar(N, R, h->g_u.p, v, h->stream);
+  }
+
+  // BEMProblem::vmult for R columns, FP64 (device in/out).
+  void system_apply64(pibem_handle *h, int R, const double *x, double *y)
+  {
+    const int64_t N = h->N();
+    cudaStream_t  s = h->stream;
+    const double *xin = x;
+    if (!h->have_dirichlet)
+      {
+        h->d_t4.alloc(size_t(R) * N);
+        PIBEM_CUDA(cudaMemcpyAsync(h->d_t4.p, x, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+        shift_by_norm(h, R, h->d_t4.p);
+        xin = h->d_t4.p;
+      }
+    set_modes(h, R, MODE_COMBINED);
+    record(h, 0);
+    launch_near_spmv<double>(h->op64, R, int(N), h->d_S.p, xin, y, false, s);
+    record(h, 1);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, R, h->d_modes.p, xin, y);
+    if (!h->have_dirichlet)
+      shift_by_norm(h, R, y);
+    h->cnt64 += R;
+  }
+
+  // Same operator in FP32 (input and output FP64).
+  void system_apply32(pibem_handle *h, int R, const double *x, double *y)
+  {
+    const int64_t N = h->N();
+    cudaStream_t  s = h->stream;
+    const double *xin = x;
+    if (!h->have_dirichlet)
+      {
+        h->d_t4.alloc(size_t(R) * N);
+        PIBEM_CUDA(cudaMemcpyAsync(h->d_t4.p, x, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+        shift_by_norm(h, R, h->d_t4.p);
+        xin = h->d_t4.p;
+      }
+    h->d_x32.alloc(size_t(R) * N);
+    h->d_y32.alloc(size_t(R) * N);
+    launch_convert_d2f(int64_t(R) * N, xin, h->d_x32.p, s);
+    set_modes(h, R, MODE_COMBINED);
+    record(h, 0);
+    launch_near_spmv<float>(h->op32, R, int(N), h->d_S32.p, h->d_x32.p, h->d_y32.p, false, s);
+    record(h, 1);
+    far_field<float>(h, h->op32, h->d_M32, h->d_L32, R, h->d_modes.p, h->d_x32.p, h->d_y32.p);
+    launch_convert_f2d(int64_t(R) * N, h->d_y32.p, y, s);
+    if (!h->have_dirichlet)
+      shift_by_norm(h, R, y);
+    h->cnt32 += R;
+  }
+
+  // ---------------------------------------------------------------------
+  // Restarted GMRES(m) for R right-hand sides in lockstep, right leaf-block
+  // Jacobi preconditioning, CGS2 Arnoldi in FP64 on the device, Givens
+  // rotations and the small least-squares problem on the host.  Stops each
+  // column at ||b - A x|| / ||b|| <= tol (true residual at every restart).
+  // ---------------------------------------------------------------------
+  struct GmresResult
+  {
+    int                 iterations = 0;
+    std::vector<double> rel;
+  };
+
+  GmresResult gmres(pibem_handle *h, int R, const double *b, double *x, double tol, int maxit,
+                    int m, const std::function<void(const double *, double *)> &A, bool prec)
+  {
+    const int64_t N    = h->N();
+    cudaStream_t  s    = h->stream;
+    const int     nblk = 2 * 152;
+    const int64_t ldr  = int64_t(m + 1) * N;
+    h->g_V.alloc(size_t(R) * (m + 1) * N);
+    h->g_w.alloc(size_t(R) * N);
+    h->g_z.alloc(size_t(R) * N);
+    h->g_u.alloc(size_t(R) * std::max<int64_t>(N, m + 2));
+    h->g_partial.alloc(size_t(R) * nblk * (m + 2));
+    h->g_h.alloc(size_t(R) * (m + 2));
+    h->g_h2.alloc(size_t(R) * (m + 2));
+    h->g_nrm.alloc(R);
+    h->g_bn.alloc(R);
+    GmresResult res;
+    res.rel.assign(R, 1.0);
+    std::vector<double> bn(R);
+    launch_dots(N, R, 1, N, N, b, b, h->g_partial.p, nblk, h->g_bn.p, s);
+    h->g_bn.download(bn.data(), R, s);
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    for (auto &v : bn)
+      v = v > 0 ? std::sqrt(v) : 1.0;
+    std::vector<double> H(size_t(R) * (m + 1) * m), cs(size_t(R) * m), sn(size_t(R) * m),
+      g(size_t(R) * (m + 1)), hh(size_t(R) * (m + 2)), h2(size_t(R) * (m + 2)), nr(R), beta(R);
+    std::vector<int>    kdone(R);
+    while (true)
+      {
+        // true residual r = b - A x into V[:,0]
+        A(x, h->g_w.p);
+        for (int r = 0; r < R; ++r)
+          {
+            PIBEM_CUDA(cudaMemcpyAsync(h->g_V.p + r * ldr, b + r * N, sizeof(double) * N,
+                                       cudaMemcpyDeviceToDevice, s));
+            launch_axpby(N, -1.0, h->g_w.p + r * N, 1.0, h->g_V.p + r * ldr, s);
+          }
+        std::vector<double> b2(R);
+        for (int r = 0; r < R; ++r)
+          launch_dots(N, 1, 1, N, N, h->g_V.p + r * ldr, h->g_V.p + r * ldr, h->g_partial.p, nblk,
+                      h->g_nrm.p + r, s);
+        h->g_nrm.download(b2.data(), R, s);
+        PIBEM_CUDA(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int r = 0; r < R; ++r)
+          {
+            beta[r]    = std::sqrt(b2[r]);
+            res.rel[r] = beta[r] / bn[r];
+            kdone[r]   = res.rel[r] <= tol ? 0 : -1;
+            any        = any || kdone[r] < 0;
+          }
+        if (!any || res.iterations >= maxit)
+          break;
+        for (int r = 0; r < R; ++r) // V[r][0] = r_r / beta_r (through the w buffer)
+          PIBEM_CUDA(cudaMemcpyAsync(h->g_w.p + r * N, h->g_V.p + r * ldr, sizeof(double) * N,
+                                     cudaMemcpyDeviceToDevice, s));
+        launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p, ldr, s);
+        std::fill(g.begin(), g.end(), 0.0);
+        for (int r = 0; r < R; ++r)
+          g[size_t(r) * (m + 1)] = beta[r];
+        int j = 0;
+        for (; j < m; ++j)
+          {
+            // z = P^-1 V_j ; w = A z
+            const double *vj = h->g_V.p + int64_t(j) * N;
+            if (prec)
+              {
+                for (int r = 0; r < R; ++r)
+                  PIBEM_CUDA(cudaMemcpyAsync(h->g_u.p + r * N, vj + r * ldr, sizeof(double) * N,
+                                             cudaMemcpyDeviceToDevice, s));
+                launch_block_apply(h->plan.nrows.size(), R, N, h->d_row_leaf.p, h->d_nrow_ptr.p,
+                                   h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, h->g_z.p,
+                                   s);
+              }
+            else
+              for (int r = 0; r < R; ++r)
+                PIBEM_CUDA(cudaMemcpyAsync(h->g_z.p + r * N, vj + r * ldr, sizeof(double) * N,
+                                           cudaMemcpyDeviceToDevice, s));
+            A(h->g_z.p, h->g_w.p);
+            // CGS2
+            launch_dots(N, R, j + 1, N, ldr, h->g_V.p, h->g_w.p, h->g_partial.p, nblk, h->g_h.p, s);
+            launch_gemv_sub(N, R, j + 1, N, ldr, h->g_V.p, h->g_h.p, j + 1, h->g_w.p, 1.0, s);
+            launch_dots(N, R, j + 1, N, ldr, h->g_V.p, h->g_w.p, h->g_partial.p, nblk, h->g_h2.p, s);
+            launch_gemv_sub(N, R, j + 1, N, ldr, h->g_V.p, h->g_h2.p, j + 1, h->g_w.p, 1.0, s);
+            for (int r = 0; r < R; ++r)
+              launch_dots(N, 1, 1, N, N, h->g_w.p + r * N, h->g_w.p + r * N, h->g_partial.p, nblk,
+                          h->g_nrm.p + r, s);
+            launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p + int64_t(j + 1) * N, ldr, s);
+            h->g_h.download(hh.data(), size_t(R) * (j + 1), s);
+            h->g_h2.download(h2.data(), size_t(R) * (j + 1), s);
+            h->g_nrm.download(nr.data(), R, s);
+            PIBEM_CUDA(cudaStreamSynchronize(s));
+            ++res.iterations;
+            bool all = true;
+            for (int r = 0; r < R; ++r)
+              {
+                if (kdone[r] >= 0)
+                  continue;
+                double *Hc = &H[size_t(r) * (m + 1) * m];
+                for (int i = 0; i <= j; ++i)
+                  Hc[size_t(i) * m + j] = hh[size_t(r) * (j + 1) + i] + h2[size_t(r) * (j + 1) + i];
+                Hc[size_t(j + 1) * m + j] = std::sqrt(nr[r]);
+                double *c = &cs[size_t(r) * m], *sv = &sn[size_t(r) * m], *gg = &g[size_t(r) * (m + 1)];
+                for (int i = 0; i < j; ++i)
+                  {
+                    double t1 = c[i] * Hc[size_t(i) * m + j] + sv[i] * Hc[size_t(i + 1) * m + j];
+                    Hc[size_t(i + 1) * m + j] = -sv[i] * Hc[size_t(i) * m + j] + c[i] * Hc[size_t(i + 1) * m + j];
+                    Hc[size_t(i) * m + j]     = t1;
+                  }
+                double a = Hc[size_t(j) * m + j], bb = Hc[size_t(j + 1) * m + j];
+                double d = std::hypot(a, bb);
+                c[j]     = d > 0 ? a / d : 1.0;
+                sv[j]    = d > 0 ? bb / d : 0.0;
+                Hc[size_t(j) * m + j]     = d;
+                Hc[size_t(j + 1) * m + j] = 0;
+                gg[j + 1] = -sv[j] * gg[j];
+                gg[j]     = c[j] * gg[j];
+                if (std::fabs(gg[j + 1]) / bn[r] <= tol || bb == 0.0)
+                  kdone[r] = j + 1;
+                else
+                  all = false;
+              }
+            if (all || res.iterations >= maxit)
+              {
+                ++j;
+                break;
+              }
+          }
+        // x += P^-1 V y
+        std::vector<double> y(size_t(R) * (m + 1), 0.0);
+        for (int r = 0; r < R; ++r)
+          {
+            int k = kdone[r] < 0 ? j : kdone[r];
+            if (kdone[r] == 0)
+              k = 0;
+            const double *Hc = &H[size_t(r) * (m + 1) * m];
+            const double *gg = &g[size_t(r) * (m + 1)];
+            for (int i = k - 1; i >= 0; --i)
+              {
+                double sum = gg[i];
+                for (int jj = i + 1; jj < k; ++jj)
+                  sum -= Hc[size_t(i) * m + jj] * y[size_t(r) * (m + 1) + jj];
+                y[size_t(r) * (m + 1) + i] = sum / Hc[size_t(i) * m + i];
+              }
+          }
+        int kmax = j;
+        h->g_y.upload(y.data(), y.size(), s);
+        PIBEM_CUDA(cudaMemsetAsync(h->g_u.p, 0, sizeof(double) * R * N, s));
+        launch_gemv_sub(N, R, kmax, N, ldr, h->g_V.p, h->g_y.p, m + 1, h->g_u.p, -1.0, s);
+        if (prec)
+          {
+            launch_block_apply(h->plan.nrows.size(), R, N, h->d_row_leaf.p, h->d_nrow_ptr.p,
+                               h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, h->g_z.p, s);
+            launch_axpby(int64_t(R) * N, 1.0, h->g_z.p, 1.0, x, s);
+          }
+        else
+          launch_axpby(int64_t(R) * N, 1.0, h->g_u.p, 1.0, x, s);
+      }
+    return res;
+  }
+
+  void build_preconditioner(pibem_handle *h)
+  {
+    const Plan   &pl = h->plan;
+    const int     nl = int(pl.nleaf_box.size());
+    cudaStream_t  s  = h->stream;
+    h->blk_ptr.assign(nl + 1, 0);
+    for (int k = 0; k < nl; ++k)
+      {
+        int64_t nr       = pl.nrow_ptr[k + 1] - pl.nrow_ptr[k];
+        h->blk_ptr[k + 1] = h->blk_ptr[k] + nr * nr;
+      }
+    h->d_blk_ptr.upload(h->blk_ptr, s);
+    DBuf<double> blocks;
+    blocks.alloc(h->blk_ptr[nl]);
+    int64_t nrows = int64_t(pl.nrows.size());
+    if (nrows)
+      diag_block_gather_kernel<<<unsigned((nrows + 127) / 128), 128, 0, s>>>(
+        nrows, h->d_row_leaf.p, h->d_nrow_ptr.p, h->d_ncol_ptr.p, h->d_nval_ptr.p, h->d_blk_ptr.p,
+        h->d_diag_col.p, h->d_S.p, blocks.p);
+    PIBEM_CUDA(cudaGetLastError());
+    std::vector<double> hb(h->blk_ptr[nl]), inv(h->blk_ptr[nl]);
+    blocks.download(hb.data(), hb.size(), s);
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int k = 0; k < nl; ++k)
+      {
+        int n = int(pl.nrow_ptr[k + 1] - pl.nrow_ptr[k]);
+        if (!invert(n, &hb[h->blk_ptr[k]], &inv[h->blk_ptr[k]]))
+          for (int i = 0; i < n; ++i)
+            for (int j2 = 0; j2 < n; ++j2)
+              inv[h->blk_ptr[k] + size_t(i) * n + j2] = i == j2 ? 1.0 : 0.0;
+      }
+    h->d_Pinv.upload(inv, s);
+  }
+
+  void fill_operator_views(pibem_handle *h)
+  {
+    const Plan &pl = h->plan;
+    auto        fill = [&](auto &op) {
+      op.p             = pl.p;
+      op.K             = pl.K;
+      op.n_near_leaves = int(pl.nleaf_box.size());
+      op.n_rows        = int64_t(pl.nrows.size());
+      op.row_leaf      = h->d_row_leaf.p;
+      op.nrows         = h->d_nrows.p;
+      op.ncols         = h->d_ncols.p;
+      op.nrow_ptr      = h->d_nrow_ptr.p;
+      op.ncol_ptr      = h->d_ncol_ptr.p;
+      op.nval_ptr      = h->d_nval_ptr.p;
+      op.n_p2m_leaves  = int(pl.pleaf_box.size());
+      op.prow_ptr      = h->d_prow_ptr.p;
+      op.pleaf_box     = h->d_pleaf_box.p;
+      op.prow_dof      = h->d_prow_dof.p;
+      op.lleaf_box     = h->d_lleaf_box.p;
+      op.m2l_tgt       = h->d_m2l_tgt.p;
+      op.m2l_src       = h->d_m2l_src.p;
+      op.m2l_off       = h->d_m2l_off.p;
+      op.m2l_src_ptr   = h->d_m2l_src_ptr.p;
+      op.n_m2p_tgt     = int(pl.m2p_tgt.size());
+      op.m2p_tgt       = h->d_m2p_tgt.p;
+      op.m2p_src       = h->d_m2p_src.p;
+      op.m2p_src_ptr   = h->d_m2p_src_ptr.p;
+      op.l2l_box       = h->d_l2l_box.p;
+      op.m2l_level_ptr = pl.m2l_tgt_ptr_level;
+      op.l2l_level_ptr = pl.l2l_ptr_level;
+      op.parents       = h->d_parents.p;
+    };
+    fill(h->op64);
+    fill(h->op32);
+    h->op64.T1      = h->d_T1.p;
+    h->op64.T2      = h->d_T2.p;
+    h->op64.W       = h->d_W.p;
+    h->op64.m2m_ops = h->d_m2m.p;
+    h->op64.l2l_ops = h->d_l2l.p;
+    h->op64.m2l_ops = h->d_m2l.p;
+    h->op32.T1      = h->d_T1f.p;
+    h->op32.T2      = h->d_T2f.p;
+    h->op32.W       = h->d_Wf.p;
+    h->op32.m2m_ops = h->d_m2mf.p;
+    h->op32.l2l_ops = h->d_l2lf.p;
+    h->op32.m2l_ops = h->d_m2lf.p;
+    // parents grouped by their level
+    std::vector<int32_t> parents;
+    std::vector<int>     pptr(h->tree.L + 2, 0);
+    for (int l = 0; l <= h->tree.L; ++l)
+      {
+        pptr[l] = int(parents.size());
+        int a = l == 0 ? 0 : h->tree.startLevel[l], b = l == 0 ? 0 : h->tree.endLevel[l];
+        for (int bx = a; bx <= b; ++bx)
+          if (h->tree.nchild[bx] > 0)
+            parents.push_back(bx);
+      }
+    pptr[h->tree.L + 1] = int(parents.size());
+    h->d_parents.upload(parents, h->stream);
+    h->op64.parents_level_ptr = pptr;
+    h->op32.parents_level_ptr = pptr;
+    h->op64.parents           = h->d_parents.p;
+    h->op32.parents           = h->d_parents.p;
+    TreeDev &td               = h->td;
+    td.nb                     = h->tree.nb;
+    td.N                      = int(h->N());
+    td.L                      = h->tree.L;
+    td.parent                 = h->d_parent.p;
+    td.child_first            = h->d_child_first.p;
+    td.nchild                 = h->d_nchild.p;
+    td.digit                  = h->d_digit.p;
+    td.nbeg                   = h->d_nbeg.p;
+    td.nend                   = h->d_nend.p;
+    td.node_sorted            = h->d_node_sorted.p;
+    td.center                 = h->d_center.p;
+    td.delta                  = h->d_delta.p;
+    td.xyz                    = h->d_xyz.p;
+  }
+
+  // Every index a kernel will dereference is checked here, on the host, so that
+  // an inconsistent plan becomes PIBEM_EINVAL instead of a device fault.
+  void validate_plan(const MeshHost &m, const Tree &t, const Plan &pl, int nq)
+  {
+    auto need = [](bool ok, const char *what) {
+      if (!ok)
+        throw Error(PIBEM_EINVAL, std::string("internal plan check failed: ") + what);
+    };
+    const int64_t N = m.n_nodes, Q = m.n_cells * nq;
+    const int     nl = int(pl.nleaf_box.size());
+    need(pl.nrow_ptr.size() == size_t(nl + 1) && pl.ncol_ptr.size() == size_t(nl + 1) &&
+           pl.nent_ptr.size() == size_t(nl + 1) && pl.nval_ptr.size() == size_t(nl + 1),
+         "near pointer sizes");
+    need(int64_t(pl.gather_ptr.size()) == pl.ncol_ptr[nl] + 1, "gather_ptr size");
+    for (int k = 0; k < nl; ++k)
+      {
+        int64_t nr = pl.nrow_ptr[k + 1] - pl.nrow_ptr[k], nc = pl.ncol_ptr[k + 1] - pl.ncol_ptr[k],
+                ne = pl.nent_ptr[k + 1] - pl.nent_ptr[k];
+        need(nr > 0 && nc > 0 && ne > 0, "empty near leaf");
+        need(pl.nval_ptr[k + 1] - pl.nval_ptr[k] == nr * nc, "near value block size");
+        need(pl.nleaf_box[k] >= 0 && pl.nleaf_box[k] < t.nb, "near leaf box");
+        for (int64_t e = pl.nent_ptr[k]; e < pl.nent_ptr[k + 1]; ++e)
+          {
+            const NearEntry &E = pl.entries[e];
+            need(E.cell >= 0 && E.cell < m.n_cells, "entry cell");
+            need(E.qmask != 0 && (nq == 64 || (E.qmask >> nq) == 0), "entry quad mask");
+            for (int j = 0; j < 4; ++j)
+              need(E.lcol[j] >= 0 && E.lcol[j] < nc, "entry column");
+          }
+        for (int64_t c = pl.ncol_ptr[k]; c < pl.ncol_ptr[k + 1]; ++c)
+          {
+            need(pl.gather_ptr[c] <= pl.gather_ptr[c + 1], "gather order");
+            for (int g = pl.gather_ptr[c]; g < pl.gather_ptr[c + 1]; ++g)
+              need(pl.gather_ids[g] >= 0 && pl.gather_ids[g] < 4 * ne, "gather id");
+          }
+      }
+    for (int32_t v : pl.nrows)
+      need(v >= 0 && v < N, "near row node");
+    for (int32_t v : pl.ncols)
+      need(v >= 0 && v < N, "near column node");
+    for (size_t r = 0; r < pl.row_leaf.size(); ++r)
+      need(pl.row_leaf[r] >= 0 && pl.row_leaf[r] < nl && pl.nrow_ptr[pl.row_leaf[r]] <= int64_t(r) &&
+             int64_t(r) < pl.nrow_ptr[pl.row_leaf[r] + 1],
+           "row leaf");
+    const int np = int(pl.pleaf_box.size());
+    need(pl.prow_ptr.size() == size_t(np + 1), "p2m row ptr");
+    need(pl.pcontrib_ptr.size() == pl.prow_dof.size() + 1, "p2m contrib ptr");
+    for (int k = 0; k < np; ++k)
+      need(pl.prow_ptr[k + 1] > pl.prow_ptr[k] && pl.pleaf_box[k] >= 0 && pl.pleaf_box[k] < t.nb,
+           "p2m leaf");
+    for (int32_t v : pl.prow_dof)
+      need(v >= 0 && v < N, "p2m row dof");
+    for (int32_t v : pl.pcontrib_q)
+      need(v >= 0 && int64_t(v) < 4 * Q, "p2m contribution");
+    const int noff = int(pl.offsets.size() / 3);
+    need(pl.m2l_src_ptr.size() == pl.m2l_tgt.size() + 1, "m2l ptr");
+    for (size_t i = 0; i < pl.m2l_src.size(); ++i)
+      need(pl.m2l_src[i] >= 0 && pl.m2l_src[i] < t.nb && pl.m2l_off[i] >= 0 && pl.m2l_off[i] < noff,
+           "m2l pair");
+    for (int32_t v : pl.m2l_tgt)
+      need(v >= 0 && v < t.nb, "m2l target");
+    need(pl.m2p_src_ptr.size() == pl.m2p_tgt.size() + 1, "m2p ptr");
+    for (int32_t v : pl.m2p_tgt)
+      need(v >= 0 && v < t.nb && t.nend[v] > t.nbeg[v], "m2p target");
+    for (int32_t v : pl.m2p_src)
+      need(v >= 0 && v < t.nb, "m2p source");
+    for (int32_t v : pl.l2l_box)
+      need(v > 0 && v < t.nb && t.level[v] >= 2, "l2l box");
+    for (int b = 1; b < t.nb; ++b)
+      need(t.parent[b] >= 0 && t.parent[b] < b && t.digit[b] >= 0 && t.digit[b] < 8, "box parent");
+    for (int b = 0; b < t.nb; ++b)
+      need(t.nchild[b] == 0 || (t.child_first[b] > b && t.child_first[b] + t.nchild[b] <= t.nb),
+           "box children");
+  }
+
+  void set_mesh_impl(pibem_handle *h, int64_t n_nodes, const double *xyz, int64_t n_cells,
+                     const int32_t *cells, const int32_t *doff, const int32_t *dids)
+  {
+    auto t0 = std::chrono::steady_clock::now();
+    if (n_nodes <= 0 || n_cells <= 0 || !xyz || !cells)
+      throw Error(PIBEM_EINVAL, "empty mesh");
+    if ((doff == nullptr) != (dids == nullptr))
+      throw Error(PIBEM_EINVAL, "double_offsets and double_ids must both be given or both NULL");
+    if (n_nodes > INT32_MAX / 8 || n_cells * 64 > INT32_MAX)
+      throw Error(PIBEM_EINVAL, "mesh too large for 32-bit node / quadrature ids");
+    const pibem_params &P = h->prm;
+    cudaStream_t        s = h->stream;
+    h->mesh_ok = h->bc_ok = false;
+    MeshHost &m = h->mesh;
+    m.n_nodes   = n_nodes;
+    m.n_cells   = n_cells;
+    m.xyz.assign(xyz, xyz + 3 * n_nodes);
+    m.cells.assign(cells, cells + 4 * n_cells);
+    for (int64_t i = 0; i < 4 * n_cells; ++i)
+      if (cells[i] < 0 || cells[i] >= n_nodes)
+        throw Error(PIBEM_EINVAL, "cell node id out of range");
+    for (int64_t i = 0; i < 3 * n_nodes; ++i)
+      if (!std::isfinite(xyz[i]))
+        throw Error(PIBEM_EINVAL, "non-finite node coordinate");
+    m.dbl_off.assign(n_nodes + 1, 0);
+    m.dbl_ids.clear();
+    for (int64_t i = 0; i < n_nodes; ++i)
+      {
+        std::vector<int32_t> set = {int32_t(i)};
+        if (doff)
+          for (int32_t k = doff[i]; k < doff[i + 1]; ++k)
+            {
+              if (dids[k] < 0 || dids[k] >= n_nodes)
+                throw Error(PIBEM_EINVAL, "double node id out of range");
+              set.push_back(dids[k]);
+            }
+        std::sort(set.begin(), set.end());
+        set.erase(std::unique(set.begin(), set.end()), set.end());
+        m.dbl_ids.insert(m.dbl_ids.end(), set.begin(), set.end());
+        m.dbl_off[i + 1] = int32_t(m.dbl_ids.size());
+      }
+    m.elem_off.assign(n_nodes + 1, 0);
+    for (int64_t i = 0; i < 4 * n_cells; ++i)
+      m.elem_off[cells[i] + 1]++;
+    for (int64_t i = 0; i < n_nodes; ++i)
+      m.elem_off[i + 1] += m.elem_off[i];
+    m.elem_ids.assign(m.elem_off[n_nodes], 0);
+    {
+      std::vector<int32_t> fillp(m.elem_off.begin(), m.elem_off.end() - 1);
+      for (int64_t c = 0; c < n_cells; ++c)
+        for (int j = 0; j < 4; ++j)
+          m.elem_ids[fillp[cells[4 * c + j]]++] = int32_t(c);
+    }
+    // quadrature rules
+    gauss_rule_2d(P.quadrature_order, h->gpts, h->gw);
+    h->nq    = int(h->gw.size());
+    for (int v = 0; v < 4; ++v)
+      telles_rule_2d(P.singular_quadrature_order, v, h->tpts[v], h->tw[v]);
+    h->n_tel = int(h->tw[0].size());
+    set_telles_rules(h->tpts, h->tw, h->n_tel, s);
+    // device mesh and quadrature data
+    h->d_xyz.upload(m.xyz, s);
+    h->d_cells.upload(m.cells, s);
+    h->d_dbl_off.upload(m.dbl_off, s);
+    h->d_dbl_ids.upload(m.dbl_ids, s);
+    h->d_gpts.upload(h->gpts, s);
+    h->d_gw.upload(h->gw, s);
+    const int64_t Q = n_cells * h->nq;
+    h->d_qpts.alloc(3 * Q);
+    h->d_qnrm.alloc(3 * Q);
+    h->d_qjxw.alloc(Q);
+    h->d_qshape.alloc(4 * Q);
+    launch_quad_data(n_cells, h->nq, h->d_xyz.p, h->d_cells.p, h->d_gpts.p, h->d_gw.p,
+                     h->d_qpts.p, h->d_qnrm.p, h->d_qjxw.p, h->d_qshape.p, s);
+    std::vector<double> qpts(3 * Q);
+    h->d_qpts.download(qpts.data(), qpts.size(), s);
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    // octree, lists and plan
+    build_tree(m, qpts, h->nq, P.num_octree_levels, P.max_nodes_per_childless_block, h->tree);
+    build_plan(m, h->tree, h->nq, P.fma_truncation_order, h->plan);
+    const Tree &t  = h->tree;
+    const Plan &pl = h->plan;
+    const int   K  = pl.K;
+    validate_plan(m, t, pl, h->nq);
+    // tree arrays
+    std::vector<double> center(3 * size_t(t.nb));
+    for (int b = 0; b < t.nb; ++b)
+      t.center(b, &center[3 * size_t(b)]);
+    h->d_parent.upload(t.parent, s);
+    h->d_child_first.upload(t.child_first, s);
+    h->d_nchild.upload(t.nchild, s);
+    h->d_digit.upload(t.digit, s);
+    h->d_nbeg.upload(t.nbeg, s);
+    h->d_nend.upload(t.nend, s);
+    h->d_node_sorted.upload(t.node_sorted, s);
+    h->d_center.upload(center, s);
+    h->d_delta.upload(t.delta, s);
+    // plan arrays
+    h->d_nrow_ptr.upload(pl.nrow_ptr, s);
+    h->d_ncol_ptr.upload(pl.ncol_ptr, s);
+    h->d_nval_ptr.upload(pl.nval_ptr, s);
+    h->d_nent_ptr.upload(pl.nent_ptr, s);
+    h->d_row_leaf.upload(pl.row_leaf, s);
+    h->d_nrows.upload(pl.nrows, s);
+    h->d_ncols.upload(pl.ncols, s);
+    h->d_entries.upload(pl.entries, s);
+    h->d_gather_ptr.upload(pl.gather_ptr, s);
+    h->d_gather_ids.upload(pl.gather_ids, s);
+    h->d_pleaf_box.upload(pl.pleaf_box, s);
+    h->d_prow_ptr.upload(pl.prow_ptr, s);
+    h->d_prow_dof.upload(pl.prow_dof, s);
+    h->d_pcontrib_ptr.upload(pl.pcontrib_ptr, s);
+    h->d_pcontrib_q.upload(pl.pcontrib_q, s);
+    h->d_lleaf_box.upload(pl.lleaf_box, s);
+    h->d_m2l_tgt.upload(pl.m2l_tgt, s);
+    h->d_m2l_src_ptr.upload(pl.m2l_src_ptr, s);
+    h->d_m2l_src.upload(pl.m2l_src, s);
+    h->d_m2l_off.upload(pl.m2l_off, s);
+    h->d_m2p_tgt.upload(pl.m2p_tgt, s);
+    h->d_m2p_src_ptr.upload(pl.m2p_src_ptr, s);
+    h->d_m2p_src.upload(pl.m2p_src, s);
+    h->d_l2l_box.upload(pl.l2l_box, s);
+    // diagonal column of every row inside its leaf (block-Jacobi)
+    {
+      std::vector<int32_t> dc(pl.nrows.size());
+      for (size_t k = 0; k + 1 < pl.nrow_ptr.size(); ++k)
+        for (int64_t r = pl.nrow_ptr[k]; r < pl.nrow_ptr[k + 1]; ++r)
+          {
+            auto b = pl.ncols.begin() + pl.ncol_ptr[k], e = pl.ncols.begin() + pl.ncol_ptr[k + 1];
+            auto it = std::lower_bound(b, e, pl.nrows[r]);
+            if (it == e || *it != pl.nrows[r])
+              throw Error(PIBEM_EINVAL, "collocation node missing from its own near field");
+            dc[r] = int32_t(it - b);
+          }
+      h->d_diag_col.upload(dc, s);
+    }
+    // near-field integrals
+    {
+      const int            nl = int(pl.nleaf_box.size());
+      std::vector<int64_t> item_ptr(nl + 1, 0);
+      for (int k = 0; k < nl; ++k)
+        item_ptr[k + 1] = item_ptr[k] + (pl.nrow_ptr[k + 1] - pl.nrow_ptr[k]) *
+                                          (pl.nent_ptr[k + 1] - pl.nent_ptr[k]);
+      h->d_item_ptr.upload(item_ptr, s);
+      const int64_t nval = pl.nval_ptr[nl];
+      h->d_N.alloc(nval);
+      h->d_D.alloc(nval);
+      DBuf<double> staging;
+      int64_t      st_items = std::min<int64_t>(item_ptr[nl], int64_t(1) << 24);
+      int64_t      maxrow   = 0;
+      for (int k = 0; k < nl; ++k)
+        maxrow = std::max<int64_t>(maxrow, pl.nent_ptr[k + 1] - pl.nent_ptr[k]);
+      st_items = std::max(st_items, maxrow);
+      staging.alloc(8 * std::max<int64_t>(st_items, 1));
+      NearAssemblyArgs a;
+      a.n_items       = item_ptr[nl];
+      a.n_leaves      = nl;
+      a.item_ptr      = h->d_item_ptr.p;
+      a.row_ptr       = h->d_nrow_ptr.p;
+      a.ent_ptr       = h->d_nent_ptr.p;
+      a.val_ptr       = h->d_nval_ptr.p;
+      a.col_ptr       = h->d_ncol_ptr.p;
+      a.h_item_ptr    = item_ptr.data();
+      a.h_ent_ptr     = pl.nent_ptr.data();
+      a.h_val_ptr     = pl.nval_ptr.data();
+      a.rows          = h->d_nrows.p;
+      a.ents          = h->d_entries.p;
+      a.xyz           = h->d_xyz.p;
+      a.cells         = h->d_cells.p;
+      a.dbl_off       = h->d_dbl_off.p;
+      a.dbl_ids       = h->d_dbl_ids.p;
+      a.nq            = h->nq;
+      a.qpts          = h->d_qpts.p;
+      a.qnrm          = h->d_qnrm.p;
+      a.qjxw          = h->d_qjxw.p;
+      a.qshape        = h->d_qshape.p;
+      a.gather_ptr    = h->d_gather_ptr.p;
+      a.gather_ids    = h->d_gather_ids.p;
+      a.staging       = staging.p;
+      a.staging_items = st_items;
+      a.Nval          = h->d_N.p;
+      a.Dval          = h->d_D.p;
+      if (nl > 0)
+        launch_near_assembly(a, s);
+      PIBEM_CUDA(cudaStreamSynchronize(s));
+      h->d_S.alloc(nval);
+      h->d_S32.alloc(nval);
+    }
+    // P2M and L2P tables
+    {
+      const int64_t nrows_p = int64_t(pl.prow_dof.size());
+      h->d_T1.alloc(nrows_p * K);
+      h->d_T2.alloc(nrows_p * K);
+      launch_p2m_tables(nrows_p, K, pl.p, int(pl.pleaf_box.size()), h->d_prow_ptr.p,
+                        h->d_pleaf_box.p, h->d_pcontrib_ptr.p, h->d_pcontrib_q.p, h->d_center.p,
+                        h->d_delta.p, h->d_qpts.p, h->d_qnrm.p, h->d_qjxw.p, h->d_qshape.p,
+                        h->d_T1.p, h->d_T2.p, s);
+      h->d_T1f.alloc(nrows_p * K);
+      h->d_T2f.alloc(nrows_p * K);
+      launch_convert_d2f(nrows_p * K, h->d_T1.p, h->d_T1f.p, s);
+      launch_convert_d2f(nrows_p * K, h->d_T2.p, h->d_T2f.p, s);
+      const int64_t npos = int64_t(pl.lnode_ids.size());
+      h->d_W.alloc(npos * K);
+      launch_l2p_tables(npos, K, int(pl.lleaf_box.size()), h->d_nrow_ptr.p, h->d_lleaf_box.p,
+                        h->d_nrows.p, h->d_xyz.p, h->d_center.p, h->d_delta.p, h->d_W.p, s);
+      h->d_Wf.alloc(npos * K);
+      launch_convert_d2f(npos * K, h->d_W.p, h->d_Wf.p, s);
+    }
+    // translation operators
+    {
+      std::vector<double> m2m, l2l, m2l;
+      build_m2m_ops(pl.p, m2m);
+      build_l2l_ops(pl.p, l2l);
+      const int nof = int(pl.offsets.size() / 3);
+      m2l.assign(size_t(std::max(nof, 1)) * K * K, 0.0);
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int o = 0; o < nof; ++o)
+        build_m2l_op(pl.p, pl.offsets[3 * o], pl.offsets[3 * o + 1], pl.offsets[3 * o + 2],
+                     &m2l[size_t(o) * K * K]);
+      std::vector<double> td;
+      std::vector<float>  tf;
+      transpose_ops(m2m, 8, K, td);
+      h->d_m2m.upload(td, s);
+      transpose_ops(m2m, 8, K, tf);
+      h->d_m2mf.upload(tf, s);
+      transpose_ops(l2l, 8, K, td);
+      h->d_l2l.upload(td, s);
+      transpose_ops(l2l, 8, K, tf);
+      h->d_l2lf.upload(tf, s);
+      transpose_ops(m2l, std::max(nof, 1), K, td);
+      h->d_m2l.upload(td, s);
+      transpose_ops(m2l, std::max(nof, 1), K, tf);
+      h->d_m2lf.upload(tf, s);
+      PIBEM_CUDA(cudaStreamSynchronize(s));
+    }
+    fill_operator_views(h);
+    // free setup-only buffers
+    h->d_entries.release();
+    h->d_gather_ptr.release();
+    h->d_gather_ids.release();
+    h->d_item_ptr.release();
+    h->d_pcontrib_ptr.release();
+    h->d_pcontrib_q.release();
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    h->bytes_resident = h->d_N.bytes() * 3 + h->d_S32.bytes() + h->d_T1.bytes() * 2 +
+                        h->d_T1f.bytes() * 2 + h->d_W.bytes() + h->d_Wf.bytes() +
+                        h->d_m2l.bytes() + h->d_m2lf.bytes() + h->d_qpts.bytes() * 2 +
+                        h->d_qshape.bytes() + h->d_qjxw.bytes();
+    if (P.hbm_budget_gb > 0 && double(h->bytes_resident) > P.hbm_budget_gb * 1e9)
+      throw Error(PIBEM_ENOMEM_HBM, "resident operator exceeds the HBM budget");
+    h->mesh_ok       = true;
+    h->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  void set_bc_impl(pibem_handle *h, const uint8_t *mask)
+  {
+    if (!h->mesh_ok)
+      throw Error(PIBEM_EINVAL, "pibem_set_bc before pibem_set_mesh");
+    if (!mask)
+      throw Error(PIBEM_EINVAL, "null mask");
+    const int64_t N = h->N();
+    cudaStream_t  s = h->stream;
+    h->dir.assign(mask, mask + N);
+    h->have_dirichlet = false;
+    for (auto &v : h->dir)
+      {
+        v = v ? 1 : 0;
+        h->have_dirichlet |= v != 0;
+      }
+    h->d_dir.upload(h->dir, s);
+    // alpha = -N 1 (interior), -1 - N 1 (exterior)
+    h->d_alpha.alloc(N);
+    h->d_t1.alloc(N);
+    std::vector<double> ones(N, -1.0);
+    h->d_t1.upload(ones, s);
+    ker1_apply64(h, h->d_t1.p, h->d_alpha.p);
+    if (h->prm.is_external_flow)
+      {
+        std::vector<double> m1(N, 1.0);
+        h->d_t2.upload(m1, s);
+        launch_axpby(N, -1.0, h->d_t2.p, 1.0, h->d_alpha.p, s);
+      }
+    const Plan &pl = h->plan;
+    launch_build_system_matrix(pl.nval_ptr.back(), int(pl.nleaf_box.size()), h->d_nval_ptr.p,
+                               h->d_ncol_ptr.p, h->d_nrow_ptr.p, h->d_nrows.p, h->d_ncols.p,
+                               h->d_dir.p, h->d_alpha.p, h->d_N.p, h->d_D.p, h->d_S.p, h->d_S32.p,
+                               s);
+    if (h->prm.preconditioner)
+      build_preconditioner(h);
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    h->bc_ok = true;
+  }
+
+  void compute_rhs_dev(pibem_handle *h, int R, const double *tmp, double *rhs)
+  {
+    const int64_t N = h->N();
+    cudaStream_t  s = h->stream;
+    h->d_t1.alloc(size_t(R) * N);
+    h->d_t2.alloc(size_t(R) * N);
+    h->d_t3.alloc(size_t(2 * R) * N);
+    launch_split_masks(N, R, tmp, h->d_dir.p, h->d_t1.p, h->d_t2.p, s);
+    fmm_apply64(h, R, h->d_t1.p, h->d_t2.p, h->d_t3.p, h->d_t3.p + int64_t(R) * N);
+    launch_rhs_combine(N, R, tmp, h->d_dir.p, h->d_alpha.p, h->d_t3.p, h->d_t3.p + int64_t(R) * N,
+                       rhs, s);
+  }
+
+  void solve_dev(pibem_handle *h, int R, double *phi, double *dphi, const double *tmp,
+                 pibem_solve_stats *st)
+  {
+    if (!h->bc_ok)
+      throw Error(PIBEM_EINVAL, "pibem_solve before pibem_set_bc");
+    auto          t0 = std::chrono::steady_clock::now();
+    const int64_t N  = h->N();
+    cudaStream_t  s  = h->stream;
+    h->cnt64 = h->cnt32 = 0;
+    DBuf<double> b, x, r, d;
+    b.alloc(size_t(R) * N);
+    x.alloc(size_t(R) * N);
+    compute_rhs_dev(h, R, tmp, b.p);
+    PIBEM_CUDA(cudaMemcpyAsync(x.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+    const pibem_params &P    = h->prm;
+    const bool          prec = P.preconditioner != 0;
+    auto A64 = [h, R](const double *in, double *out) { system_apply64(h, R, in, out); };
+    auto A32 = [h, R](const double *in, double *out) { system_apply32(h, R, in, out); };
+    int                 iters = 0, refine = 0;
+    std::vector<double> rel;
+    if (P.precision_mode == PIBEM_PRECISION_FP64)
+      {
+        GmresResult gr = gmres(h, R, b.p, x.p, P.solver_tolerance, P.solver_max_steps,
+                               P.gmres_restart, A64, prec);
+        iters          = gr.iterations;
+        rel            = gr.rel;
+      }
+    else
+      {
+        // FP64 iterative refinement around an FP32-operator GMRES
+        r.alloc(size_t(R) * N);
+        d.alloc(size_t(R) * N);
+        DBuf<double> w;
+        w.alloc(size_t(R) * N);
+        const int max_refine = 12;
+        rel.assign(R, 1.0);
+        std::vector<double> bn(R), rn(R);
+        DBuf<double>        part, nrm;
+        part.alloc(size_t(R) * 64);
+        nrm.alloc(R);
+        for (int c = 0; c < R; ++c)
+          launch_dots(N, 1, 1, N, N, b.p + c * N, b.p + c * N, part.p, 64, nrm.p + c, s);
+        nrm.download(bn.data(), R, s);
+        PIBEM_CUDA(cudaStreamSynchronize(s));
+        for (auto &v : bn)
+          v = v > 0 ? std::sqrt(v) : 1.0;
+        for (; refine <= max_refine; ++refine)
+          {
+            A64(x.p, w.p);
+            PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+            launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
+            for (int c = 0; c < R; ++c)
+              launch_dots(N, 1, 1, N, N, r.p + c * N, r.p + c * N, part.p, 64, nrm.p + c, s);
+            nrm.download(rn.data(), R, s);
+            PIBEM_CUDA(cudaStreamSynchronize(s));
+            bool ok = true;
+            for (int c = 0; c < R; ++c)
+              {
+                rel[c] = std::sqrt(rn[c]) / bn[c];
+                ok     = ok && rel[c] <= P.solver_tolerance;
+              }
+            if (ok || refine == max_refine || iters >= P.solver_max_steps)
+              break;
+            // inner tolerance relative to this residual, never tighter than needed
+            double worst = *std::max_element(rel.begin(), rel.end());
+            double itol  = std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / worst);
+            PIBEM_CUDA(cudaMemsetAsync(d.p, 0, sizeof(double) * R * N, s));
+            GmresResult gr = gmres(h, R, r.p, d.p, itol, P.solver_max_steps - iters,
+                                   P.gmres_restart, A32, prec);
+            iters += gr.iterations;
+            launch_axpby(int64_t(R) * N, 1.0, d.p, 1.0, x.p, s);
+          }
+      }
+    launch_scatter(N, R, x.p, h->d_dir.p, phi, dphi, s);
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    double worst = rel.empty() ? 0 : *std::max_element(rel.begin(), rel.end());
+    if (st)
+      {
+        st->iterations        = iters;
+        st->refinement_steps  = refine;
+        st->fp64_matvecs      = h->cnt64;
+        st->fp32_matvecs      = h->cnt32;
+        st->relative_residual = worst;
+        st->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      }
+    if (!(worst <= P.solver_tolerance))
+      throw Error(PIBEM_ENOCONV, "GMRES did not reach the tolerance (relative residual " +
+                                   std::to_string(worst) + ")");
+  }
+
+  // host <-> device staging helpers for the host-pointer entry points
+  struct HostIO
+  {
+    pibem_handle *h;
+    std::vector<DBuf<double> *> bufs;
+    double *in(const double *hp, size_t n)
+    {
+      auto *b = new DBuf<double>();
+      b->upload(hp, n, h->stream);
+      bufs.push_back(b);
+      return b->p;
+    }
+    double *scratch(size_t n)
+    {
+      auto *b = new DBuf<double>();
+      b->alloc(n);
+      bufs.push_back(b);
+      return b->p;
+    }
+    ~HostIO()
+    {
+      for (auto *b : bufs)
+        delete b;
+    }
+  };
+} // namespace
+
+extern "C"
+{
+  int pibem_create(const pibem_params *params, pibem_handle **out)
+  {
+    if (!params || !out)
+      return PIBEM_EINVAL;
+    *out = nullptr;
+    const pibem_params &P = *params;
+    if (P.fma_truncation_order < 1 || P.fma_truncation_order > 10 || P.num_octree_levels < 1 ||
+        P.num_octree_levels > 20 || P.max_nodes_per_childless_block < 1 ||
+        P.quadrature_order < 1 || P.quadrature_order > 8 || P.singular_quadrature_order < 1 ||
+        P.singular_quadrature_order > 12 || P.gmres_restart < 1 || P.solver_max_steps < 1 ||
+        !(P.solver_tolerance > 0))
+      return PIBEM_EINVAL;
+    pibem_handle *h = new (std::nothrow) pibem_handle();
+    if (!h)
+      return PIBEM_ENOMEM_HBM;
+    h->prm = P;
+    try
+      {
+        PIBEM_CUDA(cudaSetDevice(P.device));
+        PIBEM_CUDA(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
+        h->stream = h->own;
+        const char *env = std::getenv("PIBEM_PHASE_TIMING");
+        h->timing       = env && env[0] == '1';
+        for (auto &e : h->ev)
+          PIBEM_CUDA(cudaEventCreate(&e));
+      }
+    catch (const Error &e)
+      {
+        int c = e.code;
+        delete h;
+        return c;
+      }
+    *out = h;
+    return PIBEM_OK;
+  }
+
+  int pibem_destroy(pibem_handle *h)
+  {
+    if (!h)
+      return PIBEM_EINVAL;
+    cudaSetDevice(h->prm.device);
+    if (h->stream)
+      cudaStreamSynchronize(h->stream);
+    for (auto &e : h->ev)
+      if (e)
+        cudaEventDestroy(e);
+    cudaStream_t own = h->own;
+    delete h;
+    if (own)
+      cudaStreamDestroy(own);
+    return PIBEM_OK;
+  }
+
+  const char *pibem_last_error(const pibem_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+  int pibem_set_stream(pibem_handle *h, void *stream)
+  {
+    return guarded(h, [&] { h->stream = stream ? (cudaStream_t)stream : h->own; });
+  }
+
+  int pibem_set_mesh(pibem_handle *h, int64_t n_nodes, const double *xyz, int64_t n_cells,
+                     const int32_t *cell_nodes, const int32_t *doff, const int32_t *dids)
+  {
+    return guarded(h, [&] { set_mesh_impl(h, n_nodes, xyz, n_cells, cell_nodes, doff, dids); });
+  }
+
+  int pibem_set_bc(pibem_handle *h, const uint8_t *mask)
+  {
+    return guarded(h, [&] { set_bc_impl(h, mask); });
+  }
+
+  int pibem_fmm_matvec(pibem_handle *h, int32_t R, const double *phi, const double *dphi,
+                       double *oN, double *oD)
+  {
+    return guarded(h, [&] {
+      if (!h->mesh_ok)
+        throw Error(PIBEM_EINVAL, "pibem_fmm_matvec before pibem_set_mesh");
+      if (R < 1 || !phi || !dphi || !oN || !oD)
+        throw Error(PIBEM_EINVAL, "bad arguments");
+      const size_t n = size_t(R) * h->N();
+      HostIO       io{h, {}};
+      double      *dp = io.in(phi, n), *dd = io.in(dphi, n);
+      double      *on = io.scratch(n), *od = io.scratch(n);
+      if (h->d_dir.n == 0)
+        {
+          std::vector<uint8_t> z(h->N(), 0);
+          h->d_dir.upload(z, h->stream);
+        }
+      fmm_apply64(h, R, dp, dd, on, od);
+      finish_timing(h);
+      PIBEM_CUDA(cudaMemcpyAsync(oN, on, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      PIBEM_CUDA(cudaMemcpyAsync(oD, od, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_compute_alpha(pibem_handle *h, double *alpha)
+  {
+    return guarded(h, [&] {
+      if (!h->bc_ok)
+        throw Error(PIBEM_EINVAL, "pibem_compute_alpha before pibem_set_bc");
+      h->d_alpha.download(alpha, h->N(), h->stream);
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_system_matvec(pibem_handle *h, int32_t R, const double *x, double *y)
+  {
+    return guarded(h, [&] {
+      if (!h->bc_ok)
+        throw Error(PIBEM_EINVAL, "pibem_system_matvec before pibem_set_bc");
+      if (R < 1 || !x || !y)
+        throw Error(PIBEM_EINVAL, "bad arguments");
+      const size_t n  = size_t(R) * h->N();
+      HostIO       io{h, {}};
+      double      *dx = io.in(x, n), *dy = io.scratch(n);
+      if (h->prm.precision_mode == PIBEM_PRECISION_MIXED && std::getenv("PIBEM_MATVEC_FP32"))
+        system_apply32(h, R, dx, dy);
+      else
+        system_apply64(h, R, dx, dy);
+      finish_timing(h);
+      PIBEM_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_compute_rhs(pibem_handle *h, int32_t R, const double *tmp, double *rhs)
+  {
+    return guarded(h, [&] {
+      if (!h->bc_ok)
+        throw Error(PIBEM_EINVAL, "pibem_compute_rhs before pibem_set_bc");
+      const size_t n  = size_t(R) * h->N();
+      HostIO       io{h, {}};
+      double      *dt = io.in(tmp, n), *db = io.scratch(n);
+      compute_rhs_dev(h, R, dt, db);
+      PIBEM_CUDA(cudaMemcpyAsync(rhs, db, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_solve(pibem_handle *h, int32_t R, double *phi, double *dphi, const double *tmp,
+                  pibem_solve_stats *st)
+  {
+    int rc = guarded(h, [&] {
+      if (R < 1 || !phi || !dphi || !tmp)
+        throw Error(PIBEM_EINVAL, "bad arguments");
+      const size_t n  = size_t(R) * h->N();
+      HostIO       io{h, {}};
+      double      *dp = io.in(phi, n), *dd = io.in(dphi, n), *dt = io.in(tmp, n);
+      int          code = PIBEM_OK;
+      std::string  msg;
+      try
+        {
+          solve_dev(h, R, dp, dd, dt, st);
+        }
+      catch (const Error &e)
+        {
+          if (e.code != PIBEM_ENOCONV)
+            throw;
+          code = e.code;
+          msg  = e.what();
+        }
+      PIBEM_CUDA(cudaMemcpyAsync(phi, dp, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      PIBEM_CUDA(cudaMemcpyAsync(dphi, dd, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+      if (code != PIBEM_OK)
+        throw Error(code, msg);
+    });
+    return rc;
+  }
+
+  int pibem_solve_device(pibem_handle *h, int32_t R, double *phi, double *dphi, const double *tmp,
+                         pibem_solve_stats *st)
+  {
+    return guarded(h, [&] {
+      if (R < 1 || !phi || !dphi || !tmp)
+        throw Error(PIBEM_EINVAL, "bad arguments");
+      solve_dev(h, R, phi, dphi, tmp, st);
+    });
+  }
+
+  int pibem_tree_info_get(pibem_handle *h, pibem_tree_info *info)
+  {
+    return guarded(h, [&] {
+      if (!h->mesh_ok || !info)
+        throw Error(PIBEM_EINVAL, "no mesh");
+      info->n_boxes       = h->tree.nb;
+      info->n_levels      = h->tree.L;
+      info->n_leaves      = int(h->tree.childless.size());
+      info->n_m2l_pairs   = h->plan.n_m2l;
+      info->n_m2p_pairs   = h->plan.n_m2p;
+      info->near_nnz      = h->plan.nval_ptr.back();
+      info->p2m_rows      = int64_t(h->plan.prow_dof.size());
+      info->n_quad_points = h->mesh.n_cells * h->nq;
+      info->n_m2l_offsets = int(h->plan.offsets.size() / 3);
+      info->setup_seconds = h->setup_seconds;
+    });
+  }
+
+  int pibem_tree_boxes(pibem_handle *h, int32_t *level, int32_t *parent, int32_t *nchild,
+                       double *pmin, double *delta, int32_t *n_nodes, int32_t *n_quads)
+  {
+    return guarded(h, [&] {
+      if (!h->mesh_ok)
+        throw Error(PIBEM_EINVAL, "no mesh");
+      const Tree &t = h->tree;
+      for (int b = 0; b < t.nb; ++b)
+        {
+          level[b]  = t.level[b];
+          parent[b] = t.parent[b];
+          nchild[b] = t.nchild[b];
+          for (int k = 0; k < 3; ++k)
+            pmin[3 * b + k] = t.pmin[3 * b + k];
+          delta[b]   = t.delta[b];
+          n_nodes[b] = t.nend[b] - t.nbeg[b];
+          n_quads[b] = t.qend[b] - t.qbeg[b];
+        }
+    });
+  }
+
+  int pibem_tree_list_sublevels(pibem_handle *h, int32_t box)
+  {
+    if (!h || !h->mesh_ok || box < 0 || box >= h->tree.nb)
+      return -1;
+    return int(h->tree.nn[box].size());
+  }
+
+  int pibem_tree_list(pibem_handle *h, int32_t kind, int32_t box, int32_t sub, int32_t *out,
+                      int32_t cap)
+  {
+    if (!h || !h->mesh_ok || box < 0 || box >= h->tree.nb || kind < 0 || kind > 2)
+      return -1;
+    const auto &L = kind == 0 ? h->tree.nn[box] : (kind == 1 ? h->tree.il[box] : h->tree.nil[box]);
+    if (sub < 0 || sub >= int(L.size()))
+      return -1;
+    const auto &v = L[sub];
+    for (int i = 0; i < int(v.size()) && i < cap; ++i)
+      out[i] = v[i];
+    return int(v.size());
+  }
+
+  int64_t pibem_near_nnz(pibem_handle *h)
+  {
+    if (!h || !h->mesh_ok)
+      return -1;
+    // distinct (row, col) pairs = sum of leaf block sizes
+    return h->plan.nval_ptr.back();
+  }
+
+  int pibem_near_export(pibem_handle *h, int32_t *rows, int32_t *cols, double *Nout, double *Dout)
+  {
+    return guarded(h, [&] {
+      if (!h->mesh_ok)
+        throw Error(PIBEM_EINVAL, "no mesh");
+      const Plan         &pl = h->plan;
+      const int64_t       nv = pl.nval_ptr.back();
+      std::vector<double> Nv(nv), Dv(nv);
+      h->d_N.download(Nv.data(), nv, h->stream);
+      h->d_D.download(Dv.data(), nv, h->stream);
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+      // rows sorted globally: collect (row, col, idx) and sort
+      std::vector<std::pair<std::pair<int, int>, int64_t>> all;
+      all.reserve(nv);
+      for (size_t k = 0; k + 1 < pl.nrow_ptr.size(); ++k)
+        {
+          int64_t nc = pl.ncol_ptr[k + 1] - pl.ncol_ptr[k];
+          for (int64_t r = pl.nrow_ptr[k]; r < pl.nrow_ptr[k + 1]; ++r)
+            for (int64_t c = 0; c < nc; ++c)
+              all.push_back({{pl.nrows[r], pl.ncols[pl.ncol_ptr[k] + c]},
+                             pl.nval_ptr[k] + (r - pl.nrow_ptr[k]) * nc + c});
+        }
+      std::sort(all.begin(), all.end());
+      for (int64_t i = 0; i < nv; ++i)
+        {
+          rows[i] = all[i].first.first;
+          cols[i] = all[i].first.second;
+          Nout[i] = Nv[all[i].second];
+          Dout[i] = Dv[all[i].second];
+        }
+    });
+  }
+
+  int pibem_quad_points(pibem_handle *h, double *pts)
+  {
+    return guarded(h, [&] {
+      if (!h->mesh_ok)
+        throw Error(PIBEM_EINVAL, "no mesh");
+      h->d_qpts.download(pts, h->d_qpts.n, h->stream);
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_last_phase_ms(pibem_handle *h, double *ms7)
+  {
+    if (!h || !ms7)
+      return PIBEM_EINVAL;
+    for (int i = 0; i < 7; ++i)
+      ms7[i] = h->phase_ms[i];
+    return PIBEM_OK;
+  }
+}

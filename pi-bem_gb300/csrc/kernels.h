@@ -1,0 +1,130 @@
+// Launch interfaces of the device kernels (setup.cu, fmm.cu, krylov.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "pibem_internal.h"
+
+namespace pibem
+{
+  // ---- setup (FP64) -------------------------------------------------------
+  struct NearAssemblyArgs
+  {
+    int64_t          n_items = 0; // sum over leaves of rows * entries
+    int              n_leaves = 0;
+    const int64_t   *item_ptr = nullptr, *row_ptr = nullptr, *ent_ptr = nullptr,
+                    *val_ptr = nullptr, *col_ptr = nullptr;
+    const int64_t   *h_item_ptr = nullptr, *h_ent_ptr = nullptr, *h_val_ptr = nullptr;
+    const int32_t   *rows = nullptr;
+    const NearEntry *ents = nullptr;
+    const double    *xyz = nullptr;
+    const int32_t   *cells = nullptr, *dbl_off = nullptr, *dbl_ids = nullptr;
+    int              nq = 0;
+    const double    *qpts = nullptr, *qnrm = nullptr, *qjxw = nullptr, *qshape = nullptr;
+    const int32_t   *gather_ptr = nullptr, *gather_ids = nullptr;
+    double          *staging = nullptr;
+    int64_t          staging_items = 0;
+    double          *Nval = nullptr, *Dval = nullptr;
+  };
+
+  void set_telles_rules(const std::vector<double> pts[4], const std::vector<double> w[4], int n,
+                        cudaStream_t s);
+  void launch_quad_data(int64_t n_cells, int nq, const double *xyz, const int32_t *cells,
+                        const double *gpts, const double *gw, double *qpts, double *qnrm,
+                        double *qjxw, double *qshape, cudaStream_t s);
+  void launch_near_assembly(const NearAssemblyArgs &a, cudaStream_t s);
+  void launch_p2m_tables(int64_t n_rows, int K, int p, int n_leaves, const int64_t *row_ptr,
+                         const int32_t *leaf_box, const int64_t *contrib_ptr,
+                         const int32_t *contrib_q, const double *box_center,
+                         const double *box_delta, const double *qpts, const double *qnrm,
+                         const double *qjxw, const double *qshape, double *T1, double *T2,
+                         cudaStream_t s);
+  void launch_l2p_tables(int64_t n_pos, int K, int n_leaves, const int64_t *pos_ptr,
+                         const int32_t *leaf_box, const int32_t *nodes, const double *xyz,
+                         const double *box_center, const double *box_delta, double *W,
+                         cudaStream_t s);
+
+  // ---- operator (T = double or float) -------------------------------------
+  // Column modes of the multipole pass.
+  enum : uint8_t
+  {
+    MODE_COMBINED = 0, // strengths (1-dir) Ker1 - dir Ker2 (system operator)
+    MODE_KER1     = 1, // double layer only (N)
+    MODE_KER2     = 2  // single layer only (D)
+  };
+
+  struct TreeDev
+  {
+    int            nb = 0, N = 0, L = 0;
+    const int32_t *parent = nullptr, *child_first = nullptr, *nchild = nullptr,
+                  *digit = nullptr, *nbeg = nullptr, *nend = nullptr, *node_sorted = nullptr;
+    const double  *center = nullptr, *delta = nullptr;
+    const double  *xyz = nullptr;
+  };
+
+  template <typename T>
+  struct OperatorDev
+  {
+    int p = 0, K = 0;
+    // near field (leaf blocks)
+    int            n_near_leaves = 0;
+    int64_t        n_rows = 0;
+    const int32_t *row_leaf = nullptr, *nrows = nullptr, *ncols = nullptr;
+    const int64_t *nrow_ptr = nullptr, *ncol_ptr = nullptr, *nval_ptr = nullptr;
+    // p2m
+    int            n_p2m_leaves = 0;
+    const int64_t *prow_ptr = nullptr;
+    const int32_t *pleaf_box = nullptr, *prow_dof = nullptr;
+    const T       *T1 = nullptr, *T2 = nullptr;
+    // l2p (same row positions as the near field)
+    const int32_t *lleaf_box = nullptr;
+    const T       *W = nullptr;
+    // translations (transposed: [op][in][out])
+    const T       *m2m_ops = nullptr, *l2l_ops = nullptr, *m2l_ops = nullptr;
+    // M2L per target CSR
+    const int32_t *m2l_tgt = nullptr, *m2l_src = nullptr, *m2l_off = nullptr;
+    const int64_t *m2l_src_ptr = nullptr;
+    // M2P per target CSR
+    int            n_m2p_tgt = 0;
+    const int32_t *m2p_tgt = nullptr, *m2p_src = nullptr;
+    const int64_t *m2p_src_ptr = nullptr;
+    // L2L boxes
+    const int32_t *l2l_box = nullptr;
+    // per-level ranges (host)
+    std::vector<int> m2l_level_ptr, l2l_level_ptr, parents_level_ptr;
+    const int32_t   *parents = nullptr; // boxes with children, grouped by level of the box
+  };
+
+  template <typename T>
+  void launch_near_spmv(const OperatorDev<T> &op, int R, int N, const T *vals, const T *x, T *y,
+                        bool accumulate, cudaStream_t s);
+  template <typename T>
+  void launch_p2m_apply(const OperatorDev<T> &op, int R, int N, const uint8_t *dir,
+                        const uint8_t *modes, const T *x, T *M, cudaStream_t s);
+  template <typename T>
+  void launch_m2m_level(const OperatorDev<T> &op, const TreeDev &td, int R, int parent_level, T *M,
+                        cudaStream_t s);
+  template <typename T>
+  void launch_l2l_level(const OperatorDev<T> &op, const TreeDev &td, int R, int level, T *Lx,
+                        cudaStream_t s);
+  template <typename T>
+  void launch_m2l_level(const OperatorDev<T> &op, int R, int level, const T *M, T *Lx,
+                        cudaStream_t s);
+  template <typename T>
+  void launch_m2p(const OperatorDev<T> &op, const TreeDev &td, int R, int N, const T *M, T *y,
+                  cudaStream_t s);
+  template <typename T>
+  void launch_l2p(const OperatorDev<T> &op, int R, int N, const T *Lx, T *y, cudaStream_t s);
+
+  // ---- vector kernels (krylov.cu) -------------------------------------------
+  void launch_convert_d2f(int64_t n, const double *a, float *b, cudaStream_t s);
+  void launch_convert_f2d(int64_t n, const float *a, double *b, cudaStream_t s);
+  void launch_build_system_matrix(int64_t n_vals, int n_leaves, const int64_t *val_ptr,
+                                  const int64_t *col_ptr, const int64_t *row_ptr,
+                                  const int32_t *rows, const int32_t *cols, const uint8_t *dir,
+                                  const double *alpha, const double *Nval, const double *Dval,
+                                  double *S, float *S32, cudaStream_t s);
+} // namespace pibem

@@ -1,0 +1,329 @@
+// Vector kernels of the device-resident GMRES (FP64 Arnoldi with classical
+// Gram-Schmidt applied twice) and of the BEMProblem wrappers (masks, rhs,
+// system matrix).  Reductions are two-stage with a fixed order, so results do
+// not depend on scheduling.
+#include "krylov.h"
+
+namespace pibem
+{
+  namespace
+  {
+    constexpr int kDotBlock = 256;
+
+    // partial[(r * nblk + blk) * ncols + i] = sum over the block's rows of V[r][i][t] w[r][t]
+    __global__ void dots_partial_kernel(int64_t n, int ncols, int64_t ldv, int64_t ldr,
+                                        const double *__restrict__ V,
+                                        const double *__restrict__ w, int nblk,
+                                        double *__restrict__ partial)
+    {
+      __shared__ double red[kDotBlock / 32];
+      const int     r   = blockIdx.y;
+      const int     blk = blockIdx.x;
+      const double *Vr  = V + int64_t(r) * ldr;
+      const double *wr  = w + int64_t(r) * n;
+      const int64_t chunk = (n + nblk - 1) / nblk;
+      const int64_t t0 = int64_t(blk) * chunk, t1 = min(n, t0 + chunk);
+      for (int i = 0; i < ncols; ++i)
+        {
+          double s = 0;
+          for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x)
+            s += Vr[int64_t(i) * ldv + t] * wr[t];
+          for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+          if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = s;
+          __syncthreads();
+          if (threadIdx.x == 0)
+            {
+              double tot = 0;
+              for (int k = 0; k < int(blockDim.x >> 5); ++k)
+                tot += red[k];
+              partial[(int64_t(r) * nblk + blk) * ncols + i] = tot;
+            }
+          __syncthreads();
+        }
+    }
+
+    __global__ void dots_final_kernel(int R, int ncols, int nblk, const double *__restrict__ partial,
+                                      double *__restrict__ out)
+    {
+      int idx = blockIdx.x * blockDim.x + threadIdx.x;
+      if (idx >= R * ncols)
+        return;
+      int    r = idx / ncols, i = idx % ncols;
+      double s = 0;
+      for (int b = 0; b < nblk; ++b)
+        s += partial[(int64_t(r) * nblk + b) * ncols + i];
+      out[idx] = s;
+    }
+
+    // w[r][t] -= sum_i V[r][i][t] h[r][i]   (h on the device, layout [r][ldh])
+    __global__ void gemv_sub_kernel(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
+                                    const double *__restrict__ V, const double *__restrict__ h,
+                                    int ldh, double *__restrict__ w, double sign)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      int64_t r = idx / n, t = idx % n;
+      double  s = 0;
+      for (int i = 0; i < ncols; ++i)
+        s += V[r * ldr + int64_t(i) * ldv + t] * h[r * ldh + i];
+      w[idx] -= sign * s;
+    }
+
+    // V[r][j+1] = w[r] / hn[r]  (hn > 0), else 0
+    __global__ void normalize_kernel(int64_t n, int R, const double *__restrict__ w,
+                                     const double *__restrict__ nrm, double *__restrict__ out,
+                                     int64_t ldr)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      int64_t r = idx / n, t = idx % n;
+      double  h = sqrt(nrm[r]);
+      out[r * ldr + t] = h > 0 ? w[idx] / h : 0.0;
+    }
+
+    __global__ void axpby_kernel(int64_t n, double a, const double *__restrict__ x, double b,
+                                 double *__restrict__ y)
+    {
+      int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i < n)
+        y[i] = a * x[i] + b * y[i];
+    }
+
+    __global__ void d2f_kernel(int64_t n, const double *__restrict__ a, float *__restrict__ b)
+    {
+      int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i < n)
+        b[i] = float(a[i]);
+    }
+    __global__ void f2d_kernel(int64_t n, const float *__restrict__ a, double *__restrict__ b)
+    {
+      int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i < n)
+        b[i] = double(a[i]);
+    }
+
+    // S = N where the column dof is Neumann, -D where Dirichlet, + alpha on the
+    // diagonal of Neumann rows (BEMProblem::vmult FMA branch, bem_problem.cc:1199-1209,
+    // as one matrix like BEMFMA's init_preconditioner, bem_fma.cc:952-962).
+    __global__ void system_matrix_kernel(int64_t n_vals, int n_leaves,
+                                         const int64_t *__restrict__ val_ptr,
+                                         const int64_t *__restrict__ col_ptr,
+                                         const int64_t *__restrict__ row_ptr,
+                                         const int32_t *__restrict__ rows,
+                                         const int32_t *__restrict__ cols,
+                                         const uint8_t *__restrict__ dir,
+                                         const double *__restrict__ alpha,
+                                         const double *__restrict__ Nv,
+                                         const double *__restrict__ Dv, double *__restrict__ S,
+                                         float *__restrict__ S32)
+    {
+      int64_t vi = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (vi >= n_vals)
+        return;
+      int lo = 0, hi = n_leaves - 1;
+      while (lo < hi)
+        {
+          int mid = (lo + hi + 1) >> 1;
+          if (val_ptr[mid] <= vi)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+      const int64_t nc  = col_ptr[lo + 1] - col_ptr[lo];
+      const int64_t loc = vi - val_ptr[lo];
+      const int     row = rows[row_ptr[lo] + loc / nc];
+      const int     col = cols[col_ptr[lo] + loc % nc];
+      double        v   = dir[col] ? -Dv[vi] : Nv[vi];
+      if (row == col && !dir[row])
+        v += alpha[row];
+      S[vi]   = v;
+      S32[vi] = float(v);
+    }
+
+    // rhs = -(outN + alpha*(tmp.dir)) + outD  (BEMProblem::compute_rhs, bem_problem.cc:1240-1258)
+    __global__ void rhs_combine_kernel(int64_t n, int R, const double *__restrict__ tmp,
+                                       const uint8_t *__restrict__ dir,
+                                       const double *__restrict__ alpha,
+                                       const double *__restrict__ oN, const double *__restrict__ oD,
+                                       double *__restrict__ rhs)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      int64_t t  = idx % n;
+      double  sp = dir[t] ? tmp[idx] : 0.0;
+      rhs[idx]   = -(oN[idx] + alpha[t] * sp) + oD[idx];
+    }
+
+    // split tmp_rhs into (tmp.dir, tmp.neu)
+    __global__ void split_masks_kernel(int64_t n, int R, const double *__restrict__ tmp,
+                                       const uint8_t *__restrict__ dir, double *__restrict__ a,
+                                       double *__restrict__ b)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      int64_t t = idx % n;
+      a[idx]    = dir[t] ? tmp[idx] : 0.0;
+      b[idx]    = dir[t] ? 0.0 : tmp[idx];
+    }
+
+    // scatter: phi(i) = sol(i) on Neumann nodes, dphi_dn(i) = sol(i) on Dirichlet nodes
+    __global__ void scatter_kernel(int64_t n, int R, const double *__restrict__ sol,
+                                   const uint8_t *__restrict__ dir, double *__restrict__ phi,
+                                   double *__restrict__ dphi)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      int64_t t = idx % n;
+      if (dir[t])
+        dphi[idx] = sol[idx];
+      else
+        phi[idx] = sol[idx];
+    }
+
+    __global__ void add_scalar_kernel(int64_t n, int R, const double *__restrict__ shift,
+                                      double *__restrict__ x)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      x[idx] += shift[idx / n];
+    }
+
+    // z[node] = sum_c Pinv[leaf][r][c] v[rows_c]  (leaf-block Jacobi, right preconditioner)
+    __global__ void block_apply_kernel(int64_t n_rows, int R, int64_t n,
+                                       const int32_t *__restrict__ row_leaf,
+                                       const int64_t *__restrict__ row_ptr,
+                                       const int64_t *__restrict__ blk_ptr,
+                                       const int32_t *__restrict__ rows,
+                                       const double *__restrict__ Pinv,
+                                       const double *__restrict__ v, double *__restrict__ z)
+    {
+      const int64_t row  = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+      const int     lane = threadIdx.x & 31;
+      if (row >= n_rows)
+        return;
+      const int     leaf = row_leaf[row];
+      const int64_t r0 = row_ptr[leaf], nr = row_ptr[leaf + 1] - r0;
+      const double *P    = Pinv + blk_ptr[leaf] + (row - r0) * nr;
+      const int     node = rows[row];
+      for (int rr = 0; rr < R; ++rr)
+        {
+          double s = 0;
+          for (int64_t c = lane; c < nr; c += 32)
+            s += P[c] * v[int64_t(rr) * n + rows[r0 + c]];
+          for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+          if (lane == 0)
+            z[int64_t(rr) * n + node] = s;
+        }
+    }
+
+    inline unsigned nblocks(int64_t n, int t = 256) { return unsigned((n + t - 1) / t); }
+  } // namespace
+
+  void launch_dots(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
+                   const double *w, double *partial, int nblk, double *out, cudaStream_t s)
+  {
+    dim3 grid(nblk, R);
+    dots_partial_kernel<<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, w, nblk, partial);
+    dots_final_kernel<<<nblocks(int64_t(R) * ncols, 128), 128, 0, s>>>(R, ncols, nblk, partial, out);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
+                       const double *h, int ldh, double *w, double sign, cudaStream_t s)
+  {
+    gemv_sub_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, ncols, ldv, ldr, V, h, ldh, w, sign);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
+                        int64_t ldr, cudaStream_t s)
+  {
+    normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s)
+  {
+    if (n == 0)
+      return;
+    axpby_kernel<<<nblocks(n), 256, 0, s>>>(n, a, x, b, y);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_convert_d2f(int64_t n, const double *a, float *b, cudaStream_t s)
+  {
+    if (n == 0)
+      return;
+    d2f_kernel<<<nblocks(n), 256, 0, s>>>(n, a, b);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+  void launch_convert_f2d(int64_t n, const float *a, double *b, cudaStream_t s)
+  {
+    if (n == 0)
+      return;
+    f2d_kernel<<<nblocks(n), 256, 0, s>>>(n, a, b);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_build_system_matrix(int64_t n_vals, int n_leaves, const int64_t *val_ptr,
+                                  const int64_t *col_ptr, const int64_t *row_ptr,
+                                  const int32_t *rows, const int32_t *cols, const uint8_t *dir,
+                                  const double *alpha, const double *Nval, const double *Dval,
+                                  double *S, float *S32, cudaStream_t s)
+  {
+    if (n_vals == 0)
+      return;
+    system_matrix_kernel<<<nblocks(n_vals), 256, 0, s>>>(n_vals, n_leaves, val_ptr, col_ptr,
+                                                         row_ptr, rows, cols, dir, alpha, Nval,
+                                                         Dval, S, S32);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_rhs_combine(int64_t n, int R, const double *tmp, const uint8_t *dir,
+                          const double *alpha, const double *oN, const double *oD, double *rhs,
+                          cudaStream_t s)
+  {
+    rhs_combine_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, tmp, dir, alpha, oN, oD, rhs);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_split_masks(int64_t n, int R, const double *tmp, const uint8_t *dir, double *a,
+                          double *b, cudaStream_t s)
+  {
+    split_masks_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, tmp, dir, a, b);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_scatter(int64_t n, int R, const double *sol, const uint8_t *dir, double *phi,
+                      double *dphi, cudaStream_t s)
+  {
+    scatter_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, sol, dir, phi, dphi);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_add_scalar(int64_t n, int R, const double *shift, double *x, cudaStream_t s)
+  {
+    add_scalar_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, shift, x);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_block_apply(int64_t n_rows, int R, int64_t n, const int32_t *row_leaf,
+                          const int64_t *row_ptr, const int64_t *blk_ptr, const int32_t *rows,
+                          const double *Pinv, const double *v, double *z, cudaStream_t s)
+  {
+    if (n_rows == 0)
+      return;
+    block_apply_kernel<<<nblocks(n_rows * 32), 256, 0, s>>>(n_rows, R, n, row_leaf, row_ptr,
+                                                            blk_ptr, rows, Pinv, v, z);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+} // namespace pibem

@@ -1,0 +1,26 @@
+// Launchers of the vector kernels (krylov.cu).
+#pragma once
+
+#include "kernels.h"
+
+namespace pibem
+{
+  void launch_dots(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
+                   const double *w, double *partial, int nblk, double *out, cudaStream_t s);
+  void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
+                       const double *h, int ldh, double *w, double sign, cudaStream_t s);
+  void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
+                        int64_t ldr, cudaStream_t s);
+  void launch_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s);
+  void launch_rhs_combine(int64_t n, int R, const double *tmp, const uint8_t *dir,
+                          const double *alpha, const double *oN, const double *oD, double *rhs,
+                          cudaStream_t s);
+  void launch_split_masks(int64_t n, int R, const double *tmp, const uint8_t *dir, double *a,
+                          double *b, cudaStream_t s);
+  void launch_scatter(int64_t n, int R, const double *sol, const uint8_t *dir, double *phi,
+                      double *dphi, cudaStream_t s);
+  void launch_add_scalar(int64_t n, int R, const double *shift, double *x, cudaStream_t s);
+  void launch_block_apply(int64_t n_rows, int R, int64_t n, const int32_t *row_leaf,
+                          const int64_t *row_ptr, const int64_t *blk_ptr, const int32_t *rows,
+                          const double *Pinv, const double *v, double *z, cudaStream_t s);
+} // namespace pibem

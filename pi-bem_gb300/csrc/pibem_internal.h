@@ -1,0 +1,183 @@
+// Internal declarations of the GB300 FMM-BEM library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pibem_gpu.h"
+
+namespace pibem
+{
+  // Error raised inside the library; converted to a status code at the ABI.
+  struct Error : std::runtime_error
+  {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+  };
+
+#define PIBEM_CUDA(call)                                                                       \
+  do                                                                                           \
+    {                                                                                          \
+      cudaError_t e_ = (call);                                                                 \
+      if (e_ != cudaSuccess)                                                                   \
+        throw ::pibem::Error(e_ == cudaErrorMemoryAllocation ? PIBEM_ENOMEM_HBM : PIBEM_ECUDA, \
+                             std::string(#call) + ": " + cudaGetErrorString(e_));              \
+    }                                                                                          \
+  while (0)
+
+  // Owning device buffer.
+  template <typename T>
+  struct DBuf
+  {
+    T     *p = nullptr;
+    size_t n = 0;
+    DBuf() {}
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void release()
+    {
+      if (p)
+        cudaFree(p);
+      p = nullptr;
+      n = 0;
+    }
+    // Grows only: a buffer keeps its capacity n once allocated.
+    void alloc(size_t count)
+    {
+      if (count <= n && p)
+        return;
+      release();
+      if (count == 0)
+        return;
+      PIBEM_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+      n = count;
+    }
+    void zero(cudaStream_t s)
+    {
+      if (n)
+        PIBEM_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    void upload(const T *h, size_t count, cudaStream_t s)
+    {
+      alloc(count);
+      if (count)
+        PIBEM_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void upload(const std::vector<T> &v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+    void download(T *h, size_t count, cudaStream_t s) const
+    {
+      if (count)
+        PIBEM_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    size_t bytes() const { return n * sizeof(T); }
+  };
+
+  // ---------------------------------------------------------------------
+  // Octree and interaction lists (host, built once per mesh).
+  // Box ids follow the reference's numbering: level by level, parents in
+  // order, children in the reference child order (bem_fma.cc:3811-3822).
+  // ---------------------------------------------------------------------
+  struct Tree
+  {
+    int                 L  = 0;
+    int                 nb = 0;
+    std::vector<int>    level, parent, nchild, child_first, digit;
+    std::vector<int>    ic;    // 3 per box: lattice coordinates at the box level
+    std::vector<double> pmin;  // 3 per box
+    std::vector<double> delta; // per box
+    std::vector<int>    nbeg, nend, qbeg, qend; // ranges in node_sorted / quad_sorted
+    std::vector<int>    node_sorted, quad_sorted;
+    std::vector<int>    startLevel, endLevel;
+    std::vector<int>    childless; // reference childlessList order
+    std::vector<char>   is_childless;
+    std::vector<std::vector<int>> dofs_filled; // per level: boxes with nodes
+    std::vector<int>    qbox; // (L+1) * Q: box of each quad point at each level (leaf if shallower)
+    // lists[box][sub] sorted unique
+    std::vector<std::vector<std::vector<int>>> nn, il, nil;
+    std::vector<int>    node_leaf; // childless box of each node
+
+    void center(int b, double c[3]) const
+    {
+      for (int k = 0; k < 3; ++k)
+        c[k] = pmin[3 * b + k] + delta[b] / 2.;
+    }
+  };
+
+  struct MeshHost
+  {
+    int64_t              n_nodes = 0, n_cells = 0;
+    std::vector<double>  xyz;
+    std::vector<int32_t> cells;
+    std::vector<int32_t> dbl_off, dbl_ids; // always filled (each set includes the node)
+    std::vector<int32_t> elem_off, elem_ids; // dof -> cells CSR
+  };
+
+  // Builds the octree and the near / interaction / non-interaction lists with
+  // the reference semantics (bem_fma.cc:3615-4801).
+  void build_tree(const MeshHost &mesh, const std::vector<double> &qpts, int nq, int levels,
+                  int max_nodes, Tree &t);
+
+  // ---------------------------------------------------------------------
+  // Operator structure derived from the lists.
+  // ---------------------------------------------------------------------
+  struct NearEntry
+  {
+    int32_t  cell;
+    int32_t  singular_ok; // 1: the intList part (Telles rule if singular)
+    uint64_t qmask;       // quadrature points of the cell taken into account
+    int32_t  lcol[4];     // local column of each cell dof in the leaf block
+  };
+
+  struct Plan
+  {
+    int p = 0, K = 0;
+    // near field, per leaf with nodes
+    std::vector<int32_t>  nleaf_box;          // box id
+    std::vector<int64_t>  nrow_ptr, ncol_ptr, nent_ptr, nval_ptr;
+    std::vector<int32_t>  nrows, ncols;       // node ids of rows / columns
+    std::vector<NearEntry> entries;
+    std::vector<int32_t>  gather_ptr, gather_ids; // per (leaf col): entry*4+j, offset by ncol_ptr
+    std::vector<int32_t>  row_leaf;           // leaf index of each row position
+    // P2M tables, per childless box with quad points
+    std::vector<int32_t>  pleaf_box;
+    std::vector<int64_t>  prow_ptr;
+    std::vector<int32_t>  prow_dof;
+    std::vector<int64_t>  pcontrib_ptr;
+    std::vector<int32_t>  pcontrib_q;         // quad point id * 4 + j
+    // L2P: per childless box with nodes, nodes listed
+    std::vector<int32_t>  lleaf_box;
+    std::vector<int64_t>  lnode_ptr;
+    std::vector<int32_t>  lnode_ids;
+    // M2M: per level (1..L) boxes of that level are children; parents contiguous
+    // M2L: per level pairs grouped by target
+    std::vector<int32_t>  m2l_tgt_ptr_level;  // per level: range into m2l_tgt
+    std::vector<int32_t>  m2l_tgt;            // target boxes
+    std::vector<int64_t>  m2l_src_ptr;        // per target
+    std::vector<int32_t>  m2l_src, m2l_off;   // source box, offset id
+    std::vector<int32_t>  offsets;            // distinct offsets, 3 per id
+    // M2P pairs grouped by target
+    std::vector<int32_t>  m2p_tgt;
+    std::vector<int64_t>  m2p_src_ptr;
+    std::vector<int32_t>  m2p_src;
+    // L2L per level: boxes with nodes at levels >= 2
+    std::vector<int32_t>  l2l_ptr_level, l2l_box;
+    int64_t               n_m2l = 0, n_m2p = 0;
+  };
+
+  void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &plan);
+
+  // Real-form translation operators (scaled expansions), row-major K x K.
+  void build_m2m_ops(int p, std::vector<double> &ops8);
+  void build_l2l_ops(int p, std::vector<double> &ops8);
+  void build_m2l_op(int p, int dx, int dy, int dz, double *T);
+
+  // Gauss-Legendre and Telles rules on [0,1]^2 (x index fastest).
+  void gauss_rule_2d(int n, std::vector<double> &pts, std::vector<double> &w);
+  void telles_rule_2d(int n, int vertex, std::vector<double> &pts, std::vector<double> &w);
+} // namespace pibem

@@ -206,16 +206,11 @@ def wigley_hull(nx: int, nz: int, ny_lid: int, L=1.0, B=0.1, T=0.0625) -> Mesh:
                         k = node(("lid", ii, jj), [x, y, 0.0])
                     quad.append(k)
             cells.append(quad)  # d/dx x d/deta = +z (outward for the lid)
+    # The lid cells at the bow and stern keep a collapsed edge (two equal
+    # vertices): the surface stays closed and the bilinear map is still
+    # regular at the interior quadrature points.
     xyz = np.asarray(pts, dtype=np.float64)
     cells = np.asarray(cells, dtype=np.int32)
-    # drop degenerate cells (bow/stern collapse all four vertices onto y=0 lines)
-    keep = np.array([len(set(c)) == 4 for c in cells.tolist()])
-    cells = cells[keep]
-    used = np.unique(cells)
-    remap = -np.ones(len(xyz), dtype=np.int64)
-    remap[used] = np.arange(len(used))
-    xyz = xyz[used]
-    cells = remap[cells].astype(np.int32)
     return Mesh(xyz, cells, _nodal_normals(xyz, cells))
 
 

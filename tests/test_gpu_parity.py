@@ -1,0 +1,175 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle (CPU restatement
+of source/bem_fma.cc and source/bem_problem.cc) on the same seeded inputs.
+
+Tolerances (FP64 path):
+  quadrature points, octree boxes and lists      bit-exact / identical sets
+  near-field N and D entries                     1e-12 relative to the largest entry
+  FMM matvec (BEMFMA parity), alpha, vmult, rhs  1e-10 relative (2-norm)
+  solution of the solve vs the oracle solve      1e-7 relative, residual <= 1e-8
+Mixed path: solution within 1e-7 of the FP64 path at residual 1e-8.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _sphere(S):
+    mesh, mask, tmp, exact = S.sphere_dirichlet_case(16)
+    return dict(mesh=mesh, mask=mask, tmp=tmp, exact=exact, p=4, leaf=30, levels=10, ext=False)
+
+
+def _spheroid(S):
+    mesh, mask, tmp, ph, dn = S.spheroid_mixed_case(20, seed=2)
+    return dict(mesh=mesh, mask=mask, tmp=tmp, exact=None, p=8, leaf=40, levels=10, ext=True)
+
+
+def _perturbed(S):
+    mesh = S.perturbed_sphere(14, seed=11)
+    mesh, mask, tmp, ph, dn = S.spheroid_mixed_case(0, seed=4, mesh=mesh)
+    return dict(mesh=mesh, mask=mask, tmp=tmp, exact=None, p=6, leaf=12, levels=6, ext=True)
+
+
+def _wigley(S):
+    mesh = S.wigley_hull(48, 8, 6)
+    rng = np.random.Generator(np.random.PCG64(3))
+    src = np.stack([rng.uniform(-0.3, 0.3, 4), np.zeros(4), rng.uniform(-0.04, -0.02, 4)], 1)
+    phi, grad = S.point_source_field(src, rng.uniform(-1, 1, 4))
+    mask = S.mixed_bc_by_cell_centroid(mesh, z_split=-0.03)
+    tmp = np.where(mask == 1, phi(mesh.xyz), (grad(mesh.xyz) * mesh.normals).sum(1))
+    return dict(mesh=mesh, mask=mask, tmp=tmp, exact=None, p=10, leaf=20, levels=10, ext=True)
+
+
+CASES = {"sphere_p4": _sphere, "spheroid_p8": _spheroid, "perturbed_p6": _perturbed,
+         "wigley_p10": _wigley}
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def case(request, synthetic, oracle_mod, pibem_mod):
+    c = CASES[request.param](synthetic)
+    m = c["mesh"]
+    o = oracle_mod.Oracle(p=c["p"], levels=c["levels"], max_nodes=c["leaf"], external=c["ext"])
+    o.set_mesh(m.xyz, m.cells)
+    o.set_bc(c["mask"])
+    g = pibem_mod.BEMSolver(fma_truncation_order=c["p"], num_octree_levels=c["levels"],
+                            max_nodes_per_childless_block=c["leaf"], is_external_flow=int(c["ext"]),
+                            solver_tolerance=1e-8, solver_max_steps=2000)
+    g.set_mesh(m.xyz, m.cells)
+    g.set_bc(c["mask"])
+    c.update(name=request.param, oracle=o, gpu=g)
+    yield c
+    g.close()
+
+
+def test_quadrature_points_bitwise(case):
+    pts_o, _, _ = case["oracle"].quad_data()
+    pts_g = case["gpu"].quad_points()
+    assert np.array_equal(pts_o, pts_g)
+
+
+def test_octree_and_lists_match_reference_semantics(case):
+    o, g = case["oracle"], case["gpu"]
+    to, tg = o.tree(), g.tree()
+    assert len(to["level"]) == len(tg["level"])
+    for k in ("level", "parent", "nchild", "n_nodes", "n_quads"):
+        assert np.array_equal(to[k], tg[k]), k
+    assert np.array_equal(to["pmin"], tg["pmin"]) and np.array_equal(to["delta"], tg["delta"])
+    nb = len(to["level"])
+    for b in range(nb):
+        for kind in range(3):
+            lo, lg = o.lists(b, kind), g.lists(b, kind)
+            assert len(lo) == len(lg)
+            for a, bb in zip(lo, lg):
+                assert np.array_equal(a, bb), (b, kind)
+
+
+def test_near_field_matches_oracle(case):
+    ro, co, No, Do = case["oracle"].near()
+    rg, cg, Ng, Dg = case["gpu"].near()
+    assert np.array_equal(ro, rg) and np.array_equal(co, cg)
+    assert np.abs(Ng - No).max() <= 1e-12 * np.abs(No).max()
+    assert np.abs(Dg - Do).max() <= 1e-12 * np.abs(Do).max()
+
+
+def test_fmm_matvec_matches_oracle(case):
+    n = case["mesh"].n_nodes
+    rng = np.random.Generator(np.random.PCG64(7))
+    phi, dphi = rng.normal(size=n), rng.normal(size=n)
+    oN, oD = case["oracle"].fmm_matvec(phi, dphi)
+    gN, gD = case["gpu"].fmm_matvec(phi, dphi)
+    assert rel(gN, oN) < 1e-10, rel(gN, oN)
+    assert rel(gD, oD) < 1e-10, rel(gD, oD)
+
+
+def test_fmm_matvec_multi_rhs(case):
+    n = case["mesh"].n_nodes
+    rng = np.random.Generator(np.random.PCG64(8))
+    phi, dphi = rng.normal(size=(3, n)), rng.normal(size=(3, n))
+    gN, gD = case["gpu"].fmm_matvec(phi, dphi)
+    for r in range(3):
+        sN, sD = case["gpu"].fmm_matvec(phi[r], dphi[r])
+        assert rel(gN[r], sN) < 1e-13 and rel(gD[r], sD) < 1e-13
+
+
+def test_alpha_rhs_vmult_match_oracle(case):
+    o, g = case["oracle"], case["gpu"]
+    ao, ag = o.alpha(), g.alpha()
+    assert rel(ag, ao) < 1e-10
+    bo, bg = o.rhs(ao, case["tmp"]), g.rhs(case["tmp"])
+    assert rel(bg, bo) < 1e-10
+    x = np.random.Generator(np.random.PCG64(9)).normal(size=case["mesh"].n_nodes)
+    assert rel(g.system_matvec(x), o.system_matvec(ao, x)) < 1e-10
+
+
+def test_solve_fp64_matches_oracle(case):
+    o, g = case["oracle"], case["gpu"]
+    po, do, its_o, res_o = o.solve(case["tmp"], tol=1e-10, max_steps=3000)
+    pg, dg, st = g.solve(case["tmp"])
+    assert st["relative_residual"] <= 1e-8
+    so = np.where(case["mask"] == 1, do, po)
+    sg = np.where(case["mask"] == 1, dg, pg)
+    assert rel(sg, so) < 1e-7, rel(sg, so)
+    # known entries are left untouched
+    assert np.array_equal(np.where(case["mask"] == 1, pg, 0), np.where(case["mask"] == 1, case["tmp"], 0))
+    if case["exact"] is not None:
+        # discretisation error against the analytic dphi/dn (p=4 FMM, 1538 nodes)
+        assert rel(dg, case["exact"]) < 2e-2
+
+
+def test_solve_mixed_matches_fp64(case, pibem_mod):
+    m = case["mesh"]
+    g2 = pibem_mod.BEMSolver(fma_truncation_order=case["p"], num_octree_levels=case["levels"],
+                             max_nodes_per_childless_block=case["leaf"],
+                             is_external_flow=int(case["ext"]), solver_tolerance=1e-8,
+                             precision_mode=pibem_mod.PRECISION_MIXED, solver_max_steps=2000)
+    g2.set_mesh(m.xyz, m.cells)
+    g2.set_bc(case["mask"])
+    p64, d64, _ = case["gpu"].solve(case["tmp"])
+    p32, d32, st = g2.solve(case["tmp"])
+    assert st["relative_residual"] <= 1e-8
+    assert st["fp32_matvecs"] > 0
+    s64 = np.where(case["mask"] == 1, d64, p64)
+    s32 = np.where(case["mask"] == 1, d32, p32)
+    assert rel(s32, s64) < 1e-7, rel(s32, s64)
+    g2.close()
+
+
+def test_batched_solve_equals_single(case):
+    g = case["gpu"]
+    t = np.stack([case["tmp"], 0.5 * case["tmp"] + 0.1, -case["tmp"]])
+    pb, db, st = g.solve(t)
+    for r in range(3):
+        ps, ds, _ = g.solve(t[r])
+        sb = np.where(case["mask"] == 1, db[r], pb[r])
+        ss = np.where(case["mask"] == 1, ds, ps)
+        assert rel(sb, ss) < 1e-8
+
+
+def test_deterministic(case):
+    n = case["mesh"].n_nodes
+    x = np.random.Generator(np.random.PCG64(10)).normal(size=n)
+    a = case["gpu"].system_matvec(x)
+    b = case["gpu"].system_matvec(x)
+    assert np.array_equal(a, b)
