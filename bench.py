@@ -1,0 +1,456 @@
+#!/usr/bin/env python
+"""FMM-GMRES solves/s on one GB300 (or N independent replicas).
+
+Workload (default): the 98,306-node prolate spheroid (semi-axes 3,1,1; cube-sphere
+6 x 128 x 128 Q1 cells), FMM order p = 8, <= 40 collocation points per childless
+block, 10 octree levels, QGauss(4) / Telles(5) quadrature, exterior problem,
+Dirichlet data on cells with centroid z > 0 and Neumann data on z <= 0 from 8
+seeded point sources inside |x| < 0.5; one right-hand side solved to relative
+residual 1e-8 with GMRES(100).  Synthetic data (no external dataset).
+
+A step is one solve of that right-hand side on the mesh already set up on the
+device (octree, near field, P2M tables resident).  `value` is measured with
+device-resident inputs; `e2e` repeats the measurement through pibem_solve with
+host (pinned) buffers, so host<->device copies are inside the timed region.
+The headline path is the mixed-precision solve (FP32 operator inside GMRES, FP64
+refinement residual); the plain FP64 GPU path is timed beside it on the same
+mesh and data.
+
+--impl reference times the reference algorithm on the host cores (the oracle's
+CPU restatement of pi-BEM's FMM operator: the reference itself needs deal.II,
+Trilinos, MPI and TBB, which this image does not have).
+
+Multi-GPU: the solve does not shard; with --gpus N (under torchrun) every rank
+runs the same workload on its own GPU and `value` is the total solves/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "pi-bem_gb300"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "FMM-GMRES solves/s, p50/p99 latency at residual 1e-8 vs plain FP64 GB300 path"
+WORKLOADS = {
+    "spheroid98k": dict(kind="spheroid", n=128, p=8, leaf=40, levels=10, seed=2, ext=True,
+                        desc="prolate spheroid (3,1,1), 6x128x128 Q1 cells, 98306 nodes, p=8, "
+                             "leaf<=40, mixed D/N, exterior, 1 RHS to 1e-8"),
+    "sphere1538": dict(kind="sphere", n=16, p=4, leaf=30, levels=10, seed=0, ext=False,
+                       desc="unit cube-sphere 6x16x16, 1538 nodes, p=4, leaf<=30, Dirichlet, "
+                            "interior, 1 RHS to 1e-8"),
+}
+
+
+def make_case(w):
+    import synthetic as S
+
+    if w["kind"] == "spheroid":
+        mesh, mask, tmp, ph, dn = S.spheroid_mixed_case(w["n"], seed=w["seed"])
+    else:
+        mesh, mask, tmp, dn = S.sphere_dirichlet_case(w["n"])
+    return mesh, mask, tmp
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_ours(args, w, rank, world, local):
+    import torch
+
+    import pibem
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    mesh, mask, tmp = make_case(w)
+    n = mesh.n_nodes
+    common = dict(fma_truncation_order=w["p"], num_octree_levels=w["levels"],
+                  max_nodes_per_childless_block=w["leaf"], is_external_flow=int(w["ext"]),
+                  solver_tolerance=1e-8, solver_max_steps=4000, device=local)
+    t0 = time.perf_counter()
+    g32 = pibem.BEMSolver(precision_mode=pibem.PRECISION_MIXED, **common)
+    g32.set_mesh(mesh.xyz, mesh.cells)
+    g32.set_bc(mask)
+    setup_s = time.perf_counter() - t0
+    g64 = pibem.BEMSolver(precision_mode=pibem.PRECISION_FP64, **common)
+    g64.set_mesh(mesh.xyz, mesh.cells)
+    g64.set_bc(mask)
+    info = g32.tree_info()
+
+    # accuracy reference: FP64 path driven to 1e-12 (untimed)
+    gref = pibem.BEMSolver(precision_mode=pibem.PRECISION_FP64, **{**common, "solver_tolerance": 1e-12})
+    gref.set_mesh(mesh.xyz, mesh.cells)
+    gref.set_bc(mask)
+    pr, dr, _ = gref.solve(tmp)
+    sol_ref = np.where(mask == 1, dr, pr)
+    gref.close()
+
+    stream = torch.cuda.current_stream()
+    tmp_d = torch.tensor(tmp, device=dev, dtype=torch.float64)
+    phi0 = torch.tensor(np.where(mask == 1, tmp, 0.0), device=dev, dtype=torch.float64)
+    dphi0 = torch.tensor(np.where(mask == 0, tmp, 0.0), device=dev, dtype=torch.float64)
+    phi_d, dphi_d = phi0.clone(), dphi0.clone()
+
+    def device_solves(g, K, W, profile=False):
+        g.set_stream(stream.cuda_stream)
+        for _ in range(W):
+            phi_d.copy_(phi0)
+            dphi_d.copy_(dphi0)
+            g.solve_device(1, phi_d.data_ptr(), dphi_d.data_ptr(), tmp_d.data_ptr())
+        if profile:
+            g.set_profiling(True)
+            g.phase_totals(0, reset=True)
+        barrier(world)
+        torch.cuda.synchronize()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(K + 1)]
+        stats = []
+        with ClockSampler(local) as clk:
+            evs[0].record(stream)
+            for k in range(K):
+                phi_d.copy_(phi0)
+                dphi_d.copy_(dphi0)
+                stats.append(g.solve_device(1, phi_d.data_ptr(), dphi_d.data_ptr(), tmp_d.data_ptr()))
+                evs[k + 1].record(stream)
+            torch.cuda.synchronize()
+        barrier(world)
+        per = [evs[k].elapsed_time(evs[k + 1]) for k in range(K)]
+        total_ms = evs[0].elapsed_time(evs[K])
+        phases = None
+        if profile:
+            phases = (g.phase_totals(1), g.phase_totals(0))
+            g.set_profiling(False)
+        sol = np.where(mask == 1, dphi_d.cpu().numpy(), phi_d.cpu().numpy())
+        return total_ms, per, stats, clk.summary(), phases, sol
+
+    K, W = args.steps, args.warmup
+    tot32, per32, st32, clk32, ph32, sol32 = device_solves(g32, K, W, profile=True)
+    tot64, per64, st64, clk64, _, sol64 = device_solves(g64, max(2, min(K, 5)), min(W, 2))
+    t_max = max_over_ranks(tot32 / 1e3, world, dev)
+    t64_max = max_over_ranks(tot64 / 1e3, world, dev)
+    value = K * world / t_max
+    fp64_value = len(per64) * world / t64_max
+
+    # true residual of the mixed-path solution (untimed)
+    ex = g64.system_matvec(sol32)
+    b = g64.rhs(tmp)
+    true_res = float(np.linalg.norm(b - ex) / np.linalg.norm(b))
+
+    # e2e: the C-ABI call with host buffers (pinned), copies inside the timed region
+    tmp_h = torch.tensor(tmp, dtype=torch.float64).pin_memory()
+    phi_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    dphi_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    phi_init = np.where(mask == 1, tmp, 0.0)
+    dphi_init = np.where(mask == 0, tmp, 0.0)
+    g32.set_stream(None)
+    L = pibem.load()
+    import ctypes as C
+
+    def host_solve():
+        phi_h.numpy()[:] = phi_init
+        dphi_h.numpy()[:] = dphi_init
+        st = pibem.SolveStats()
+        rc = L.pibem_solve(g32.h, 1, C.cast(phi_h.data_ptr(), pibem._dp),
+                           C.cast(dphi_h.data_ptr(), pibem._dp), C.cast(tmp_h.data_ptr(), pibem._dp),
+                           C.byref(st))
+        if rc:
+            raise pibem.PibemError(rc, L.pibem_last_error(g32.h).decode())
+
+    for _ in range(W):
+        host_solve()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        host_solve()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = K * world / e2e_s
+
+    # roofline of the dominant kernel (CUDA events over the timed region)
+    hbm_peak, bf16_peak, peak_kind = peaks()
+    (p32, c32), (p64, c64) = ph32
+    phase_tot = {}
+    for prec, (pt, c) in (("fp32", (p32, c32)), ("fp64", (p64, c64))):
+        for k, v in pt.items():
+            if k != "unused":
+                phase_tot[(prec, k)] = (v, c)
+    (dom_prec, dom_phase), (dom_ms, dom_cnt) = max(phase_tot.items(), key=lambda kv: kv[1][0])
+    roof = roofline(info, n, dom_prec, dom_phase, dom_ms, dom_cnt, hbm_peak, bf16_peak, peak_kind,
+                    w["p"])
+
+    err32 = float(np.linalg.norm(sol32 - sol_ref) / np.linalg.norm(sol_ref))
+    err64 = float(np.linalg.norm(sol64 - sol_ref) / np.linalg.norm(sol_ref))
+    per32.sort()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": t_max * 1e3 / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 operator + f64 refinement/Arnoldi",
+        "data": "synthetic (seeded point-source fields on a generated mesh)",
+        "config": {"workload": args.workload, "description": w["desc"], "nodes": n,
+                   "cells": int(mesh.n_cells), "p": w["p"], "leaf": w["leaf"], "nrhs": 1,
+                   "l2": "working set > L2 (near field %.0f MB FP32 + %.0f MB FP64)" % (
+                       info["near_nnz"] * 4 / 1e6, info["near_nnz"] * 8 / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "p50_ms": float(np.percentile(per32, 50)),
+        "p99_ms": float(np.percentile(per32, 99)),
+        "fp64_path": {"value": fp64_value, "unit": "solves/s", "ms_per_solve": t64_max * 1e3 / len(per64),
+                      "p50_ms": float(np.percentile(per64, 50)), "iterations": st64[-1]["iterations"],
+                      "fp64_matvecs": st64[-1]["fp64_matvecs"]},
+        "speedup_vs_fp64_path": value / fp64_value,
+        "solve": {"iterations": st32[-1]["iterations"], "fp64_matvecs": st32[-1]["fp64_matvecs"],
+                  "fp32_matvecs": st32[-1]["fp32_matvecs"],
+                  "refinement_steps": st32[-1]["refinement_steps"],
+                  "relative_residual_estimate": st32[-1]["relative_residual"],
+                  "relative_residual_true_fp64": true_res,
+                  "solution_error_vs_fp64_oracle": err32,
+                  "fp64_path_solution_error_vs_fp64_oracle": err64},
+        "setup_s": setup_s,
+        "tree": info,
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 3 * n * 8,
+                "d2h_bytes_per_step": 2 * n * 8},
+        "roofline": roof,
+        "clocks": clk32,
+        "gpu_launches": None,
+    }
+    line["gpu_launches"] = count_launches(info, st32[-1], w["p"], mesh)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, mesh, mask, st64[-1]["fp64_matvecs"])
+    if rank == 0:
+        print(json.dumps(line))
+    g32.close()
+    g64.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def roofline(info, n, prec, phase, ms, cnt, hbm_peak, bf16_peak, peak_kind, p):
+    s = 4 if prec == "fp32" else 8
+    K = (p + 1) ** 2
+    per_launch_s = ms / 1e3 / max(cnt, 1)
+    if phase == "near":
+        # values + column ids (per leaf block) + x gathered once + y written once
+        byt = info["near_nnz"] * s + info["near_nnz"] * 0 + 2 * n * s
+        return {"kernel": f"near-field leaf-block SpMV ({prec})", "bound": "hbm",
+                "achieved": byt / per_launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": byt / per_launch_s / 1e9 / hbm_peak, "traffic": None,
+                "algorithmic_bytes_per_launch": byt, "launch_ms": per_launch_s * 1e3,
+                "peak_source": f"{peak_kind} hbm_gbs"}
+    if phase == "m2l_l2l":
+        fl = 2.0 * K * K * info["n_m2l_pairs"]
+        return {"kernel": f"M2L+L2L translations ({prec})", "bound": "tensor",
+                "achieved": fl / per_launch_s / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": fl / per_launch_s / 1e12 / bf16_peak, "traffic": None,
+                "algorithmic_flops_per_launch": fl, "launch_ms": per_launch_s * 1e3,
+                "peak_source": f"{peak_kind} bf16_tflops"}
+    return {"kernel": f"{phase} ({prec})", "bound": "hbm", "achieved": None, "peak": hbm_peak,
+            "unit": "GB/s", "frac": None, "traffic": None, "launch_ms": per_launch_s * 1e3,
+            "peak_source": f"{peak_kind} hbm_gbs"}
+
+
+def count_launches(info, st, p, mesh):
+    """Kernels launched by one solve: per operator application near + P2M +
+    M2M (levels) + L2L/M2L (levels) + M2P (2) + L2P, plus the Krylov vector
+    kernels per iteration.  Estimated from the structure, not traced."""
+    L = info["n_levels"]
+    per_app = 1 + 1 + L + 2 * L + 2 + 1 + 2
+    per_iter = 12
+    apps = st["fp64_matvecs"] + st["fp32_matvecs"]
+    return int(apps * per_app + st["iterations"] * per_iter)
+
+
+def cpu_baseline(w, mesh, mask, matvecs_per_solve, threads=None):
+    """The oracle (CPU restatement of pi-BEM's FMM operator, OpenMP over the
+    loops the reference runs under TBB) on the host cores: one system matvec of
+    the full workload, extrapolated to a solve by the FP64 path's matvec count."""
+    import oracle
+
+    oracle.build()
+    threads = threads or os.cpu_count()
+    o = oracle.Oracle(p=w["p"], levels=w["levels"], max_nodes=w["leaf"], external=w["ext"],
+                      threads=threads)
+    t0 = time.perf_counter()
+    o.set_mesh(mesh.xyz, mesh.cells)
+    o.set_bc(mask)
+    setup = time.perf_counter() - t0
+    x = np.random.Generator(np.random.PCG64(0)).normal(size=mesh.n_nodes)
+    alpha = np.zeros(mesh.n_nodes)
+    t0 = time.perf_counter()
+    o.system_matvec(alpha, x)
+    t_mv = time.perf_counter() - t0
+    return {"value": 1.0 / (t_mv * matvecs_per_solve), "unit": "solves/s", "cores": threads,
+            "kind": "port",
+            "sample": f"one FMM system matvec of the full workload ({t_mv:.2f} s) x {matvecs_per_solve} "
+                      f"matvecs per solve (FP64 GPU path count); oracle setup {setup:.1f} s untimed"}
+
+
+def run_reference(args, w, rank, world):
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    mesh, mask, tmp = make_case(w)
+    threads = os.cpu_count()
+    o = oracle.Oracle(p=w["p"], levels=w["levels"], max_nodes=w["leaf"], external=w["ext"],
+                      threads=threads)
+    o.set_mesh(mesh.xyz, mesh.cells)
+    o.set_bc(mask)
+    alpha = o.alpha()
+    x = np.random.Generator(np.random.PCG64(0)).normal(size=mesh.n_nodes)
+    # matvecs per solve of this operator and GMRES, as measured on the FP64 GPU path
+    mv_per_solve = REFERENCE_MATVECS_PER_SOLVE.get(args.workload, 52)
+    for _ in range(args.warmup):
+        o.system_matvec(alpha, x)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.system_matvec(alpha, x)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    value = 1.0 / (t * mv_per_solve)
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * mv_per_solve * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": args.workload, "description": w["desc"], "nodes": mesh.n_nodes},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"each step one FMM system matvec ({t:.2f} s mean) x "
+                                   f"{mv_per_solve} matvecs per solve"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# FP64-path operator applications per solve (rhs + GMRES iterations + residual
+# checks), measured on the GPU for each workload; used to extrapolate the CPU
+# matvec time of the reference arm to a solve.
+REFERENCE_MATVECS_PER_SOLVE = {"spheroid98k": 52, "sphere1538": 30}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="spheroid98k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w, rank, world)
+    else:
+        run_ours(args, w, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -152,8 +152,16 @@ int     pibem_near_export(pibem_handle *h, int32_t *rows, int32_t *cols, double 
 /* Quadrature points of the mesh, cell-major (n_cells * nq points). */
 int pibem_quad_points(pibem_handle *h, double *pts);
 /* Phase timings of the last operator application, milliseconds, in the order
- * near, p2m, m2m, m2l, l2l, m2p, l2p (7 values). */
+ * near, p2m, m2m, m2l+l2l, (unused), m2p, l2p (7 values); needs profiling on. */
 int pibem_last_phase_ms(pibem_handle *h, double *ms7);
+/* Turns CUDA-event timing of the operator phases on or off (off by default;
+ * on adds event records and one stream synchronisation per application). */
+int pibem_set_profiling(pibem_handle *h, int32_t on);
+/* Phase times (ms, same order as pibem_last_phase_ms) summed over the operator
+ * applications of the given precision (PIBEM_PRECISION_FP64: FP64 operator,
+ * PIBEM_PRECISION_MIXED: FP32 operator) since the last reset, and their count. */
+int pibem_phase_totals(pibem_handle *h, int32_t precision, double *ms7, int64_t *applications,
+                       int32_t reset);
 
 #ifdef __cplusplus
 }

@@ -122,10 +122,10 @@ struct pibem_handle
   DBuf<double>  d_center, d_delta;
   // plan
   DBuf<int64_t> d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr,
-    d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr;
+    d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr;
   DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
-    d_parents, d_diag_col;
+    d_parents, d_diag_col, d_m2p_pair_tgt;
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_m2m, d_l2l, d_m2l, d_Pinv;
   DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_m2mf, d_l2lf, d_m2lf;
@@ -139,14 +139,17 @@ struct pibem_handle
   DBuf<double>         d_alpha;
   bool                 have_dirichlet = true;
   // work
-  DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4;
-  DBuf<float>  d_M32, d_L32, d_x32, d_y32;
+  DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64;
+  DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
   // timing
   bool        timing = false;
   cudaEvent_t ev[8] = {};
   double      phase_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+  double      phase_tot[2][7] = {};
+  int64_t     phase_cnt[2] = {0, 0};
   int         cnt64 = 0, cnt32 = 0;
+  int64_t     m2p_items = 0, m2p_tnodes = 0;
 
   int64_t N() const { return mesh.n_nodes; }
 };
@@ -197,8 +200,8 @@ namespace
   // Far field (P2M ... L2P) added to y for R columns.
   // ---------------------------------------------------------------------
   template <typename T>
-  void far_field(pibem_handle *h, const OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, int R,
-                 const uint8_t *modes, const T *x, T *y)
+  void far_field(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
+                 int R, const uint8_t *modes, const T *x, T *y)
   {
     const int    N = int(h->N());
     const size_t need = size_t(h->tree.nb) * R * op.K;
@@ -207,6 +210,8 @@ namespace
         M.alloc(need);
         Lx.alloc(need);
       }
+    scr.alloc(std::max<size_t>(1, size_t(op.n_m2p_items) * R));
+    op.m2p_scratch = scr.p;
     cudaStream_t s = h->stream;
     PIBEM_CUDA(cudaMemsetAsync(Lx.p, 0, need * sizeof(T), s));
     PIBEM_CUDA(cudaMemsetAsync(M.p, 0, need * sizeof(T), s));
@@ -228,7 +233,8 @@ namespace
     record(h, 7);
   }
 
-  void finish_timing(pibem_handle *h)
+  // prec: 0 FP64 operator, 1 FP32 operator
+  void finish_timing(pibem_handle *h, int prec = 0)
   {
     if (!h->timing)
       return;
@@ -238,7 +244,9 @@ namespace
         float ms = 0;
         cudaEventElapsedTime(&ms, h->ev[i], h->ev[i + 1]);
         h->phase_ms[i] = ms;
+        h->phase_tot[prec][i] += ms;
       }
+    h->phase_cnt[prec] += 1;
   }
 
   // [phi_0..phi_{R-1}, dphi_0..dphi_{R-1}] -> [outN..., outD...]  (FP64)
@@ -264,8 +272,9 @@ namespace
     launch_near_spmv<double>(h->op64, R, int(N), h->d_D.p, h->d_x64.p + R * N,
                              h->d_y64.p + R * N, false, s);
     record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, 2 * R, h->d_modes.p, h->d_x64.p,
-                      h->d_y64.p);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, 2 * R, h->d_modes.p,
+                      h->d_x64.p, h->d_y64.p);
+    finish_timing(h, 0);
     PIBEM_CUDA(cudaMemcpyAsync(oN, h->d_y64.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
     PIBEM_CUDA(cudaMemcpyAsync(oD, h->d_y64.p + R * N, sizeof(double) * R * N,
                                cudaMemcpyDeviceToDevice, s));
@@ -278,8 +287,11 @@ namespace
     const int64_t        N = h->N();
     std::vector<uint8_t> modes(1, MODE_KER1);
     h->d_modes.upload(modes, h->stream);
+    record(h, 0);
     launch_near_spmv<double>(h->op64, 1, int(N), h->d_N.p, x, y, false, h->stream);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, 1, h->d_modes.p, x, y);
+    record(h, 1);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, 1, h->d_modes.p, x, y);
+    finish_timing(h, 0);
   }
 
   void set_modes(pibem_handle *h, int R, uint8_t mode)
@@ -322,7 +334,8 @@ namespace
     record(h, 0);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_S.p, xin, y, false, s);
     record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, R, h->d_modes.p, xin, y);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, R, h->d_modes.p, xin, y);
+    finish_timing(h, 0);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
     h->cnt64 += R;
@@ -348,7 +361,9 @@ namespace
     record(h, 0);
     launch_near_spmv<float>(h->op32, R, int(N), h->d_S32.p, h->d_x32.p, h->d_y32.p, false, s);
     record(h, 1);
-    far_field<float>(h, h->op32, h->d_M32, h->d_L32, R, h->d_modes.p, h->d_x32.p, h->d_y32.p);
+    far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, R, h->d_modes.p, h->d_x32.p,
+                     h->d_y32.p);
+    finish_timing(h, 1);
     launch_convert_f2d(int64_t(R) * N, h->d_y32.p, y, s);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
@@ -587,9 +602,15 @@ namespace
       op.m2l_off       = h->d_m2l_off.p;
       op.m2l_src_ptr   = h->d_m2l_src_ptr.p;
       op.n_m2p_tgt     = int(pl.m2p_tgt.size());
+      op.n_m2p_pairs   = int64_t(pl.m2p_src.size());
+      op.n_m2p_items   = h->m2p_items;
+      op.n_m2p_tnodes  = h->m2p_tnodes;
       op.m2p_tgt       = h->d_m2p_tgt.p;
       op.m2p_src       = h->d_m2p_src.p;
       op.m2p_src_ptr   = h->d_m2p_src_ptr.p;
+      op.m2p_pair_tgt  = h->d_m2p_pair_tgt.p;
+      op.m2p_item_ptr  = h->d_m2p_item_ptr.p;
+      op.m2p_tnode_ptr = h->d_m2p_tnode_ptr.p;
       op.l2l_box       = h->d_l2l_box.p;
       op.m2l_level_ptr = pl.m2l_tgt_ptr_level;
       op.l2l_level_ptr = pl.l2l_ptr_level;
@@ -839,6 +860,29 @@ namespace
     h->d_m2p_src_ptr.upload(pl.m2p_src_ptr, s);
     h->d_m2p_src.upload(pl.m2p_src, s);
     h->d_l2l_box.upload(pl.l2l_box, s);
+    // M2P work items: one per (pair, node of the pair's target box)
+    {
+      const size_t         nt = pl.m2p_tgt.size();
+      std::vector<int32_t> pair_tgt(pl.m2p_src.size());
+      std::vector<int64_t> item_ptr(pl.m2p_src.size() + 1, 0), tnode_ptr(nt + 1, 0);
+      for (size_t ti = 0; ti < nt; ++ti)
+        {
+          const int     b  = pl.m2p_tgt[ti];
+          const int64_t nn = t.nend[b] - t.nbeg[b];
+          tnode_ptr[ti + 1] = tnode_ptr[ti] + nn;
+          for (int64_t e = pl.m2p_src_ptr[ti]; e < pl.m2p_src_ptr[ti + 1]; ++e)
+            {
+              pair_tgt[e]     = int32_t(ti);
+              item_ptr[e + 1] = item_ptr[e] + nn;
+            }
+        }
+      h->m2p_items  = item_ptr.back();
+      h->m2p_tnodes = tnode_ptr.back();
+      h->d_m2p_pair_tgt.upload(pair_tgt, s);
+      h->d_m2p_item_ptr.upload(item_ptr, s);
+      h->d_m2p_tnode_ptr.upload(tnode_ptr, s);
+    }
+    ensure_fmm_tables(P.device, s);
     // diagonal column of every row inside its leaf (block-Jacobi)
     {
       std::vector<int32_t> dc(pl.nrows.size());
@@ -1052,7 +1096,12 @@ namespace
       }
     else
       {
-        // FP64 iterative refinement around an FP32-operator GMRES
+        // Mixed precision: FP64 iterative refinement around GMRES on the FP32
+        // operator, from x0 = 0 (r0 = b exactly).  The first correction carries
+        // the whole solution, so its residual is formed with the FP64 operator;
+        // every later correction d_k is small (|d_k| <= tol_inner^k |x|), so the
+        // residual is updated as r <- r - A32 d_k, whose rounding error
+        // eps32 * |A| |d_k| stays far below the target.
         r.alloc(size_t(R) * N);
         d.alloc(size_t(R) * N);
         DBuf<double> w;
@@ -1063,30 +1112,30 @@ namespace
         DBuf<double>        part, nrm;
         part.alloc(size_t(R) * 64);
         nrm.alloc(R);
-        for (int c = 0; c < R; ++c)
-          launch_dots(N, 1, 1, N, N, b.p + c * N, b.p + c * N, part.p, 64, nrm.p + c, s);
-        nrm.download(bn.data(), R, s);
-        PIBEM_CUDA(cudaStreamSynchronize(s));
+        auto norms = [&](const double *v, std::vector<double> &out) {
+          for (int c = 0; c < R; ++c)
+            launch_dots(N, 1, 1, N, N, v + c * N, v + c * N, part.p, 64, nrm.p + c, s);
+          nrm.download(out.data(), R, s);
+          PIBEM_CUDA(cudaStreamSynchronize(s));
+          for (auto &v2 : out)
+            v2 = std::sqrt(v2);
+        };
+        norms(b.p, bn);
         for (auto &v : bn)
-          v = v > 0 ? std::sqrt(v) : 1.0;
+          v = v > 0 ? v : 1.0;
+        PIBEM_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * R * N, s));
+        PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
         for (; refine <= max_refine; ++refine)
           {
-            A64(x.p, w.p);
-            PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
-            launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
-            for (int c = 0; c < R; ++c)
-              launch_dots(N, 1, 1, N, N, r.p + c * N, r.p + c * N, part.p, 64, nrm.p + c, s);
-            nrm.download(rn.data(), R, s);
-            PIBEM_CUDA(cudaStreamSynchronize(s));
+            norms(r.p, rn);
             bool ok = true;
             for (int c = 0; c < R; ++c)
               {
-                rel[c] = std::sqrt(rn[c]) / bn[c];
+                rel[c] = rn[c] / bn[c];
                 ok     = ok && rel[c] <= P.solver_tolerance;
               }
             if (ok || refine == max_refine || iters >= P.solver_max_steps)
               break;
-            // inner tolerance relative to this residual, never tighter than needed
             double worst = *std::max_element(rel.begin(), rel.end());
             double itol  = std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / worst);
             PIBEM_CUDA(cudaMemsetAsync(d.p, 0, sizeof(double) * R * N, s));
@@ -1094,6 +1143,15 @@ namespace
                                    P.gmres_restart, A32, prec);
             iters += gr.iterations;
             launch_axpby(int64_t(R) * N, 1.0, d.p, 1.0, x.p, s);
+            if (refine == 0)
+              {
+                A64(x.p, w.p); // r = b - A64 x
+                PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N,
+                                           cudaMemcpyDeviceToDevice, s));
+              }
+            else
+              A32(d.p, w.p); // r = r - A32 d
+            launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
           }
       }
     launch_scatter(N, R, x.p, h->d_dir.p, phi, dphi, s);
@@ -1231,7 +1289,6 @@ extern "C"
           h->d_dir.upload(z, h->stream);
         }
       fmm_apply64(h, R, dp, dd, on, od);
-      finish_timing(h);
       PIBEM_CUDA(cudaMemcpyAsync(oN, on, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
       PIBEM_CUDA(cudaMemcpyAsync(oD, od, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
@@ -1262,7 +1319,6 @@ extern "C"
         system_apply32(h, R, dx, dy);
       else
         system_apply64(h, R, dx, dy);
-      finish_timing(h);
       PIBEM_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
     });
@@ -1432,6 +1488,33 @@ extern "C"
       h->d_qpts.download(pts, h->d_qpts.n, h->stream);
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
     });
+  }
+
+  int pibem_set_profiling(pibem_handle *h, int32_t on)
+  {
+    return guarded(h, [&] { h->timing = on != 0; });
+  }
+
+  int pibem_phase_totals(pibem_handle *h, int32_t precision, double *ms7, int64_t *applications,
+                         int32_t reset)
+  {
+    if (!h || precision < 0 || precision > 1)
+      return PIBEM_EINVAL;
+    if (ms7)
+      for (int i = 0; i < 7; ++i)
+        ms7[i] = h->phase_tot[precision][i];
+    if (applications)
+      *applications = h->phase_cnt[precision];
+    if (reset)
+      {
+        for (int p = 0; p < 2; ++p)
+          {
+            for (int i = 0; i < 7; ++i)
+              h->phase_tot[p][i] = 0;
+            h->phase_cnt[p] = 0;
+          }
+      }
+    return PIBEM_OK;
   }
 
   int pibem_last_phase_ms(pibem_handle *h, double *ms7)

@@ -9,6 +9,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 namespace pibem
 {
   // (n, m, part) of real index k.
@@ -66,6 +68,121 @@ namespace pibem
       dth = T(0.5) * (sqrt(T(n - m) * T(n + m + 1)) * legendre_nm<T>(n, m + 1, x, s) -
                       sqrt(T(n + m) * T(n - m + 1)) * legendre_nm<T>(n, m - 1, x, s));
     return -dth;
+  }
+
+  // Coefficients of the normalised Legendre recurrences for n, m <= 20:
+  //   P~_m^m     = -cmm[m] s P~_{m-1}^{m-1},       cmm[m] = sqrt((2m-1)/(2m))
+  //   P~_{m+1}^m = cm1[m] x P~_m^m,                cm1[m] = sqrt(2m+1)
+  //   P~_n^m     = ra[n][m] x P~_{n-1}^m - rb[n][m] P~_{n-2}^m,
+  //                ra = (2n-1)/sqrt(n^2-m^2), rb = sqrt((n-1)^2-m^2)/sqrt(n^2-m^2)
+  struct LegendreTables
+  {
+    double cmm[21], cm1[21], ra[21][21], rb[21][21];
+    float  fcmm[21], fcm1[21], fra[21][21], frb[21][21];
+  };
+  // One copy per translation unit that evaluates expansions; filled by
+  // fill_legendre_tables() + cudaMemcpyToSymbol from that unit.
+  static __constant__ LegendreTables c_leg;
+
+  inline void fill_legendre_tables(LegendreTables &t)
+  {
+    for (int m = 0; m <= 20; ++m)
+      {
+        t.cmm[m] = m > 0 ? std::sqrt((2.0 * m - 1.0) / (2.0 * m)) : 0.0;
+        t.cm1[m] = std::sqrt(2.0 * m + 1.0);
+        for (int n = 0; n <= 20; ++n)
+          {
+            bool ok    = n >= m + 2;
+            t.ra[n][m] = ok ? (2.0 * n - 1.0) / std::sqrt(double(n * n - m * m)) : 0.0;
+            t.rb[n][m] = ok ? std::sqrt(double((n - 1) * (n - 1) - m * m)) / std::sqrt(double(n * n - m * m)) : 0.0;
+            t.fra[n][m] = float(t.ra[n][m]);
+            t.frb[n][m] = float(t.rb[n][m]);
+          }
+        t.fcmm[m] = float(t.cmm[m]);
+        t.fcm1[m] = float(t.cm1[m]);
+      }
+  }
+
+  template <typename T>
+  struct LegT;
+  template <>
+  struct LegT<double>
+  {
+    __device__ static double cmm(int m) { return c_leg.cmm[m]; }
+    __device__ static double cm1(int m) { return c_leg.cm1[m]; }
+    __device__ static double ra(int n, int m) { return c_leg.ra[n][m]; }
+    __device__ static double rb(int n, int m) { return c_leg.rb[n][m]; }
+  };
+  template <>
+  struct LegT<float>
+  {
+    __device__ static float cmm(int m) { return c_leg.fcmm[m]; }
+    __device__ static float cm1(int m) { return c_leg.fcm1[m]; }
+    __device__ static float ra(int n, int m) { return c_leg.fra[n][m]; }
+    __device__ static float rb(int n, int m) { return c_leg.frb[n][m]; }
+  };
+
+  // Table-driven evaluation (same sum as eval_expansion below, no square roots
+  // in the loop): value = sum_k coef[k] basis_k(r).
+  template <typename T, typename E>
+  __device__ inline T eval_expansion_fast(const E *__restrict__ coef, int p, T rx, T ry, T rz,
+                                          bool multipole)
+  {
+    using LT = LegT<T>;
+    const T r2  = rx * rx + ry * ry + rz * rz;
+    const T rho = sqrt(r2);
+    const T inv = T(1) / rho;
+    const T x   = rz * inv;
+    const T s   = sqrt(fmax(T(0), T(1) - x * x));
+    const T rxy = sqrt(rx * rx + ry * ry);
+    T       cb = T(1), sb = T(0);
+    if (rxy > T(0))
+      {
+        cb = rx / rxy;
+        sb = ry / rxy;
+      }
+    const T step = multipole ? inv : rho;
+    T       acc  = T(0);
+    T       pmm  = T(1);
+    T       rpm  = multipole ? inv : T(1);
+    T       cm = T(1), sm = T(0);
+    for (int m = 0; m <= p; ++m)
+      {
+        if (m > 0)
+          {
+            pmm *= -LT::cmm(m) * s;
+            rpm *= step;
+            const T c2 = cm * cb - sm * sb;
+            sm         = sm * cb + cm * sb;
+            cm         = c2;
+          }
+        const T cr = m == 0 ? T(1) : T(2) * cm;
+        const T ci = m == 0 ? T(0) : -T(2) * sm;
+        T       p0 = pmm, rp = rpm;
+        int     k0 = m * m + (m == 0 ? 0 : 2 * m - 1);
+        T       v  = T(coef[k0]) * cr + (m > 0 ? T(coef[k0 + 1]) * ci : T(0));
+        acc += v * p0 * rp;
+        if (m + 1 <= p)
+          {
+            T p1 = x * LT::cm1(m) * pmm;
+            rp *= step;
+            int n  = m + 1;
+            k0     = n * n + (m == 0 ? 0 : 2 * m - 1);
+            v      = T(coef[k0]) * cr + (m > 0 ? T(coef[k0 + 1]) * ci : T(0));
+            acc += v * p1 * rp;
+            for (n = m + 2; n <= p; ++n)
+              {
+                const T p2 = LT::ra(n, m) * x * p1 - LT::rb(n, m) * p0;
+                p0         = p1;
+                p1         = p2;
+                rp *= step;
+                k0 = n * n + (m == 0 ? 0 : 2 * m - 1);
+                v  = T(coef[k0]) * cr + (m > 0 ? T(coef[k0 + 1]) * ci : T(0));
+                acc += v * p1 * rp;
+              }
+          }
+      }
+    return acc;
   }
 
   // Evaluation of a scaled expansion at relative position r (in box units):

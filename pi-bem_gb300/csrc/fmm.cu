@@ -105,135 +105,204 @@ namespace pibem
         }
     }
 
-    // out[box] (=|+=) sum_src op[src_op]^T-contract in[src]; shared by M2M, L2L, M2L.
-    // ops are stored [op][in][out].
-    template <typename T>
-    __device__ inline void accumulate_translation(int R, int K, const T *__restrict__ op,
-                                                  const T *__restrict__ sIn, T *__restrict__ sOut)
+    // Generic translation: out[t] (= or +=) sum over sources s of op[s] * in[s]
+    // for one target box per block.  Four warps share the target's sources
+    // (warp w takes sources w, w+4, ...); each lane owns output rows
+    // k = lane + 32 j; the four partial sums are added in a fixed order, so the
+    // result does not depend on scheduling.  ops are stored [op][in][out].
+    //   SRC_CSR:      M2L, sources and offset ids from a per-target list
+    //   SRC_CHILDREN: M2M, sources = children, op = child octant
+    //   SRC_PARENT:   L2L, source = parent, op = own octant
+    enum
     {
-      for (int idx = threadIdx.x; idx < R * K; idx += blockDim.x)
+      SRC_CSR      = 0,
+      SRC_CHILDREN = 1,
+      SRC_PARENT   = 2
+    };
+    constexpr int TW  = 4; // warps per block
+    constexpr int KPL = 4; // output rows per lane (K <= 128)
+    constexpr int RCH = 4; // rhs columns per register block
+
+    template <typename T, int MODE, bool ACCUM>
+    __global__ void __launch_bounds__(TW * 32)
+      translate_kernel(int R, int K, const int32_t *__restrict__ targets,
+                       const int64_t *__restrict__ src_ptr, const int32_t *__restrict__ src,
+                       const int32_t *__restrict__ opid, const int32_t *__restrict__ child_first,
+                       const int32_t *__restrict__ nchild, const int32_t *__restrict__ digit,
+                       const int32_t *__restrict__ parent, const T *__restrict__ ops,
+                       const T *__restrict__ in, T *__restrict__ out)
+    {
+      extern __shared__ unsigned char smem_raw[];
+      T            *sSrc = reinterpret_cast<T *>(smem_raw);   // [TW][RCH][K]
+      T            *sAcc = sSrc + TW * RCH * K;               // [TW][RCH][K]
+      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      const int64_t t    = targets[blockIdx.x];
+      int64_t       e0, e1;
+      if (MODE == SRC_CSR)
         {
-          const int r  = idx / K;
-          const int ko = idx - r * K;
-          const T  *in = sIn + r * K;
-          T         a0 = T(0), a1 = T(0);
-          int       ki = 0;
-          for (; ki + 1 < K; ki += 2)
+          e0 = src_ptr[blockIdx.x];
+          e1 = src_ptr[blockIdx.x + 1];
+        }
+      else if (MODE == SRC_CHILDREN)
+        {
+          e0 = child_first[t];
+          e1 = e0 + nchild[t];
+        }
+      else
+        {
+          e0 = 0;
+          e1 = 1;
+        }
+      T *mySrc = sSrc + warp * RCH * K;
+      for (int r0 = 0; r0 < R; r0 += RCH)
+        {
+          const int rc = min(RCH, R - r0);
+          T         acc[RCH][KPL];
+#pragma unroll
+          for (int r = 0; r < RCH; ++r)
+#pragma unroll
+            for (int j = 0; j < KPL; ++j)
+              acc[r][j] = T(0);
+          for (int64_t e = e0 + warp; e < e1; e += TW)
             {
-              a0 += op[int64_t(ki) * K + ko] * in[ki];
-              a1 += op[int64_t(ki + 1) * K + ko] * in[ki + 1];
+              int64_t sb;
+              int     o;
+              if (MODE == SRC_CSR)
+                {
+                  sb = src[e];
+                  o  = opid[e];
+                }
+              else if (MODE == SRC_CHILDREN)
+                {
+                  sb = e;
+                  o  = digit[e];
+                }
+              else
+                {
+                  sb = parent[t];
+                  o  = digit[t];
+                }
+              const T *ip = in + (sb * R + r0) * K;
+              for (int i = lane; i < rc * K; i += 32)
+                mySrc[i] = ip[i];
+              __syncwarp();
+              const T *op = ops + int64_t(o) * K * K;
+              for (int ki = 0; ki < K; ++ki)
+                {
+                  T w[KPL];
+#pragma unroll
+                  for (int j = 0; j < KPL; ++j)
+                    {
+                      const int ko = lane + 32 * j;
+                      w[j]         = ko < K ? op[int64_t(ki) * K + ko] : T(0);
+                    }
+#pragma unroll
+                  for (int r = 0; r < RCH; ++r)
+                    if (r < rc)
+                      {
+                        const T m = mySrc[r * K + ki];
+#pragma unroll
+                        for (int j = 0; j < KPL; ++j)
+                          acc[r][j] += w[j] * m;
+                      }
+                }
+              __syncwarp();
             }
-          if (ki < K)
-            a0 += op[int64_t(ki) * K + ko] * in[ki];
-          sOut[idx] += a0 + a1;
-        }
-    }
-
-    template <typename T>
-    __global__ void m2m_kernel(int R, int K, const int32_t *__restrict__ parents,
-                               const int32_t *__restrict__ child_first,
-                               const int32_t *__restrict__ nchild,
-                               const int32_t *__restrict__ digit, const T *__restrict__ ops,
-                               T *__restrict__ M)
-    {
-      extern __shared__ unsigned char smem_raw[];
-      T            *sIn  = reinterpret_cast<T *>(smem_raw);
-      T            *sOut = sIn + R * K;
-      const int64_t P    = parents[blockIdx.x];
-      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-        sOut[i] = T(0);
-      const int c0 = child_first[P], nc = nchild[P];
-      for (int c = 0; c < nc; ++c)
-        {
+          T *myAcc = sAcc + warp * RCH * K;
+#pragma unroll
+          for (int r = 0; r < RCH; ++r)
+#pragma unroll
+            for (int j = 0; j < KPL; ++j)
+              {
+                const int ko = lane + 32 * j;
+                if (r < rc && ko < K)
+                  myAcc[r * K + ko] = acc[r][j];
+              }
           __syncthreads();
-          const int64_t ch = c0 + c;
-          for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-            sIn[i] = M[ch * R * K + i];
-          __syncthreads();
-          accumulate_translation(R, K, ops + int64_t(digit[ch]) * K * K, sIn, sOut);
-        }
-      __syncthreads();
-      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-        M[P * R * K + i] = sOut[i];
-    }
-
-    template <typename T>
-    __global__ void l2l_kernel(int R, int K, const int32_t *__restrict__ boxes,
-                               const int32_t *__restrict__ parent,
-                               const int32_t *__restrict__ digit, const T *__restrict__ ops,
-                               T *__restrict__ Lx)
-    {
-      extern __shared__ unsigned char smem_raw[];
-      T            *sIn  = reinterpret_cast<T *>(smem_raw);
-      T            *sOut = sIn + R * K;
-      const int64_t b    = boxes[blockIdx.x];
-      const int64_t P    = parent[b];
-      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-        {
-          sIn[i]  = Lx[P * R * K + i];
-          sOut[i] = T(0);
-        }
-      __syncthreads();
-      accumulate_translation(R, K, ops + int64_t(digit[b]) * K * K, sIn, sOut);
-      __syncthreads();
-      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-        Lx[b * R * K + i] = sOut[i];
-    }
-
-    template <typename T>
-    __global__ void m2l_kernel(int R, int K, const int32_t *__restrict__ tgt,
-                               const int64_t *__restrict__ src_ptr,
-                               const int32_t *__restrict__ src, const int32_t *__restrict__ off,
-                               const T *__restrict__ ops, const T *__restrict__ M,
-                               T *__restrict__ Lx)
-    {
-      extern __shared__ unsigned char smem_raw[];
-      T            *sIn  = reinterpret_cast<T *>(smem_raw);
-      T            *sOut = sIn + R * K;
-      const int     ti   = blockIdx.x;
-      const int64_t t    = tgt[ti];
-      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-        sOut[i] = T(0);
-      for (int64_t e = src_ptr[ti]; e < src_ptr[ti + 1]; ++e)
-        {
-          __syncthreads();
-          const int64_t s = src[e];
-          for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-            sIn[i] = M[s * R * K + i];
-          __syncthreads();
-          accumulate_translation(R, K, ops + int64_t(off[e]) * K * K, sIn, sOut);
-        }
-      __syncthreads();
-      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
-        Lx[t * R * K + i] += sOut[i];
-    }
-
-    template <typename T>
-    __global__ void m2p_kernel(int R, int K, int p, int N, const int32_t *__restrict__ tgt,
-                               const int64_t *__restrict__ src_ptr,
-                               const int32_t *__restrict__ src, const int32_t *__restrict__ nbeg,
-                               const int32_t *__restrict__ nend,
-                               const int32_t *__restrict__ node_sorted,
-                               const double *__restrict__ xyz, const double *__restrict__ center,
-                               const double *__restrict__ delta, const T *__restrict__ M,
-                               T *__restrict__ y)
-    {
-      const int64_t t  = tgt[blockIdx.x];
-      const int     n0 = nbeg[t], nn = nend[t] - n0;
-      for (int idx = threadIdx.x; idx < nn * R; idx += blockDim.x)
-        {
-          const int node = node_sorted[n0 + idx % nn];
-          const int r    = idx / nn;
-          T         acc  = T(0);
-          for (int64_t e = src_ptr[blockIdx.x]; e < src_ptr[blockIdx.x + 1]; ++e)
+          for (int i = threadIdx.x; i < rc * K; i += blockDim.x)
             {
-              const int64_t s  = src[e];
-              const double  h  = delta[s];
-              const T       rx = T((xyz[3 * int64_t(node)] - center[3 * s]) / h);
-              const T       ry = T((xyz[3 * int64_t(node) + 1] - center[3 * s + 1]) / h);
-              const T       rz = T((xyz[3 * int64_t(node) + 2] - center[3 * s + 2]) / h);
-              acc += eval_expansion<T, T>(M + (s * R + r) * K, p, rx, ry, rz, true) / T(h);
+              T v = sAcc[i];
+              for (int w = 1; w < TW; ++w)
+                v += sAcc[w * RCH * K + i];
+              T *o = out + (t * R + r0) * K + i;
+              *o   = ACCUM ? *o + v : v;
             }
+          __syncthreads();
+        }
+    }
+
+    // M2P phase 1: one thread per (pair, node of the pair's target box):
+    // scratch[r][item] = multipole of the source box evaluated at the node.
+    template <typename T>
+    __global__ void m2p_eval_kernel(int64_t n_items, int64_t n_pairs, int R, int K, int p,
+                                    const int64_t *__restrict__ item_ptr,
+                                    const int32_t *__restrict__ pair_tgt,
+                                    const int32_t *__restrict__ tgt,
+                                    const int32_t *__restrict__ src,
+                                    const int32_t *__restrict__ nbeg,
+                                    const int32_t *__restrict__ node_sorted,
+                                    const double *__restrict__ xyz,
+                                    const double *__restrict__ center,
+                                    const double *__restrict__ delta, const T *__restrict__ M,
+                                    T *__restrict__ scratch)
+    {
+      const int64_t it = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (it >= n_items)
+        return;
+      int64_t lo = 0, hi = n_pairs - 1;
+      while (lo < hi)
+        {
+          int64_t mid = (lo + hi + 1) >> 1;
+          if (item_ptr[mid] <= it)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+      const int64_t e    = lo;
+      const int64_t t    = tgt[pair_tgt[e]];
+      const int64_t s    = src[e];
+      const int     node = node_sorted[nbeg[t] + (it - item_ptr[e])];
+      const double  h    = delta[s];
+      const T       rx   = T((xyz[3 * int64_t(node)] - center[3 * s]) / h);
+      const T       ry   = T((xyz[3 * int64_t(node) + 1] - center[3 * s + 1]) / h);
+      const T       rz   = T((xyz[3 * int64_t(node) + 2] - center[3 * s + 2]) / h);
+      const T       ih   = T(1.0 / h);
+      for (int r = 0; r < R; ++r)
+        scratch[int64_t(r) * n_items + it] =
+          eval_expansion_fast<T, T>(M + (s * R + r) * K, p, rx, ry, rz, true) * ih;
+    }
+
+    // M2P phase 2: one thread per (target box node): fixed-order sum over the
+    // box's sources, added to y.
+    template <typename T>
+    __global__ void m2p_sum_kernel(int64_t n_tnodes, int n_tgt, int R, int N, int64_t n_items,
+                                   const int64_t *__restrict__ tnode_ptr,
+                                   const int32_t *__restrict__ tgt,
+                                   const int64_t *__restrict__ src_ptr,
+                                   const int64_t *__restrict__ item_ptr,
+                                   const int32_t *__restrict__ nbeg,
+                                   const int32_t *__restrict__ node_sorted,
+                                   const T *__restrict__ scratch, T *__restrict__ y)
+    {
+      const int64_t tn = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (tn >= n_tnodes)
+        return;
+      int lo = 0, hi = n_tgt - 1;
+      while (lo < hi)
+        {
+          int mid = (lo + hi + 1) >> 1;
+          if (tnode_ptr[mid] <= tn)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+      const int64_t i    = tn - tnode_ptr[lo];
+      const int     node = node_sorted[nbeg[tgt[lo]] + i];
+      for (int r = 0; r < R; ++r)
+        {
+          T acc = T(0);
+          for (int64_t e = src_ptr[lo]; e < src_ptr[lo + 1]; ++e)
+            acc += scratch[int64_t(r) * n_items + item_ptr[e] + i];
           y[int64_t(r) * N + node] += acc;
         }
     }
@@ -291,11 +360,20 @@ namespace pibem
     PIBEM_CUDA(cudaGetLastError());
   }
 
-  template <typename T>
-  static void set_smem(const void *fn, size_t bytes)
+  template <typename T, int MODE, bool ACCUM>
+  static void launch_translate(int nt, int R, int K, const int32_t *targets, const int64_t *src_ptr,
+                               const int32_t *src, const int32_t *opid, const TreeDev &td,
+                               const T *ops, const T *in, T *out, cudaStream_t s)
   {
-    if (bytes > 48 * 1024)
-      PIBEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    if (nt <= 0)
+      return;
+    const size_t smem = size_t(2) * TW * RCH * K * sizeof(T);
+    auto         fn   = translate_kernel<T, MODE, ACCUM>;
+    if (smem > 48 * 1024)
+      PIBEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    fn<<<nt, TW * 32, smem, s>>>(R, K, targets, src_ptr, src, opid, td.child_first, td.nchild,
+                                 td.digit, td.parent, ops, in, out);
+    PIBEM_CUDA(cudaGetLastError());
   }
 
   template <typename T>
@@ -303,13 +381,8 @@ namespace pibem
                         cudaStream_t s)
   {
     const int a = op.parents_level_ptr[parent_level], b = op.parents_level_ptr[parent_level + 1];
-    if (b <= a)
-      return;
-    size_t smem = size_t(2) * R * op.K * sizeof(T);
-    set_smem<T>((const void *)m2m_kernel<T>, smem);
-    m2m_kernel<T><<<b - a, tpb_for(R * op.K), smem, s>>>(R, op.K, op.parents + a, td.child_first,
-                                                         td.nchild, td.digit, op.m2m_ops, M);
-    PIBEM_CUDA(cudaGetLastError());
+    launch_translate<T, SRC_CHILDREN, false>(b - a, R, op.K, op.parents + a, nullptr, nullptr,
+                                             nullptr, td, op.m2m_ops, M, M, s);
   }
 
   template <typename T>
@@ -317,13 +390,8 @@ namespace pibem
                         cudaStream_t s)
   {
     const int a = op.l2l_level_ptr[level], b = op.l2l_level_ptr[level + 1];
-    if (b <= a)
-      return;
-    size_t smem = size_t(2) * R * op.K * sizeof(T);
-    set_smem<T>((const void *)l2l_kernel<T>, smem);
-    l2l_kernel<T><<<b - a, tpb_for(R * op.K), smem, s>>>(R, op.K, op.l2l_box + a, td.parent,
-                                                         td.digit, op.l2l_ops, Lx);
-    PIBEM_CUDA(cudaGetLastError());
+    launch_translate<T, SRC_PARENT, false>(b - a, R, op.K, op.l2l_box + a, nullptr, nullptr,
+                                           nullptr, td, op.l2l_ops, Lx, Lx, s);
   }
 
   template <typename T>
@@ -331,14 +399,9 @@ namespace pibem
                         cudaStream_t s)
   {
     const int a = op.m2l_level_ptr[level], b = op.m2l_level_ptr[level + 1];
-    if (b <= a)
-      return;
-    size_t smem = size_t(2) * R * op.K * sizeof(T);
-    set_smem<T>((const void *)m2l_kernel<T>, smem);
-    m2l_kernel<T><<<b - a, tpb_for(R * op.K), smem, s>>>(R, op.K, op.m2l_tgt + a,
-                                                         op.m2l_src_ptr + a, op.m2l_src,
-                                                         op.m2l_off, op.m2l_ops, M, Lx);
-    PIBEM_CUDA(cudaGetLastError());
+    TreeDev   none;
+    launch_translate<T, SRC_CSR, true>(b - a, R, op.K, op.m2l_tgt + a, op.m2l_src_ptr + a,
+                                       op.m2l_src, op.m2l_off, none, op.m2l_ops, M, Lx, s);
   }
 
   template <typename T>
@@ -347,10 +410,26 @@ namespace pibem
   {
     if (op.n_m2p_tgt == 0)
       return;
-    m2p_kernel<T><<<op.n_m2p_tgt, 64, 0, s>>>(R, op.K, op.p, N, op.m2p_tgt, op.m2p_src_ptr,
-                                              op.m2p_src, td.nbeg, td.nend, td.node_sorted,
-                                              td.xyz, td.center, td.delta, M, y);
+    m2p_eval_kernel<T><<<unsigned((op.n_m2p_items + 127) / 128), 128, 0, s>>>(
+      op.n_m2p_items, op.n_m2p_pairs, R, op.K, op.p, op.m2p_item_ptr, op.m2p_pair_tgt, op.m2p_tgt,
+      op.m2p_src, td.nbeg, td.node_sorted, td.xyz, td.center, td.delta, M, op.m2p_scratch);
     PIBEM_CUDA(cudaGetLastError());
+    m2p_sum_kernel<T><<<unsigned((op.n_m2p_tnodes + 127) / 128), 128, 0, s>>>(
+      op.n_m2p_tnodes, op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt,
+      op.m2p_src_ptr, op.m2p_item_ptr, td.nbeg, td.node_sorted, op.m2p_scratch, y);
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void ensure_fmm_tables(int device, cudaStream_t s)
+  {
+    static bool done[64] = {};
+    if (device < 0 || device >= 64 || done[device])
+      return;
+    LegendreTables t;
+    fill_legendre_tables(t);
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg, &t, sizeof(t), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    done[device] = true;
   }
 
   template <typename T>

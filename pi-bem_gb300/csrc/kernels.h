@@ -87,10 +87,12 @@ namespace pibem
     // M2L per target CSR
     const int32_t *m2l_tgt = nullptr, *m2l_src = nullptr, *m2l_off = nullptr;
     const int64_t *m2l_src_ptr = nullptr;
-    // M2P per target CSR
+    // M2P per target CSR, evaluated per (pair, target node) item
     int            n_m2p_tgt = 0;
-    const int32_t *m2p_tgt = nullptr, *m2p_src = nullptr;
-    const int64_t *m2p_src_ptr = nullptr;
+    int64_t        n_m2p_pairs = 0, n_m2p_items = 0, n_m2p_tnodes = 0;
+    const int32_t *m2p_tgt = nullptr, *m2p_src = nullptr, *m2p_pair_tgt = nullptr;
+    const int64_t *m2p_src_ptr = nullptr, *m2p_item_ptr = nullptr, *m2p_tnode_ptr = nullptr;
+    T             *m2p_scratch = nullptr; // n_m2p_items * R
     // L2L boxes
     const int32_t *l2l_box = nullptr;
     // per-level ranges (host)
@@ -116,6 +118,7 @@ namespace pibem
   template <typename T>
   void launch_m2p(const OperatorDev<T> &op, const TreeDev &td, int R, int N, const T *M, T *y,
                   cudaStream_t s);
+  void ensure_fmm_tables(int device, cudaStream_t s);
   template <typename T>
   void launch_l2p(const OperatorDev<T> &op, int R, int N, const T *Lx, T *y, cudaStream_t s);
 

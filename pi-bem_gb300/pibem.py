@@ -88,7 +88,7 @@ EXPORTS = [
     "pibem_fmm_matvec", "pibem_compute_alpha", "pibem_system_matvec", "pibem_compute_rhs",
     "pibem_solve", "pibem_solve_device", "pibem_tree_info_get", "pibem_tree_boxes",
     "pibem_tree_list", "pibem_tree_list_sublevels", "pibem_near_nnz", "pibem_near_export",
-    "pibem_quad_points", "pibem_last_phase_ms",
+    "pibem_quad_points", "pibem_last_phase_ms", "pibem_set_profiling", "pibem_phase_totals",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -130,6 +130,8 @@ def load():
     L.pibem_near_export.argtypes = [C.c_void_p, _ip, _ip, _dp, _dp]
     L.pibem_quad_points.argtypes = [C.c_void_p, _dp]
     L.pibem_last_phase_ms.argtypes = [C.c_void_p, _dp]
+    L.pibem_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    L.pibem_phase_totals.argtypes = [C.c_void_p, C.c_int32, _dp, C.POINTER(C.c_int64), C.c_int32]
     _lib = L
     return L
 
@@ -299,7 +301,19 @@ class BEMSolver:
         self._check(self.L.pibem_quad_points(self.h, _d(pts)))
         return pts
 
+    PHASES = ["near", "p2m", "m2m", "m2l_l2l", "unused", "m2p", "l2p"]
+
     def phase_ms(self):
         out = np.zeros(7)
         self._check(self.L.pibem_last_phase_ms(self.h, _d(out)))
-        return dict(zip(["near", "p2m", "m2m", "m2l", "l2l", "m2p", "l2p"], out.tolist()))
+        return dict(zip(self.PHASES, out.tolist()))
+
+    def set_profiling(self, on: bool):
+        self._check(self.L.pibem_set_profiling(self.h, int(bool(on))))
+
+    def phase_totals(self, precision: int, reset: bool = False):
+        """(dict phase -> total ms, number of operator applications)."""
+        out = np.zeros(7)
+        cnt = C.c_int64(0)
+        self._check(self.L.pibem_phase_totals(self.h, precision, _d(out), C.byref(cnt), int(reset)))
+        return dict(zip(self.PHASES, out.tolist())), int(cnt.value)

@@ -5,8 +5,10 @@ Tolerances (FP64 path):
   quadrature points, octree boxes and lists      bit-exact / identical sets
   near-field N and D entries                     1e-12 relative to the largest entry
   FMM matvec (BEMFMA parity), alpha, vmult, rhs  1e-10 relative (2-norm)
-  solution of the solve vs the oracle solve      1e-7 relative, residual <= 1e-8
-Mixed path: solution within 1e-7 of the FP64 path at residual 1e-8.
+  solve, both driven to residual 1e-11           1e-8 relative
+  solve at the working residual 1e-8             residual met; 1e-5 relative
+                                                 (cond(A) * 1e-8 with cond(A) < 1e3)
+Mixed path: same bounds against the FP64 path.
 """
 import numpy as np
 import pytest
@@ -123,37 +125,57 @@ def test_alpha_rhs_vmult_match_oracle(case):
     assert rel(g.system_matvec(x), o.system_matvec(ao, x)) < 1e-10
 
 
-def test_solve_fp64_matches_oracle(case):
-    o, g = case["oracle"], case["gpu"]
-    po, do, its_o, res_o = o.solve(case["tmp"], tol=1e-10, max_steps=3000)
-    pg, dg, st = g.solve(case["tmp"])
+def _solver(pibem_mod, case, **kw):
+    m = case["mesh"]
+    g = pibem_mod.BEMSolver(fma_truncation_order=case["p"], num_octree_levels=case["levels"],
+                            max_nodes_per_childless_block=case["leaf"],
+                            is_external_flow=int(case["ext"]), solver_max_steps=4000, **kw)
+    g.set_mesh(m.xyz, m.cells)
+    g.set_bc(case["mask"])
+    return g
+
+
+def _sol(case, phi, dphi):
+    return np.where(case["mask"] == 1, dphi, phi)
+
+
+def test_solve_fp64_matches_oracle(case, pibem_mod):
+    """Arithmetic parity of the whole solve: GPU and oracle both driven to a
+    relative residual of 1e-11 agree to 1e-8; at the working tolerance 1e-8 the
+    GPU residual is met and the solution is within cond(A) * 1e-8 of it."""
+    o = case["oracle"]
+    po, do, its_o, res_o = o.solve(case["tmp"], tol=1e-11, max_steps=4000)
+    assert res_o <= 1e-11
+    tight = _solver(pibem_mod, case, solver_tolerance=1e-11)
+    pt, dt, st = tight.solve(case["tmp"])
+    assert st["relative_residual"] <= 1e-11
+    assert rel(_sol(case, pt, dt), _sol(case, po, do)) < 1e-8
+    pg, dg, st = case["gpu"].solve(case["tmp"])
     assert st["relative_residual"] <= 1e-8
-    so = np.where(case["mask"] == 1, do, po)
-    sg = np.where(case["mask"] == 1, dg, pg)
-    assert rel(sg, so) < 1e-7, rel(sg, so)
+    assert rel(_sol(case, pg, dg), _sol(case, po, do)) < 1e-5
     # known entries are left untouched
     assert np.array_equal(np.where(case["mask"] == 1, pg, 0), np.where(case["mask"] == 1, case["tmp"], 0))
     if case["exact"] is not None:
         # discretisation error against the analytic dphi/dn (p=4 FMM, 1538 nodes)
         assert rel(dg, case["exact"]) < 2e-2
+    tight.close()
 
 
 def test_solve_mixed_matches_fp64(case, pibem_mod):
-    m = case["mesh"]
-    g2 = pibem_mod.BEMSolver(fma_truncation_order=case["p"], num_octree_levels=case["levels"],
-                             max_nodes_per_childless_block=case["leaf"],
-                             is_external_flow=int(case["ext"]), solver_tolerance=1e-8,
-                             precision_mode=pibem_mod.PRECISION_MIXED, solver_max_steps=2000)
-    g2.set_mesh(m.xyz, m.cells)
-    g2.set_bc(case["mask"])
-    p64, d64, _ = case["gpu"].solve(case["tmp"])
-    p32, d32, st = g2.solve(case["tmp"])
+    """FP32 operator + FP64 refinement: reaches the FP64 solution (both at
+    residual 1e-11: 1e-8 apart) and meets residual 1e-8 at the working tolerance."""
+    ref = _solver(pibem_mod, case, solver_tolerance=1e-11)
+    mix_t = _solver(pibem_mod, case, solver_tolerance=1e-11, precision_mode=pibem_mod.PRECISION_MIXED)
+    p64, d64, _ = ref.solve(case["tmp"])
+    p32, d32, st = mix_t.solve(case["tmp"])
+    assert st["relative_residual"] <= 1e-11 and st["fp32_matvecs"] > 0
+    assert rel(_sol(case, p32, d32), _sol(case, p64, d64)) < 1e-8
+    mix = _solver(pibem_mod, case, solver_tolerance=1e-8, precision_mode=pibem_mod.PRECISION_MIXED)
+    p, d, st = mix.solve(case["tmp"])
     assert st["relative_residual"] <= 1e-8
-    assert st["fp32_matvecs"] > 0
-    s64 = np.where(case["mask"] == 1, d64, p64)
-    s32 = np.where(case["mask"] == 1, d32, p32)
-    assert rel(s32, s64) < 1e-7, rel(s32, s64)
-    g2.close()
+    assert rel(_sol(case, p, d), _sol(case, p64, d64)) < 1e-5
+    for g in (ref, mix_t, mix):
+        g.close()
 
 
 def test_batched_solve_equals_single(case):
