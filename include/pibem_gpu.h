@@ -162,6 +162,8 @@ int pibem_set_profiling(pibem_handle *h, int32_t on);
  * PIBEM_PRECISION_MIXED: FP32 operator) since the last reset, and their count. */
 int pibem_phase_totals(pibem_handle *h, int32_t precision, double *ms7, int64_t *applications,
                        int32_t reset);
+/* Number of CUDA kernels this library has launched so far (all handles). */
+int64_t pibem_launch_count(void);
 
 #ifdef __cplusplus
 }

@@ -11,6 +11,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
@@ -23,6 +24,14 @@
 #include "pibem_internal.h"
 
 using namespace pibem;
+
+static std::atomic<int64_t> g_launches{0};
+
+namespace pibem
+{
+  void    note_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+  int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+} // namespace pibem
 
 namespace
 {
@@ -39,9 +48,9 @@ namespace
       return;
     int     leaf = row_leaf[row];
     int64_t r0 = row_ptr[leaf], nr = row_ptr[leaf + 1] - r0, r = row - r0;
-    int64_t nc = col_ptr[leaf + 1] - col_ptr[leaf];
+    int64_t ld = (col_ptr[leaf + 1] - col_ptr[leaf] + 3) / 4 * 4;
     for (int64_t c = 0; c < nr; ++c)
-      B[blk_ptr[leaf] + r * nr + c] = S[val_ptr[leaf] + r * nc + diag_col[r0 + c]];
+      B[blk_ptr[leaf] + r * nr + c] = S[val_ptr[leaf] + r * ld + diag_col[r0 + c]];
   }
 
   // Gauss-Jordan inverse with partial pivoting (host, small dense blocks).
@@ -122,13 +131,15 @@ struct pibem_handle
   DBuf<double>  d_center, d_delta;
   // plan
   DBuf<int64_t> d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr,
-    d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr;
+    d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr,
+    d_up_q_ptr, d_down_q_ptr;
   DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
-    d_parents, d_diag_col, d_m2p_pair_tgt;
+    d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
+    d_down_box, d_up_q, d_down_q;
   DBuf<NearEntry> d_entries;
-  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_m2m, d_l2l, d_m2l, d_Pinv;
-  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_m2mf, d_l2lf, d_m2lf;
+  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv;
+  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf;
   std::vector<int64_t> blk_ptr;
   OperatorDev<double> op64;
   OperatorDev<float>  op32;
@@ -139,8 +150,8 @@ struct pibem_handle
   DBuf<double>         d_alpha;
   bool                 have_dirichlet = true;
   // work
-  DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64;
-  DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32;
+  DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64;
+  DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32, d_Y32;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
   // timing
   bool        timing = false;
@@ -201,8 +212,9 @@ namespace
   // ---------------------------------------------------------------------
   template <typename T>
   void far_field(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
-                 int R, const uint8_t *modes, const T *x, T *y)
+                 DBuf<T> &Y, int R, const uint8_t *modes, const T *x, T *y)
   {
+    Y.alloc(std::max<size_t>(1, size_t(op.n_pairs) * R * op.K));
     const int    N = int(h->N());
     const size_t need = size_t(h->tree.nb) * R * op.K;
     if (M.n < need)
@@ -213,18 +225,15 @@ namespace
     scr.alloc(std::max<size_t>(1, size_t(op.n_m2p_items) * R));
     op.m2p_scratch = scr.p;
     cudaStream_t s = h->stream;
-    PIBEM_CUDA(cudaMemsetAsync(Lx.p, 0, need * sizeof(T), s));
     PIBEM_CUDA(cudaMemsetAsync(M.p, 0, need * sizeof(T), s));
     launch_p2m_apply<T>(op, R, N, h->d_dir.p, modes, x, M.p, s);
     record(h, 2);
-    for (int pl = h->tree.L - 1; pl >= 0; --pl)
-      launch_m2m_level<T>(op, h->td, R, pl, M.p, s);
+    for (int l = h->tree.L; l >= 1; --l)
+      launch_upward_level<T>(op, R, l, M.p, Y.p, s);
     record(h, 3);
+    launch_m2l_gemm<T>(op, R, M.p, Y.p, s);
     for (int l = 1; l <= h->tree.L; ++l)
-      {
-        launch_l2l_level<T>(op, h->td, R, l, Lx.p, s);
-        launch_m2l_level<T>(op, R, l, M.p, Lx.p, s);
-      }
+      launch_downward_level<T>(op, R, l, Lx.p, Y.p, s);
     record(h, 4);
     record(h, 5);
     launch_m2p<T>(op, h->td, R, N, M.p, y, s);
@@ -272,7 +281,7 @@ namespace
     launch_near_spmv<double>(h->op64, R, int(N), h->d_D.p, h->d_x64.p + R * N,
                              h->d_y64.p + R * N, false, s);
     record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, 2 * R, h->d_modes.p,
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, 2 * R, h->d_modes.p,
                       h->d_x64.p, h->d_y64.p);
     finish_timing(h, 0);
     PIBEM_CUDA(cudaMemcpyAsync(oN, h->d_y64.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
@@ -290,7 +299,7 @@ namespace
     record(h, 0);
     launch_near_spmv<double>(h->op64, 1, int(N), h->d_N.p, x, y, false, h->stream);
     record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, 1, h->d_modes.p, x, y);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, 1, h->d_modes.p, x, y);
     finish_timing(h, 0);
   }
 
@@ -334,7 +343,7 @@ namespace
     record(h, 0);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_S.p, xin, y, false, s);
     record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, R, h->d_modes.p, xin, y);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, xin, y);
     finish_timing(h, 0);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
@@ -361,7 +370,7 @@ namespace
     record(h, 0);
     launch_near_spmv<float>(h->op32, R, int(N), h->d_S32.p, h->d_x32.p, h->d_y32.p, false, s);
     record(h, 1);
-    far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, R, h->d_modes.p, h->d_x32.p,
+    far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, h->d_Y32, R, h->d_modes.p, h->d_x32.p,
                      h->d_y32.p);
     finish_timing(h, 1);
     launch_convert_f2d(int64_t(R) * N, h->d_y32.p, y, s);
@@ -563,6 +572,7 @@ namespace
         nrows, h->d_row_leaf.p, h->d_nrow_ptr.p, h->d_ncol_ptr.p, h->d_nval_ptr.p, h->d_blk_ptr.p,
         h->d_diag_col.p, h->d_S.p, blocks.p);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
     std::vector<double> hb(h->blk_ptr[nl]), inv(h->blk_ptr[nl]);
     blocks.download(hb.data(), hb.size(), s);
     PIBEM_CUDA(cudaStreamSynchronize(s));
@@ -597,10 +607,25 @@ namespace
       op.pleaf_box     = h->d_pleaf_box.p;
       op.prow_dof      = h->d_prow_dof.p;
       op.lleaf_box     = h->d_lleaf_box.p;
-      op.m2l_tgt       = h->d_m2l_tgt.p;
-      op.m2l_src       = h->d_m2l_src.p;
-      op.m2l_off       = h->d_m2l_off.p;
-      op.m2l_src_ptr   = h->d_m2l_src_ptr.p;
+      op.q_src         = h->d_q_src.p;
+      op.ch_start      = h->d_ch_start.p;
+      op.ch_cnt        = h->d_ch_cnt.p;
+      op.ch_op         = h->d_ch_op.p;
+      op.m2l_chunk_end = pl.m2l_chunk_end;
+      op.up_chunk_ptr  = pl.up_chunk_ptr;
+      op.down_chunk_ptr = pl.down_chunk_ptr;
+      op.up_box_ptr    = pl.up_box_ptr;
+      op.down_box_ptr  = pl.down_box_ptr;
+      op.up_box        = h->d_up_box.p;
+      op.down_box      = h->d_down_box.p;
+      op.up_q          = h->d_up_q.p;
+      op.down_q        = h->d_down_q.p;
+      op.up_q_ptr      = h->d_up_q_ptr.p;
+      op.down_q_ptr    = h->d_down_q_ptr.p;
+      op.n_pairs       = int64_t(pl.q_src.size());
+      op.max_near_cols = 0;
+      for (size_t k2 = 0; k2 + 1 < pl.ncol_ptr.size(); ++k2)
+        op.max_near_cols = std::max<int64_t>(op.max_near_cols, pl.ncol_ptr[k2 + 1] - pl.ncol_ptr[k2]);
       op.n_m2p_tgt     = int(pl.m2p_tgt.size());
       op.n_m2p_pairs   = int64_t(pl.m2p_src.size());
       op.n_m2p_items   = h->m2p_items;
@@ -611,42 +636,17 @@ namespace
       op.m2p_pair_tgt  = h->d_m2p_pair_tgt.p;
       op.m2p_item_ptr  = h->d_m2p_item_ptr.p;
       op.m2p_tnode_ptr = h->d_m2p_tnode_ptr.p;
-      op.l2l_box       = h->d_l2l_box.p;
-      op.m2l_level_ptr = pl.m2l_tgt_ptr_level;
-      op.l2l_level_ptr = pl.l2l_ptr_level;
-      op.parents       = h->d_parents.p;
     };
     fill(h->op64);
     fill(h->op32);
     h->op64.T1      = h->d_T1.p;
     h->op64.T2      = h->d_T2.p;
     h->op64.W       = h->d_W.p;
-    h->op64.m2m_ops = h->d_m2m.p;
-    h->op64.l2l_ops = h->d_l2l.p;
-    h->op64.m2l_ops = h->d_m2l.p;
+    h->op64.ops     = h->d_ops.p;
     h->op32.T1      = h->d_T1f.p;
     h->op32.T2      = h->d_T2f.p;
     h->op32.W       = h->d_Wf.p;
-    h->op32.m2m_ops = h->d_m2mf.p;
-    h->op32.l2l_ops = h->d_l2lf.p;
-    h->op32.m2l_ops = h->d_m2lf.p;
-    // parents grouped by their level
-    std::vector<int32_t> parents;
-    std::vector<int>     pptr(h->tree.L + 2, 0);
-    for (int l = 0; l <= h->tree.L; ++l)
-      {
-        pptr[l] = int(parents.size());
-        int a = l == 0 ? 0 : h->tree.startLevel[l], b = l == 0 ? 0 : h->tree.endLevel[l];
-        for (int bx = a; bx <= b; ++bx)
-          if (h->tree.nchild[bx] > 0)
-            parents.push_back(bx);
-      }
-    pptr[h->tree.L + 1] = int(parents.size());
-    h->d_parents.upload(parents, h->stream);
-    h->op64.parents_level_ptr = pptr;
-    h->op32.parents_level_ptr = pptr;
-    h->op64.parents           = h->d_parents.p;
-    h->op32.parents           = h->d_parents.p;
+    h->op32.ops     = h->d_opsf.p;
     TreeDev &td               = h->td;
     td.nb                     = h->tree.nb;
     td.N                      = int(h->N());
@@ -682,7 +682,8 @@ namespace
         int64_t nr = pl.nrow_ptr[k + 1] - pl.nrow_ptr[k], nc = pl.ncol_ptr[k + 1] - pl.ncol_ptr[k],
                 ne = pl.nent_ptr[k + 1] - pl.nent_ptr[k];
         need(nr > 0 && nc > 0 && ne > 0, "empty near leaf");
-        need(pl.nval_ptr[k + 1] - pl.nval_ptr[k] == nr * nc, "near value block size");
+        need(pl.nval_ptr[k + 1] - pl.nval_ptr[k] == nr * ((nc + 3) / 4 * 4), "near value block size");
+        need(pl.nval_ptr[k] % 4 == 0, "near value block alignment");
         need(pl.nleaf_box[k] >= 0 && pl.nleaf_box[k] < t.nb, "near leaf box");
         for (int64_t e = pl.nent_ptr[k]; e < pl.nent_ptr[k + 1]; ++e)
           {
@@ -718,6 +719,29 @@ namespace
     for (int32_t v : pl.pcontrib_q)
       need(v >= 0 && int64_t(v) < 4 * Q, "p2m contribution");
     const int noff = int(pl.offsets.size() / 3);
+    const int64_t nq_pairs = int64_t(pl.q_src.size());
+    need(pl.q_op.size() == size_t(nq_pairs), "pair arrays");
+    for (size_t i = 0; i < pl.q_src.size(); ++i)
+      need(pl.q_src[i] >= 0 && pl.q_src[i] < t.nb && pl.q_op[i] >= 0 && pl.q_op[i] < noff + 16,
+           "translation pair");
+    for (size_t ch = 0; ch < pl.ch_start.size(); ++ch)
+      {
+        need(pl.ch_cnt[ch] > 0 && pl.ch_cnt[ch] <= 64 && pl.ch_start[ch] >= 0 &&
+               int64_t(pl.ch_start[ch]) + pl.ch_cnt[ch] <= nq_pairs,
+             "translation chunk");
+        for (int i = 0; i < pl.ch_cnt[ch]; ++i)
+          need(pl.q_op[pl.ch_start[ch] + i] == pl.ch_op[ch], "chunk operator");
+      }
+    need(pl.up_q_ptr.size() == pl.up_box.size() + 1 && pl.down_q_ptr.size() == pl.down_box.size() + 1,
+         "gather sizes");
+    for (int32_t v : pl.up_box)
+      need(v >= 0 && v < t.nb, "up box");
+    for (int32_t v : pl.down_box)
+      need(v >= 0 && v < t.nb, "down box");
+    for (int32_t v : pl.up_q)
+      need(v >= 0 && v < nq_pairs, "up pair");
+    for (int32_t v : pl.down_q)
+      need(v >= 0 && v < nq_pairs, "down pair");
     need(pl.m2l_src_ptr.size() == pl.m2l_tgt.size() + 1, "m2l ptr");
     for (size_t i = 0; i < pl.m2l_src.size(); ++i)
       need(pl.m2l_src[i] >= 0 && pl.m2l_src[i] < t.nb && pl.m2l_off[i] >= 0 && pl.m2l_off[i] < noff,
@@ -729,8 +753,6 @@ namespace
       need(v >= 0 && v < t.nb && t.nend[v] > t.nbeg[v], "m2p target");
     for (int32_t v : pl.m2p_src)
       need(v >= 0 && v < t.nb, "m2p source");
-    for (int32_t v : pl.l2l_box)
-      need(v > 0 && v < t.nb && t.level[v] >= 2, "l2l box");
     for (int b = 1; b < t.nb; ++b)
       need(t.parent[b] >= 0 && t.parent[b] < b && t.digit[b] >= 0 && t.digit[b] < 8, "box parent");
     for (int b = 0; b < t.nb; ++b)
@@ -859,7 +881,16 @@ namespace
     h->d_m2p_tgt.upload(pl.m2p_tgt, s);
     h->d_m2p_src_ptr.upload(pl.m2p_src_ptr, s);
     h->d_m2p_src.upload(pl.m2p_src, s);
-    h->d_l2l_box.upload(pl.l2l_box, s);
+    h->d_q_src.upload(pl.q_src, s);
+    h->d_ch_start.upload(pl.ch_start, s);
+    h->d_ch_cnt.upload(pl.ch_cnt, s);
+    h->d_ch_op.upload(pl.ch_op, s);
+    h->d_up_box.upload(pl.up_box, s);
+    h->d_down_box.upload(pl.down_box, s);
+    h->d_up_q.upload(pl.up_q, s);
+    h->d_down_q.upload(pl.down_q, s);
+    h->d_up_q_ptr.upload(pl.up_q_ptr, s);
+    h->d_down_q_ptr.upload(pl.down_q_ptr, s);
     // M2P work items: one per (pair, node of the pair's target box)
     {
       const size_t         nt = pl.m2p_tgt.size();
@@ -908,6 +939,8 @@ namespace
       const int64_t nval = pl.nval_ptr[nl];
       h->d_N.alloc(nval);
       h->d_D.alloc(nval);
+      h->d_N.zero(s);
+      h->d_D.zero(s);
       DBuf<double> staging;
       int64_t      st_items = std::min<int64_t>(item_ptr[nl], int64_t(1) << 24);
       int64_t      maxrow   = 0;
@@ -952,16 +985,19 @@ namespace
     // P2M and L2P tables
     {
       const int64_t nrows_p = int64_t(pl.prow_dof.size());
-      h->d_T1.alloc(nrows_p * K);
-      h->d_T2.alloc(nrows_p * K);
+      const int64_t K4      = (K + 3) / 4 * 4;
+      h->d_T1.alloc(nrows_p * K4);
+      h->d_T2.alloc(nrows_p * K4);
+      h->d_T1.zero(s);
+      h->d_T2.zero(s);
       launch_p2m_tables(nrows_p, K, pl.p, int(pl.pleaf_box.size()), h->d_prow_ptr.p,
                         h->d_pleaf_box.p, h->d_pcontrib_ptr.p, h->d_pcontrib_q.p, h->d_center.p,
                         h->d_delta.p, h->d_qpts.p, h->d_qnrm.p, h->d_qjxw.p, h->d_qshape.p,
                         h->d_T1.p, h->d_T2.p, s);
-      h->d_T1f.alloc(nrows_p * K);
-      h->d_T2f.alloc(nrows_p * K);
-      launch_convert_d2f(nrows_p * K, h->d_T1.p, h->d_T1f.p, s);
-      launch_convert_d2f(nrows_p * K, h->d_T2.p, h->d_T2f.p, s);
+      h->d_T1f.alloc(nrows_p * K4);
+      h->d_T2f.alloc(nrows_p * K4);
+      launch_convert_d2f(nrows_p * K4, h->d_T1.p, h->d_T1f.p, s);
+      launch_convert_d2f(nrows_p * K4, h->d_T2.p, h->d_T2f.p, s);
       const int64_t npos = int64_t(pl.lnode_ids.size());
       h->d_W.alloc(npos * K);
       launch_l2p_tables(npos, K, int(pl.lleaf_box.size()), h->d_nrow_ptr.p, h->d_lleaf_box.p,
@@ -980,20 +1016,18 @@ namespace
       for (int o = 0; o < nof; ++o)
         build_m2l_op(pl.p, pl.offsets[3 * o], pl.offsets[3 * o + 1], pl.offsets[3 * o + 2],
                      &m2l[size_t(o) * K * K]);
+      // concatenated table [M2L offsets | 8 M2M | 8 L2L], [in][out] per operator
+      const int nops = nof + 16;
+      std::vector<double> all(size_t(nops) * K * K);
+      std::copy(m2l.begin(), m2l.begin() + size_t(nof) * K * K, all.begin());
+      std::copy(m2m.begin(), m2m.end(), all.begin() + size_t(nof) * K * K);
+      std::copy(l2l.begin(), l2l.end(), all.begin() + size_t(nof + 8) * K * K);
       std::vector<double> td;
       std::vector<float>  tf;
-      transpose_ops(m2m, 8, K, td);
-      h->d_m2m.upload(td, s);
-      transpose_ops(m2m, 8, K, tf);
-      h->d_m2mf.upload(tf, s);
-      transpose_ops(l2l, 8, K, td);
-      h->d_l2l.upload(td, s);
-      transpose_ops(l2l, 8, K, tf);
-      h->d_l2lf.upload(tf, s);
-      transpose_ops(m2l, std::max(nof, 1), K, td);
-      h->d_m2l.upload(td, s);
-      transpose_ops(m2l, std::max(nof, 1), K, tf);
-      h->d_m2lf.upload(tf, s);
+      transpose_ops(all, nops, K, td);
+      h->d_ops.upload(td, s);
+      transpose_ops(all, nops, K, tf);
+      h->d_opsf.upload(tf, s);
       PIBEM_CUDA(cudaStreamSynchronize(s));
     }
     fill_operator_views(h);
@@ -1007,7 +1041,7 @@ namespace
     PIBEM_CUDA(cudaStreamSynchronize(s));
     h->bytes_resident = h->d_N.bytes() * 3 + h->d_S32.bytes() + h->d_T1.bytes() * 2 +
                         h->d_T1f.bytes() * 2 + h->d_W.bytes() + h->d_Wf.bytes() +
-                        h->d_m2l.bytes() + h->d_m2lf.bytes() + h->d_qpts.bytes() * 2 +
+                        h->d_ops.bytes() + h->d_opsf.bytes() + h->d_qpts.bytes() * 2 +
                         h->d_qshape.bytes() + h->d_qjxw.bytes();
     if (P.hbm_budget_gb > 0 && double(h->bytes_resident) > P.hbm_budget_gb * 1e9)
       throw Error(PIBEM_ENOMEM_HBM, "resident operator exceeds the HBM budget");
@@ -1389,7 +1423,7 @@ extern "C"
       info->n_leaves      = int(h->tree.childless.size());
       info->n_m2l_pairs   = h->plan.n_m2l;
       info->n_m2p_pairs   = h->plan.n_m2p;
-      info->near_nnz      = h->plan.nval_ptr.back();
+      info->near_nnz      = pibem_near_nnz(h);
       info->p2m_rows      = int64_t(h->plan.prow_dof.size());
       info->n_quad_points = h->mesh.n_cells * h->nq;
       info->n_m2l_offsets = int(h->plan.offsets.size() / 3);
@@ -1443,8 +1477,12 @@ extern "C"
   {
     if (!h || !h->mesh_ok)
       return -1;
-    // distinct (row, col) pairs = sum of leaf block sizes
-    return h->plan.nval_ptr.back();
+    // distinct (row, col) pairs = sum of leaf block sizes (without row padding)
+    const Plan &pl = h->plan;
+    int64_t     s  = 0;
+    for (size_t k = 0; k + 1 < pl.nrow_ptr.size(); ++k)
+      s += (pl.nrow_ptr[k + 1] - pl.nrow_ptr[k]) * (pl.ncol_ptr[k + 1] - pl.ncol_ptr[k]);
+    return s;
   }
 
   int pibem_near_export(pibem_handle *h, int32_t *rows, int32_t *cols, double *Nout, double *Dout)
@@ -1458,19 +1496,20 @@ extern "C"
       h->d_N.download(Nv.data(), nv, h->stream);
       h->d_D.download(Dv.data(), nv, h->stream);
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+      const int64_t nnz = pibem_near_nnz(h);
       // rows sorted globally: collect (row, col, idx) and sort
       std::vector<std::pair<std::pair<int, int>, int64_t>> all;
       all.reserve(nv);
       for (size_t k = 0; k + 1 < pl.nrow_ptr.size(); ++k)
         {
-          int64_t nc = pl.ncol_ptr[k + 1] - pl.ncol_ptr[k];
+          int64_t nc = pl.ncol_ptr[k + 1] - pl.ncol_ptr[k], ld = (nc + 3) / 4 * 4;
           for (int64_t r = pl.nrow_ptr[k]; r < pl.nrow_ptr[k + 1]; ++r)
             for (int64_t c = 0; c < nc; ++c)
               all.push_back({{pl.nrows[r], pl.ncols[pl.ncol_ptr[k] + c]},
-                             pl.nval_ptr[k] + (r - pl.nrow_ptr[k]) * nc + c});
+                             pl.nval_ptr[k] + (r - pl.nrow_ptr[k]) * ld + c});
         }
       std::sort(all.begin(), all.end());
-      for (int64_t i = 0; i < nv; ++i)
+      for (int64_t i = 0; i < nnz; ++i)
         {
           rows[i] = all[i].first.first;
           cols[i] = all[i].first.second;
@@ -1489,6 +1528,8 @@ extern "C"
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
     });
   }
+
+  int64_t pibem_launch_count(void) { return launch_count(); }
 
   int pibem_set_profiling(pibem_handle *h, int32_t on)
   {

@@ -25,209 +25,257 @@ namespace pibem
       return v;
     }
 
-    template <typename T>
-    __global__ void near_spmv_kernel(int64_t n_rows, int R, int N, const int32_t *__restrict__ row_leaf,
-                                     const int64_t *__restrict__ nrow_ptr,
-                                     const int64_t *__restrict__ ncol_ptr,
-                                     const int64_t *__restrict__ nval_ptr,
-                                     const int32_t *__restrict__ nrows,
-                                     const int32_t *__restrict__ ncols,
-                                     const T *__restrict__ vals, const T *__restrict__ x,
-                                     T *__restrict__ y, bool acc)
+    // 4-wide loads from 16-byte aligned rows.
+    __device__ inline void load4(const float *p, float (&v)[4])
     {
-      const int64_t row  = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-      const int     lane = threadIdx.x & 31;
-      if (row >= n_rows)
-        return;
-      const int     leaf = row_leaf[row];
-      const int64_t r    = row - nrow_ptr[leaf];
-      const int64_t c0   = ncol_ptr[leaf];
-      const int64_t nc   = ncol_ptr[leaf + 1] - c0;
-      const T      *v    = vals + nval_ptr[leaf] + r * nc;
-      const int     node = nrows[row];
-      for (int r0 = 0; r0 < R; r0 += RC)
+      const float4 t = *reinterpret_cast<const float4 *>(p);
+      v[0] = t.x;
+      v[1] = t.y;
+      v[2] = t.z;
+      v[3] = t.w;
+    }
+    __device__ inline void load4(const double *p, double (&v)[4])
+    {
+      const double2 a = *reinterpret_cast<const double2 *>(p);
+      const double2 b = *reinterpret_cast<const double2 *>(p + 2);
+      v[0] = a.x;
+      v[1] = a.y;
+      v[2] = b.x;
+      v[3] = b.y;
+    }
+
+    // Near-field leaf-block SpMV: one block per childless box.  The x entries of
+    // the block's columns are gathered once into shared memory (rb rhs at a
+    // time, zero in the row padding), then each warp streams whole rows of the
+    // dense leaf block with 16-byte loads (rows padded to 4 values).
+    template <typename T>
+    __global__ void __launch_bounds__(256)
+      near_leaf_kernel(int R, int rb, int N, const int64_t *__restrict__ nrow_ptr,
+                       const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
+                       const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
+                       const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y,
+                       bool acc)
+    {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      T            *sx   = reinterpret_cast<T *>(smem_raw); // [rb][ld]
+      const int     leaf = blockIdx.x;
+      const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
+      const int64_t ld = (nc + 3) / 4 * 4;
+      const int64_t r0 = nrow_ptr[leaf], nr = nrow_ptr[leaf + 1] - r0;
+      const T      *V    = vals + nval_ptr[leaf];
+      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      const int     n4   = int(ld / 4);
+      for (int ra = 0; ra < R; ra += rb)
         {
-          T s[RC];
-#pragma unroll
-          for (int j = 0; j < RC; ++j)
-            s[j] = T(0);
-          for (int64_t c = lane; c < nc; c += 32)
+          const int rc = min(rb, R - ra);
+          __syncthreads();
+          for (int64_t i = threadIdx.x; i < rc * ld; i += blockDim.x)
             {
-              const T   a   = v[c];
-              const int col = ncols[c0 + c];
-#pragma unroll
-              for (int j = 0; j < RC; ++j)
-                if (r0 + j < R)
-                  s[j] += a * x[int64_t(r0 + j) * N + col];
+              const int64_t r = i / ld, c = i - r * ld;
+              sx[i]           = c < nc ? x[(ra + r) * int64_t(N) + ncols[c0 + c]] : T(0);
             }
+          __syncthreads();
+          for (int64_t row = warp; row < nr; row += nw)
+            {
+              const T  *v    = V + row * ld;
+              const int node = nrows[r0 + row];
+              for (int rq = 0; rq < rc; rq += 4)
+                {
+                  T s[4] = {T(0), T(0), T(0), T(0)};
+                  for (int j = lane; j < n4; j += 32)
+                    {
+                      T a[4];
+                      load4(v + 4 * j, a);
 #pragma unroll
-          for (int j = 0; j < RC; ++j)
-            s[j] = warp_sum(s[j]);
-          if (lane == 0)
-            for (int j = 0; j < RC && r0 + j < R; ++j)
-              {
-                T &o = y[int64_t(r0 + j) * N + node];
-                o    = acc ? o + s[j] : s[j];
-              }
+                      for (int rr = 0; rr < 4; ++rr)
+                        if (rq + rr < rc)
+                          {
+                            const T *xs = sx + (rq + rr) * ld + 4 * j;
+                            s[rr] += a[0] * xs[0] + a[1] * xs[1] + a[2] * xs[2] + a[3] * xs[3];
+                          }
+                    }
+#pragma unroll
+                  for (int rr = 0; rr < 4; ++rr)
+                    if (rq + rr < rc)
+                      {
+                        const T t = warp_sum(s[rr]);
+                        if (lane == 0)
+                          {
+                            T &o = y[(ra + rq + rr) * int64_t(N) + node];
+                            o    = acc ? o + t : t;
+                          }
+                      }
+                }
+            }
         }
     }
 
+    // P2M apply: M^[leaf][r][k] = sum_rows w(row, r) T[row][k] x_r[dof(row)],
+    // w selecting the double layer (Ker1), the single layer (Ker2) or the
+    // combined system strengths.  Warp w of the block takes rows w, w+8, ...;
+    // lane l owns coefficients 4l..4l+3 (table rows padded to 4 values); the
+    // eight partial sums are added in a fixed order.
     template <typename T>
-    __global__ void p2m_apply_kernel(int R, int K, int N, const int64_t *__restrict__ prow_ptr,
-                                     const int32_t *__restrict__ pleaf_box,
-                                     const int32_t *__restrict__ prow_dof,
-                                     const T *__restrict__ T1, const T *__restrict__ T2,
-                                     const uint8_t *__restrict__ dir,
-                                     const uint8_t *__restrict__ modes, const T *__restrict__ x,
-                                     T *__restrict__ M)
+    __global__ void __launch_bounds__(256)
+      p2m_apply_kernel(int R, int K, int N, const int64_t *__restrict__ prow_ptr,
+                       const int32_t *__restrict__ pleaf_box, const int32_t *__restrict__ prow_dof,
+                       const T *__restrict__ T1, const T *__restrict__ T2,
+                       const uint8_t *__restrict__ dir, const uint8_t *__restrict__ modes,
+                       const T *__restrict__ x, T *__restrict__ M)
     {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      const int     K4   = (K + 3) / 4 * 4;
+      T            *part = reinterpret_cast<T *>(smem_raw); // [8][4][K4]
       const int     leaf = blockIdx.x;
       const int64_t box  = pleaf_box[leaf];
       const int64_t rb = prow_ptr[leaf], re = prow_ptr[leaf + 1];
-      for (int idx = threadIdx.x; idx < R * K; idx += blockDim.x)
-        {
-          const int     r    = idx / K;
-          const int     k    = idx - r * K;
-          const uint8_t mode = modes[r];
-          T             acc  = T(0);
-          for (int64_t row = rb; row < re; ++row)
-            {
-              const int dof = prow_dof[row];
-              const T   xv  = x[int64_t(r) * N + dof];
-              if (mode == MODE_KER1)
-                acc += T1[row * K + k] * xv;
-              else if (mode == MODE_KER2)
-                acc += T2[row * K + k] * xv;
-              else
-                acc += dir[dof] ? -T2[row * K + k] * xv : T1[row * K + k] * xv;
-            }
-          M[(box * R + r) * K + k] = acc;
-        }
-    }
-
-    // Generic translation: out[t] (= or +=) sum over sources s of op[s] * in[s]
-    // for one target box per block.  Four warps share the target's sources
-    // (warp w takes sources w, w+4, ...); each lane owns output rows
-    // k = lane + 32 j; the four partial sums are added in a fixed order, so the
-    // result does not depend on scheduling.  ops are stored [op][in][out].
-    //   SRC_CSR:      M2L, sources and offset ids from a per-target list
-    //   SRC_CHILDREN: M2M, sources = children, op = child octant
-    //   SRC_PARENT:   L2L, source = parent, op = own octant
-    enum
-    {
-      SRC_CSR      = 0,
-      SRC_CHILDREN = 1,
-      SRC_PARENT   = 2
-    };
-    constexpr int TW  = 4; // warps per block
-    constexpr int KPL = 4; // output rows per lane (K <= 128)
-    constexpr int RCH = 4; // rhs columns per register block
-
-    template <typename T, int MODE, bool ACCUM>
-    __global__ void __launch_bounds__(TW * 32)
-      translate_kernel(int R, int K, const int32_t *__restrict__ targets,
-                       const int64_t *__restrict__ src_ptr, const int32_t *__restrict__ src,
-                       const int32_t *__restrict__ opid, const int32_t *__restrict__ child_first,
-                       const int32_t *__restrict__ nchild, const int32_t *__restrict__ digit,
-                       const int32_t *__restrict__ parent, const T *__restrict__ ops,
-                       const T *__restrict__ in, T *__restrict__ out)
-    {
-      extern __shared__ unsigned char smem_raw[];
-      T            *sSrc = reinterpret_cast<T *>(smem_raw);   // [TW][RCH][K]
-      T            *sAcc = sSrc + TW * RCH * K;               // [TW][RCH][K]
       const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      const int64_t t    = targets[blockIdx.x];
-      int64_t       e0, e1;
-      if (MODE == SRC_CSR)
+      const bool    act  = 4 * lane < K4;
+      for (int rq = 0; rq < R; rq += 4)
         {
-          e0 = src_ptr[blockIdx.x];
-          e1 = src_ptr[blockIdx.x + 1];
-        }
-      else if (MODE == SRC_CHILDREN)
-        {
-          e0 = child_first[t];
-          e1 = e0 + nchild[t];
-        }
-      else
-        {
-          e0 = 0;
-          e1 = 1;
-        }
-      T *mySrc = sSrc + warp * RCH * K;
-      for (int r0 = 0; r0 < R; r0 += RCH)
-        {
-          const int rc = min(RCH, R - r0);
-          T         acc[RCH][KPL];
+          const int rc = min(4, R - rq);
+          T         acc[4][4];
 #pragma unroll
-          for (int r = 0; r < RCH; ++r)
+          for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int j = 0; j < KPL; ++j)
-              acc[r][j] = T(0);
-          for (int64_t e = e0 + warp; e < e1; e += TW)
-            {
-              int64_t sb;
-              int     o;
-              if (MODE == SRC_CSR)
-                {
-                  sb = src[e];
-                  o  = opid[e];
-                }
-              else if (MODE == SRC_CHILDREN)
-                {
-                  sb = e;
-                  o  = digit[e];
-                }
-              else
-                {
-                  sb = parent[t];
-                  o  = digit[t];
-                }
-              const T *ip = in + (sb * R + r0) * K;
-              for (int i = lane; i < rc * K; i += 32)
-                mySrc[i] = ip[i];
-              __syncwarp();
-              const T *op = ops + int64_t(o) * K * K;
-              for (int ki = 0; ki < K; ++ki)
-                {
-                  T w[KPL];
-#pragma unroll
-                  for (int j = 0; j < KPL; ++j)
-                    {
-                      const int ko = lane + 32 * j;
-                      w[j]         = ko < K ? op[int64_t(ki) * K + ko] : T(0);
-                    }
-#pragma unroll
-                  for (int r = 0; r < RCH; ++r)
-                    if (r < rc)
-                      {
-                        const T m = mySrc[r * K + ki];
-#pragma unroll
-                        for (int j = 0; j < KPL; ++j)
-                          acc[r][j] += w[j] * m;
-                      }
-                }
-              __syncwarp();
-            }
-          T *myAcc = sAcc + warp * RCH * K;
-#pragma unroll
-          for (int r = 0; r < RCH; ++r)
-#pragma unroll
-            for (int j = 0; j < KPL; ++j)
+            for (int b = 0; b < 4; ++b)
+              acc[a][b] = T(0);
+          if (act)
+            for (int64_t row = rb + warp; row < re; row += 8)
               {
-                const int ko = lane + 32 * j;
-                if (r < rc && ko < K)
-                  myAcc[r * K + ko] = acc[r][j];
+                const int dof = prow_dof[row];
+                T         t1[4], t2[4];
+                load4(T1 + row * K4 + 4 * lane, t1);
+                load4(T2 + row * K4 + 4 * lane, t2);
+                const bool d = dir[dof] != 0;
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr)
+                  if (rr < rc)
+                    {
+                      const uint8_t mode = modes[rq + rr];
+                      const T       xv   = x[int64_t(rq + rr) * N + dof];
+                      const T       w1   = mode == MODE_KER2 ? T(0) : (mode == MODE_KER1 ? xv : (d ? T(0) : xv));
+                      const T       w2   = mode == MODE_KER1 ? T(0) : (mode == MODE_KER2 ? xv : (d ? -xv : T(0)));
+#pragma unroll
+                      for (int c = 0; c < 4; ++c)
+                        acc[rr][c] += w1 * t1[c] + w2 * t2[c];
+                    }
               }
+          if (act)
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                part[(warp * 4 + rr) * K4 + 4 * lane + c] = acc[rr][c];
           __syncthreads();
           for (int i = threadIdx.x; i < rc * K; i += blockDim.x)
             {
-              T v = sAcc[i];
-              for (int w = 1; w < TW; ++w)
-                v += sAcc[w * RCH * K + i];
-              T *o = out + (t * R + r0) * K + i;
-              *o   = ACCUM ? *o + v : v;
+              const int rr = i / K, k = i - rr * K;
+              T         s  = part[rr * K4 + k];
+              for (int w = 1; w < 8; ++w)
+                s += part[(w * 4 + rr) * K4 + k];
+              M[(box * R + rq + rr) * K + k] = s;
             }
           __syncthreads();
+        }
+    }
+
+    // Batched translation GEMM.  Scaled operators do not depend on the level:
+    // M2L depends only on the integer source-target offset, M2M / L2L only on
+    // the child octant.  Pairs sharing an operator are cut into chunks of <= 64;
+    // block c computes  Y[q] = T_op(c) E[src(q)]  for the chunk's pairs (x R
+    // columns) with the operator staged once in shared memory (CUDA-core FMA,
+    // 16x16 threads, 8x4 outputs per thread).
+    constexpr int GB_COLS = 64;
+    constexpr int GB_LDB  = GB_COLS + 1;
+
+    template <typename T>
+    __global__ void __launch_bounds__(256)
+      trans_gemm_kernel(int R, int K, int chunk0, const int32_t *__restrict__ chunk_start,
+                      const int32_t *__restrict__ chunk_cnt, const int32_t *__restrict__ chunk_off,
+                      const int32_t *__restrict__ q_src, const T *__restrict__ ops,
+                      const T *__restrict__ M, T *__restrict__ Y)
+    {
+      extern __shared__ unsigned char smem_raw[];
+      T        *sT    = reinterpret_cast<T *>(smem_raw); // [K][K] in-major
+      T        *sB    = sT + K * K;                      // [K][GB_LDB]
+      const int ch    = chunk0 + blockIdx.x;
+      const int start = chunk_start[ch], cnt = chunk_cnt[ch];
+      const T  *op    = ops + int64_t(chunk_off[ch]) * K * K;
+      for (int i = threadIdx.x; i < K * K; i += blockDim.x)
+        sT[i] = op[i];
+      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+      const int ncols = cnt * R;
+      for (int c0 = 0; c0 < ncols; c0 += GB_COLS)
+        {
+          const int nc = min(GB_COLS, ncols - c0);
+          __syncthreads();
+          for (int idx = threadIdx.x; idx < nc * K; idx += blockDim.x)
+            {
+              const int     c  = idx / K, ki = idx - c * K;
+              const int     cg = c0 + c;
+              const int64_t q  = start + cg / R;
+              const int     r  = cg % R;
+              sB[ki * GB_LDB + c] = M[(int64_t(q_src[q]) * R + r) * K + ki];
+            }
+          __syncthreads();
+          T acc[8][4];
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              acc[i][j] = T(0);
+          for (int ki = 0; ki < K; ++ki)
+            {
+              T a[8], b[4];
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+                {
+                  const int ko = tx + 16 * i;
+                  a[i]         = ko < K ? sT[ki * K + ko] : T(0);
+                }
+#pragma unroll
+              for (int j = 0; j < 4; ++j)
+                b[j] = sB[ki * GB_LDB + ty + 16 * j];
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                  acc[i][j] += a[i] * b[j];
+            }
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            {
+              const int c = ty + 16 * j;
+              if (c >= nc)
+                continue;
+              const int     cg = c0 + c;
+              const int64_t q  = start + cg / R;
+              const int     r  = cg % R;
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+                {
+                  const int ko = tx + 16 * i;
+                  if (ko < K)
+                    Y[(q * R + r) * K + ko] = acc[i][j];
+                }
+            }
+        }
+    }
+
+    // out[box] = sum of the box's translation products Y[q], in list order.
+    template <typename T>
+    __global__ void gather_kernel(int R, int K, const int32_t *__restrict__ boxes,
+                                  const int64_t *__restrict__ q_ptr, const int32_t *__restrict__ q,
+                                  const T *__restrict__ Y, T *__restrict__ out)
+    {
+      const int64_t b = boxes[blockIdx.x];
+      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
+        {
+          T acc = T(0);
+          for (int64_t e = q_ptr[blockIdx.x]; e < q_ptr[blockIdx.x + 1]; ++e)
+            acc += Y[int64_t(q[e]) * R * K + i];
+          out[b * R * K + i] = acc;
         }
     }
 
@@ -340,13 +388,20 @@ namespace pibem
   void launch_near_spmv(const OperatorDev<T> &op, int R, int N, const T *vals, const T *x, T *y,
                         bool accumulate, cudaStream_t s)
   {
-    if (op.n_rows == 0)
+    if (op.n_near_leaves == 0)
       return;
-    const int64_t threads = op.n_rows * 32;
-    near_spmv_kernel<T><<<unsigned((threads + 255) / 256), 256, 0, s>>>(
-      op.n_rows, R, N, op.row_leaf, op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols, vals,
-      x, y, accumulate);
+    const int64_t maxnc = (std::max<int64_t>(op.max_near_cols, 1) + 3) / 4 * 4;
+    int           rb    = int(std::max<int64_t>(1, (96 * 1024) / (maxnc * int64_t(sizeof(T)))));
+    rb                  = std::min(rb, R);
+    const size_t smem   = size_t(rb) * maxnc * sizeof(T);
+    if (smem > 48 * 1024)
+      PIBEM_CUDA(cudaFuncSetAttribute(near_leaf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(smem)));
+    near_leaf_kernel<T><<<op.n_near_leaves, 256, smem, s>>>(R, rb, N, op.nrow_ptr, op.ncol_ptr,
+                                                          op.nval_ptr, op.nrows, op.ncols, vals, x,
+                                                          y, accumulate);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   template <typename T>
@@ -355,53 +410,61 @@ namespace pibem
   {
     if (op.n_p2m_leaves == 0)
       return;
-    p2m_apply_kernel<T><<<op.n_p2m_leaves, tpb_for(R * op.K), 0, s>>>(
+    const size_t smem = size_t(8) * 4 * ((op.K + 3) / 4 * 4) * sizeof(T);
+    p2m_apply_kernel<T><<<op.n_p2m_leaves, 256, smem, s>>>(
       R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof, op.T1, op.T2, dir, modes, x, M);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
-  template <typename T, int MODE, bool ACCUM>
-  static void launch_translate(int nt, int R, int K, const int32_t *targets, const int64_t *src_ptr,
-                               const int32_t *src, const int32_t *opid, const TreeDev &td,
-                               const T *ops, const T *in, T *out, cudaStream_t s)
+  template <typename T>
+  static void launch_trans_gemm(const OperatorDev<T> &op, int R, int c0, int c1, const T *E, T *Y,
+                                cudaStream_t s)
   {
-    if (nt <= 0)
+    if (c1 <= c0)
       return;
-    const size_t smem = size_t(2) * TW * RCH * K * sizeof(T);
-    auto         fn   = translate_kernel<T, MODE, ACCUM>;
+    const size_t smem = (size_t(op.K) * op.K + size_t(op.K) * GB_LDB) * sizeof(T);
     if (smem > 48 * 1024)
-      PIBEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    fn<<<nt, TW * 32, smem, s>>>(R, K, targets, src_ptr, src, opid, td.child_first, td.nchild,
-                                 td.digit, td.parent, ops, in, out);
+      PIBEM_CUDA(cudaFuncSetAttribute(trans_gemm_kernel<T>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    trans_gemm_kernel<T><<<c1 - c0, 256, smem, s>>>(R, op.K, c0, op.ch_start, op.ch_cnt, op.ch_op,
+                                                    op.q_src, op.ops, E, Y);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   template <typename T>
-  void launch_m2m_level(const OperatorDev<T> &op, const TreeDev &td, int R, int parent_level, T *M,
-                        cudaStream_t s)
+  static void launch_gather(int R, int K, int nbox, const int32_t *boxes, const int64_t *q_ptr,
+                            const int32_t *q, const T *Y, T *out, cudaStream_t s)
   {
-    const int a = op.parents_level_ptr[parent_level], b = op.parents_level_ptr[parent_level + 1];
-    launch_translate<T, SRC_CHILDREN, false>(b - a, R, op.K, op.parents + a, nullptr, nullptr,
-                                             nullptr, td, op.m2m_ops, M, M, s);
+    if (nbox <= 0)
+      return;
+    gather_kernel<T><<<nbox, R * K >= 128 ? 128 : 96, 0, s>>>(R, K, boxes, q_ptr, q, Y, out);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   template <typename T>
-  void launch_l2l_level(const OperatorDev<T> &op, const TreeDev &td, int R, int level, T *Lx,
-                        cudaStream_t s)
+  void launch_upward_level(const OperatorDev<T> &op, int R, int level, T *M, T *Y, cudaStream_t s)
   {
-    const int a = op.l2l_level_ptr[level], b = op.l2l_level_ptr[level + 1];
-    launch_translate<T, SRC_PARENT, false>(b - a, R, op.K, op.l2l_box + a, nullptr, nullptr,
-                                           nullptr, td, op.l2l_ops, Lx, Lx, s);
+    launch_trans_gemm<T>(op, R, op.up_chunk_ptr[level], op.up_chunk_ptr[level + 1], M, Y, s);
+    const int a = op.up_box_ptr[level], b = op.up_box_ptr[level + 1];
+    launch_gather<T>(R, op.K, b - a, op.up_box + a, op.up_q_ptr + a, op.up_q, Y, M, s);
   }
 
   template <typename T>
-  void launch_m2l_level(const OperatorDev<T> &op, int R, int level, const T *M, T *Lx,
-                        cudaStream_t s)
+  void launch_m2l_gemm(const OperatorDev<T> &op, int R, const T *M, T *Y, cudaStream_t s)
   {
-    const int a = op.m2l_level_ptr[level], b = op.m2l_level_ptr[level + 1];
-    TreeDev   none;
-    launch_translate<T, SRC_CSR, true>(b - a, R, op.K, op.m2l_tgt + a, op.m2l_src_ptr + a,
-                                       op.m2l_src, op.m2l_off, none, op.m2l_ops, M, Lx, s);
+    launch_trans_gemm<T>(op, R, 0, op.m2l_chunk_end, M, Y, s);
+  }
+
+  template <typename T>
+  void launch_downward_level(const OperatorDev<T> &op, int R, int level, T *Lx, T *Y,
+                             cudaStream_t s)
+  {
+    launch_trans_gemm<T>(op, R, op.down_chunk_ptr[level], op.down_chunk_ptr[level + 1], Lx, Y, s);
+    const int a = op.down_box_ptr[level], b = op.down_box_ptr[level + 1];
+    launch_gather<T>(R, op.K, b - a, op.down_box + a, op.down_q_ptr + a, op.down_q, Y, Lx, s);
   }
 
   template <typename T>
@@ -414,10 +477,12 @@ namespace pibem
       op.n_m2p_items, op.n_m2p_pairs, R, op.K, op.p, op.m2p_item_ptr, op.m2p_pair_tgt, op.m2p_tgt,
       op.m2p_src, td.nbeg, td.node_sorted, td.xyz, td.center, td.delta, M, op.m2p_scratch);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
     m2p_sum_kernel<T><<<unsigned((op.n_m2p_tnodes + 127) / 128), 128, 0, s>>>(
       op.n_m2p_tnodes, op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt,
       op.m2p_src_ptr, op.m2p_item_ptr, td.nbeg, td.node_sorted, op.m2p_scratch, y);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void ensure_fmm_tables(int device, cudaStream_t s)
@@ -441,6 +506,7 @@ namespace pibem
     l2p_kernel<T><<<unsigned((threads + 255) / 256), 256, 0, s>>>(
       op.n_rows, R, op.K, N, op.row_leaf, op.lleaf_box, op.nrows, op.W, Lx, y);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
 #define PIBEM_INSTANTIATE(T)                                                                      \
@@ -448,12 +514,10 @@ namespace pibem
                                     bool, cudaStream_t);                                         \
   template void launch_p2m_apply<T>(const OperatorDev<T> &, int, int, const uint8_t *,           \
                                     const uint8_t *, const T *, T *, cudaStream_t);              \
-  template void launch_m2m_level<T>(const OperatorDev<T> &, const TreeDev &, int, int, T *,      \
-                                    cudaStream_t);                                               \
-  template void launch_l2l_level<T>(const OperatorDev<T> &, const TreeDev &, int, int, T *,      \
-                                    cudaStream_t);                                               \
-  template void launch_m2l_level<T>(const OperatorDev<T> &, int, int, const T *, T *,            \
-                                    cudaStream_t);                                               \
+  template void launch_upward_level<T>(const OperatorDev<T> &, int, int, T *, T *, cudaStream_t); \
+  template void launch_m2l_gemm<T>(const OperatorDev<T> &, int, const T *, T *, cudaStream_t);    \
+  template void launch_downward_level<T>(const OperatorDev<T> &, int, int, T *, T *,             \
+                                         cudaStream_t);                                          \
   template void launch_m2p<T>(const OperatorDev<T> &, const TreeDev &, int, int, const T *, T *, \
                               cudaStream_t);                                                     \
   template void launch_l2p<T>(const OperatorDev<T> &, int, int, const T *, T *, cudaStream_t);

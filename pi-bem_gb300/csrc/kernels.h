@@ -82,22 +82,22 @@ namespace pibem
     // l2p (same row positions as the near field)
     const int32_t *lleaf_box = nullptr;
     const T       *W = nullptr;
-    // translations (transposed: [op][in][out])
-    const T       *m2m_ops = nullptr, *l2l_ops = nullptr, *m2l_ops = nullptr;
-    // M2L per target CSR
-    const int32_t *m2l_tgt = nullptr, *m2l_src = nullptr, *m2l_off = nullptr;
-    const int64_t *m2l_src_ptr = nullptr;
+    // batched translations: operator table [M2L offsets | 8 M2M | 8 L2L],
+    // each K x K stored [in][out]; pair / chunk arrays of the plan
+    const T       *ops = nullptr;
+    const int32_t *q_src = nullptr, *ch_start = nullptr, *ch_cnt = nullptr, *ch_op = nullptr;
+    int            m2l_chunk_end = 0;
+    std::vector<int> up_chunk_ptr, down_chunk_ptr, up_box_ptr, down_box_ptr;
+    const int32_t *up_box = nullptr, *down_box = nullptr, *up_q = nullptr, *down_q = nullptr;
+    const int64_t *up_q_ptr = nullptr, *down_q_ptr = nullptr;
+    int64_t        n_pairs = 0;
+    int64_t        max_near_cols = 0;
     // M2P per target CSR, evaluated per (pair, target node) item
     int            n_m2p_tgt = 0;
     int64_t        n_m2p_pairs = 0, n_m2p_items = 0, n_m2p_tnodes = 0;
     const int32_t *m2p_tgt = nullptr, *m2p_src = nullptr, *m2p_pair_tgt = nullptr;
     const int64_t *m2p_src_ptr = nullptr, *m2p_item_ptr = nullptr, *m2p_tnode_ptr = nullptr;
     T             *m2p_scratch = nullptr; // n_m2p_items * R
-    // L2L boxes
-    const int32_t *l2l_box = nullptr;
-    // per-level ranges (host)
-    std::vector<int> m2l_level_ptr, l2l_level_ptr, parents_level_ptr;
-    const int32_t   *parents = nullptr; // boxes with children, grouped by level of the box
   };
 
   template <typename T>
@@ -106,15 +106,16 @@ namespace pibem
   template <typename T>
   void launch_p2m_apply(const OperatorDev<T> &op, int R, int N, const uint8_t *dir,
                         const uint8_t *modes, const T *x, T *M, cudaStream_t s);
+  // upward level l: M2M of the level-l children, gathered into the parents
   template <typename T>
-  void launch_m2m_level(const OperatorDev<T> &op, const TreeDev &td, int R, int parent_level, T *M,
-                        cudaStream_t s);
+  void launch_upward_level(const OperatorDev<T> &op, int R, int level, T *M, T *Y, cudaStream_t s);
+  // M2L products of all levels into Y
   template <typename T>
-  void launch_l2l_level(const OperatorDev<T> &op, const TreeDev &td, int R, int level, T *Lx,
-                        cudaStream_t s);
+  void launch_m2l_gemm(const OperatorDev<T> &op, int R, const T *M, T *Y, cudaStream_t s);
+  // downward level l: L2L products, then L[b] = L2L + sum of M2L products
   template <typename T>
-  void launch_m2l_level(const OperatorDev<T> &op, int R, int level, const T *M, T *Lx,
-                        cudaStream_t s);
+  void launch_downward_level(const OperatorDev<T> &op, int R, int level, T *Lx, T *Y,
+                             cudaStream_t s);
   template <typename T>
   void launch_m2p(const OperatorDev<T> &op, const TreeDev &td, int R, int N, const T *M, T *y,
                   cudaStream_t s);

@@ -44,17 +44,22 @@ namespace pibem
         }
     }
 
+    // one warp per output: lanes stride over the block partials, fixed-order tree
     __global__ void dots_final_kernel(int R, int ncols, int nblk, const double *__restrict__ partial,
                                       double *__restrict__ out)
     {
-      int idx = blockIdx.x * blockDim.x + threadIdx.x;
+      const int idx  = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+      const int lane = threadIdx.x & 31;
       if (idx >= R * ncols)
         return;
-      int    r = idx / ncols, i = idx % ncols;
-      double s = 0;
-      for (int b = 0; b < nblk; ++b)
+      const int r = idx / ncols, i = idx % ncols;
+      double    s = 0;
+      for (int b = lane; b < nblk; b += 32)
         s += partial[(int64_t(r) * nblk + b) * ncols + i];
-      out[idx] = s;
+      for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0)
+        out[idx] = s;
     }
 
     // w[r][t] -= sum_i V[r][i][t] h[r][i]   (h on the device, layout [r][ldh])
@@ -134,9 +139,16 @@ namespace pibem
             hi = mid - 1;
         }
       const int64_t nc  = col_ptr[lo + 1] - col_ptr[lo];
+      const int64_t ld  = (nc + 3) / 4 * 4;
       const int64_t loc = vi - val_ptr[lo];
-      const int     row = rows[row_ptr[lo] + loc / nc];
-      const int     col = cols[col_ptr[lo] + loc % nc];
+      if (loc % ld >= nc)
+        {
+          S[vi]   = 0.0;
+          S32[vi] = 0.0f;
+          return;
+        }
+      const int row = rows[row_ptr[lo] + loc / ld];
+      const int col = cols[col_ptr[lo] + loc % ld];
       double        v   = dir[col] ? -Dv[vi] : Nv[vi];
       if (row == col && !dir[row])
         v += alpha[row];
@@ -233,8 +245,9 @@ namespace pibem
   {
     dim3 grid(nblk, R);
     dots_partial_kernel<<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, w, nblk, partial);
-    dots_final_kernel<<<nblocks(int64_t(R) * ncols, 128), 128, 0, s>>>(R, ncols, nblk, partial, out);
+    dots_final_kernel<<<nblocks(int64_t(R) * ncols * 32, 256), 256, 0, s>>>(R, ncols, nblk, partial, out);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch(2);
   }
 
   void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
@@ -242,6 +255,7 @@ namespace pibem
   {
     gemv_sub_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, ncols, ldv, ldr, V, h, ldh, w, sign);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
@@ -249,6 +263,7 @@ namespace pibem
   {
     normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s)
@@ -257,6 +272,7 @@ namespace pibem
       return;
     axpby_kernel<<<nblocks(n), 256, 0, s>>>(n, a, x, b, y);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_convert_d2f(int64_t n, const double *a, float *b, cudaStream_t s)
@@ -265,6 +281,7 @@ namespace pibem
       return;
     d2f_kernel<<<nblocks(n), 256, 0, s>>>(n, a, b);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
   void launch_convert_f2d(int64_t n, const float *a, double *b, cudaStream_t s)
   {
@@ -272,6 +289,7 @@ namespace pibem
       return;
     f2d_kernel<<<nblocks(n), 256, 0, s>>>(n, a, b);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_build_system_matrix(int64_t n_vals, int n_leaves, const int64_t *val_ptr,
@@ -286,6 +304,7 @@ namespace pibem
                                                          row_ptr, rows, cols, dir, alpha, Nval,
                                                          Dval, S, S32);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_rhs_combine(int64_t n, int R, const double *tmp, const uint8_t *dir,
@@ -294,6 +313,7 @@ namespace pibem
   {
     rhs_combine_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, tmp, dir, alpha, oN, oD, rhs);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_split_masks(int64_t n, int R, const double *tmp, const uint8_t *dir, double *a,
@@ -301,6 +321,7 @@ namespace pibem
   {
     split_masks_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, tmp, dir, a, b);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_scatter(int64_t n, int R, const double *sol, const uint8_t *dir, double *phi,
@@ -308,12 +329,14 @@ namespace pibem
   {
     scatter_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, sol, dir, phi, dphi);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_add_scalar(int64_t n, int R, const double *shift, double *x, cudaStream_t s)
   {
     add_scalar_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, shift, x);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_block_apply(int64_t n_rows, int R, int64_t n, const int32_t *row_leaf,
@@ -325,5 +348,6 @@ namespace pibem
     block_apply_kernel<<<nblocks(n_rows * 32), 256, 0, s>>>(n_rows, R, n, row_leaf, row_ptr,
                                                             blk_ptr, rows, Pinv, v, z);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 } // namespace pibem

@@ -30,6 +30,10 @@ namespace pibem
     }                                                                                          \
   while (0)
 
+  // Counts kernel launches of this library (all handles, all streams).
+  void    note_launch(int64_t n = 1);
+  int64_t launch_count();
+
   // Owning device buffer.
   template <typename T>
   struct DBuf
@@ -161,6 +165,19 @@ namespace pibem
     std::vector<int64_t>  m2l_src_ptr;        // per target
     std::vector<int32_t>  m2l_src, m2l_off;   // source box, offset id
     std::vector<int32_t>  offsets;            // distinct offsets, 3 per id
+    // Batched translations.  One pair space q for M2L (all levels), M2M and
+    // L2L (per level); pair q reads the expansion of box q_src[q] and applies
+    // operator q_op[q] of the concatenated table [M2L offsets | 8 M2M | 8 L2L];
+    // pairs are cut into chunks of <= 64 pairs sharing one operator.
+    std::vector<int32_t>  q_src, q_op;
+    std::vector<int32_t>  ch_start, ch_cnt, ch_op;
+    int                   m2l_chunk_end = 0;            // chunks [0, m2l_chunk_end) are M2L
+    std::vector<int32_t>  up_chunk_ptr, down_chunk_ptr; // per level l: chunk range
+    // gathers: per level, boxes and the pairs summed into each (fixed order)
+    std::vector<int32_t>  up_box_ptr, down_box_ptr;     // per level: range in up_box / down_box
+    std::vector<int32_t>  up_box, down_box;
+    std::vector<int64_t>  up_q_ptr, down_q_ptr;         // per listed box
+    std::vector<int32_t>  up_q, down_q;
     // M2P pairs grouped by target
     std::vector<int32_t>  m2p_tgt;
     std::vector<int64_t>  m2p_src_ptr;

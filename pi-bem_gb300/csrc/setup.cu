@@ -223,10 +223,13 @@ namespace pibem
         }
       const int     leaf = lo;
       const int64_t nc   = col_ptr[leaf + 1] - col_ptr[leaf];
+      const int64_t ld   = (nc + 3) / 4 * 4; // padded row stride
       const int64_t ne   = ent_ptr[leaf + 1] - ent_ptr[leaf];
       const int64_t loc  = vi - val_ptr[leaf];
-      const int64_t r    = loc / nc;
-      const int64_t cc   = loc % nc;
+      const int64_t r    = loc / ld;
+      const int64_t cc   = loc % ld;
+      if (cc >= nc)
+        return; // padding (stays zero)
       const int64_t gcol = col_ptr[leaf] + cc;
       const int64_t ib   = item_ptr[leaf] + r * ne;
       if (ib < item_base || ib + ne > item_end)
@@ -320,8 +323,9 @@ namespace pibem
           // e^{-i m beta} (A + i B)
           a1 += ws * (part == 0 ? (cb * A + sb * B) : (cb * B - sb * A));
         }
-      T1[row * K + k] = a1;
-      T2[row * K + k] = a2;
+      const int K4    = (K + 3) / 4 * 4; // padded row stride (16-byte vector loads)
+      T1[row * K4 + k] = a1;
+      T2[row * K4 + k] = a2;
     }
 
     // L2P tables: W[pos][k] such that the field at node rows[pos] of its leaf is
@@ -406,6 +410,7 @@ namespace pibem
     quad_data_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n_cells, nq, xyz, cells, gpts, gw,
                                                                qpts, qnrm, qjxw, qshape);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_near_assembly(const NearAssemblyArgs &a, cudaStream_t s)
@@ -440,6 +445,7 @@ namespace pibem
           end, a.n_leaves, a.item_ptr, a.row_ptr, a.ent_ptr, a.rows, a.ents, a.xyz, a.cells,
           a.dbl_off, a.dbl_ids, a.nq, a.qpts, a.qnrm, a.qjxw, a.qshape, start, a.staging);
         PIBEM_CUDA(cudaGetLastError());
+    note_launch();
         // gather: all values whose row lies in [start, end)
         // value range: leaves covering the batch
         int l0 = 0, hi = a.n_leaves - 1;
@@ -466,6 +472,7 @@ namespace pibem
             v1, a.n_leaves, a.val_ptr, a.col_ptr, a.ent_ptr, a.item_ptr, a.gather_ptr,
             a.gather_ids, start, end, a.staging, a.Nval, a.Dval, v0);
         PIBEM_CUDA(cudaGetLastError());
+    note_launch();
         start = end;
       }
   }
@@ -484,6 +491,7 @@ namespace pibem
       n_rows, K, p, n_leaves, row_ptr, leaf_box, contrib_ptr, contrib_q, box_center, box_delta,
       qpts, qnrm, qjxw, qshape, T1, T2);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_l2p_tables(int64_t n_pos, int K, int n_leaves, const int64_t *pos_ptr,
@@ -498,5 +506,6 @@ namespace pibem
                                                                leaf_box, nodes, xyz, box_center,
                                                                box_delta, W);
     PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 } // namespace pibem

@@ -451,7 +451,8 @@ namespace pibem
         pl.nrow_ptr[k + 1] = pl.nrow_ptr[k] + int64_t(rows[k].size());
         pl.ncol_ptr[k + 1] = pl.ncol_ptr[k] + int64_t(cols[k].size());
         pl.nent_ptr[k + 1] = pl.nent_ptr[k] + int64_t(ents[k].size());
-        pl.nval_ptr[k + 1] = pl.nval_ptr[k] + int64_t(rows[k].size()) * int64_t(cols[k].size());
+        // rows padded to a multiple of 4 values (16-byte vector loads)
+        pl.nval_ptr[k + 1] = pl.nval_ptr[k] + int64_t(rows[k].size()) * ((int64_t(cols[k].size()) + 3) / 4 * 4);
       }
     pl.gather_ptr.reserve(pl.ncol_ptr[nl] + nl);
     for (int k = 0; k < nl; ++k)
@@ -584,6 +585,115 @@ namespace pibem
     pl.m2l_tgt_ptr_level[t.L + 1] = int(pl.m2l_tgt.size());
     pl.n_m2l = int64_t(pl.m2l_src.size());
     pl.n_m2p = int64_t(pl.m2p_src.size());
+    // ---- batched translation pairs
+    {
+      const int noff = int(pl.offsets.size() / 3);
+      // chunk helper: pairs already grouped by operator in [a, b)
+      auto cut = [&](int64_t a, int64_t b) {
+        int64_t i = a;
+        while (i < b)
+          {
+            int64_t j = i;
+            while (j < b && pl.q_op[j] == pl.q_op[i] && j - i < 64)
+              ++j;
+            pl.ch_start.push_back(int32_t(i));
+            pl.ch_cnt.push_back(int32_t(j - i));
+            pl.ch_op.push_back(pl.q_op[i]);
+            i = j;
+          }
+      };
+      // M2L pairs of all levels, grouped by offset (stable)
+      const int64_t        np = pl.n_m2l;
+      std::vector<int64_t> cnt(noff + 1, 0);
+      for (int64_t e = 0; e < np; ++e)
+        cnt[pl.m2l_off[e] + 1]++;
+      for (int o = 0; o < noff; ++o)
+        cnt[o + 1] += cnt[o];
+      std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1), qof(np);
+      pl.q_src.assign(np, 0);
+      pl.q_op.assign(np, 0);
+      for (int64_t e = 0; e < np; ++e)
+        {
+          int64_t q   = pos[pl.m2l_off[e]]++;
+          qof[e]      = q;
+          pl.q_src[q] = pl.m2l_src[e];
+          pl.q_op[q]  = pl.m2l_off[e];
+        }
+      cut(0, np);
+      pl.m2l_chunk_end = int(pl.ch_start.size());
+      // M2M: children at level l -> parents at level l-1, grouped by octant
+      pl.up_chunk_ptr.assign(t.L + 2, 0);
+      pl.up_box_ptr.assign(t.L + 2, 0);
+      pl.up_q_ptr.push_back(0);
+      std::vector<int64_t> child_q(t.nb, -1);
+      for (int l = 1; l <= t.L; ++l)
+        {
+          pl.up_chunk_ptr[l] = int(pl.ch_start.size());
+          int64_t q0         = int64_t(pl.q_src.size());
+          for (int dg = 0; dg < 8; ++dg)
+            for (int b = t.startLevel[l]; b <= t.endLevel[l] && t.startLevel[l] <= t.endLevel[l]; ++b)
+              if (t.digit[b] == dg)
+                {
+                  child_q[b] = int64_t(pl.q_src.size());
+                  pl.q_src.push_back(b);
+                  pl.q_op.push_back(noff + dg);
+                }
+          cut(q0, int64_t(pl.q_src.size()));
+          pl.up_box_ptr[l] = int(pl.up_box.size());
+          // parents (level l-1) gather their children's products
+          int a = l == 1 ? 0 : t.startLevel[l - 1], e = l == 1 ? 0 : t.endLevel[l - 1];
+          for (int P = a; P <= e; ++P)
+            if (t.nchild[P] > 0)
+              {
+                pl.up_box.push_back(P);
+                for (int c = 0; c < t.nchild[P]; ++c)
+                  pl.up_q.push_back(int32_t(child_q[t.child_first[P] + c]));
+                pl.up_q_ptr.push_back(int64_t(pl.up_q.size()));
+              }
+        }
+      pl.up_chunk_ptr[t.L + 1] = int(pl.ch_start.size());
+      pl.up_box_ptr[t.L + 1]   = int(pl.up_box.size());
+      // L2L: parent (level l-1) -> child with nodes (level l >= 2), by octant;
+      // gather per box with nodes: its L2L product, then its M2L products.
+      pl.down_chunk_ptr.assign(t.L + 2, 0);
+      pl.down_box_ptr.assign(t.L + 2, 0);
+      pl.down_q_ptr.push_back(0);
+      std::vector<int64_t> l2l_q(t.nb, -1);
+      std::vector<int64_t> m2l_first(t.nb, -1);
+      for (size_t ti = 0; ti < pl.m2l_tgt.size(); ++ti)
+        m2l_first[pl.m2l_tgt[ti]] = int64_t(ti);
+      for (int l = 1; l <= t.L; ++l)
+        {
+          pl.down_chunk_ptr[l] = int(pl.ch_start.size());
+          int64_t q0           = int64_t(pl.q_src.size());
+          if (l >= 2)
+            for (int dg = 0; dg < 8; ++dg)
+              for (int b : t.dofs_filled[l])
+                if (t.digit[b] == dg)
+                  {
+                    l2l_q[b] = int64_t(pl.q_src.size());
+                    pl.q_src.push_back(t.parent[b]);
+                    pl.q_op.push_back(noff + 8 + dg);
+                  }
+          cut(q0, int64_t(pl.q_src.size()));
+          pl.down_box_ptr[l] = int(pl.down_box.size());
+          for (int b : t.dofs_filled[l])
+            {
+              pl.down_box.push_back(b);
+              if (l2l_q[b] >= 0)
+                pl.down_q.push_back(int32_t(l2l_q[b]));
+              if (m2l_first[b] >= 0)
+                {
+                  int64_t ti = m2l_first[b];
+                  for (int64_t e = pl.m2l_src_ptr[ti]; e < pl.m2l_src_ptr[ti + 1]; ++e)
+                    pl.down_q.push_back(int32_t(qof[e]));
+                }
+              pl.down_q_ptr.push_back(int64_t(pl.down_q.size()));
+            }
+        }
+      pl.down_chunk_ptr[t.L + 1] = int(pl.ch_start.size());
+      pl.down_box_ptr[t.L + 1]   = int(pl.down_box.size());
+    }
 
     // ---- L2L: boxes with nodes at levels >= 2
     pl.l2l_ptr_level.assign(t.L + 2, 0);

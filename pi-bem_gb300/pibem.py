@@ -89,6 +89,7 @@ EXPORTS = [
     "pibem_solve", "pibem_solve_device", "pibem_tree_info_get", "pibem_tree_boxes",
     "pibem_tree_list", "pibem_tree_list_sublevels", "pibem_near_nnz", "pibem_near_export",
     "pibem_quad_points", "pibem_last_phase_ms", "pibem_set_profiling", "pibem_phase_totals",
+    "pibem_launch_count",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -132,8 +133,15 @@ def load():
     L.pibem_last_phase_ms.argtypes = [C.c_void_p, _dp]
     L.pibem_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     L.pibem_phase_totals.argtypes = [C.c_void_p, C.c_int32, _dp, C.POINTER(C.c_int64), C.c_int32]
+    L.pibem_launch_count.restype = C.c_int64
+    L.pibem_launch_count.argtypes = []
     _lib = L
     return L
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far (all handles)."""
+    return int(load().pibem_launch_count())
 
 
 def default_params(**kw) -> Params:
