@@ -139,7 +139,9 @@ struct pibem_handle
     d_down_box, d_up_q, d_down_q;
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv;
-  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf;
+  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg;
+  DBuf<int>     d_err;
+  bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
   OperatorDev<double> op64;
   OperatorDev<float>  op32;
@@ -647,6 +649,8 @@ namespace
     h->op32.T2      = h->d_T2f.p;
     h->op32.W       = h->d_Wf.p;
     h->op32.ops     = h->d_opsf.p;
+    h->op32.tc_images = h->d_tcimg.n ? h->d_tcimg.p : nullptr;
+    h->op32.tc_err    = h->d_err.p;
     TreeDev &td               = h->td;
     td.nb                     = h->tree.nb;
     td.N                      = int(h->N());
@@ -726,7 +730,7 @@ namespace
            "translation pair");
     for (size_t ch = 0; ch < pl.ch_start.size(); ++ch)
       {
-        need(pl.ch_cnt[ch] > 0 && pl.ch_cnt[ch] <= 64 && pl.ch_start[ch] >= 0 &&
+        need(pl.ch_cnt[ch] > 0 && pl.ch_cnt[ch] <= 128 && pl.ch_start[ch] >= 0 &&
                int64_t(pl.ch_start[ch]) + pl.ch_cnt[ch] <= nq_pairs,
              "translation chunk");
         for (int i = 0; i < pl.ch_cnt[ch]; ++i)
@@ -1028,6 +1032,15 @@ namespace
       h->d_ops.upload(td, s);
       transpose_ops(all, nops, K, tf);
       h->d_opsf.upload(tf, s);
+      h->d_tcimg.release();
+      if (h->use_tc && tc_geometry(K).ok)
+        {
+          std::vector<float> img;
+          build_tc_images(all, nops, K, img);
+          h->d_tcimg.upload(img, s);
+        }
+      h->d_err.alloc(1);
+      h->d_err.zero(s);
       PIBEM_CUDA(cudaStreamSynchronize(s));
     }
     fill_operator_views(h);
@@ -1086,6 +1099,22 @@ namespace
       build_preconditioner(h);
     PIBEM_CUDA(cudaStreamSynchronize(s));
     h->bc_ok = true;
+  }
+
+  // A bounded device wait that gave up (tensor-core translations) is reported
+  // as PIBEM_ETIMEDOUT; the flag is cleared for the next call.
+  void check_device_error(pibem_handle *h)
+  {
+    if (!h->d_err.n)
+      return;
+    int e = 0;
+    h->d_err.download(&e, 1, h->stream);
+    PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    if (e)
+      {
+        h->d_err.zero(h->stream);
+        throw Error(PIBEM_ETIMEDOUT, "a bounded device wait timed out in the tensor-core translations");
+      }
   }
 
   void compute_rhs_dev(pibem_handle *h, int R, const double *tmp, double *rhs)
@@ -1190,6 +1219,7 @@ namespace
       }
     launch_scatter(N, R, x.p, h->d_dir.p, phi, dphi, s);
     PIBEM_CUDA(cudaStreamSynchronize(s));
+    check_device_error(h);
     double worst = rel.empty() ? 0 : *std::max_element(rel.begin(), rel.end());
     if (st)
       {
@@ -1257,6 +1287,8 @@ extern "C"
         h->stream = h->own;
         const char *env = std::getenv("PIBEM_PHASE_TIMING");
         h->timing       = env && env[0] == '1';
+        const char *tc  = std::getenv("PIBEM_TENSOR_CORE_M2L");
+        h->use_tc       = !(tc && tc[0] == '0');
         for (auto &e : h->ev)
           PIBEM_CUDA(cudaEventCreate(&e));
       }
@@ -1353,6 +1385,7 @@ extern "C"
         system_apply32(h, R, dx, dy);
       else
         system_apply64(h, R, dx, dy);
+      check_device_error(h);
       PIBEM_CUDA(cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
     });

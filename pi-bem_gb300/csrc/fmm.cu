@@ -8,6 +8,8 @@
 //   M2P for deeper non-interaction boxes (bem_fma.cc:2664-2704)
 //   L2P at the nodes of childless boxes (bem_fma.cc:2959-2986)
 // Expansions are laid out [box][rhs][k] with K = (p+1)^2 scaled reals.
+#include <type_traits>
+
 #include "devmath.cuh"
 #include "kernels.h"
 
@@ -423,6 +425,12 @@ namespace pibem
   {
     if (c1 <= c0)
       return;
+    if constexpr (std::is_same<T, float>::value)
+      if (op.tc_images)
+        {
+          launch_tc_gemm(op, R, c0, c1, E, Y, op.tc_err, s);
+          return;
+        }
     const size_t smem = (size_t(op.K) * op.K + size_t(op.K) * GB_LDB) * sizeof(T);
     if (smem > 48 * 1024)
       PIBEM_CUDA(cudaFuncSetAttribute(trans_gemm_kernel<T>,

@@ -92,6 +92,9 @@ namespace pibem
     const int64_t *up_q_ptr = nullptr, *down_q_ptr = nullptr;
     int64_t        n_pairs = 0;
     int64_t        max_near_cols = 0;
+    // tensor-core path of the FP32 translations (null: CUDA-core GEMM)
+    const float   *tc_images = nullptr;
+    int           *tc_err    = nullptr;
     // M2P per target CSR, evaluated per (pair, target node) item
     int            n_m2p_tgt = 0;
     int64_t        n_m2p_pairs = 0, n_m2p_items = 0, n_m2p_tnodes = 0;
@@ -122,6 +125,20 @@ namespace pibem
   void ensure_fmm_tables(int device, cudaStream_t s);
   template <typename T>
   void launch_l2p(const OperatorDev<T> &op, int R, int N, const T *Lx, T *y, cudaStream_t s);
+
+  // ---- tensor-core translations (m2l_tc.cu) ----------------------------------
+  struct TcGeometry
+  {
+    int    K = 0, Kp = 0, Np = 0;
+    size_t smem = 0;
+    bool   ok   = false;
+  };
+  TcGeometry tc_geometry(int K);
+  // hi/lo TF32 images of row-major [out][in] operators in the MMA B layout
+  void build_tc_images(const std::vector<double> &ops_out_in, int nops, int K,
+                       std::vector<float> &img);
+  void launch_tc_gemm(const OperatorDev<float> &op, int R, int c0, int c1, const float *E, float *Y,
+                      int *err, cudaStream_t s);
 
   // ---- vector kernels (krylov.cu) -------------------------------------------
   void launch_convert_d2f(int64_t n, const double *a, float *b, cudaStream_t s);

@@ -1,0 +1,352 @@
+// Tensor-core batched translation GEMM (M2L, M2M, L2L) of the FP32 operator,
+// on the 5th-generation tensor cores: tcgen05.mma kind::tf32, accumulator in
+// tensor memory, operator tiles staged by bulk TMA copies (cp.async.bulk).
+//
+// For one chunk of pairs sharing an operator T (K x K, scaled real form):
+//     Y[row][k_out] = sum_{k_in} E[src(row)][k_in] T[k_out][k_in]
+// with row = (pair, rhs).  One block computes a 128-row tile:
+//     A (M = 128 rows x K_in)  source expansions, gathered into shared memory
+//     B (N = K_out x K_in)     operator, pre-laid-out image copied by TMA
+//     D (128 x N) fp32         tensor memory
+// FP32 accuracy from TF32 products by splitting both operands,
+//     x = hi + lo (hi = TF32 rounding of x),   A B ~ Ah Bh + Al Bh + Ah Bl,
+// all three products accumulated into the same FP32 accumulator.
+//
+// Shared-memory operands use the canonical no-swizzle K-major layout: core
+// matrices of 8 rows x 16 bytes; adjacent core matrices along K are 128 bytes
+// apart (leading byte offset), adjacent 8-row groups Kp/4 * 128 bytes apart
+// (stride byte offset).  Each MMA consumes K = 8 (two core matrices).
+//
+// Every wait is bounded: on timeout the block records the failure in *err,
+// waits (bounded) for its copies and MMAs in flight, frees its tensor memory
+// and returns; the host turns the flag into PIBEM_ETIMEDOUT.
+#include <cstdint>
+#include <cstring>
+
+#include "kernels.h"
+
+namespace pibem
+{
+  namespace
+  {
+    constexpr int      TC_ROWS    = 128;
+    constexpr int      TC_THREADS = 128;
+    constexpr uint32_t TC_TMEM_COLS = 128;
+    constexpr long     TC_SPIN_LIMIT = 1L << 26;
+
+    __host__ __device__ inline uint32_t img_off(int row, int k, int Kp)
+    {
+      return uint32_t((row >> 3) * (Kp / 4) * 128 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+    }
+
+    __device__ inline uint32_t smem_u32(const void *p)
+    {
+      return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    }
+
+    __device__ inline uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+    {
+      uint64_t d = 0;
+      d |= uint64_t((saddr >> 4) & 0x3FFFu);
+      d |= uint64_t((lbo >> 4) & 0x3FFFu) << 16;
+      d |= uint64_t((sbo >> 4) & 0x3FFFu) << 32;
+      d |= uint64_t(1) << 46; // descriptor version of sm_100-class tensor cores
+      return d;                // base offset 0, no swizzle
+    }
+
+    __device__ inline float tf32_hi(float x)
+    {
+      uint32_t r;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+      return __uint_as_float(r);
+    }
+
+    __device__ inline bool mbar_wait(uint32_t addr, uint32_t parity)
+    {
+      for (long it = 0; it < TC_SPIN_LIMIT; ++it)
+        {
+          uint32_t done;
+          asm volatile("{\n\t.reg .pred p;\n\t"
+                       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                       "selp.u32 %0, 1, 0, p;\n\t}"
+                       : "=r"(done)
+                       : "r"(addr), "r"(parity)
+                       : "memory");
+          if (done)
+            return true;
+        }
+      return false;
+    }
+
+    __device__ inline void tma_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+    {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   :
+                   : "r"(mbar), "r"(bytes)
+                   : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   :
+                   : "r"(dst), "l"(src), "r"(bytes), "r"(mbar)
+                   : "memory");
+    }
+
+    __device__ inline void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                    uint32_t accumulate)
+    {
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "setp.ne.b32 p, %4, 0;\n\t"
+                   "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                   :
+                   : "r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+                   : "memory");
+    }
+
+    __device__ inline void mma_commit(uint32_t mbar)
+    {
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                   :
+                   : "r"(mbar)
+                   : "memory");
+    }
+
+    __device__ inline void tmem_ld32(uint32_t taddr, float (&v)[32])
+    {
+      uint32_t r[32];
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                   "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                   "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                     "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                     "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
+                     "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                     "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                     "=r"(r[30]), "=r"(r[31])
+                   : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        v[j] = __uint_as_float(r[j]);
+    }
+
+    __global__ void __launch_bounds__(TC_THREADS, 1)
+      tc_gemm_kernel(int R, int K, int Kp, int Np, int chunk0, const int32_t *__restrict__ ch_start,
+                     const int32_t *__restrict__ ch_cnt, const int32_t *__restrict__ ch_op,
+                     const int32_t *__restrict__ q_src, const float *__restrict__ images,
+                     const float *__restrict__ E, float *__restrict__ Y, int *__restrict__ err)
+    {
+      extern __shared__ __align__(1024) uint8_t smem[];
+      const uint32_t a_bytes = uint32_t(TC_ROWS) * Kp * 4, b_bytes = uint32_t(Np) * Kp * 4;
+      uint8_t       *sAh = smem, *sAl = smem + a_bytes, *sB = smem + 2 * a_bytes;
+      uint64_t      *mbar      = reinterpret_cast<uint64_t *>(sB + b_bytes); // [0] tma, [1] mma
+      uint32_t      *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
+      const int      tid = threadIdx.x, warp = tid >> 5;
+      const int      ch = chunk0 + blockIdx.x;
+      const int      start = ch_start[ch], cnt = ch_cnt[ch], op = ch_op[ch];
+      const int      rows_total = cnt * R;
+      const uint32_t mb_tma = smem_u32(&mbar[0]), mb_mma = smem_u32(&mbar[1]);
+
+      if (warp == 0)
+        {
+          asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                       :
+                       : "r"(smem_u32(tmem_slot)), "r"(TC_TMEM_COLS)
+                       : "memory");
+          asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        }
+      if (tid == 0)
+        {
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(mb_tma) : "memory");
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(mb_mma) : "memory");
+          asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tmem = *tmem_slot;
+
+      const float   *Bhi = images + size_t(op) * 2 * Np * Kp;
+      const float   *Blo = Bhi + size_t(Np) * Kp;
+      const uint32_t sbo_a = uint32_t(Kp / 4) * 128, sbo_b = sbo_a, lbo = 128;
+      // instruction descriptor: D f32, A/B tf32, both K-major, N, M
+      const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(Np >> 3) << 17) |
+                             (uint32_t(TC_ROWS >> 4) << 24);
+      const int      ksteps = Kp / 8;
+      uint32_t       ph_tma = 0, ph_mma = 0;
+      bool           ok     = true;
+
+      for (int t0 = 0; t0 < rows_total && ok; t0 += TC_ROWS)
+        {
+          if (tid == 0)
+            tma_load(smem_u32(sB), Bhi, b_bytes, mb_tma);
+          // gather and split the tile's rows (one row per thread)
+          {
+            const int  i     = t0 + tid;
+            const bool valid = i < rows_total;
+            const float *src = nullptr;
+            if (valid)
+              {
+                const int64_t q = start + i / R;
+                const int     r = i - (i / R) * R;
+                src             = E + (int64_t(q_src[q]) * R + r) * K;
+              }
+            for (int k4 = 0; k4 < Kp / 4; ++k4)
+              {
+                float h[4], l[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                  {
+                    const int   k = 4 * k4 + c;
+                    const float x = (valid && k < K) ? src[k] : 0.0f;
+                    h[c]          = tf32_hi(x);
+                    l[c]          = x - h[c];
+                  }
+                const uint32_t o = img_off(tid, 4 * k4, Kp);
+                *reinterpret_cast<float4 *>(sAh + o) = make_float4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<float4 *>(sAl + o) = make_float4(l[0], l[1], l[2], l[3]);
+              }
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncthreads();
+          ok = __syncthreads_and(mbar_wait(mb_tma, ph_tma));
+          if (!ok)
+            break;
+          ph_tma ^= 1;
+          if (tid == 0)
+            {
+              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+              const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), b = smem_u32(sB);
+              for (int s = 0; s < ksteps; ++s)
+                mma_tf32(tmem, smem_desc(ah + 256 * s, lbo, sbo_a), smem_desc(b + 256 * s, lbo, sbo_b),
+                         idesc, s > 0);
+              for (int s = 0; s < ksteps; ++s)
+                mma_tf32(tmem, smem_desc(al + 256 * s, lbo, sbo_a), smem_desc(b + 256 * s, lbo, sbo_b),
+                         idesc, 1);
+              mma_commit(mb_mma);
+            }
+          ok = __syncthreads_and(mbar_wait(mb_mma, ph_mma));
+          if (!ok)
+            break;
+          ph_mma ^= 1;
+          // second operator half (lo) into the same buffer: the MMAs above are done
+          if (tid == 0)
+            tma_load(smem_u32(sB), Blo, b_bytes, mb_tma);
+          ok = __syncthreads_and(mbar_wait(mb_tma, ph_tma));
+          if (!ok)
+            break;
+          ph_tma ^= 1;
+          if (tid == 0)
+            {
+              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+              const uint32_t ah = smem_u32(sAh), b = smem_u32(sB);
+              for (int s = 0; s < ksteps; ++s)
+                mma_tf32(tmem, smem_desc(ah + 256 * s, lbo, sbo_a), smem_desc(b + 256 * s, lbo, sbo_b),
+                         idesc, 1);
+              mma_commit(mb_mma);
+            }
+          ok = __syncthreads_and(mbar_wait(mb_mma, ph_mma));
+          if (!ok)
+            break;
+          ph_mma ^= 1;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          // epilogue: warp w reads lanes 32w..32w+31, i.e. row t0 + tid
+          {
+            const int     i     = t0 + tid;
+            const bool    valid = i < rows_total;
+            float        *dst   = nullptr;
+            if (valid)
+              {
+                const int64_t q = start + i / R;
+                const int     r = i - (i / R) * R;
+                dst             = Y + (q * R + r) * K;
+              }
+            for (int c0 = 0; c0 < Np; c0 += 32)
+              {
+                float v[32];
+                tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+                if (valid)
+#pragma unroll
+                  for (int j = 0; j < 32; ++j)
+                    if (c0 + j < K)
+                      dst[c0 + j] = v[j];
+              }
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncthreads();
+        }
+      if (!ok)
+        {
+          if (tid == 0)
+            atomicExch(err, 1);
+          // bounded drain of whatever may still be in flight
+          mbar_wait(mb_mma, ph_mma);
+          mbar_wait(mb_tma, ph_tma);
+        }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     :
+                     : "r"(tmem), "r"(TC_TMEM_COLS)
+                     : "memory");
+    }
+
+    inline float tf32_round_host(float x)
+    {
+      uint32_t b;
+      std::memcpy(&b, &x, 4);
+      b = (b + 0x1000u) & ~0x1FFFu; // round to nearest, ties away from zero, 10-bit mantissa
+      float r;
+      std::memcpy(&r, &b, 4);
+      return r;
+    }
+  } // namespace
+
+  TcGeometry tc_geometry(int K)
+  {
+    TcGeometry g;
+    g.K  = K;
+    g.Kp = (K + 7) / 8 * 8;
+    g.Np = (K + 15) / 16 * 16;
+    g.smem = size_t(2) * TC_ROWS * g.Kp * 4 + size_t(g.Np) * g.Kp * 4 + 32;
+    g.ok = g.Np <= 256 && g.smem <= 220 * 1024;
+    return g;
+  }
+
+  void build_tc_images(const std::vector<double> &ops_out_in, int nops, int K,
+                       std::vector<float> &img)
+  {
+    const TcGeometry g = tc_geometry(K);
+    const size_t     half = size_t(g.Np) * g.Kp;
+    img.assign(size_t(nops) * 2 * half, 0.0f);
+    for (int o = 0; o < nops; ++o)
+      {
+        float *hi = img.data() + size_t(o) * 2 * half, *lo = hi + half;
+        for (int n = 0; n < K; ++n)
+          for (int k = 0; k < K; ++k)
+            {
+              const double v  = ops_out_in[size_t(o) * K * K + size_t(n) * K + k];
+              const float  h  = tf32_round_host(float(v));
+              const float  l  = float(v - double(h));
+              const size_t at = img_off(n, k, g.Kp) / 4;
+              hi[at]          = h;
+              lo[at]          = l;
+            }
+      }
+  }
+
+  void launch_tc_gemm(const OperatorDev<float> &op, int R, int c0, int c1, const float *E, float *Y,
+                      int *err, cudaStream_t s)
+  {
+    if (c1 <= c0)
+      return;
+    const TcGeometry g = tc_geometry(op.K);
+    PIBEM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(g.smem)));
+    tc_gemm_kernel<<<c1 - c0, TC_THREADS, g.smem, s>>>(R, op.K, g.Kp, g.Np, c0, op.ch_start,
+                                                       op.ch_cnt, op.ch_op, op.q_src, op.tc_images,
+                                                       E, Y, err);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+} // namespace pibem

@@ -594,7 +594,7 @@ namespace pibem
         while (i < b)
           {
             int64_t j = i;
-            while (j < b && pl.q_op[j] == pl.q_op[i] && j - i < 64)
+            while (j < b && pl.q_op[j] == pl.q_op[i] && j - i < 128)
               ++j;
             pl.ch_start.push_back(int32_t(i));
             pl.ch_cnt.push_back(int32_t(j - i));
