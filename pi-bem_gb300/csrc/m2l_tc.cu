@@ -128,6 +128,9 @@ namespace pibem
         v[j] = __uint_as_float(r[j]);
     }
 
+    // ALL_LEVELS_M2L only names the instantiation used for the batched M2L of all
+    // levels (so that profilers can select it); the code is the same.
+    template <bool ALL_LEVELS_M2L>
     __global__ void __launch_bounds__(TC_THREADS, 1)
       tc_gemm_kernel(int R, int K, int Kp, int Np, int chunk0, const int32_t *__restrict__ ch_start,
                      const int32_t *__restrict__ ch_cnt, const int32_t *__restrict__ ch_op,
@@ -341,11 +344,10 @@ namespace pibem
     if (c1 <= c0)
       return;
     const TcGeometry g = tc_geometry(op.K);
-    PIBEM_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(g.smem)));
-    tc_gemm_kernel<<<c1 - c0, TC_THREADS, g.smem, s>>>(R, op.K, g.Kp, g.Np, c0, op.ch_start,
-                                                       op.ch_cnt, op.ch_op, op.q_src, op.tc_images,
-                                                       E, Y, err);
+    auto fn = (c0 == 0 && c1 == op.m2l_chunk_end) ? tc_gemm_kernel<true> : tc_gemm_kernel<false>;
+    PIBEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
+    fn<<<c1 - c0, TC_THREADS, g.smem, s>>>(R, op.K, g.Kp, g.Np, c0, op.ch_start, op.ch_cnt, op.ch_op,
+                                           op.q_src, op.tc_images, E, Y, err);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
