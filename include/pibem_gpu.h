@@ -165,6 +165,27 @@ int pibem_phase_totals(pibem_handle *h, int32_t precision, double *ms7, int64_t 
 /* Number of CUDA kernels this library has launched so far (all handles). */
 int64_t pibem_launch_count(void);
 
+/* Allocation-free FMM matvec.  No counterpart in the reference.
+ * Same result as pibem_fmm_matvec (outN = N phi, outD = D dphi_dn), but with
+ * device pointers and without allocating any device memory during the call:
+ * every temporary of the call lives in one file-scope device array of
+ * PIBEM_NOALLOC_SCRATCH_BYTES that each GPU holds from library load to exit.
+ * For callers that must not allocate at call time: applications that reserve
+ * all device memory for themselves up front, and loops that cannot afford the
+ * device-wide synchronisation that cudaMalloc / cudaFree imply.  The mesh must
+ * be set up (pibem_set_mesh, which does allocate) beforehand.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - Work is ordered on the handle's stream; the call returns before it ends.
+ *  - All calls share the array and it keeps the last call's contents, so calls
+ *    whose work overlaps on the GPU (other streams, other handles) race.
+ *  - A mesh / nrhs whose temporaries exceed the array is rejected with
+ *    PIBEM_EINVAL and a message giving the size it would need. */
+#define PIBEM_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int pibem_fmm_matvec_noalloc(pibem_handle *h, int32_t nrhs, const double *d_phi,
+                             const double *d_dphi_dn, double *d_outN, double *d_outD);
+
 #ifdef __cplusplus
 }
 #endif

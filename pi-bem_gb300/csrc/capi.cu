@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <functional>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1599,4 +1600,107 @@ extern "C"
       ms7[i] = h->phase_ms[i];
     return PIBEM_OK;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free FMM matvec (pibem_fmm_matvec_noalloc).
+//
+// For callers that must not allocate device memory while they run: every
+// temporary of the call (multipole and local expansions, translation
+// products, M2P values, Dirichlet flags and column modes) is carved out of the
+// file-scope array below, which each GPU that loads the library holds until
+// the process exits.  Host code must not take the array's name as a device
+// address: the address is looked up once per device with cudaGetSymbolAddress
+// (first call on that device, device current) and kept.  Successive calls share
+// the array and find the previous call's contents; what must start at zero (the
+// multipole expansions, the flags) is cleared by each call.  Calls whose work
+// overlaps on the GPU race on the array.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_noalloc_scratch[PIBEM_NOALLOC_SCRATCH_BYTES / sizeof(double)];
+
+namespace
+{
+  std::mutex g_noalloc_mutex;
+  double    *g_noalloc_ptr[64] = {};
+
+  double *noalloc_scratch(int device)
+  {
+    if (device < 0 || device >= 64)
+      throw Error(PIBEM_EINVAL, "device ordinal out of range for the allocation-free scratch");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device])
+      {
+        void       *p  = nullptr;
+        cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (rc != cudaSuccess || !p)
+          throw Error(PIBEM_ECUDA, std::string("cudaGetSymbolAddress of the allocation-free scratch: ") +
+                                     cudaGetErrorString(rc));
+        g_noalloc_ptr[device] = static_cast<double *>(p);
+      }
+    return g_noalloc_ptr[device];
+  }
+
+  // The far-field launch sequence of far_field() on caller-provided buffers.
+  void far_field_on(pibem_handle *h, OperatorDev<double> &op, int R, const uint8_t *dir,
+                    const uint8_t *modes, const double *x, double *y, double *M, double *Lx,
+                    double *Y)
+  {
+    const int    N = int(h->N());
+    cudaStream_t s = h->stream;
+    PIBEM_CUDA(cudaMemsetAsync(M, 0, size_t(h->tree.nb) * R * op.K * sizeof(double), s));
+    launch_p2m_apply<double>(op, R, N, dir, modes, x, M, s);
+    for (int l = h->tree.L; l >= 1; --l)
+      launch_upward_level<double>(op, R, l, M, Y, s);
+    launch_m2l_gemm<double>(op, R, M, Y, s);
+    for (int l = 1; l <= h->tree.L; ++l)
+      launch_downward_level<double>(op, R, l, Lx, Y, s);
+    launch_m2p<double>(op, h->td, R, N, M, y, s);
+    launch_l2p<double>(op, R, N, Lx, y, s);
+  }
+} // namespace
+
+extern "C" int pibem_fmm_matvec_noalloc(pibem_handle *h, int32_t R, const double *d_phi,
+                                        const double *d_dphi, double *d_outN, double *d_outD)
+{
+  return guarded(h, [&] {
+    if (!h->mesh_ok)
+      throw Error(PIBEM_EINVAL, "pibem_fmm_matvec_noalloc before pibem_set_mesh");
+    if (R < 1 || !d_phi || !d_dphi || !d_outN || !d_outD)
+      throw Error(PIBEM_EINVAL, "bad arguments");
+    const int64_t N  = h->N();
+    const int64_t K  = h->plan.K;
+    const size_t  nM = size_t(h->tree.nb) * R * K;
+    const size_t  nY = std::max<size_t>(1, size_t(h->op64.n_pairs) * R * K);
+    const size_t  nS = std::max<size_t>(1, size_t(h->op64.n_m2p_items) * R);
+    const size_t  nF = (size_t(N) + size_t(R) + 7) / 8; // flags, in doubles
+    const size_t  need = (2 * nM + nY + nS + nF) * sizeof(double);
+    if (need > PIBEM_NOALLOC_SCRATCH_BYTES)
+      throw Error(PIBEM_EINVAL, "pibem_fmm_matvec_noalloc: this mesh and nrhs need " +
+                                  std::to_string(need / (1024.0 * 1024.0)) +
+                                  " MiB of scratch, more than the " +
+                                  std::to_string(PIBEM_NOALLOC_SCRATCH_BYTES >> 20) + " MiB array");
+    double      *M = noalloc_scratch(h->prm.device);
+    double      *Lx = M + nM, *Y = Lx + nM, *S = Y + nY;
+    uint8_t     *dir   = reinterpret_cast<uint8_t *>(S + nS);
+    uint8_t     *modes = dir + N;
+    cudaStream_t s     = h->stream;
+    // the handle's operator view, with the M2P scratch pointed into the array
+    // for the duration of the call (no host-side copy of the view)
+    OperatorDev<double> &op    = h->op64;
+    double *const        saved = op.m2p_scratch;
+    struct Restore
+    {
+      OperatorDev<double> &op;
+      double              *p;
+      ~Restore() { op.m2p_scratch = p; }
+    } restore{op, saved};
+    op.m2p_scratch = S;
+    PIBEM_CUDA(cudaMemsetAsync(dir, 0, size_t(N), s));
+    launch_near_spmv<double>(op, R, int(N), h->d_N.p, d_phi, d_outN, false, s);
+    launch_near_spmv<double>(op, R, int(N), h->d_D.p, d_dphi, d_outD, false, s);
+    PIBEM_CUDA(cudaMemsetAsync(modes, MODE_KER1, size_t(R), s));
+    far_field_on(h, op, R, dir, modes, d_phi, d_outN, M, Lx, Y);
+    PIBEM_CUDA(cudaMemsetAsync(modes, MODE_KER2, size_t(R), s));
+    far_field_on(h, op, R, dir, modes, d_dphi, d_outD, M, Lx, Y);
+  });
 }

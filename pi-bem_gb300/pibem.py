@@ -89,7 +89,7 @@ EXPORTS = [
     "pibem_solve", "pibem_solve_device", "pibem_tree_info_get", "pibem_tree_boxes",
     "pibem_tree_list", "pibem_tree_list_sublevels", "pibem_near_nnz", "pibem_near_export",
     "pibem_quad_points", "pibem_last_phase_ms", "pibem_set_profiling", "pibem_phase_totals",
-    "pibem_launch_count",
+    "pibem_launch_count", "pibem_fmm_matvec_noalloc",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -135,6 +135,8 @@ def load():
     L.pibem_phase_totals.argtypes = [C.c_void_p, C.c_int32, _dp, C.POINTER(C.c_int64), C.c_int32]
     L.pibem_launch_count.restype = C.c_int64
     L.pibem_launch_count.argtypes = []
+    L.pibem_fmm_matvec_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
