@@ -49,6 +49,20 @@ WORKLOADS = {
     "sphere1538": dict(kind="sphere", n=16, p=4, leaf=30, levels=10, seed=0, ext=False,
                        desc="unit cube-sphere 6x16x16, 1538 nodes, p=4, leaf<=30, Dirichlet, "
                             "interior, 1 RHS to 1e-8"),
+    "wigley393k": dict(kind="wigley", nx=768, nz=192, ny_lid=128, p=10, leaf=40, levels=10,
+                       seed=3, ext=True, cpu=False,
+                       desc="Wigley hull (L=1, B=0.1, T=0.0625) closed by a lid, sides 2x768x192 "
+                            "+ lid 768x128 Q1 cells, 393090 nodes, p=10, leaf<=40, mixed D/N "
+                            "(z > -T/2 Dirichlet), exterior, 1 RHS to 1e-8"),
+    "batched": dict(kind="batched",
+                    desc="one step = the 98,306-node spheroid (p=8, leaf<=40) x 64 RHS (seeds "
+                         "100..163) in one lockstep solve, concurrently with 32 perturbed spheres "
+                         "(n ~ log-U[12,100], 866..60,002 nodes, p in {6,8,10}, leaf and M2L "
+                         "engine by the autotuner), each handle on its own stream; 96 solves"),
+    "served": dict(kind="served",
+                   desc="request loop: Poisson arrivals over 12 meshes (perturbed spheres and "
+                        "Wigley hulls, N ~ log-U[2k,200k], D/N split by a seeded random plane), "
+                        "1-16 RHS per request, continuous batching per mesh, HBM budget 150 GB"),
 }
 
 
@@ -57,6 +71,8 @@ def make_case(w):
 
     if w["kind"] == "spheroid":
         mesh, mask, tmp, ph, dn = S.spheroid_mixed_case(w["n"], seed=w["seed"])
+    elif w["kind"] == "wigley":
+        mesh, mask, tmp, ph, dn = S.wigley_mixed_case(w["nx"], w["nz"], w["ny_lid"], seed=w["seed"])
     else:
         mesh, mask, tmp, dn = S.sphere_dirichlet_case(w["n"])
     return mesh, mask, tmp
@@ -327,7 +343,7 @@ def run_ours(args, w, rank, world, local):
     line["phases_ms_per_application"] = {
         prec: {k: v / max(c, 1) for k, v in pt.items() if k != "unused"} | {"applications": c}
         for prec, (pt, c) in (("fp32", ph32[0]), ("fp64", ph32[1]))}
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and w.get("cpu", True):
         line["cpu_baseline"] = cpu_baseline(w, mesh, mask, st64[-1]["fp64_matvecs"])
     if rank == 0:
         print(json.dumps(line))
@@ -337,6 +353,311 @@ def run_ours(args, w, rank, world, local):
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def _init_dist(world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    return dev
+
+
+def _done_dist(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def _base_line(w, args, world, value, unit, ms_per_step, dtype, config):
+    return {"metric": METRIC, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic (seeded point-source fields on generated meshes)",
+            "config": dict({"workload": args.workload, "description": w["desc"],
+                            "parallelism": f"replicas x{world}"}, **config)}
+
+
+def run_batched(args, w, rank, world, local):
+    """Many right-hand sides and many meshes on one GPU at once (see WORKLOADS)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import torch
+
+    import autotune
+    import pibem
+    import synthetic as S
+
+    dev = _init_dist(world, local)
+    base = dict(num_octree_levels=10, is_external_flow=1, solver_tolerance=1e-8,
+                solver_max_steps=4000, device=local)
+    # part A: spheroid x 64 RHS
+    meshA, maskA, _, _, _ = S.spheroid_mixed_case(128, seed=2)
+    tmpA = np.stack([S.spheroid_mixed_case(0, seed=sd, mesh=meshA)[2] for sd in range(100, 164)])
+    prmA = dict(base, fma_truncation_order=8, max_nodes_per_childless_block=40)
+    # part B: 32 perturbed spheres
+    rng = np.random.Generator(np.random.PCG64(4))
+    partB = []
+    for i in range(32):
+        n = int(round(np.exp(rng.uniform(np.log(12), np.log(100)))))
+        p = int(rng.choice([6, 8, 10]))
+        m = S.perturbed_sphere(n, seed=200 + i)
+        mask = S.mixed_bc_by_cell_centroid(m)
+        r2 = np.random.Generator(np.random.PCG64(300 + i))
+        q = r2.uniform(-1, 1, 8)
+        tmp = S.point_source_data(m, mask, S.sources_in_ball(r2, 8), q)[0]
+        partB.append((m, mask, tmp, p))
+    # autotuner: leaf size and translation engine per order, on the median mesh of each order
+    tuned, t0 = {}, time.perf_counter()
+    for p in (6, 8, 10):
+        cls = sorted([x for x in partB if x[3] == p], key=lambda x: x[0].n_nodes)
+        if not cls:
+            continue
+        m, mask, tmp, _ = cls[len(cls) // 2]
+        best, table = autotune.autotune(m.xyz, m.cells, mask, tmp, leaves=(20, 30, 40, 60),
+                                        repeats=1, precision_mode=pibem.PRECISION_MIXED,
+                                        fma_truncation_order=p, **base)
+        tuned[p] = {"leaf": best["max_nodes_per_childless_block"],
+                    "m2l_engine": ["tensor cores", "CUDA cores"][best["m2l_engine"]],
+                    "params": best, "trials_s": [(lf, e, round(t, 4)) for lf, e, t in table],
+                    "tuned_on_nodes": m.n_nodes}
+    autotune_s = time.perf_counter() - t0
+
+    def make(mode):
+        t0 = time.perf_counter()
+        hA = pibem.BEMSolver(precision_mode=mode, **prmA)
+        hA.set_mesh(meshA.xyz, meshA.cells)
+        hA.set_bc(maskA)
+        hB = []
+        for m, mask, tmp, p in partB:
+            g = pibem.BEMSolver(**dict(tuned[p]["params"], precision_mode=mode))
+            g.set_mesh(m.xyz, m.cells)
+            g.set_bc(mask)
+            hB.append(g)
+        return hA, hB, time.perf_counter() - t0
+
+    hA, hB, setup_s = make(pibem.PRECISION_MIXED)
+    # device-resident inputs and outputs per handle (each handle solves on its own stream)
+    def dev_bufs(tmp, mask, R):
+        t = torch.tensor(tmp.reshape(-1), device=dev, dtype=torch.float64)
+        m = np.tile(mask, R)
+        p0 = torch.tensor(np.where(m == 1, tmp.reshape(-1), 0.0), device=dev, dtype=torch.float64)
+        d0 = torch.tensor(np.where(m == 0, tmp.reshape(-1), 0.0), device=dev, dtype=torch.float64)
+        return t, p0, d0, p0.clone(), d0.clone()
+
+    bufA = dev_bufs(tmpA, maskA, 64)
+    bufB = [dev_bufs(tmp, mask, 1) for _, mask, tmp, _ in partB]
+    torch.cuda.synchronize()
+
+    def solve_dev(g, buf, R):
+        # the solve writes only the unknown entries of phi / dphi_dn (the known
+        # ones keep their data), so the buffers need no reset between steps
+        t, p0, d0, ph, dp = buf
+        return g.solve_device(R, ph.data_ptr(), dp.data_ptr(), t.data_ptr())
+
+    def solve_host(g, tmp):
+        return g.solve(tmp.reshape(-1))
+
+    workers = 5
+
+    def step(fa, fb):
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            futs = [ex.submit(fa)] + [ex.submit(fb, i) for i in range(len(partB))]
+            return [f.result() for f in futs]
+
+    dev_step = lambda: step(lambda: solve_dev(hA, bufA, 64), lambda i: solve_dev(hB[i], bufB[i], 1))
+    host_step = lambda: step(lambda: solve_host(hA, tmpA), lambda i: solve_host(hB[i], partB[i][2]))
+    K, W = args.steps, args.warmup
+    for _ in range(W):
+        dev_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    l0 = pibem.launch_count()
+    times, stats = [], None
+    with ClockSampler(local) as clk:
+        for _ in range(K):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            stats = dev_step()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+    launches = pibem.launch_count() - l0
+    t_max = max_over_ranks(sum(times), world, dev)
+    n_solves = 64 + len(partB)
+    value = K * n_solves * world / t_max
+    # e2e: the same batch through pibem_solve with host arrays
+    for _ in range(1):
+        host_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        host_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    # accuracy: true FP64 residual of every column, and alone == batched for two columns
+    g64 = pibem.BEMSolver(precision_mode=pibem.PRECISION_FP64, **prmA)
+    g64.set_mesh(meshA.xyz, meshA.cells)
+    g64.set_bc(maskA)
+    t, p0, d0, ph, dp = bufA
+    sol = np.where(np.tile(maskA, 64) == 1, dp.cpu().numpy(), ph.cpu().numpy()).reshape(64, -1)
+    b = g64.rhs(tmpA.reshape(-1)).reshape(64, -1)
+    res = np.linalg.norm(b - g64.system_matvec(sol.reshape(-1)).reshape(64, -1), axis=1)
+    worst_res = float((res / np.linalg.norm(b, axis=1)).max())
+    same = True
+    for c in (0, 37):
+        phc, dpc, _ = hA.solve(tmpA[c])
+        same = same and np.array_equal(np.where(maskA == 1, dpc, phc), sol[c])
+    # the same batch on the plain FP64 GPU path (one step)
+    for g in [hA] + hB:
+        g.close()
+    hA64, hB64, _ = make(pibem.PRECISION_FP64)
+    bufA64 = dev_bufs(tmpA, maskA, 64)
+    dev64 = lambda: step(lambda: solve_dev(hA64, bufA64, 64), lambda i: solve_dev(hB64[i], bufB[i], 1))
+    dev64()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev64()
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    for g in [hA64] + hB64:
+        g.close()
+    g64.close()
+    nB = [x[0].n_nodes for x in partB]
+    line = _base_line(w, args, world, value, "solves/s", t_max * 1e3 / K,
+                      "f32 operator + f64 refinement/Arnoldi",
+                      {"nodes_A": meshA.n_nodes, "nrhs_A": 64, "meshes_B": len(partB),
+                       "nodes_B_min_max": [min(nB), max(nB)],
+                       "orders_B": {str(p): sum(1 for x in partB if x[3] == p) for p in (6, 8, 10)},
+                       "concurrency": f"{workers} host threads, one CUDA stream per handle",
+                       "timing": "host clock around synchronised concurrent solves (inputs device-resident)",
+                       "l2": "working set > L2 (spheroid near field 230 MB FP32 + 461 MB FP64)"})
+    line.update({
+        "p50_ms": float(np.percentile(times, 50) * 1e3), "p99_ms": float(np.percentile(times, 99) * 1e3),
+        "fp64_path": {"value": n_solves / t64, "unit": "solves/s", "ms_per_step": t64 * 1e3},
+        "speedup_vs_fp64_path": value / (n_solves * world / t64),
+        "solve": {"A_iterations": stats[0]["iterations"], "A_fp32_matvecs": stats[0]["fp32_matvecs"],
+                  "A_fp64_matvecs": stats[0]["fp64_matvecs"],
+                  "A_worst_relative_residual_true_fp64": worst_res,
+                  "A_column_alone_equals_batched": bool(same)},
+        "autotune": {str(p): {k: v for k, v in d.items() if k != "params"} for p, d in tuned.items()},
+        "autotune_s": autotune_s, "setup_s": setup_s,
+        "e2e": {"value": K * n_solves * world / e2e_s, "unit": "solves/s",
+                "h2d_bytes_per_step": int(8 * 3 * (64 * meshA.n_nodes + sum(nB))),
+                "d2h_bytes_per_step": int(8 * 2 * (64 * meshA.n_nodes + sum(nB)))},
+        "clocks": clk.summary(), "gpu_launches": launches})
+    if rank == 0:
+        print(json.dumps(line))
+    _done_dist(world)
+
+
+def run_served(args, w, rank, world, local):
+    """Poisson request stream over a pool of meshes through serve.BEMServer."""
+    import threading as th
+
+    import torch
+
+    import pibem
+    import serve
+    import synthetic as S
+
+    dev = _init_dist(world, local)
+    rng = np.random.Generator(np.random.PCG64(5))
+    pool = []
+    for i in range(12):
+        N = float(np.exp(rng.uniform(np.log(2e3), np.log(2e5))))
+        if i % 2 == 0:
+            mesh, kind = S.perturbed_sphere(S.sphere_n_for_nodes(N), seed=500 + i), "ball"
+        else:
+            mesh, kind = S.wigley_hull(*S.wigley_for_nodes(N)), "wigley"
+        pool.append((f"{'sphere' if kind == 'ball' else 'wigley'}{i}", mesh,
+                     S.random_plane_mask(mesh, 600 + i), kind))
+    prm = dict(fma_truncation_order=8, max_nodes_per_childless_block=40, num_octree_levels=10,
+               is_external_flow=1, solver_tolerance=1e-8, solver_max_steps=4000, device=local,
+               precision_mode=pibem.PRECISION_MIXED)
+
+    def rhs(mesh, mask, kind, seed, R):
+        r = np.random.Generator(np.random.PCG64(seed))
+        cols = []
+        for _ in range(R):
+            src = S.sources_in_ball(r, 8) if kind == "ball" else S.sources_in_wigley(r, 8)
+            cols.append(S.point_source_data(mesh, mask, src, r.uniform(-1, 1, 8))[0])
+        return np.stack(cols)
+
+    srv = serve.BEMServer(hbm_budget_gb=150.0, workers=4, max_batch_rhs=16, **prm)
+    t0 = time.perf_counter()
+    for mid, mesh, mask, _ in pool:
+        srv.add_mesh(mid, mesh.xyz, mesh.cells, mask)
+        srv.preload(mid)
+    setup_s = time.perf_counter() - t0
+    # service time of one mean-sized request (8 RHS) per mesh, alone: sets the arrival rate
+    svc = []
+    for j, (mid, mesh, mask, kind) in enumerate(pool):
+        for _ in range(2):
+            r = srv.submit(mid, rhs(mesh, mask, kind, 9000 + j, 8))
+            r.wait()
+            if r.error:
+                raise r.error
+        svc.append(r.end - r.start)
+    mean_svc = float(np.mean(svc))
+    lam = 0.8 / mean_svc  # offered load 0.8 of one-at-a-time capacity
+    n_req = 24 + 12 * args.steps
+    n_warm = 12
+    gaps = rng.exponential(1.0 / lam, n_req)
+    picks = rng.integers(0, len(pool), n_req)
+    nrhs = rng.integers(1, 17, n_req)
+    data = [rhs(pool[k][1], pool[k][2], pool[k][3], 10_000 + j, int(R))
+            for j, (k, R) in enumerate(zip(picks, nrhs))]
+    reqs = []
+    torch.cuda.synchronize()
+    l0 = pibem.launch_count()
+    with ClockSampler(local) as clk:
+        t_start = time.perf_counter()
+        arrivals = t_start + np.cumsum(gaps)
+        for j in range(n_req):
+            d = arrivals[j] - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            reqs.append(srv.submit(pool[picks[j]][0], data[j], arrival=float(arrivals[j])))
+        for r in reqs:
+            r.wait()
+            if r.error:
+                raise r.error
+        torch.cuda.synchronize()
+    launches = pibem.launch_count() - l0
+    timed = reqs[n_warm:]
+    lat = np.array([r.latency for r in timed]) * 1e3
+    span = max(r.end for r in timed) - min(r.arrival for r in timed)
+    cols = sum(r.nrhs for r in timed)
+    value = cols / span
+    worst = max(r.stats["relative_residual"] for r in reqs)
+    resident = srv.resident_bytes()
+    counters = dict(srv.counters)
+    srv.close()
+    h2d = sum(3 * r.nrhs * r.tmp.shape[1] * 8 for r in timed) / len(timed)
+    line = _base_line(w, args, world, value, "solves/s", float(np.mean(lat)),
+                      "f32 operator + f64 refinement/Arnoldi",
+                      {"meshes": [(mid, m.n_nodes) for mid, m, _, _ in pool],
+                       "requests_timed": len(timed), "requests_warmup": n_warm,
+                       "rhs_per_request": "U{1..16}", "arrival_rate_per_s": lam,
+                       "offered_load": "0.8 x 1 / mean alone service time of an 8-RHS request",
+                       "workers": 4, "max_batch_rhs": 16, "hbm_budget_gb": 150.0,
+                       "p": 8, "leaf": 40,
+                       "timing": "host clock from each request's arrival to its completion"})
+    line.update({
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "mean_alone_service_ms_8rhs": mean_svc * 1e3,
+        "worst_relative_residual": worst, "resident_gb": resident / 1e9,
+        "server": counters, "setup_s": setup_s,
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(h2d * 2 / 3)},
+        "clocks": clk.summary(), "gpu_launches": launches})
+    if rank == 0:
+        print(json.dumps(line))
+    _done_dist(world)
 
 
 def roofline(info, n, prec, phase, ms, cnt, hbm_peak, bf16_peak, peak_kind, p):
@@ -449,7 +770,17 @@ def main():
     rank, world, local = dist_env()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
+        if w["kind"] in ("batched", "served"):
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable":
+                                  "the reference has no batched or served solve; its CPU operator "
+                                  "is timed on the single-mesh workloads"}))
+            return
         run_reference(args, w, rank, world)
+    elif w["kind"] == "batched":
+        run_batched(args, w, rank, world, local)
+    elif w["kind"] == "served":
+        run_served(args, w, rank, world, local)
     else:
         run_ours(args, w, rank, world, local)
 

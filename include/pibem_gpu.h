@@ -33,7 +33,14 @@ extern "C" {
 
 /* Arithmetic of the solve. */
 #define PIBEM_PRECISION_FP64 0  /* plain path: every matvec in FP64 */
-#define PIBEM_PRECISION_MIXED 1 /* FP32 operator inside GMRES + FP64 refinement residual */
+#define PIBEM_PRECISION_MIXED 1 /* FP32 operator inside GMRES + FP64-accurate refinement residual
+                                   (float-float translations, FP64 elsewhere) */
+#define PIBEM_PRECISION_FLOAT_FLOAT 2 /* every matvec FP64-accurate: FP64 near field and
+                                         expansions, translations in FP32-pair arithmetic */
+
+/* Engine of the FP32 translation GEMMs (M2L, M2M, L2L). */
+#define PIBEM_M2L_TENSOR_CORE 0 /* tcgen05 3xTF32 where the order fits (p <= 10), else CUDA cores */
+#define PIBEM_M2L_CUDA_CORE 1   /* FP32 FMA on CUDA cores */
 
 typedef struct pibem_handle pibem_handle;
 
@@ -64,6 +71,7 @@ typedef struct pibem_params
   int32_t device;                        /* CUDA device ordinal */
   double  inner_tolerance;               /* mixed mode: inner FP32 GMRES tolerance */
   double  hbm_budget_gb;                 /* 0 = unlimited */
+  int32_t m2l_engine;                    /* FP32 translations: PIBEM_M2L_* */
 } pibem_params;
 
 typedef struct pibem_solve_stats
@@ -164,6 +172,11 @@ int pibem_phase_totals(pibem_handle *h, int32_t precision, double *ms7, int64_t 
                        int32_t reset);
 /* Number of CUDA kernels this library has launched so far (all handles). */
 int64_t pibem_launch_count(void);
+/* Device memory the handle holds now (resident operator, tree, plan and its
+ * grow-only work buffers), in bytes.  No counterpart in the reference (its
+ * operator lives in host memory); serving loops use it to keep a set of
+ * resident meshes inside an HBM budget. */
+int pibem_device_bytes(const pibem_handle *h, uint64_t *bytes);
 
 /* Allocation-free FMM matvec.  No counterpart in the reference.
  * Same result as pibem_fmm_matvec (outN = N phi, outD = D dphi_dn), but with

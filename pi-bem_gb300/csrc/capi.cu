@@ -16,6 +16,8 @@
 #include <cmath>
 #include <cstdlib>
 #include <functional>
+#include <limits>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -27,11 +29,32 @@
 using namespace pibem;
 
 static std::atomic<int64_t> g_launches{0};
+static std::mutex          g_near_assembly_mu; // see set_mesh_impl
 
 namespace pibem
 {
-  void    note_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+  // launches made by this host thread (stream capture counts its own kernels)
+  static thread_local int64_t t_launches = 0;
+  void    note_launch(int64_t n)
+  {
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+    t_launches += n;
+  }
   int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+  void raise_smem_limit(const void *fn, size_t bytes)
+  {
+    static std::mutex                                   mu;
+    static std::map<std::pair<int, const void *>, size_t> set;
+    int dev = 0;
+    PIBEM_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = set[{dev, fn}];
+    if (bytes <= cur)
+      return;
+    PIBEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    cur = bytes;
+  }
 } // namespace pibem
 
 namespace
@@ -141,6 +164,7 @@ struct pibem_handle
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv;
   DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg;
+  DBuf<float2>  d_opsff; // the FP64 operator table as (hi, lo) FP32 pairs
   DBuf<int>     d_err;
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
@@ -149,13 +173,23 @@ struct pibem_handle
   TreeDev             td;
   // boundary conditions
   std::vector<uint8_t> dir;
-  DBuf<uint8_t>        d_dir, d_modes;
+  DBuf<uint8_t>        d_dir, d_modes, d_modes32;
+  int                  modes32_R = 0; // d_modes32 holds MODE_COMBINED for this many columns
   DBuf<double>         d_alpha;
   bool                 have_dirichlet = true;
   // work
   DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64;
   DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32, d_Y32;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
+  // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
+  // and so no device-wide synchronisation, once a handle has solved its largest batch)
+  DBuf<double> sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm;
+  DBuf<double> io_buf[4];
+  // the FP32 operator (near SpMV + far field on d_x32 -> d_y32) as one CUDA
+  // graph, captured for the buffers and column count in g32_key
+  cudaGraphExec_t g32_exec = nullptr;
+  uintptr_t       g32_key[8] = {};
+  int64_t         g32_kernels = 0;
   // timing
   bool        timing = false;
   cudaEvent_t ev[8] = {};
@@ -166,6 +200,32 @@ struct pibem_handle
   int64_t     m2p_items = 0, m2p_tnodes = 0;
 
   int64_t N() const { return mesh.n_nodes; }
+
+  // Device memory held by the handle (every buffer above, at its capacity).
+  size_t device_bytes() const
+  {
+    size_t t = 0;
+    auto   add = [&t](const auto &...b) { ((t += b.bytes()), ...); };
+    add(d_xyz, d_qpts, d_qnrm, d_qjxw, d_qshape, d_gpts, d_gw, d_cells, d_dbl_off, d_dbl_ids);
+    add(d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted, d_center,
+        d_delta);
+    add(d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr, d_m2l_src_ptr,
+        d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr, d_up_q_ptr,
+        d_down_q_ptr);
+    add(d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
+        d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
+        d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
+        d_up_box, d_down_box, d_up_q, d_down_q);
+    add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_S32, d_T1f, d_T2f, d_Wf,
+        d_opsf, d_opsff, d_tcimg, d_err, d_dir, d_modes, d_modes32, d_alpha);
+    add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
+        d_y32, d_m2p32, d_Y32);
+    add(g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
+        sv_part, sv_nrm);
+    for (const auto &b : io_buf)
+      t += b.bytes();
+    return t;
+  }
 };
 
 namespace
@@ -353,6 +413,103 @@ namespace
     h->cnt64 += R;
   }
 
+  // Near SpMV + far field of the FP32 system operator, d_x32 -> d_y32.
+  void operator32_body(pibem_handle *h, int R)
+  {
+    const int64_t N = h->N();
+    record(h, 0);
+    launch_near_spmv<float>(h->op32, R, int(N), h->d_S32.p, h->d_x32.p, h->d_y32.p, false,
+                            h->stream);
+    record(h, 1);
+    far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, h->d_Y32, R, h->d_modes32.p,
+                     h->d_x32.p, h->d_y32.p);
+  }
+
+  void drop_graph(pibem_handle *h)
+  {
+    if (h->g32_exec)
+      cudaGraphExecDestroy(h->g32_exec);
+    h->g32_exec = nullptr;
+  }
+
+  // The FP32 operator is applied once per GMRES iteration with the same buffers,
+  // so it is captured once as a CUDA graph (about 45 kernels) and replayed: one
+  // launch instead of ~45, and no launch gaps between its small kernels.  Not
+  // used while phase timing is on (its events are host-recorded) or when the
+  // caller's stream is itself being captured.
+  void operator32(pibem_handle *h, int R)
+  {
+    cudaStream_t s = h->stream;
+    if (h->modes32_R != R)
+      {
+        std::vector<uint8_t> modes(R, MODE_COMBINED);
+        h->d_modes32.upload(modes, s);
+        h->modes32_R = R;
+      }
+    bool graph = !h->timing;
+    if (graph)
+      {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        PIBEM_CUDA(cudaStreamIsCapturing(s, &cs));
+        graph = cs == cudaStreamCaptureStatusNone;
+      }
+    if (!graph)
+      {
+        operator32_body(h, R);
+        return;
+      }
+    auto key_of = [&](uintptr_t k[8]) {
+      k[0] = uintptr_t(R);
+      k[1] = uintptr_t(h->d_x32.p);
+      k[2] = uintptr_t(h->d_y32.p);
+      k[3] = uintptr_t(h->d_M32.p);
+      k[4] = uintptr_t(h->d_L32.p);
+      k[5] = uintptr_t(h->d_Y32.p);
+      k[6] = uintptr_t(h->d_m2p32.p);
+      k[7] = uintptr_t(h->d_modes32.p) ^ uintptr_t(s);
+    };
+    uintptr_t key[8];
+    key_of(key);
+    if (h->g32_exec && std::equal(key, key + 8, h->g32_key))
+      {
+        PIBEM_CUDA(cudaGraphLaunch(h->g32_exec, s));
+        note_launch(h->g32_kernels);
+        return;
+      }
+    // New buffers or column count: apply once directly (this also grows the
+    // work buffers to their final size), then capture the same sequence.
+    drop_graph(h);
+    operator32_body(h, R);
+    key_of(key);
+    const int64_t l0 = t_launches;
+    cudaGraph_t   g  = nullptr;
+    PIBEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    try
+      {
+        operator32_body(h, R);
+      }
+    catch (...)
+      {
+        cudaStreamEndCapture(s, &g);
+        if (g)
+          cudaGraphDestroy(g);
+        throw;
+      }
+    PIBEM_CUDA(cudaStreamEndCapture(s, &g));
+    const cudaError_t e = cudaGraphInstantiate(&h->g32_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+      {
+        h->g32_exec = nullptr;
+        throw Error(PIBEM_ECUDA, std::string("graph instantiation: ") + cudaGetErrorString(e));
+      }
+    // the captured kernels did not run: count them at each replay instead
+    h->g32_kernels = t_launches - l0;
+    g_launches.fetch_sub(h->g32_kernels, std::memory_order_relaxed);
+    t_launches = l0;
+    std::copy(key, key + 8, h->g32_key);
+  }
+
   // Same operator in FP32 (input and output FP64).
   void system_apply32(pibem_handle *h, int R, const double *x, double *y)
   {
@@ -369,12 +526,7 @@ namespace
     h->d_x32.alloc(size_t(R) * N);
     h->d_y32.alloc(size_t(R) * N);
     launch_convert_d2f(int64_t(R) * N, xin, h->d_x32.p, s);
-    set_modes(h, R, MODE_COMBINED);
-    record(h, 0);
-    launch_near_spmv<float>(h->op32, R, int(N), h->d_S32.p, h->d_x32.p, h->d_y32.p, false, s);
-    record(h, 1);
-    far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, h->d_Y32, R, h->d_modes.p, h->d_x32.p,
-                     h->d_y32.p);
+    operator32(h, R);
     finish_timing(h, 1);
     launch_convert_f2d(int64_t(R) * N, h->d_y32.p, y, s);
     if (!h->have_dirichlet)
@@ -385,8 +537,11 @@ namespace
   // ---------------------------------------------------------------------
   // Restarted GMRES(m) for R right-hand sides in lockstep, right leaf-block
   // Jacobi preconditioning, CGS2 Arnoldi in FP64 on the device, Givens
-  // rotations and the small least-squares problem on the host.  Stops each
-  // column at ||b - A x|| / ||b|| <= tol (true residual at every restart).
+  // rotations and the small least-squares problem on the host.  Stops column r
+  // at ||b - A x|| / ||b|| <= tol[r] (true residual at every restart); a column
+  // with tol[r] = +inf is left unchanged.  The columns share the operator
+  // applications but no arithmetic, so a column's iterates do not depend on the
+  // other columns of the batch.
   // ---------------------------------------------------------------------
   struct GmresResult
   {
@@ -394,8 +549,17 @@ namespace
     std::vector<double> rel;
   };
 
-  GmresResult gmres(pibem_handle *h, int R, const double *b, double *x, double tol, int maxit,
-                    int m, const std::function<void(const double *, double *)> &A, bool prec)
+  // R columns of n doubles from src (column stride lds) to dst (column stride ldd)
+  void copy_cols(double *dst, int64_t ldd, const double *src, int64_t lds, int64_t n, int R,
+                 cudaStream_t s)
+  {
+    PIBEM_CUDA(cudaMemcpy2DAsync(dst, size_t(ldd) * sizeof(double), src, size_t(lds) * sizeof(double),
+                                 size_t(n) * sizeof(double), size_t(R), cudaMemcpyDeviceToDevice, s));
+  }
+
+  GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
+                    const std::vector<double> &tol, int maxit, int m,
+                    const std::function<void(const double *, double *)> &A, bool prec)
   {
     const int64_t N    = h->N();
     cudaStream_t  s    = h->stream;
@@ -425,16 +589,11 @@ namespace
       {
         // true residual r = b - A x into V[:,0]
         A(x, h->g_w.p);
-        for (int r = 0; r < R; ++r)
-          {
-            PIBEM_CUDA(cudaMemcpyAsync(h->g_V.p + r * ldr, b + r * N, sizeof(double) * N,
-                                       cudaMemcpyDeviceToDevice, s));
-            launch_axpby(N, -1.0, h->g_w.p + r * N, 1.0, h->g_V.p + r * ldr, s);
-          }
+        // w <- b - w, then V[r][0] <- w[r]
+        launch_axpby(int64_t(R) * N, 1.0, b, -1.0, h->g_w.p, s);
+        copy_cols(h->g_V.p, ldr, h->g_w.p, N, N, R, s);
         std::vector<double> b2(R);
-        for (int r = 0; r < R; ++r)
-          launch_dots(N, 1, 1, N, N, h->g_V.p + r * ldr, h->g_V.p + r * ldr, h->g_partial.p, nblk,
-                      h->g_nrm.p + r, s);
+        launch_dots(N, R, 1, N, N, h->g_w.p, h->g_w.p, h->g_partial.p, nblk, h->g_nrm.p, s);
         h->g_nrm.download(b2.data(), R, s);
         PIBEM_CUDA(cudaStreamSynchronize(s));
         bool any = false;
@@ -442,15 +601,12 @@ namespace
           {
             beta[r]    = std::sqrt(b2[r]);
             res.rel[r] = beta[r] / bn[r];
-            kdone[r]   = res.rel[r] <= tol ? 0 : -1;
+            kdone[r]   = res.rel[r] <= tol[r] ? 0 : -1;
             any        = any || kdone[r] < 0;
           }
         if (!any || res.iterations >= maxit)
           break;
-        for (int r = 0; r < R; ++r) // V[r][0] = r_r / beta_r (through the w buffer)
-          PIBEM_CUDA(cudaMemcpyAsync(h->g_w.p + r * N, h->g_V.p + r * ldr, sizeof(double) * N,
-                                     cudaMemcpyDeviceToDevice, s));
-        launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p, ldr, s);
+        launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p, ldr, s); // V[r][0] = r_r / beta_r
         std::fill(g.begin(), g.end(), 0.0);
         for (int r = 0; r < R; ++r)
           g[size_t(r) * (m + 1)] = beta[r];
@@ -461,26 +617,20 @@ namespace
             const double *vj = h->g_V.p + int64_t(j) * N;
             if (prec)
               {
-                for (int r = 0; r < R; ++r)
-                  PIBEM_CUDA(cudaMemcpyAsync(h->g_u.p + r * N, vj + r * ldr, sizeof(double) * N,
-                                             cudaMemcpyDeviceToDevice, s));
+                copy_cols(h->g_u.p, N, vj, ldr, N, R, s);
                 launch_block_apply(h->plan.nrows.size(), R, N, h->d_row_leaf.p, h->d_nrow_ptr.p,
                                    h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, h->g_z.p,
                                    s);
               }
             else
-              for (int r = 0; r < R; ++r)
-                PIBEM_CUDA(cudaMemcpyAsync(h->g_z.p + r * N, vj + r * ldr, sizeof(double) * N,
-                                           cudaMemcpyDeviceToDevice, s));
+              copy_cols(h->g_z.p, N, vj, ldr, N, R, s);
             A(h->g_z.p, h->g_w.p);
             // CGS2
             launch_dots(N, R, j + 1, N, ldr, h->g_V.p, h->g_w.p, h->g_partial.p, nblk, h->g_h.p, s);
             launch_gemv_sub(N, R, j + 1, N, ldr, h->g_V.p, h->g_h.p, j + 1, h->g_w.p, 1.0, s);
             launch_dots(N, R, j + 1, N, ldr, h->g_V.p, h->g_w.p, h->g_partial.p, nblk, h->g_h2.p, s);
             launch_gemv_sub(N, R, j + 1, N, ldr, h->g_V.p, h->g_h2.p, j + 1, h->g_w.p, 1.0, s);
-            for (int r = 0; r < R; ++r)
-              launch_dots(N, 1, 1, N, N, h->g_w.p + r * N, h->g_w.p + r * N, h->g_partial.p, nblk,
-                          h->g_nrm.p + r, s);
+            launch_dots(N, R, 1, N, N, h->g_w.p, h->g_w.p, h->g_partial.p, nblk, h->g_nrm.p, s);
             launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p + int64_t(j + 1) * N, ldr, s);
             h->g_h.download(hh.data(), size_t(R) * (j + 1), s);
             h->g_h2.download(h2.data(), size_t(R) * (j + 1), s);
@@ -511,7 +661,7 @@ namespace
                 Hc[size_t(j + 1) * m + j] = 0;
                 gg[j + 1] = -sv[j] * gg[j];
                 gg[j]     = c[j] * gg[j];
-                if (std::fabs(gg[j + 1]) / bn[r] <= tol || bb == 0.0)
+                if (std::fabs(gg[j + 1]) / bn[r] <= tol[r] || bb == 0.0)
                   kdone[r] = j + 1;
                 else
                   all = false;
@@ -615,6 +765,7 @@ namespace
       op.ch_cnt        = h->d_ch_cnt.p;
       op.ch_op         = h->d_ch_op.p;
       op.m2l_chunk_end = pl.m2l_chunk_end;
+      op.max_chunk_pairs = pl.ch_cnt.empty() ? 0 : *std::max_element(pl.ch_cnt.begin(), pl.ch_cnt.end());
       op.up_chunk_ptr  = pl.up_chunk_ptr;
       op.down_chunk_ptr = pl.down_chunk_ptr;
       op.up_box_ptr    = pl.up_box_ptr;
@@ -646,6 +797,7 @@ namespace
     h->op64.T2      = h->d_T2.p;
     h->op64.W       = h->d_W.p;
     h->op64.ops     = h->d_ops.p;
+    h->op64.ops_ff  = h->prm.precision_mode == PIBEM_PRECISION_FLOAT_FLOAT ? h->d_opsff.p : nullptr;
     h->op32.T1      = h->d_T1f.p;
     h->op32.T2      = h->d_T2f.p;
     h->op32.W       = h->d_Wf.p;
@@ -769,6 +921,7 @@ namespace
                      const int32_t *cells, const int32_t *doff, const int32_t *dids)
   {
     auto t0 = std::chrono::steady_clock::now();
+    drop_graph(h); // its kernels carry the previous mesh's sizes
     if (n_nodes <= 0 || n_cells <= 0 || !xyz || !cells)
       throw Error(PIBEM_EINVAL, "empty mesh");
     if ((doff == nullptr) != (dids == nullptr))
@@ -824,7 +977,6 @@ namespace
     for (int v = 0; v < 4; ++v)
       telles_rule_2d(P.singular_quadrature_order, v, h->tpts[v], h->tw[v]);
     h->n_tel = int(h->tw[0].size());
-    set_telles_rules(h->tpts, h->tw, h->n_tel, s);
     // device mesh and quadrature data
     h->d_xyz.upload(m.xyz, s);
     h->d_cells.upload(m.cells, s);
@@ -982,7 +1134,14 @@ namespace
       a.Nval          = h->d_N.p;
       a.Dval          = h->d_D.p;
       if (nl > 0)
-        launch_near_assembly(a, s);
+        {
+          // the singular rules live in constant memory shared by every handle of
+          // the process: one near-field assembly at a time
+          std::lock_guard<std::mutex> lock(g_near_assembly_mu);
+          set_telles_rules(h->tpts, h->tw, h->n_tel, s);
+          launch_near_assembly(a, s);
+          PIBEM_CUDA(cudaStreamSynchronize(s));
+        }
       PIBEM_CUDA(cudaStreamSynchronize(s));
       h->d_S.alloc(nval);
       h->d_S32.alloc(nval);
@@ -1033,6 +1192,15 @@ namespace
       h->d_ops.upload(td, s);
       transpose_ops(all, nops, K, tf);
       h->d_opsf.upload(tf, s);
+      {
+        std::vector<float2> ff(td.size());
+        for (size_t i = 0; i < td.size(); ++i)
+          {
+            const float hi = float(td[i]);
+            ff[i]          = make_float2(hi, float(td[i] - double(hi)));
+          }
+        h->d_opsff.upload(ff, s);
+      }
       h->d_tcimg.release();
       if (h->use_tc && tc_geometry(K).ok)
         {
@@ -1065,6 +1233,7 @@ namespace
 
   void set_bc_impl(pibem_handle *h, const uint8_t *mask)
   {
+    drop_graph(h);
     if (!h->mesh_ok)
       throw Error(PIBEM_EINVAL, "pibem_set_bc before pibem_set_mesh");
     if (!mask)
@@ -1140,7 +1309,17 @@ namespace
     const int64_t N  = h->N();
     cudaStream_t  s  = h->stream;
     h->cnt64 = h->cnt32 = 0;
-    DBuf<double> b, x, r, d;
+    // The mixed path forms its right-hand side and FP64 residuals with the
+    // FP64-accurate float-float translations (FP64 near field and expansions).
+    struct FfGuard
+    {
+      OperatorDev<double> &op;
+      const float2        *prev;
+      ~FfGuard() { op.ops_ff = prev; }
+    } ff_guard{h->op64, h->op64.ops_ff};
+    if (h->prm.precision_mode == PIBEM_PRECISION_MIXED)
+      h->op64.ops_ff = h->d_opsff.p;
+    DBuf<double> &b = h->sv_b, &x = h->sv_x, &r = h->sv_r, &d = h->sv_d, &w = h->sv_w;
     b.alloc(size_t(R) * N);
     x.alloc(size_t(R) * N);
     compute_rhs_dev(h, R, tmp, b.p);
@@ -1151,10 +1330,10 @@ namespace
     auto A32 = [h, R](const double *in, double *out) { system_apply32(h, R, in, out); };
     int                 iters = 0, refine = 0;
     std::vector<double> rel;
-    if (P.precision_mode == PIBEM_PRECISION_FP64)
+    if (P.precision_mode != PIBEM_PRECISION_MIXED)
       {
-        GmresResult gr = gmres(h, R, b.p, x.p, P.solver_tolerance, P.solver_max_steps,
-                               P.gmres_restart, A64, prec);
+        GmresResult gr = gmres(h, R, b.p, x.p, std::vector<double>(R, P.solver_tolerance),
+                               P.solver_max_steps, P.gmres_restart, A64, prec);
         iters          = gr.iterations;
         rel            = gr.rel;
       }
@@ -1165,21 +1344,21 @@ namespace
         // the whole solution, so its residual is formed with the FP64 operator;
         // every later correction d_k is small (|d_k| <= tol_inner^k |x|), so the
         // residual is updated as r <- r - A32 d_k, whose rounding error
-        // eps32 * |A| |d_k| stays far below the target.
+        // eps32 * |A| |d_k| stays far below the target.  Each column has its own
+        // inner tolerance and stops refining once it meets the target (its later
+        // corrections are zero), so a column's solution is the same alone or in a
+        // batch.
         r.alloc(size_t(R) * N);
         d.alloc(size_t(R) * N);
-        DBuf<double> w;
         w.alloc(size_t(R) * N);
+        h->sv_part.alloc(size_t(R) * 64);
+        h->sv_nrm.alloc(R);
         const int max_refine = 12;
         rel.assign(R, 1.0);
-        std::vector<double> bn(R), rn(R);
-        DBuf<double>        part, nrm;
-        part.alloc(size_t(R) * 64);
-        nrm.alloc(R);
+        std::vector<double> bn(R), rn(R), itol(R);
         auto norms = [&](const double *v, std::vector<double> &out) {
-          for (int c = 0; c < R; ++c)
-            launch_dots(N, 1, 1, N, N, v + c * N, v + c * N, part.p, 64, nrm.p + c, s);
-          nrm.download(out.data(), R, s);
+          launch_dots(N, R, 1, N, N, v, v, h->sv_part.p, 64, h->sv_nrm.p, s);
+          h->sv_nrm.download(out.data(), R, s);
           PIBEM_CUDA(cudaStreamSynchronize(s));
           for (auto &v2 : out)
             v2 = std::sqrt(v2);
@@ -1195,13 +1374,14 @@ namespace
             bool ok = true;
             for (int c = 0; c < R; ++c)
               {
-                rel[c] = rn[c] / bn[c];
-                ok     = ok && rel[c] <= P.solver_tolerance;
+                rel[c]  = rn[c] / bn[c];
+                itol[c] = rel[c] <= P.solver_tolerance
+                            ? std::numeric_limits<double>::infinity()
+                            : std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / rel[c]);
+                ok = ok && rel[c] <= P.solver_tolerance;
               }
             if (ok || refine == max_refine || iters >= P.solver_max_steps)
               break;
-            double worst = *std::max_element(rel.begin(), rel.end());
-            double itol  = std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / worst);
             PIBEM_CUDA(cudaMemsetAsync(d.p, 0, sizeof(double) * R * N, s));
             GmresResult gr = gmres(h, R, r.p, d.p, itol, P.solver_max_steps - iters,
                                    P.gmres_restart, A32, prec);
@@ -1236,29 +1416,23 @@ namespace
                                    std::to_string(worst) + ")");
   }
 
-  // host <-> device staging helpers for the host-pointer entry points
+  // host <-> device staging of the host-pointer entry points, in the handle's
+  // grow-only slots
   struct HostIO
   {
     pibem_handle *h;
-    std::vector<DBuf<double> *> bufs;
+    int           next = 0;
     double *in(const double *hp, size_t n)
     {
-      auto *b = new DBuf<double>();
-      b->upload(hp, n, h->stream);
-      bufs.push_back(b);
-      return b->p;
+      DBuf<double> &b = h->io_buf[next++];
+      b.upload(hp, n, h->stream);
+      return b.p;
     }
     double *scratch(size_t n)
     {
-      auto *b = new DBuf<double>();
-      b->alloc(n);
-      bufs.push_back(b);
-      return b->p;
-    }
-    ~HostIO()
-    {
-      for (auto *b : bufs)
-        delete b;
+      DBuf<double> &b = h->io_buf[next++];
+      b.alloc(n);
+      return b.p;
     }
   };
 } // namespace
@@ -1275,7 +1449,9 @@ extern "C"
         P.num_octree_levels > 20 || P.max_nodes_per_childless_block < 1 ||
         P.quadrature_order < 1 || P.quadrature_order > 8 || P.singular_quadrature_order < 1 ||
         P.singular_quadrature_order > 12 || P.gmres_restart < 1 || P.solver_max_steps < 1 ||
-        !(P.solver_tolerance > 0))
+        !(P.solver_tolerance > 0) || P.precision_mode < PIBEM_PRECISION_FP64 ||
+        P.precision_mode > PIBEM_PRECISION_FLOAT_FLOAT || P.m2l_engine < PIBEM_M2L_TENSOR_CORE ||
+        P.m2l_engine > PIBEM_M2L_CUDA_CORE)
       return PIBEM_EINVAL;
     pibem_handle *h = new (std::nothrow) pibem_handle();
     if (!h)
@@ -1288,8 +1464,7 @@ extern "C"
         h->stream = h->own;
         const char *env = std::getenv("PIBEM_PHASE_TIMING");
         h->timing       = env && env[0] == '1';
-        const char *tc  = std::getenv("PIBEM_TENSOR_CORE_M2L");
-        h->use_tc       = !(tc && tc[0] == '0');
+        h->use_tc       = P.m2l_engine != PIBEM_M2L_CUDA_CORE;
         for (auto &e : h->ev)
           PIBEM_CUDA(cudaEventCreate(&e));
       }
@@ -1314,6 +1489,7 @@ extern "C"
       if (e)
         cudaEventDestroy(e);
     cudaStream_t own = h->own;
+    drop_graph(h);
     delete h;
     if (own)
       cudaStreamDestroy(own);
@@ -1347,7 +1523,7 @@ extern "C"
       if (R < 1 || !phi || !dphi || !oN || !oD)
         throw Error(PIBEM_EINVAL, "bad arguments");
       const size_t n = size_t(R) * h->N();
-      HostIO       io{h, {}};
+      HostIO       io{h};
       double      *dp = io.in(phi, n), *dd = io.in(dphi, n);
       double      *on = io.scratch(n), *od = io.scratch(n);
       if (h->d_dir.n == 0)
@@ -1380,7 +1556,7 @@ extern "C"
       if (R < 1 || !x || !y)
         throw Error(PIBEM_EINVAL, "bad arguments");
       const size_t n  = size_t(R) * h->N();
-      HostIO       io{h, {}};
+      HostIO       io{h};
       double      *dx = io.in(x, n), *dy = io.scratch(n);
       if (h->prm.precision_mode == PIBEM_PRECISION_MIXED && std::getenv("PIBEM_MATVEC_FP32"))
         system_apply32(h, R, dx, dy);
@@ -1398,7 +1574,7 @@ extern "C"
       if (!h->bc_ok)
         throw Error(PIBEM_EINVAL, "pibem_compute_rhs before pibem_set_bc");
       const size_t n  = size_t(R) * h->N();
-      HostIO       io{h, {}};
+      HostIO       io{h};
       double      *dt = io.in(tmp, n), *db = io.scratch(n);
       compute_rhs_dev(h, R, dt, db);
       PIBEM_CUDA(cudaMemcpyAsync(rhs, db, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1413,7 +1589,7 @@ extern "C"
       if (R < 1 || !phi || !dphi || !tmp)
         throw Error(PIBEM_EINVAL, "bad arguments");
       const size_t n  = size_t(R) * h->N();
-      HostIO       io{h, {}};
+      HostIO       io{h};
       double      *dp = io.in(phi, n), *dd = io.in(dphi, n), *dt = io.in(tmp, n);
       int          code = PIBEM_OK;
       std::string  msg;
@@ -1445,6 +1621,14 @@ extern "C"
         throw Error(PIBEM_EINVAL, "bad arguments");
       solve_dev(h, R, phi, dphi, tmp, st);
     });
+  }
+
+  int pibem_device_bytes(const pibem_handle *h, uint64_t *bytes)
+  {
+    if (!h || !bytes)
+      return PIBEM_EINVAL;
+    *bytes = uint64_t(h->device_bytes());
+    return PIBEM_OK;
   }
 
   int pibem_tree_info_get(pibem_handle *h, pibem_tree_info *info)

@@ -8,6 +8,7 @@
 //   M2P for deeper non-interaction boxes (bem_fma.cc:2664-2704)
 //   L2P at the nodes of childless boxes (bem_fma.cc:2959-2986)
 // Expansions are laid out [box][rhs][k] with K = (p+1)^2 scaled reals.
+#include <mutex>
 #include <type_traits>
 
 #include "devmath.cuh"
@@ -184,83 +185,179 @@ namespace pibem
 
     // Batched translation GEMM.  Scaled operators do not depend on the level:
     // M2L depends only on the integer source-target offset, M2M / L2L only on
-    // the child octant.  Pairs sharing an operator are cut into chunks of <= 64;
-    // block c computes  Y[q] = T_op(c) E[src(q)]  for the chunk's pairs (x R
-    // columns) with the operator staged once in shared memory (CUDA-core FMA,
-    // 16x16 threads, 8x4 outputs per thread).
+    // the child octant.  Pairs sharing an operator are cut into chunks of <= 128;
+    // block (c, t) computes  Y[q] = T_op(c) E[src(q)]  for columns 64t..64t+63 of
+    // chunk c (column = (pair, rhs)), with the operator staged in shared memory
+    // (CUDA-core FMA, 16x16 threads, KI x 4 outputs per thread, KI = ceil(K/16)
+    // so that no thread computes rows beyond K).
     constexpr int GB_COLS = 64;
     constexpr int GB_LDB  = GB_COLS + 1;
 
-    template <typename T>
-    __global__ void __launch_bounds__(256)
+    template <typename T, int KI>
+    __global__ void __launch_bounds__(256, 2)
       trans_gemm_kernel(int R, int K, int chunk0, const int32_t *__restrict__ chunk_start,
-                      const int32_t *__restrict__ chunk_cnt, const int32_t *__restrict__ chunk_off,
-                      const int32_t *__restrict__ q_src, const T *__restrict__ ops,
-                      const T *__restrict__ M, T *__restrict__ Y)
+                        const int32_t *__restrict__ chunk_cnt, const int32_t *__restrict__ chunk_off,
+                        const int32_t *__restrict__ q_src, const T *__restrict__ ops,
+                        const T *__restrict__ M, T *__restrict__ Y)
     {
       extern __shared__ unsigned char smem_raw[];
       T        *sT    = reinterpret_cast<T *>(smem_raw); // [K][K] in-major
       T        *sB    = sT + K * K;                      // [K][GB_LDB]
       const int ch    = chunk0 + blockIdx.x;
-      const int start = chunk_start[ch], cnt = chunk_cnt[ch];
-      const T  *op    = ops + int64_t(chunk_off[ch]) * K * K;
+      const int start = chunk_start[ch], ncols = chunk_cnt[ch] * R;
+      const int c0    = blockIdx.y * GB_COLS;
+      if (c0 >= ncols)
+        return;
+      const int nc = min(GB_COLS, ncols - c0);
+      const T  *op = ops + int64_t(chunk_off[ch]) * K * K;
       for (int i = threadIdx.x; i < K * K; i += blockDim.x)
         sT[i] = op[i];
-      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-      const int ncols = cnt * R;
-      for (int c0 = 0; c0 < ncols; c0 += GB_COLS)
+      for (int idx = threadIdx.x; idx < nc * K; idx += blockDim.x)
         {
-          const int nc = min(GB_COLS, ncols - c0);
-          __syncthreads();
-          for (int idx = threadIdx.x; idx < nc * K; idx += blockDim.x)
+          const int     c  = idx / K, ki = idx - c * K;
+          const int     cg = c0 + c;
+          const int64_t q  = start + cg / R;
+          const int     r  = cg % R;
+          sB[ki * GB_LDB + c] = M[(int64_t(q_src[q]) * R + r) * K + ki];
+        }
+      __syncthreads();
+      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+      T         acc[KI][4];
+#pragma unroll
+      for (int i = 0; i < KI; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          acc[i][j] = T(0);
+      for (int ki = 0; ki < K; ++ki)
+        {
+          T a[KI], b[4];
+#pragma unroll
+          for (int i = 0; i < KI; ++i)
             {
-              const int     c  = idx / K, ki = idx - c * K;
-              const int     cg = c0 + c;
-              const int64_t q  = start + cg / R;
-              const int     r  = cg % R;
-              sB[ki * GB_LDB + c] = M[(int64_t(q_src[q]) * R + r) * K + ki];
-            }
-          __syncthreads();
-          T acc[8][4];
-#pragma unroll
-          for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-              acc[i][j] = T(0);
-          for (int ki = 0; ki < K; ++ki)
-            {
-              T a[8], b[4];
-#pragma unroll
-              for (int i = 0; i < 8; ++i)
-                {
-                  const int ko = tx + 16 * i;
-                  a[i]         = ko < K ? sT[ki * K + ko] : T(0);
-                }
-#pragma unroll
-              for (int j = 0; j < 4; ++j)
-                b[j] = sB[ki * GB_LDB + ty + 16 * j];
-#pragma unroll
-              for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                  acc[i][j] += a[i] * b[j];
+              const int ko = tx + 16 * i;
+              a[i]         = ko < K ? sT[ki * K + ko] : T(0);
             }
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            {
-              const int c = ty + 16 * j;
-              if (c >= nc)
-                continue;
-              const int     cg = c0 + c;
-              const int64_t q  = start + cg / R;
-              const int     r  = cg % R;
+            b[j] = sB[ki * GB_LDB + ty + 16 * j];
 #pragma unroll
-              for (int i = 0; i < 8; ++i)
-                {
-                  const int ko = tx + 16 * i;
-                  if (ko < K)
-                    Y[(q * R + r) * K + ko] = acc[i][j];
-                }
+          for (int i = 0; i < KI; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              acc[i][j] += a[i] * b[j];
+        }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        {
+          const int c = ty + 16 * j;
+          if (c >= nc)
+            continue;
+          const int     cg = c0 + c;
+          const int64_t q  = start + cg / R;
+          const int     r  = cg % R;
+#pragma unroll
+          for (int i = 0; i < KI; ++i)
+            {
+              const int ko = tx + 16 * i;
+              if (ko < K)
+                Y[(q * R + r) * K + ko] = acc[i][j];
+            }
+        }
+    }
+
+    // s + c += a * b in FP32-pair ("float-float") arithmetic: a = (hi, lo),
+    // b = (hi, lo) with hi = fl32(x), lo = fl32(x - hi).  The leading product
+    // is split exactly with an FMA (Dekker's TwoProduct), the cross terms are
+    // added to its error, and the leading sum is carried exactly with Knuth's
+    // TwoSum; the lo * lo term (2^-48 relative) is dropped.  Relative error of a
+    // K-term dot product ~ K 2^-47.  Round-to-nearest intrinsics throughout, so
+    // the compiler cannot contract or reassociate the steps.
+    __device__ __forceinline__ void ff_mac(float &s, float &c, float2 a, float2 b)
+    {
+      const float p = __fmul_rn(a.x, b.x);
+      float       e = __fmaf_rn(a.x, b.x, -p);
+      e             = __fmaf_rn(a.x, b.y, e);
+      e             = __fmaf_rn(a.y, b.x, e);
+      const float t = __fadd_rn(s, p);
+      const float z = __fsub_rn(t, s);
+      const float d = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+      c             = __fadd_rn(c, __fadd_rn(d, e));
+      s             = t;
+    }
+
+    // The translation GEMM of the FP64 operator in float-float arithmetic on
+    // the FP32 pipes (FP64 in, FP64 out): same tiling as trans_gemm_kernel,
+    // operator pre-split into (hi, lo) pairs, expansions split on load.
+    template <int KI>
+    __global__ void __launch_bounds__(256, 1)
+      ff_gemm_kernel(int R, int K, int chunk0, const int32_t *__restrict__ chunk_start,
+                     const int32_t *__restrict__ chunk_cnt, const int32_t *__restrict__ chunk_off,
+                     const int32_t *__restrict__ q_src, const float2 *__restrict__ ops,
+                     const double *__restrict__ M, double *__restrict__ Y)
+    {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      float2   *sT    = reinterpret_cast<float2 *>(smem_raw); // [K][K] in-major
+      float2   *sB    = sT + K * K;                           // [K][GB_LDB]
+      const int ch    = chunk0 + blockIdx.x;
+      const int start = chunk_start[ch], ncols = chunk_cnt[ch] * R;
+      const int c0    = blockIdx.y * GB_COLS;
+      if (c0 >= ncols)
+        return;
+      const int     nc = min(GB_COLS, ncols - c0);
+      const float2 *op = ops + int64_t(chunk_off[ch]) * K * K;
+      for (int i = threadIdx.x; i < K * K; i += blockDim.x)
+        sT[i] = op[i];
+      for (int idx = threadIdx.x; idx < nc * K; idx += blockDim.x)
+        {
+          const int     c  = idx / K, ki = idx - c * K;
+          const int     cg = c0 + c;
+          const int64_t q  = start + cg / R;
+          const int     r  = cg % R;
+          const double  x  = M[(int64_t(q_src[q]) * R + r) * K + ki];
+          const float   hi = __double2float_rn(x);
+          sB[ki * GB_LDB + c] = make_float2(hi, __double2float_rn(__dsub_rn(x, double(hi))));
+        }
+      __syncthreads();
+      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+      float     sh[KI][4], sl[KI][4];
+#pragma unroll
+      for (int i = 0; i < KI; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          sh[i][j] = sl[i][j] = 0.0f;
+      for (int ki = 0; ki < K; ++ki)
+        {
+          float2 a[KI], b[4];
+#pragma unroll
+          for (int i = 0; i < KI; ++i)
+            {
+              const int ko = tx + 16 * i;
+              a[i]         = ko < K ? sT[ki * K + ko] : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            b[j] = sB[ki * GB_LDB + ty + 16 * j];
+#pragma unroll
+          for (int i = 0; i < KI; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              ff_mac(sh[i][j], sl[i][j], a[i], b[j]);
+        }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        {
+          const int c = ty + 16 * j;
+          if (c >= nc)
+            continue;
+          const int     cg = c0 + c;
+          const int64_t q  = start + cg / R;
+          const int     r  = cg % R;
+#pragma unroll
+          for (int i = 0; i < KI; ++i)
+            {
+              const int ko = tx + 16 * i;
+              if (ko < K)
+                Y[(q * R + r) * K + ko] = __dadd_rn(double(sh[i][j]), double(sl[i][j]));
             }
         }
     }
@@ -397,8 +494,7 @@ namespace pibem
     rb                  = std::min(rb, R);
     const size_t smem   = size_t(rb) * maxnc * sizeof(T);
     if (smem > 48 * 1024)
-      PIBEM_CUDA(cudaFuncSetAttribute(near_leaf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(smem)));
+      raise_smem_limit(reinterpret_cast<const void *>(near_leaf_kernel<T>), smem);
     near_leaf_kernel<T><<<op.n_near_leaves, 256, smem, s>>>(R, rb, N, op.nrow_ptr, op.ncol_ptr,
                                                           op.nval_ptr, op.nrows, op.ncols, vals, x,
                                                           y, accumulate);
@@ -431,12 +527,52 @@ namespace pibem
           launch_tc_gemm(op, R, c0, c1, E, Y, op.tc_err, s);
           return;
         }
+    // largest column count of the chunks in [c0, c1): R x (<= 128 pairs)
+    const dim3 grid(unsigned(c1 - c0), unsigned((op.max_chunk_pairs * R + GB_COLS - 1) / GB_COLS));
+    const int  KI = (op.K + 15) / 16;
+    if constexpr (std::is_same<T, double>::value)
+      if (op.ops_ff)
+        {
+          const size_t smem = (size_t(op.K) * op.K + size_t(op.K) * GB_LDB) * sizeof(float2);
+          auto launch = [&](auto kern) {
+            if (smem > 48 * 1024)
+              raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
+            kern<<<grid, 256, smem, s>>>(R, op.K, c0, op.ch_start, op.ch_cnt, op.ch_op, op.q_src,
+                                         op.ops_ff, E, Y);
+          };
+          switch (KI)
+            {
+              case 1: launch(ff_gemm_kernel<1>); break;
+              case 2: launch(ff_gemm_kernel<2>); break;
+              case 3: launch(ff_gemm_kernel<3>); break;
+              case 4: launch(ff_gemm_kernel<4>); break;
+              case 5: launch(ff_gemm_kernel<5>); break;
+              case 6: launch(ff_gemm_kernel<6>); break;
+              case 7: launch(ff_gemm_kernel<7>); break;
+              default: launch(ff_gemm_kernel<8>); break;
+            }
+          PIBEM_CUDA(cudaGetLastError());
+          note_launch();
+          return;
+        }
     const size_t smem = (size_t(op.K) * op.K + size_t(op.K) * GB_LDB) * sizeof(T);
-    if (smem > 48 * 1024)
-      PIBEM_CUDA(cudaFuncSetAttribute(trans_gemm_kernel<T>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    trans_gemm_kernel<T><<<c1 - c0, 256, smem, s>>>(R, op.K, c0, op.ch_start, op.ch_cnt, op.ch_op,
-                                                    op.q_src, op.ops, E, Y);
+    auto launch = [&](auto kern) {
+      if (smem > 48 * 1024)
+        raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
+      kern<<<grid, 256, smem, s>>>(R, op.K, c0, op.ch_start, op.ch_cnt, op.ch_op, op.q_src, op.ops,
+                                   E, Y);
+    };
+    switch (KI)
+      {
+        case 1: launch(trans_gemm_kernel<T, 1>); break;
+        case 2: launch(trans_gemm_kernel<T, 2>); break;
+        case 3: launch(trans_gemm_kernel<T, 3>); break;
+        case 4: launch(trans_gemm_kernel<T, 4>); break;
+        case 5: launch(trans_gemm_kernel<T, 5>); break;
+        case 6: launch(trans_gemm_kernel<T, 6>); break;
+        case 7: launch(trans_gemm_kernel<T, 7>); break;
+        default: launch(trans_gemm_kernel<T, 8>); break;
+      }
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -495,7 +631,9 @@ namespace pibem
 
   void ensure_fmm_tables(int device, cudaStream_t s)
   {
-    static bool done[64] = {};
+    static bool       done[64] = {};
+    static std::mutex mu; // handles may be set up from several host threads
+    std::lock_guard<std::mutex> lock(mu);
     if (device < 0 || device >= 64 || done[device])
       return;
     LegendreTables t;

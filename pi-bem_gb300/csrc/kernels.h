@@ -85,7 +85,11 @@ namespace pibem
     // batched translations: operator table [M2L offsets | 8 M2M | 8 L2L],
     // each K x K stored [in][out]; pair / chunk arrays of the plan
     const T       *ops = nullptr;
+    // FP64 operator only: the table as (hi, lo) FP32 pairs; non-null selects
+    // the float-float translation GEMM
+    const float2  *ops_ff = nullptr;
     const int32_t *q_src = nullptr, *ch_start = nullptr, *ch_cnt = nullptr, *ch_op = nullptr;
+    int            max_chunk_pairs = 0;
     int            m2l_chunk_end = 0;
     std::vector<int> up_chunk_ptr, down_chunk_ptr, up_box_ptr, down_box_ptr;
     const int32_t *up_box = nullptr, *down_box = nullptr, *up_q = nullptr, *down_q = nullptr;

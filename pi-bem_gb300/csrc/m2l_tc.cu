@@ -1,10 +1,11 @@
 // Tensor-core batched translation GEMM (M2L, M2M, L2L) of the FP32 operator,
-// on the 5th-generation tensor cores: tcgen05.mma kind::tf32, accumulator in
+// on the 5th-generation tensor cores: tcgen05.mma kind::tf32, accumulators in
 // tensor memory, operator tiles staged by bulk TMA copies (cp.async.bulk).
 //
 // For one chunk of pairs sharing an operator T (K x K, scaled real form):
 //     Y[row][k_out] = sum_{k_in} E[src(row)][k_in] T[k_out][k_in]
-// with row = (pair, rhs).  One block computes a 128-row tile:
+// with row = (pair, rhs); the rows of a chunk are consecutive in Y.  A tile is
+// 128 rows:
 //     A (M = 128 rows x K_in)  source expansions, gathered into shared memory
 //     B (N = K_out x K_in)     operator, pre-laid-out image copied by TMA
 //     D (128 x N) fp32         tensor memory
@@ -12,14 +13,26 @@
 //     x = hi + lo (hi = TF32 rounding of x),   A B ~ Ah Bh + Al Bh + Ah Bl,
 // all three products accumulated into the same FP32 accumulator.
 //
-// Shared-memory operands use the canonical no-swizzle K-major layout: core
-// matrices of 8 rows x 16 bytes; adjacent core matrices along K are 128 bytes
-// apart (leading byte offset), adjacent 8-row groups Kp/4 * 128 bytes apart
-// (stride byte offset).  Each MMA consumes K = 8 (two core matrices).
+// Persistent, warp-specialised pipeline (one block per SM, 9 warps):
+//   warps 0-3  producers: per K chunk of 32, gather the 128 rows of A with
+//              coalesced loads (lane = k), split hi/lo and store them in the
+//              128-byte-swizzled K-major layout (a row's 32 values fill one
+//              128-byte line, 16-byte chunks XOR-permuted by row & 7, so the
+//              stores are free of bank conflicts); thread 0 copies the chunk's
+//              B hi/lo images with cp.async.bulk.  TC_STAGES-deep ring.
+//   warp 8     one thread issues the MMAs (4 K-steps x 3 products per chunk)
+//              into one of two tensor-memory accumulators and commits.
+//   warps 4-7  epilogue: tcgen05.ld of the accumulator (warp 4+q reads lanes
+//              32q..32q+31), staged per warp through shared memory and written
+//              as contiguous 128-byte row segments.
+// The accumulator double buffer lets the epilogue of tile i overlap the MMAs
+// of tile i+1, and the stage ring lets the gathers run ahead of the MMAs.
 //
-// Every wait is bounded: on timeout the block records the failure in *err,
-// waits (bounded) for its copies and MMAs in flight, frees its tensor memory
-// and returns; the host turns the flag into PIBEM_ETIMEDOUT.
+// Every wait is bounded: on timeout a role records the failure in *err, raises
+// a shared abort flag (so the other roles stop waiting), waits (bounded) for
+// its copies and MMAs in flight, and the block frees its tensor memory and
+// returns; the host turns the flag into PIBEM_ETIMEDOUT.
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 
@@ -29,14 +42,26 @@ namespace pibem
 {
   namespace
   {
-    constexpr int      TC_ROWS    = 128;
-    constexpr int      TC_THREADS = 128;
-    constexpr uint32_t TC_TMEM_COLS = 128;
+    constexpr int      TC_ROWS       = 128;
+    constexpr int      TC_KC         = 32;  // K values per stage: one 128-byte line of TF32
+    constexpr int      TC_STAGES     = 3;
+    constexpr int      TC_PRODUCERS  = 128; // warps 0-3
+    constexpr int      TC_EPI_WARP0  = 4;   // warps 4-7
+    constexpr int      TC_MMA_WARP   = 8;
+    constexpr int      TC_THREADS    = 9 * 32;
+    constexpr int      TC_EPI_LD     = 33;  // staging row stride (floats)
+    constexpr int      TC_ACC_COLS   = 128; // tensor-memory columns per accumulator (N <= 128)
+    constexpr uint32_t TC_TMEM_COLS  = 2 * TC_ACC_COLS;
+    constexpr uint32_t TC_A_BYTES    = TC_ROWS * TC_KC * 4; // 16 KB
     constexpr long     TC_SPIN_LIMIT = 1L << 26;
 
-    __host__ __device__ inline uint32_t img_off(int row, int k, int Kp)
+    // Byte offset of element (row, k), 0 <= k < 32, in a 128-byte-swizzled
+    // K-major tile: 8-row atoms of 1024 bytes, row r of an atom at r * 128,
+    // 16-byte chunk c of the row at position c ^ (r & 7).
+    __host__ __device__ inline uint32_t sw128_off(int row, int k)
     {
-      return uint32_t((row >> 3) * (Kp / 4) * 128 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+      return uint32_t((row >> 3) * 1024 + (row & 7) * 128 + ((((k >> 2) ^ row) & 7) << 4) +
+                      (k & 3) * 4);
     }
 
     __device__ inline uint32_t smem_u32(const void *p)
@@ -44,14 +69,19 @@ namespace pibem
       return static_cast<uint32_t>(__cvta_generic_to_shared(p));
     }
 
-    __device__ inline uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+    // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+    // 1024 bytes apart (stride byte offset); the leading byte offset is unused
+    // for swizzled K-major operands.  A K-step of 8 TF32 values inside the
+    // 128-byte line advances the start address by 32 bytes.
+    __device__ inline uint64_t smem_desc_sw128(uint32_t saddr)
     {
       uint64_t d = 0;
       d |= uint64_t((saddr >> 4) & 0x3FFFu);
-      d |= uint64_t((lbo >> 4) & 0x3FFFu) << 16;
-      d |= uint64_t((sbo >> 4) & 0x3FFFu) << 32;
-      d |= uint64_t(1) << 46; // descriptor version of sm_100-class tensor cores
-      return d;                // base offset 0, no swizzle
+      d |= uint64_t(1) << 16;         // leading byte offset (unused), 16 bytes
+      d |= uint64_t(1024 >> 4) << 32; // stride byte offset
+      d |= uint64_t(1) << 46;         // descriptor version of sm_100-class tensor cores
+      d |= uint64_t(2) << 61;         // swizzle mode: 128 bytes
+      return d;                       // base offset 0 (atoms are 1024-byte aligned)
     }
 
     __device__ inline float tf32_hi(float x)
@@ -61,29 +91,59 @@ namespace pibem
       return __uint_as_float(r);
     }
 
-    __device__ inline bool mbar_wait(uint32_t addr, uint32_t parity)
+    __device__ inline bool mbar_try(uint32_t addr, uint32_t parity)
+    {
+      uint32_t done;
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"(done)
+                   : "r"(addr), "r"(parity)
+                   : "memory");
+      return done != 0;
+    }
+
+    // Bounded wait; gives up early once another role has raised the abort flag.
+    __device__ inline bool mbar_wait(uint32_t addr, uint32_t parity, const volatile int *abort)
     {
       for (long it = 0; it < TC_SPIN_LIMIT; ++it)
         {
-          uint32_t done;
-          asm volatile("{\n\t.reg .pred p;\n\t"
-                       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                       "selp.u32 %0, 1, 0, p;\n\t}"
-                       : "=r"(done)
-                       : "r"(addr), "r"(parity)
-                       : "memory");
-          if (done)
+          if (mbar_try(addr, parity))
             return true;
+          if ((it & 1023) == 1023 && *abort)
+            return false;
         }
       return false;
     }
 
-    __device__ inline void tma_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+    // Bounded wait that ignores the abort flag (draining copies / MMAs in flight).
+    __device__ inline void mbar_drain(uint32_t addr, uint32_t parity)
+    {
+      for (long it = 0; it < TC_SPIN_LIMIT; ++it)
+        if (mbar_try(addr, parity))
+          return;
+    }
+
+    __device__ inline void mbar_init(uint32_t addr, uint32_t count)
+    {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(addr), "r"(count) : "memory");
+    }
+
+    __device__ inline void mbar_arrive(uint32_t addr)
+    {
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" : : "r"(addr) : "memory");
+    }
+
+    __device__ inline void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes)
     {
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                    :
-                   : "r"(mbar), "r"(bytes)
+                   : "r"(addr), "r"(bytes)
                    : "memory");
+    }
+
+    __device__ inline void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
+    {
       asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                    :
                    : "r"(dst), "l"(src), "r"(bytes), "r"(mbar)
@@ -128,162 +188,275 @@ namespace pibem
         v[j] = __uint_as_float(r[j]);
     }
 
+    __host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+    // Shared-memory layout, byte offsets from the 1024-byte aligned base:
+    // TC_STAGES x [A hi | A lo | B hi | B lo], epilogue staging, mbarriers.
+    struct TcLayout
+    {
+      uint32_t b_bytes, stage_bytes, epi, bars, total;
+      __host__ __device__ explicit TcLayout(int Np)
+      {
+        b_bytes     = uint32_t(Np) * 128;
+        stage_bytes = 2 * TC_A_BYTES + 2 * b_bytes;
+        epi         = TC_STAGES * stage_bytes;
+        bars        = epi + 4 * 32 * TC_EPI_LD * 4;
+        total       = bars + (2 * TC_STAGES + 5) * 8;
+      }
+    };
+
     // ALL_LEVELS_M2L only names the instantiation used for the batched M2L of all
     // levels (so that profilers can select it); the code is the same.
     template <bool ALL_LEVELS_M2L>
     __global__ void __launch_bounds__(TC_THREADS, 1)
-      tc_gemm_kernel(int R, int K, int Kp, int Np, int chunk0, const int32_t *__restrict__ ch_start,
-                     const int32_t *__restrict__ ch_cnt, const int32_t *__restrict__ ch_op,
-                     const int32_t *__restrict__ q_src, const float *__restrict__ images,
-                     const float *__restrict__ E, float *__restrict__ Y, int *__restrict__ err)
+      tc_gemm_kernel(int R, int K, int Np, int nkc, int chunk0, int n_chunks,
+                     const int32_t *__restrict__ ch_start, const int32_t *__restrict__ ch_cnt,
+                     const int32_t *__restrict__ ch_op, const int32_t *__restrict__ q_src,
+                     const float *__restrict__ images, const float *__restrict__ E,
+                     float *__restrict__ Y, int *__restrict__ err)
     {
-      extern __shared__ __align__(1024) uint8_t smem[];
-      const uint32_t a_bytes = uint32_t(TC_ROWS) * Kp * 4, b_bytes = uint32_t(Np) * Kp * 4;
-      uint8_t       *sAh = smem, *sAl = smem + a_bytes, *sB = smem + 2 * a_bytes;
-      uint64_t      *mbar      = reinterpret_cast<uint64_t *>(sB + b_bytes); // [0] tma, [1] mma
-      uint32_t      *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
-      const int      tid = threadIdx.x, warp = tid >> 5;
-      const int      ch = chunk0 + blockIdx.x;
-      const int      start = ch_start[ch], cnt = ch_cnt[ch], op = ch_op[ch];
-      const int      rows_total = cnt * R;
-      const uint32_t mb_tma = smem_u32(&mbar[0]), mb_mma = smem_u32(&mbar[1]);
+      extern __shared__ uint8_t smem_raw[];
+      __shared__ uint32_t       tmem_slot;
+      __shared__ volatile int   abort_flag;
+      const TcLayout  lay(Np);
+      const uint32_t  raw   = smem_u32(smem_raw);
+      const uint32_t  base  = (raw + 1023u) & ~1023u;
+      uint8_t        *gbase = smem_raw + (base - raw);
+      const int       tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+      const uint32_t  bar0 = base + lay.bars;
+      // mbarriers: full[s] (producers + copy bytes), empty[s] (MMA commit),
+      // tfull[a] (MMA commit), tempty[a] (epilogue threads), drain (MMA commit)
+      auto full   = [&](int s) { return bar0 + 8u * uint32_t(s); };
+      auto empty  = [&](int s) { return bar0 + 8u * uint32_t(TC_STAGES + s); };
+      auto tfull  = [&](int a) { return bar0 + 8u * uint32_t(2 * TC_STAGES + a); };
+      auto tempty = [&](int a) { return bar0 + 8u * uint32_t(2 * TC_STAGES + 2 + a); };
+      const uint32_t drain = bar0 + 8u * uint32_t(2 * TC_STAGES + 4);
+      const size_t   op_img_floats = size_t(nkc) * Np * TC_KC; // one half of an operator image
 
+      if (tid == 0)
+        {
+          abort_flag = 0;
+          for (int s = 0; s < TC_STAGES; ++s)
+            {
+              mbar_init(full(s), TC_PRODUCERS + 1);
+              mbar_init(empty(s), 1);
+            }
+          for (int a = 0; a < 2; ++a)
+            {
+              mbar_init(tfull(a), 1);
+              mbar_init(tempty(a), 4 * 32);
+            }
+          mbar_init(drain, 1);
+          asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
       if (warp == 0)
         {
           asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                        :
-                       : "r"(smem_u32(tmem_slot)), "r"(TC_TMEM_COLS)
+                       : "r"(smem_u32(&tmem_slot)), "r"(TC_TMEM_COLS)
                        : "memory");
           asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-        }
-      if (tid == 0)
-        {
-          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(mb_tma) : "memory");
-          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(mb_mma) : "memory");
-          asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t tmem = *tmem_slot;
+      const uint32_t tmem = tmem_slot;
+      bool           ok   = true;
 
-      const float   *Bhi = images + size_t(op) * 2 * Np * Kp;
-      const float   *Blo = Bhi + size_t(Np) * Kp;
-      const uint32_t sbo_a = uint32_t(Kp / 4) * 128, sbo_b = sbo_a, lbo = 128;
-      // instruction descriptor: D f32, A/B tf32, both K-major, N, M
-      const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(Np >> 3) << 17) |
-                             (uint32_t(TC_ROWS >> 4) << 24);
-      const int      ksteps = Kp / 8;
-      uint32_t       ph_tma = 0, ph_mma = 0;
-      bool           ok     = true;
-
-      for (int t0 = 0; t0 < rows_total && ok; t0 += TC_ROWS)
-        {
-          if (tid == 0)
-            tma_load(smem_u32(sB), Bhi, b_bytes, mb_tma);
-          // gather and split the tile's rows (one row per thread)
+      auto fail = [&]() {
+        if (ok)
           {
-            const int  i     = t0 + tid;
-            const bool valid = i < rows_total;
-            const float *src = nullptr;
-            if (valid)
-              {
-                const int64_t q = start + i / R;
-                const int     r = i - (i / R) * R;
-                src             = E + (int64_t(q_src[q]) * R + r) * K;
-              }
-            for (int k4 = 0; k4 < Kp / 4; ++k4)
-              {
-                float h[4], l[4];
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                  {
-                    const int   k = 4 * k4 + c;
-                    const float x = (valid && k < K) ? src[k] : 0.0f;
-                    h[c]          = tf32_hi(x);
-                    l[c]          = x - h[c];
-                  }
-                const uint32_t o = img_off(tid, 4 * k4, Kp);
-                *reinterpret_cast<float4 *>(sAh + o) = make_float4(h[0], h[1], h[2], h[3]);
-                *reinterpret_cast<float4 *>(sAl + o) = make_float4(l[0], l[1], l[2], l[3]);
-              }
-          }
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncthreads();
-          ok = __syncthreads_and(mbar_wait(mb_tma, ph_tma));
-          if (!ok)
-            break;
-          ph_tma ^= 1;
-          if (tid == 0)
-            {
-              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-              const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), b = smem_u32(sB);
-              for (int s = 0; s < ksteps; ++s)
-                mma_tf32(tmem, smem_desc(ah + 256 * s, lbo, sbo_a), smem_desc(b + 256 * s, lbo, sbo_b),
-                         idesc, s > 0);
-              for (int s = 0; s < ksteps; ++s)
-                mma_tf32(tmem, smem_desc(al + 256 * s, lbo, sbo_a), smem_desc(b + 256 * s, lbo, sbo_b),
-                         idesc, 1);
-              mma_commit(mb_mma);
-            }
-          ok = __syncthreads_and(mbar_wait(mb_mma, ph_mma));
-          if (!ok)
-            break;
-          ph_mma ^= 1;
-          // second operator half (lo) into the same buffer: the MMAs above are done
-          if (tid == 0)
-            tma_load(smem_u32(sB), Blo, b_bytes, mb_tma);
-          ok = __syncthreads_and(mbar_wait(mb_tma, ph_tma));
-          if (!ok)
-            break;
-          ph_tma ^= 1;
-          if (tid == 0)
-            {
-              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-              const uint32_t ah = smem_u32(sAh), b = smem_u32(sB);
-              for (int s = 0; s < ksteps; ++s)
-                mma_tf32(tmem, smem_desc(ah + 256 * s, lbo, sbo_a), smem_desc(b + 256 * s, lbo, sbo_b),
-                         idesc, 1);
-              mma_commit(mb_mma);
-            }
-          ok = __syncthreads_and(mbar_wait(mb_mma, ph_mma));
-          if (!ok)
-            break;
-          ph_mma ^= 1;
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          // epilogue: warp w reads lanes 32w..32w+31, i.e. row t0 + tid
-          {
-            const int     i     = t0 + tid;
-            const bool    valid = i < rows_total;
-            float        *dst   = nullptr;
-            if (valid)
-              {
-                const int64_t q = start + i / R;
-                const int     r = i - (i / R) * R;
-                dst             = Y + (q * R + r) * K;
-              }
-            for (int c0 = 0; c0 < Np; c0 += 32)
-              {
-                float v[32];
-                tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
-                if (valid)
-#pragma unroll
-                  for (int j = 0; j < 32; ++j)
-                    if (c0 + j < K)
-                      dst[c0 + j] = v[j];
-              }
-          }
-          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-          __syncthreads();
-        }
-      if (!ok)
-        {
-          if (tid == 0)
+            ok         = false;
+            abort_flag = 1;
             atomicExch(err, 1);
-          // bounded drain of whatever may still be in flight
-          mbar_wait(mb_mma, ph_mma);
-          mbar_wait(mb_tma, ph_tma);
+          }
+      };
+
+      if (warp < 4)
+        {
+          // ---------------- producers ----------------
+          int  it = 0;
+          bool inflight[TC_STAGES];
+          int  inflight_par[TC_STAGES];
+#pragma unroll
+          for (int s = 0; s < TC_STAGES; ++s)
+            {
+              inflight[s]     = false;
+              inflight_par[s] = 0;
+            }
+          for (int ch = chunk0 + blockIdx.x; ok && ch < chunk0 + n_chunks; ch += gridDim.x)
+            {
+              const int    start = ch_start[ch], rows_total = ch_cnt[ch] * R;
+              const float *Bhi   = images + size_t(ch_op[ch]) * 2 * op_img_floats;
+              const float *Blo   = Bhi + op_img_floats;
+              for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS)
+                {
+                  // source offset of row t0 + 32 warp + lane (-1: padding row)
+                  int64_t my_src = -1;
+                  {
+                    const int i = t0 + 32 * warp + lane;
+                    if (i < rows_total)
+                      {
+                        const int q = start + i / R, r = i - (i / R) * R;
+                        my_src      = (int64_t(q_src[q]) * R + r) * K;
+                      }
+                  }
+                  for (int kc = 0; kc < nkc; ++kc, ++it)
+                    {
+                      const int s = it % TC_STAGES, use = it / TC_STAGES;
+                      if (use > 0 && !mbar_wait(empty(s), uint32_t(use - 1) & 1u, &abort_flag))
+                        {
+                          fail();
+                          break;
+                        }
+                      inflight[s]       = false;
+                      const uint32_t st = base + uint32_t(s) * lay.stage_bytes;
+                      uint8_t       *gs = gbase + size_t(s) * lay.stage_bytes;
+                      if (tid == 0)
+                        {
+                          mbar_arrive_expect_tx(full(s), 2 * lay.b_bytes);
+                          bulk_copy(st + 2 * TC_A_BYTES, Bhi + size_t(kc) * Np * TC_KC,
+                                    lay.b_bytes, full(s));
+                          bulk_copy(st + 2 * TC_A_BYTES + lay.b_bytes,
+                                    Blo + size_t(kc) * Np * TC_KC, lay.b_bytes, full(s));
+                          inflight[s]     = true;
+                          inflight_par[s] = use & 1;
+                        }
+                      const int k = kc * TC_KC + lane;
+#pragma unroll 1
+                      for (int r0 = 0; r0 < 32; r0 += 8)
+                        {
+                          float x[8];
+#pragma unroll
+                          for (int u = 0; u < 8; ++u)
+                            {
+                              const int64_t src = __shfl_sync(0xffffffffu, my_src, r0 + u);
+                              x[u]              = (src >= 0 && k < K) ? E[src + k] : 0.0f;
+                            }
+#pragma unroll
+                          for (int u = 0; u < 8; ++u)
+                            {
+                              const uint32_t o = sw128_off(32 * warp + r0 + u, lane);
+                              const float    h = tf32_hi(x[u]);
+                              *reinterpret_cast<float *>(gs + o)              = h;
+                              *reinterpret_cast<float *>(gs + TC_A_BYTES + o) = x[u] - h;
+                            }
+                        }
+                      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                      mbar_arrive(full(s));
+                    }
+                }
+            }
+          if (!ok && tid == 0)
+            for (int s = 0; s < TC_STAGES; ++s)
+              if (inflight[s])
+                mbar_drain(full(s), uint32_t(inflight_par[s]));
         }
+      else if (warp == TC_MMA_WARP)
+        {
+          // ---------------- MMA issuer ----------------
+          if (lane == 0)
+            {
+              // D f32, A/B tf32, both K-major, N = Np, M = 128
+              const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) |
+                                     (uint32_t(Np >> 3) << 17) | (uint32_t(TC_ROWS >> 4) << 24);
+              int  it = 0, tile = 0;
+              bool issued = false;
+              for (int ch = chunk0 + blockIdx.x; ok && ch < chunk0 + n_chunks; ch += gridDim.x)
+                {
+                  const int rows_total = ch_cnt[ch] * R;
+                  for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS, ++tile)
+                    {
+                      const int a = tile & 1, use_a = tile >> 1;
+                      if (use_a > 0 &&
+                          !mbar_wait(tempty(a), uint32_t(use_a - 1) & 1u, &abort_flag))
+                        {
+                          fail();
+                          break;
+                        }
+                      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                      const uint32_t d = tmem + uint32_t(a * TC_ACC_COLS);
+                      for (int kc = 0; kc < nkc; ++kc, ++it)
+                        {
+                          const int s = it % TC_STAGES;
+                          if (!mbar_wait(full(s), uint32_t(it / TC_STAGES) & 1u, &abort_flag))
+                            {
+                              fail();
+                              break;
+                            }
+                          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                          const uint32_t st = base + uint32_t(s) * lay.stage_bytes;
+                          const uint32_t ah = st, al = st + TC_A_BYTES, bh = st + 2 * TC_A_BYTES,
+                                         bl = bh + lay.b_bytes;
+#pragma unroll
+                          for (int ks = 0; ks < TC_KC / 8; ++ks)
+                            {
+                              const uint32_t off = uint32_t(ks) * 32;
+                              const uint64_t dah = smem_desc_sw128(ah + off),
+                                             dal = smem_desc_sw128(al + off),
+                                             dbh = smem_desc_sw128(bh + off),
+                                             dbl = smem_desc_sw128(bl + off);
+                              mma_tf32(d, dah, dbh, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+                              mma_tf32(d, dal, dbh, idesc, 1u);
+                              mma_tf32(d, dah, dbl, idesc, 1u);
+                            }
+                          mma_commit(empty(s)); // frees the stage once these MMAs are done
+                          issued = true;
+                        }
+                      if (!ok)
+                        break;
+                      mma_commit(tfull(a)); // accumulator complete
+                    }
+                }
+              if (!ok && issued)
+                {
+                  // bounded wait until every MMA issued above has completed
+                  mma_commit(drain);
+                  mbar_drain(drain, 0);
+                }
+            }
+        }
+      else
+        {
+          // ---------------- epilogue (warps 4-7) ----------------
+          const int q    = warp - TC_EPI_WARP0;
+          float    *stg  = reinterpret_cast<float *>(gbase + lay.epi) + q * 32 * TC_EPI_LD;
+          int       tile = 0;
+          for (int ch = chunk0 + blockIdx.x; ok && ch < chunk0 + n_chunks; ch += gridDim.x)
+            {
+              const int start = ch_start[ch], rows_total = ch_cnt[ch] * R;
+              for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS, ++tile)
+                {
+                  const int a = tile & 1;
+                  if (!mbar_wait(tfull(a), uint32_t(tile >> 1) & 1u, &abort_flag))
+                    {
+                      fail();
+                      break;
+                    }
+                  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                  const int row0   = t0 + 32 * q;
+                  const int nvalid = min(32, rows_total - row0);
+                  float    *ybase  = Y + (int64_t(start) * R + row0) * K;
+                  for (int c0 = 0; c0 < Np; c0 += 32)
+                    {
+                      float v[32];
+                      tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(a * TC_ACC_COLS + c0), v);
+#pragma unroll
+                      for (int j = 0; j < 32; ++j)
+                        stg[lane * TC_EPI_LD + j] = v[j];
+                      __syncwarp();
+                      const int col = c0 + lane;
+                      if (col < K)
+                        for (int r = 0; r < nvalid; ++r)
+                          ybase[int64_t(r) * K + col] = stg[r * TC_EPI_LD + lane];
+                      __syncwarp();
+                    }
+                  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                  mbar_arrive(tempty(a));
+                }
+            }
+        }
+
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -309,18 +482,23 @@ namespace pibem
   {
     TcGeometry g;
     g.K  = K;
-    g.Kp = (K + 7) / 8 * 8;
-    g.Np = (K + 15) / 16 * 16;
-    g.smem = size_t(2) * TC_ROWS * g.Kp * 4 + size_t(g.Np) * g.Kp * 4 + 32;
-    g.ok = g.Np <= 256 && g.smem <= 220 * 1024;
+    g.Kp = round_up(K, TC_KC);
+    g.Np = round_up(K, 16);
+    const TcLayout lay(g.Np);
+    g.smem = size_t(lay.total) + 1024; // + alignment slack of the dynamic base
+    g.ok   = K >= 1 && g.Np <= TC_ACC_COLS && g.smem <= 220 * 1024;
     return g;
   }
 
+  // Image of one operator half: Kp / 32 chunks of [Np rows][32 k] in the swizzled
+  // K-major layout, zero beyond K; the hi and lo halves one after the other.
   void build_tc_images(const std::vector<double> &ops_out_in, int nops, int K,
                        std::vector<float> &img)
   {
-    const TcGeometry g = tc_geometry(K);
-    const size_t     half = size_t(g.Np) * g.Kp;
+    const TcGeometry g     = tc_geometry(K);
+    const int        nkc   = g.Kp / TC_KC;
+    const size_t     chunk = size_t(g.Np) * TC_KC; // floats
+    const size_t     half  = size_t(nkc) * chunk;
     img.assign(size_t(nops) * 2 * half, 0.0f);
     for (int o = 0; o < nops; ++o)
       {
@@ -331,7 +509,7 @@ namespace pibem
               const double v  = ops_out_in[size_t(o) * K * K + size_t(n) * K + k];
               const float  h  = tf32_round_host(float(v));
               const float  l  = float(v - double(h));
-              const size_t at = img_off(n, k, g.Kp) / 4;
+              const size_t at = size_t(k / TC_KC) * chunk + sw128_off(n, k % TC_KC) / 4;
               hi[at]          = h;
               lo[at]          = l;
             }
@@ -343,11 +521,16 @@ namespace pibem
   {
     if (c1 <= c0)
       return;
-    const TcGeometry g = tc_geometry(op.K);
+    int dev = 0, n_sm = 0;
+    PIBEM_CUDA(cudaGetDevice(&dev));
+    PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    const TcGeometry g   = tc_geometry(op.K);
+    const int        nch = c1 - c0;
     auto fn = (c0 == 0 && c1 == op.m2l_chunk_end) ? tc_gemm_kernel<true> : tc_gemm_kernel<false>;
-    PIBEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
-    fn<<<c1 - c0, TC_THREADS, g.smem, s>>>(R, op.K, g.Kp, g.Np, c0, op.ch_start, op.ch_cnt, op.ch_op,
-                                           op.q_src, op.tc_images, E, Y, err);
+    raise_smem_limit(reinterpret_cast<const void *>(fn), g.smem);
+    fn<<<std::min(nch, std::max(n_sm, 1)), TC_THREADS, g.smem, s>>>(
+      R, op.K, g.Np, g.Kp / TC_KC, c0, nch, op.ch_start, op.ch_cnt, op.ch_op, op.q_src,
+      op.tc_images, E, Y, err);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

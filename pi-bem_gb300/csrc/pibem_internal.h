@@ -33,6 +33,11 @@ namespace pibem
   // Counts kernel launches of this library (all handles, all streams).
   void    note_launch(int64_t n = 1);
   int64_t launch_count();
+  // Raise (never lower) a kernel's dynamic shared-memory limit on the current
+  // device.  The limit is process-wide state of the function, and handles on
+  // other host threads may launch the same kernel with other sizes at the same
+  // time: lowering it under them would make their launches fail.
+  void raise_smem_limit(const void *fn, size_t bytes);
 
   // Owning device buffer.
   template <typename T>

@@ -54,6 +54,7 @@ extern "C" int pibem_params_default(pibem_params *p)
   p->device                        = 0;
   p->inner_tolerance               = 1e-4;
   p->hbm_budget_gb                 = 0.0;
+  p->m2l_engine                    = PIBEM_M2L_TENSOR_CORE;
   return PIBEM_OK;
 }
 
@@ -115,7 +116,9 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
           if (key == "Precision mode")
             p->precision_mode = (val == "Mixed" || val == "mixed" || val == "1")
                                   ? PIBEM_PRECISION_MIXED
-                                  : PIBEM_PRECISION_FP64;
+                                  : (val == "FloatFloat" || val == "float-float" || val == "2")
+                                      ? PIBEM_PRECISION_FLOAT_FLOAT
+                                      : PIBEM_PRECISION_FP64;
           else if (key == "Preconditioner")
             p->preconditioner = (val == "none" || val == "None" || val == "0") ? 0 : 1;
           else if (key == "GMRES restart")
@@ -126,6 +129,10 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
             p->hbm_budget_gb = std::atof(v);
           else if (key == "Device")
             p->device = std::atoi(v);
+          else if (key == "M2L engine")
+            p->m2l_engine = (val == "CUDA cores" || val == "cuda" || val == "1")
+                              ? PIBEM_M2L_CUDA_CORE
+                              : PIBEM_M2L_TENSOR_CORE;
         }
     }
   return PIBEM_OK;

@@ -22,7 +22,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpibem_gb300.so")
 
 OK, EINVAL, ENOMEM_HBM, ENOCONV, ETIMEDOUT, ECUDA = 0, 1, 2, 3, 4, 5
-PRECISION_FP64, PRECISION_MIXED = 0, 1
+PRECISION_FP64, PRECISION_MIXED, PRECISION_FLOAT_FLOAT = 0, 1, 2
+M2L_TENSOR_CORE, M2L_CUDA_CORE = 0, 1
 
 
 class Params(C.Structure):
@@ -41,6 +42,7 @@ class Params(C.Structure):
         ("device", C.c_int32),
         ("inner_tolerance", C.c_double),
         ("hbm_budget_gb", C.c_double),
+        ("m2l_engine", C.c_int32),
     ]
 
 
@@ -89,7 +91,7 @@ EXPORTS = [
     "pibem_solve", "pibem_solve_device", "pibem_tree_info_get", "pibem_tree_boxes",
     "pibem_tree_list", "pibem_tree_list_sublevels", "pibem_near_nnz", "pibem_near_export",
     "pibem_quad_points", "pibem_last_phase_ms", "pibem_set_profiling", "pibem_phase_totals",
-    "pibem_launch_count", "pibem_fmm_matvec_noalloc",
+    "pibem_launch_count", "pibem_fmm_matvec_noalloc", "pibem_device_bytes",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -137,6 +139,7 @@ def load():
     L.pibem_launch_count.argtypes = []
     L.pibem_fmm_matvec_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p]
+    L.pibem_device_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
     _lib = L
     return L
 
@@ -317,6 +320,12 @@ class BEMSolver:
         out = np.zeros(7)
         self._check(self.L.pibem_last_phase_ms(self.h, _d(out)))
         return dict(zip(self.PHASES, out.tolist()))
+
+    def device_bytes(self) -> int:
+        """Device memory the handle holds now (bytes)."""
+        b = C.c_uint64(0)
+        self._check(self.L.pibem_device_bytes(self.h, C.byref(b)))
+        return int(b.value)
 
     def set_profiling(self, on: bool):
         self._check(self.L.pibem_set_profiling(self.h, int(bool(on))))

@@ -30,6 +30,13 @@ __all__ = [
     "mixed_bc_by_cell_centroid",
     "sphere_dirichlet_case",
     "spheroid_mixed_case",
+    "random_plane_mask",
+    "sources_in_ball",
+    "sources_in_wigley",
+    "point_source_data",
+    "wigley_mixed_case",
+    "wigley_for_nodes",
+    "sphere_n_for_nodes",
 ]
 
 
@@ -172,8 +179,8 @@ def wigley_hull(nx: int, nz: int, ny_lid: int, L=1.0, B=0.1, T=0.0625) -> Mesh:
         y = s * half_beam(x, z)
         if i == 0 or i == nx or j == 0:  # y == 0 lines shared by both sides
             return node(("c", i, j), [x, 0.0, z])
-        if j == nz:
-            return node(("lid", i, s * ny_lid // 2 + ny_lid // 2), [x, y, z])
+        if j == nz:  # top edge of a side = a long edge of the lid grid
+            return node(("lid", i, ny_lid if s > 0 else 0), [x, y, z])
         return node(("s", i, j, s), [x, y, z])
 
     cells = []
@@ -274,3 +281,75 @@ def spheroid_mixed_case(n: int, seed: int, n_sources: int = 8, axes=(3.0, 1.0, 1
     dn = (grad(mesh.xyz) * mesh.normals).sum(axis=1)
     tmp = np.where(mask == 1, ph, dn)
     return mesh, mask, tmp, ph, dn
+
+
+def random_plane_mask(mesh: Mesh, seed: int):
+    """Dirichlet mask from a seeded random plane: nodes of cells whose centroid
+    lies on the positive side are Dirichlet (interface nodes Dirichlet), the
+    rest Neumann.  The plane passes within a quarter of the half-extent of the
+    mesh centre, so both parts are present."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nrm = rng.normal(size=3)
+    nrm /= np.linalg.norm(nrm)
+    c = 0.5 * (mesh.xyz.min(axis=0) + mesh.xyz.max(axis=0))
+    half = 0.5 * float(np.abs((mesh.xyz - c) @ nrm).max())
+    off = rng.uniform(-0.25, 0.25) * half
+    cent = mesh.xyz[mesh.cells].mean(axis=1)
+    mask = np.zeros(mesh.n_nodes, dtype=np.uint8)
+    mask[np.unique(mesh.cells[(cent - c) @ nrm > off])] = 1
+    return mask
+
+
+def sources_in_ball(rng, n_sources: int, radius: float = 0.5):
+    """n_sources points uniform in the ball |s| < radius."""
+    dirs = rng.normal(size=(n_sources, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rad = radius * rng.uniform(0.0, 1.0, n_sources) ** (1.0 / 3.0)
+    return dirs * rad[:, None]
+
+
+def sources_in_wigley(rng, n_sources: int, L=1.0, B=0.1, T=0.0625):
+    """n_sources points inside the Wigley hull, away from its surface:
+    |x| < 0.3 L, z in [-0.65 T, -0.35 T], |y| < 0.3 of the local half-beam."""
+    x = rng.uniform(-0.3 * L, 0.3 * L, n_sources)
+    z = rng.uniform(-0.65 * T, -0.35 * T, n_sources)
+    hb = 0.5 * B * (1 - (2 * x / L) ** 2) * (1 - (z / T) ** 2)
+    y = rng.uniform(-0.3, 0.3, n_sources) * hb
+    return np.stack([x, y, z], axis=1)
+
+
+def point_source_data(mesh: Mesh, mask, sources, strengths):
+    """tmp_rhs (phi on Dirichlet nodes, dphi/dn on Neumann nodes), phi, dphi/dn."""
+    phi, grad = point_source_field(sources, strengths)
+    ph = phi(mesh.xyz)
+    dn = (grad(mesh.xyz) * mesh.normals).sum(axis=1)
+    return np.where(mask == 1, ph, dn), ph, dn
+
+
+def wigley_mixed_case(nx: int, nz: int, ny_lid: int, seed: int = 3, n_sources: int = 8,
+                      mesh: Mesh | None = None):
+    """Wigley hull with mixed data from n_sources point sources of strength
+    U(-1,1) inside the hull (exterior problem): cells with centroid
+    z > -T/2 Dirichlet, the rest Neumann.
+
+    Returns mesh, dirichlet mask, tmp_rhs, exact phi, exact dphi/dn."""
+    if mesh is None:
+        mesh = wigley_hull(nx, nz, ny_lid)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    q = rng.uniform(-1.0, 1.0, n_sources)
+    S = sources_in_wigley(rng, n_sources)
+    mask = mixed_bc_by_cell_centroid(mesh, z_split=-0.5 * 0.0625)
+    tmp, ph, dn = point_source_data(mesh, mask, S, q)
+    return mesh, mask, tmp, ph, dn
+
+
+def wigley_for_nodes(n_nodes: float) -> tuple[int, int, int]:
+    """(nx, nz, ny_lid) in the 6 : 1.5 : 1 proportion of the 768 x 192 + 768 x 128
+    hull, for about n_nodes nodes (2 nx nz + nx ny_lid)."""
+    nx = max(12, int(round(np.sqrt(1.5 * n_nodes) / 6.0)) * 6)
+    return nx, max(3, nx // 4), max(2, nx // 6)
+
+
+def sphere_n_for_nodes(n_nodes: float) -> int:
+    """Cube-sphere resolution n with 6 n^2 + 2 close to n_nodes."""
+    return max(2, int(round(np.sqrt(max(n_nodes - 2, 6) / 6.0))))

@@ -63,6 +63,7 @@ subsection BEMProblem<3>
     set Precision mode = Mixed
     set GMRES restart  = 60
     set HBM budget GB  = 150
+    set M2L engine     = CUDA cores
   end
 end
 subsection Other
@@ -86,13 +87,16 @@ def test_prm_reader(pibem_mod):
     assert p.precision_mode == pibem_mod.PRECISION_MIXED
     assert p.gmres_restart == 60
     assert p.hbm_budget_gb == pytest.approx(150)
+    assert p.m2l_engine == pibem_mod.M2L_CUDA_CORE
+    assert pibem_mod.default_params().m2l_engine == pibem_mod.M2L_TENSOR_CORE
 
 
 def test_create_rejects_bad_parameters(pibem_mod):
     L = pibem_mod.load()
     for field, bad in (("fma_truncation_order", 11), ("fma_truncation_order", 0),
                        ("num_octree_levels", 0), ("quadrature_order", 9),
-                       ("singular_quadrature_order", 13), ("solver_tolerance", 0.0)):
+                       ("singular_quadrature_order", 13), ("solver_tolerance", 0.0),
+                       ("m2l_engine", 2)):
         p = pibem_mod.default_params()
         setattr(p, field, bad)
         h = C.c_void_p()

@@ -31,12 +31,9 @@ def _mesh(S, c):
 
 
 def _handle(pibem, c, mesh, mask, mode, tc):
-    os.environ["PIBEM_TENSOR_CORE_M2L"] = "1" if tc else "0"
-    try:
-        g = pibem.BEMSolver(fma_truncation_order=c["p"], max_nodes_per_childless_block=c["leaf"],
-                            is_external_flow=int(c["ext"]), precision_mode=mode)
-    finally:
-        os.environ.pop("PIBEM_TENSOR_CORE_M2L", None)
+    g = pibem.BEMSolver(fma_truncation_order=c["p"], max_nodes_per_childless_block=c["leaf"],
+                        is_external_flow=int(c["ext"]), precision_mode=mode,
+                        m2l_engine=pibem.M2L_TENSOR_CORE if tc else pibem.M2L_CUDA_CORE)
     g.set_mesh(mesh.xyz, mesh.cells)
     g.set_bc(mask)
     return g
