@@ -178,6 +178,34 @@ int64_t pibem_launch_count(void);
  * resident meshes inside an HBM budget. */
 int pibem_device_bytes(const pibem_handle *h, uint64_t *bytes);
 
+/* ---- mesh ingestion (host only; no GPU needed) ---------------------------
+ * UCD (.inp) surface mesh, as ComputationalDomain::read_domain reads it with
+ * GridIn::read_ucd (source/computational_domain.cc:280-287).  Call once with
+ * xyz = cell_nodes = material_id = NULL to get the counts, then with arrays of
+ * at least those sizes (*n_nodes, *n_cells give the capacities).  Only "quad"
+ * cells are read; their counterclockwise UCD vertices are returned in deal.II
+ * lexicographic order (v0, v1, v3, v2), node ids renumbered 0.. in file order.
+ * On error pibem_mesh_io_error() has the message (per calling thread). */
+int pibem_ucd_read(const char *path, int64_t *n_nodes, int64_t *n_cells, double *xyz,
+                   int32_t *cell_nodes, int32_t *material_id);
+const char *pibem_mesh_io_error(void);
+/* Double-node sets: nodes closer than tol in every coordinate are one group;
+ * node i's set (offsets[i]..offsets[i+1]) lists every member of its group,
+ * itself included -- the double_nodes_set BEMProblem passes to init_fma
+ * (source/bem_problem.cc:200), in the CSR form pibem_set_mesh takes.
+ * offsets has n_nodes + 1 entries; *n_ids returns the total; ids may be NULL
+ * (size query) or hold capacity entries (PIBEM_EINVAL if too small). */
+int pibem_double_nodes(int64_t n_nodes, const double *xyz, double tol, int32_t *offsets,
+                       int32_t *ids, int64_t capacity, int64_t *n_ids);
+/* Dirichlet mask from cell material ids, as
+ * BEMProblem::compute_dirichlet_and_neumann_dofs_vectors
+ * (source/bem_problem.cc:315-411): a node is Dirichlet (1) when any of its cells
+ * carries one of the n_dirichlet_ids material ids, else Neumann (0). */
+int pibem_dirichlet_mask_from_materials(int64_t n_nodes, int64_t n_cells,
+                                        const int32_t *cell_nodes, const int32_t *material_id,
+                                        int32_t n_dirichlet_ids, const int32_t *dirichlet_ids,
+                                        uint8_t *mask);
+
 /* Allocation-free FMM matvec.  No counterpart in the reference.
  * Same result as pibem_fmm_matvec (outN = N phi, outD = D dphi_dn), but with
  * device pointers and without allocating any device memory during the call:

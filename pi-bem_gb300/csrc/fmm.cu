@@ -28,6 +28,25 @@ namespace pibem
       return v;
     }
 
+    // s + a . x for 4 values, with the rounding steps spelled out so that every
+    // code path (one column or several) computes a column bit-for-bit alike.
+    __device__ inline float dot4_acc(float s, const float (&a)[4], const float *x)
+    {
+      float d = __fmul_rn(a[0], x[0]);
+      d       = __fmaf_rn(a[1], x[1], d);
+      d       = __fmaf_rn(a[2], x[2], d);
+      d       = __fmaf_rn(a[3], x[3], d);
+      return __fadd_rn(s, d);
+    }
+    __device__ inline double dot4_acc(double s, const double (&a)[4], const double *x)
+    {
+      double d = __dmul_rn(a[0], x[0]);
+      d        = __fma_rn(a[1], x[1], d);
+      d        = __fma_rn(a[2], x[2], d);
+      d        = __fma_rn(a[3], x[3], d);
+      return __dadd_rn(s, d);
+    }
+
     // 4-wide loads from 16-byte aligned rows.
     __device__ inline void load4(const float *p, float (&v)[4])
     {
@@ -51,7 +70,7 @@ namespace pibem
     // the block's columns are gathered once into shared memory (rb rhs at a
     // time, zero in the row padding), then each warp streams whole rows of the
     // dense leaf block with 16-byte loads (rows padded to 4 values).
-    template <typename T>
+    template <typename T, bool ONE_COL>
     __global__ void __launch_bounds__(256)
       near_leaf_kernel(int R, int rb, int N, const int64_t *__restrict__ nrow_ptr,
                        const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
@@ -82,9 +101,29 @@ namespace pibem
             {
               const T  *v    = V + row * ld;
               const int node = nrows[r0 + row];
+              if (ONE_COL)
+                {
+                  // one column: several 16-byte loads of the row in flight per lane
+                  T s0 = T(0);
+#pragma unroll 4
+                  for (int j = lane; j < n4; j += 32)
+                    {
+                      T a[4];
+                      load4(v + 4 * j, a);
+                      s0 = dot4_acc(s0, a, sx + 4 * j);
+                    }
+                  const T t = warp_sum(s0);
+                  if (lane == 0)
+                    {
+                      T &o = y[ra * int64_t(N) + node];
+                      o    = acc ? o + t : t;
+                    }
+                  continue;
+                }
               for (int rq = 0; rq < rc; rq += 4)
                 {
                   T s[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll 2
                   for (int j = lane; j < n4; j += 32)
                     {
                       T a[4];
@@ -92,10 +131,7 @@ namespace pibem
 #pragma unroll
                       for (int rr = 0; rr < 4; ++rr)
                         if (rq + rr < rc)
-                          {
-                            const T *xs = sx + (rq + rr) * ld + 4 * j;
-                            s[rr] += a[0] * xs[0] + a[1] * xs[1] + a[2] * xs[2] + a[3] * xs[3];
-                          }
+                          s[rr] = dot4_acc(s[rr], a, sx + (rq + rr) * ld + 4 * j);
                     }
 #pragma unroll
                   for (int rr = 0; rr < 4; ++rr)
@@ -362,19 +398,34 @@ namespace pibem
         }
     }
 
-    // out[box] = sum of the box's translation products Y[q], in list order.
+    // out[box] = sum of the box's translation products Y[q], in list order.  The
+    // loads of 8 consecutive products are issued before they are added (same
+    // order of additions), so a thread has 8 L2 reads in flight.
     template <typename T>
     __global__ void gather_kernel(int R, int K, const int32_t *__restrict__ boxes,
                                   const int64_t *__restrict__ q_ptr, const int32_t *__restrict__ q,
                                   const T *__restrict__ Y, T *__restrict__ out)
     {
-      const int64_t b = boxes[blockIdx.x];
+      const int64_t b  = boxes[blockIdx.x];
+      const int64_t e0 = q_ptr[blockIdx.x], e1 = q_ptr[blockIdx.x + 1];
+      const int64_t RK = int64_t(R) * K;
       for (int i = threadIdx.x; i < R * K; i += blockDim.x)
         {
-          T acc = T(0);
-          for (int64_t e = q_ptr[blockIdx.x]; e < q_ptr[blockIdx.x + 1]; ++e)
-            acc += Y[int64_t(q[e]) * R * K + i];
-          out[b * R * K + i] = acc;
+          T       acc = T(0);
+          int64_t e   = e0;
+          for (; e + 8 <= e1; e += 8)
+            {
+              T v[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                v[u] = Y[int64_t(q[e + u]) * RK + i];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                acc += v[u];
+            }
+          for (; e < e1; ++e)
+            acc += Y[int64_t(q[e]) * RK + i];
+          out[b * RK + i] = acc;
         }
     }
 
@@ -445,11 +496,25 @@ namespace pibem
         }
       const int64_t i    = tn - tnode_ptr[lo];
       const int     node = node_sorted[nbeg[tgt[lo]] + i];
+      const int64_t e0 = src_ptr[lo], e1 = src_ptr[lo + 1];
       for (int r = 0; r < R; ++r)
         {
-          T acc = T(0);
-          for (int64_t e = src_ptr[lo]; e < src_ptr[lo + 1]; ++e)
-            acc += scratch[int64_t(r) * n_items + item_ptr[e] + i];
+          // 8 loads in flight, added in list order
+          const T *sc  = scratch + int64_t(r) * n_items + i;
+          T        acc = T(0);
+          int64_t  e   = e0;
+          for (; e + 8 <= e1; e += 8)
+            {
+              T v[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                v[u] = sc[item_ptr[e + u]];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                acc += v[u];
+            }
+          for (; e < e1; ++e)
+            acc += sc[item_ptr[e]];
           y[int64_t(r) * N + node] += acc;
         }
     }
@@ -493,11 +558,13 @@ namespace pibem
     int           rb    = int(std::max<int64_t>(1, (96 * 1024) / (maxnc * int64_t(sizeof(T)))));
     rb                  = std::min(rb, R);
     const size_t smem   = size_t(rb) * maxnc * sizeof(T);
+    // R == 1: the one-column kernel (fewer registers, more loads in flight);
+    // both compute a column with the same rounding steps in the same order
+    auto kern = R == 1 ? near_leaf_kernel<T, true> : near_leaf_kernel<T, false>;
     if (smem > 48 * 1024)
-      raise_smem_limit(reinterpret_cast<const void *>(near_leaf_kernel<T>), smem);
-    near_leaf_kernel<T><<<op.n_near_leaves, 256, smem, s>>>(R, rb, N, op.nrow_ptr, op.ncol_ptr,
-                                                          op.nval_ptr, op.nrows, op.ncols, vals, x,
-                                                          y, accumulate);
+      raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
+    kern<<<op.n_near_leaves, 256, smem, s>>>(R, rb, N, op.nrow_ptr, op.ncol_ptr, op.nval_ptr,
+                                             op.nrows, op.ncols, vals, x, y, accumulate);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

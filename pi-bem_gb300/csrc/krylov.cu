@@ -10,37 +10,33 @@ namespace pibem
   {
     constexpr int kDotBlock = 256;
 
-    // partial[(r * nblk + blk) * ncols + i] = sum over the block's rows of V[r][i][t] w[r][t]
+    // partial[(r * nblk + blk) * ncols + i] = sum over the block's rows of V[r][i][t] w[r][t].
+    // Warp k of the block takes columns k, k + 8, ...; its lanes stride over the
+    // block's rows (coalesced; the w slice is re-read from L1) and the warp sum is
+    // reduced in a fixed order, so the columns proceed in parallel without block
+    // barriers.
     __global__ void dots_partial_kernel(int64_t n, int ncols, int64_t ldv, int64_t ldr,
                                         const double *__restrict__ V,
                                         const double *__restrict__ w, int nblk,
                                         double *__restrict__ partial)
     {
-      __shared__ double red[kDotBlock / 32];
-      const int     r   = blockIdx.y;
-      const int     blk = blockIdx.x;
-      const double *Vr  = V + int64_t(r) * ldr;
-      const double *wr  = w + int64_t(r) * n;
+      const int     r     = blockIdx.y;
+      const int     blk   = blockIdx.x;
+      const double *Vr    = V + int64_t(r) * ldr;
+      const double *wr    = w + int64_t(r) * n;
       const int64_t chunk = (n + nblk - 1) / nblk;
       const int64_t t0 = int64_t(blk) * chunk, t1 = min(n, t0 + chunk);
-      for (int i = 0; i < ncols; ++i)
+      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      for (int i = warp; i < ncols; i += nw)
         {
-          double s = 0;
-          for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x)
-            s += Vr[int64_t(i) * ldv + t] * wr[t];
+          const double *v = Vr + int64_t(i) * ldv;
+          double        s = 0;
+          for (int64_t t = t0 + lane; t < t1; t += 32)
+            s += v[t] * wr[t];
           for (int o = 16; o > 0; o >>= 1)
             s += __shfl_xor_sync(0xffffffffu, s, o);
-          if ((threadIdx.x & 31) == 0)
-            red[threadIdx.x >> 5] = s;
-          __syncthreads();
-          if (threadIdx.x == 0)
-            {
-              double tot = 0;
-              for (int k = 0; k < int(blockDim.x >> 5); ++k)
-                tot += red[k];
-              partial[(int64_t(r) * nblk + blk) * ncols + i] = tot;
-            }
-          __syncthreads();
+          if (lane == 0)
+            partial[(int64_t(r) * nblk + blk) * ncols + i] = s;
         }
     }
 

@@ -13,16 +13,18 @@
 //     x = hi + lo (hi = TF32 rounding of x),   A B ~ Ah Bh + Al Bh + Ah Bl,
 // all three products accumulated into the same FP32 accumulator.
 //
-// Persistent, warp-specialised pipeline (one block per SM, 9 warps):
-//   warps 0-3  producers: per K chunk of 32, gather the 128 rows of A with
-//              coalesced loads (lane = k), split hi/lo and store them in the
-//              128-byte-swizzled K-major layout (a row's 32 values fill one
-//              128-byte line, 16-byte chunks XOR-permuted by row & 7, so the
-//              stores are free of bank conflicts); thread 0 copies the chunk's
-//              B hi/lo images with cp.async.bulk.  TC_STAGES-deep ring.
-//   warp 8     one thread issues the MMAs (4 K-steps x 3 products per chunk)
+// Persistent, warp-specialised pipeline (one block per SM, 13 warps):
+//   warps 0-7  producers, two groups of 4 warps filling alternate stages: per
+//              K chunk of 32, gather the 128 rows of A with coalesced loads
+//              (lane = k, all 32 rows of a warp in flight), split hi/lo and
+//              store them in the 128-byte-swizzled K-major layout (a row's 32
+//              values fill one 128-byte line, 16-byte chunks XOR-permuted by
+//              row & 7, so the stores are free of bank conflicts); the group's
+//              first thread copies the chunk's B hi/lo images with
+//              cp.async.bulk.  TC_STAGES-deep ring.
+//   warp 12    one thread issues the MMAs (4 K-steps x 3 products per chunk)
 //              into one of two tensor-memory accumulators and commits.
-//   warps 4-7  epilogue: tcgen05.ld of the accumulator (warp 4+q reads lanes
+//   warps 8-11 epilogue: tcgen05.ld of the accumulator (warp 8+q reads lanes
 //              32q..32q+31), staged per warp through shared memory and written
 //              as contiguous 128-byte row segments.
 // The accumulator double buffer lets the epilogue of tile i overlap the MMAs
@@ -45,10 +47,10 @@ namespace pibem
     constexpr int      TC_ROWS       = 128;
     constexpr int      TC_KC         = 32;  // K values per stage: one 128-byte line of TF32
     constexpr int      TC_STAGES     = 3;
-    constexpr int      TC_PRODUCERS  = 128; // warps 0-3
-    constexpr int      TC_EPI_WARP0  = 4;   // warps 4-7
-    constexpr int      TC_MMA_WARP   = 8;
-    constexpr int      TC_THREADS    = 9 * 32;
+    constexpr int      TC_GROUP      = 128; // producer group: 4 warps, one row per lane
+    constexpr int      TC_EPI_WARP0  = 8;   // warps 8-11
+    constexpr int      TC_MMA_WARP   = 12;
+    constexpr int      TC_THREADS    = 13 * 32;
     constexpr int      TC_EPI_LD     = 33;  // staging row stride (floats)
     constexpr int      TC_ACC_COLS   = 128; // tensor-memory columns per accumulator (N <= 128)
     constexpr uint32_t TC_TMEM_COLS  = 2 * TC_ACC_COLS;
@@ -238,7 +240,7 @@ namespace pibem
           abort_flag = 0;
           for (int s = 0; s < TC_STAGES; ++s)
             {
-              mbar_init(full(s), TC_PRODUCERS + 1);
+              mbar_init(full(s), TC_GROUP + 1);
               mbar_init(empty(s), 1);
             }
           for (int a = 0; a < 2; ++a)
@@ -272,9 +274,13 @@ namespace pibem
           }
       };
 
-      if (warp < 4)
+      if (warp < 8)
         {
           // ---------------- producers ----------------
+          // Two groups of 4 warps fill alternate stages (group g takes the
+          // stage iterations it with it % 2 == g), so two gathers are in flight;
+          // warp w of a group owns tile rows 32 (w % 4) .. 32 (w % 4) + 31.
+          const int grp = warp >> 2, gw = warp & 3, gtid = tid & (TC_GROUP - 1);
           int  it = 0;
           bool inflight[TC_STAGES];
           int  inflight_par[TC_STAGES];
@@ -291,10 +297,10 @@ namespace pibem
               const float *Blo   = Bhi + op_img_floats;
               for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS)
                 {
-                  // source offset of row t0 + 32 warp + lane (-1: padding row)
+                  // source offset of row t0 + 32 gw + lane (-1: padding row)
                   int64_t my_src = -1;
                   {
-                    const int i = t0 + 32 * warp + lane;
+                    const int i = t0 + 32 * gw + lane;
                     if (i < rows_total)
                       {
                         const int q = start + i / R, r = i - (i / R) * R;
@@ -303,6 +309,8 @@ namespace pibem
                   }
                   for (int kc = 0; kc < nkc; ++kc, ++it)
                     {
+                      if ((it & 1) != grp)
+                        continue;
                       const int s = it % TC_STAGES, use = it / TC_STAGES;
                       if (use > 0 && !mbar_wait(empty(s), uint32_t(use - 1) & 1u, &abort_flag))
                         {
@@ -312,7 +320,7 @@ namespace pibem
                       inflight[s]       = false;
                       const uint32_t st = base + uint32_t(s) * lay.stage_bytes;
                       uint8_t       *gs = gbase + size_t(s) * lay.stage_bytes;
-                      if (tid == 0)
+                      if (gtid == 0)
                         {
                           mbar_arrive_expect_tx(full(s), 2 * lay.b_bytes);
                           bulk_copy(st + 2 * TC_A_BYTES, Bhi + size_t(kc) * Np * TC_KC,
@@ -322,32 +330,30 @@ namespace pibem
                           inflight[s]     = true;
                           inflight_par[s] = use & 1;
                         }
+                      // all 32 row loads of the warp in flight at once (coalesced:
+                      // lane = k), then split and store
                       const int k = kc * TC_KC + lane;
-#pragma unroll 1
-                      for (int r0 = 0; r0 < 32; r0 += 8)
+                      float     x[32];
+#pragma unroll
+                      for (int u = 0; u < 32; ++u)
                         {
-                          float x[8];
+                          const int64_t src = __shfl_sync(0xffffffffu, my_src, u);
+                          x[u]              = (src >= 0 && k < K) ? E[src + k] : 0.0f;
+                        }
 #pragma unroll
-                          for (int u = 0; u < 8; ++u)
-                            {
-                              const int64_t src = __shfl_sync(0xffffffffu, my_src, r0 + u);
-                              x[u]              = (src >= 0 && k < K) ? E[src + k] : 0.0f;
-                            }
-#pragma unroll
-                          for (int u = 0; u < 8; ++u)
-                            {
-                              const uint32_t o = sw128_off(32 * warp + r0 + u, lane);
-                              const float    h = tf32_hi(x[u]);
-                              *reinterpret_cast<float *>(gs + o)              = h;
-                              *reinterpret_cast<float *>(gs + TC_A_BYTES + o) = x[u] - h;
-                            }
+                      for (int u = 0; u < 32; ++u)
+                        {
+                          const uint32_t o = sw128_off(32 * gw + u, lane);
+                          const float    h = tf32_hi(x[u]);
+                          *reinterpret_cast<float *>(gs + o)              = h;
+                          *reinterpret_cast<float *>(gs + TC_A_BYTES + o) = x[u] - h;
                         }
                       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                       mbar_arrive(full(s));
                     }
                 }
             }
-          if (!ok && tid == 0)
+          if (!ok && gtid == 0)
             for (int s = 0; s < TC_STAGES; ++s)
               if (inflight[s])
                 mbar_drain(full(s), uint32_t(inflight_par[s]));

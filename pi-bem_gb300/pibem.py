@@ -92,6 +92,8 @@ EXPORTS = [
     "pibem_tree_list", "pibem_tree_list_sublevels", "pibem_near_nnz", "pibem_near_export",
     "pibem_quad_points", "pibem_last_phase_ms", "pibem_set_profiling", "pibem_phase_totals",
     "pibem_launch_count", "pibem_fmm_matvec_noalloc", "pibem_device_bytes",
+    "pibem_ucd_read", "pibem_mesh_io_error", "pibem_double_nodes",
+    "pibem_dirichlet_mask_from_materials",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -140,6 +142,14 @@ def load():
     L.pibem_fmm_matvec_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p]
     L.pibem_device_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
+    L.pibem_ucd_read.argtypes = [C.c_char_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _dp, _ip,
+                                 _ip]
+    L.pibem_mesh_io_error.restype = C.c_char_p
+    L.pibem_mesh_io_error.argtypes = []
+    L.pibem_double_nodes.argtypes = [C.c_int64, _dp, C.c_double, _ip, _ip, C.c_int64,
+                                     C.POINTER(C.c_int64)]
+    L.pibem_dirichlet_mask_from_materials.argtypes = [C.c_int64, C.c_int64, _ip, _ip, C.c_int32,
+                                                      _ip, _u8p]
     _lib = L
     return L
 
@@ -167,6 +177,56 @@ def params_from_prm(text: str, **kw) -> Params:
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+def read_ucd(path: str):
+    """UCD (.inp) surface mesh -> (xyz (N,3) float64, cells (C,4) int32 in deal.II
+    vertex order, material ids (C,) int32)."""
+    L = load()
+    nn, nc = C.c_int64(0), C.c_int64(0)
+    rc = L.pibem_ucd_read(os.fsencode(path), C.byref(nn), C.byref(nc), None, None, None)
+    if rc:
+        raise PibemError(rc, L.pibem_mesh_io_error().decode())
+    xyz = np.zeros((nn.value, 3))
+    cells = np.zeros((nc.value, 4), np.int32)
+    mat = np.zeros(nc.value, np.int32)
+    rc = L.pibem_ucd_read(os.fsencode(path), C.byref(nn), C.byref(nc), _d(xyz), _i(cells), _i(mat))
+    if rc:
+        raise PibemError(rc, L.pibem_mesh_io_error().decode())
+    return xyz, cells, mat
+
+
+def double_nodes(xyz, tol: float = 1e-10):
+    """Double-node sets of coincident nodes -> (offsets (N+1,), ids) int32 CSR, every
+    node's set including itself (the form set_mesh takes)."""
+    L = load()
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    n = xyz.shape[0]
+    off = np.zeros(n + 1, np.int32)
+    tot = C.c_int64(0)
+    rc = L.pibem_double_nodes(n, _d(xyz), tol, _i(off), None, 0, C.byref(tot))
+    if rc:
+        raise PibemError(rc, "double_nodes")
+    ids = np.zeros(max(tot.value, 1), np.int32)
+    rc = L.pibem_double_nodes(n, _d(xyz), tol, _i(off), _i(ids), len(ids), C.byref(tot))
+    if rc:
+        raise PibemError(rc, "double_nodes")
+    return off, ids[:tot.value]
+
+
+def dirichlet_mask(n_nodes: int, cells, material, dirichlet_ids):
+    """Nodes of cells whose material id is in dirichlet_ids -> 1, others 0."""
+    L = load()
+    cells = np.ascontiguousarray(cells, np.int32).reshape(-1, 4)
+    material = np.ascontiguousarray(material, np.int32)
+    ids = np.ascontiguousarray(list(dirichlet_ids) or [0], np.int32)
+    mask = np.zeros(n_nodes, np.uint8)
+    rc = L.pibem_dirichlet_mask_from_materials(n_nodes, cells.shape[0], _i(cells), _i(material),
+                                               len(list(dirichlet_ids)), _i(ids),
+                                               mask.ctypes.data_as(_u8p))
+    if rc:
+        raise PibemError(rc, "dirichlet_mask")
+    return mask
 
 
 def _d(a):

@@ -47,8 +47,11 @@ def test_outward_normals(synthetic):
 
 def test_node_count_helpers(synthetic):
     S = synthetic
+    for n in (2000, 20000):
+        assert abs(S.wigley_hull(*S.wigley_for_nodes(n)).n_nodes - n) < 0.1 * n
+    nx, nz, ny = S.wigley_for_nodes(393000)
+    assert (nx, nz, ny) == (768, 192, 128)
     for n in (2000, 20000, 200000):
-        assert abs(S.wigley_hull(*S.wigley_for_nodes(n)).n_nodes - n) < 0.1 * n if n <= 20000 else True
         k = S.sphere_n_for_nodes(n)
         assert abs(6 * k * k + 2 - n) < 0.1 * n
 
