@@ -244,7 +244,11 @@ def run_ours(args, w, rank, world, local):
     pr, dr, _ = gref.solve(tmp)
     sol_ref = np.where(mask == 1, dr, pr)
     gref.close()
-    tot32, per32, st32, clk32, ph32, sol32, nl32 = device_solves(g32, K, W, profile=True)
+    # timed solves (no phase timing: the FP32 operator replays as a CUDA graph)
+    tot32, per32, st32, clk32, _, sol32, nl32 = device_solves(g32, K, W)
+    # phase breakdown from two more solves with CUDA-event phase timing (their
+    # host-recorded events disable the graph; used only for the roofline)
+    prof_ms, _, _, _, ph32, _, _ = device_solves(g32, 2, 0, profile=True)
     tot64, per64, st64, clk64, _, sol64, _ = device_solves(g64, max(2, min(K, 5)), min(W, 2))
     t_max = max_over_ranks(tot32 / 1e3, world, dev)
     t64_max = max_over_ranks(tot64 / 1e3, world, dev)
@@ -285,17 +289,20 @@ def run_ours(args, w, rank, world, local):
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
     e2e_value = K * world / e2e_s
 
-    # roofline of the dominant kernel (CUDA events over the timed region)
+    # roofline of the dominant kernel (CUDA events over the timed region): the
+    # single-kernel phase (M2L GEMM, near SpMV) with the largest total time
     hbm_peak, bf16_peak, peak_kind = peaks()
     (p32, c32), (p64, c64) = ph32
     phase_tot = {}
     for prec, (pt, c) in (("fp32", (p32, c32)), ("fp64", (p64, c64))):
         for k, v in pt.items():
-            if k != "unused":
-                phase_tot[(prec, k)] = (v, c)
-    (dom_prec, dom_phase), (dom_ms, dom_cnt) = max(phase_tot.items(), key=lambda kv: kv[1][0])
+            phase_tot[(prec, k)] = (v, c)
+    single = {k: v for k, v in phase_tot.items() if k[1] in ("m2l", "near") and k[0] == "fp32"}
+    (dom_prec, dom_phase), (dom_ms, dom_cnt) = max(single.items(), key=lambda kv: kv[1][0])
     roof = roofline(info, n, dom_prec, dom_phase, dom_ms, dom_cnt, hbm_peak, bf16_peak, peak_kind,
-                    w["p"])
+                    w["p"], args.workload)
+    roof["phase_share_of_solve"] = {f"{pr}:{k}": round(v[0] / (prof_ms if prof_ms else 1), 4)
+                                    for (pr, k), v in phase_tot.items()}
 
     err32 = float(np.linalg.norm(sol32 - sol_ref) / np.linalg.norm(sol_ref))
     err64 = float(np.linalg.norm(sol64 - sol_ref) / np.linalg.norm(sol_ref))
@@ -341,7 +348,7 @@ def run_ours(args, w, rank, world, local):
     }
     line["gpu_launches"] = nl32
     line["phases_ms_per_application"] = {
-        prec: {k: v / max(c, 1) for k, v in pt.items() if k != "unused"} | {"applications": c}
+        prec: {k: v / max(c, 1) for k, v in pt.items()} | {"applications": c}
         for prec, (pt, c) in (("fp32", ph32[0]), ("fp64", ph32[1]))}
     if rank == 0 and world == 1 and not args.no_cpu_baseline and w.get("cpu", True):
         line["cpu_baseline"] = cpu_baseline(w, mesh, mask, st64[-1]["fp64_matvecs"])
@@ -660,27 +667,41 @@ def run_served(args, w, rank, world, local):
     _done_dist(world)
 
 
-def roofline(info, n, prec, phase, ms, cnt, hbm_peak, bf16_peak, peak_kind, p):
+# DRAM traffic per launch of the roofline kernels, from one ncu capture each of
+# `bench.py --mode profile` on the workload (dram__bytes_read.sum +
+# dram__bytes_write.sum); the summaries are in profiles/.
+NCU_TRAFFIC_MB = {("spheroid98k", "m2l"): 56.4, ("spheroid98k", "near"): 251.7}
+
+
+def roofline(info, n, prec, phase, ms, cnt, hbm_peak, bf16_peak, peak_kind, p, workload):
     s = 4 if prec == "fp32" else 8
     K = (p + 1) ** 2
     per_launch_s = ms / 1e3 / max(cnt, 1)
+    mb = NCU_TRAFFIC_MB.get((workload, phase))
+    traffic = None if mb is None else mb * 1e6
     if phase == "near":
-        # values + column ids (per leaf block) + x gathered once + y written once
-        byt = info["near_nnz"] * s + info["near_nnz"] * 0 + 2 * n * s
+        # values (one combined system matrix) + x gathered once + y written once;
+        # column ids are per leaf block (negligible)
+        byt = info["near_nnz"] * s + 2 * n * s
         return {"kernel": f"near-field leaf-block SpMV ({prec})", "bound": "hbm",
                 "achieved": byt / per_launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                "frac": byt / per_launch_s / 1e9 / hbm_peak, "traffic": None,
+                "frac": byt / per_launch_s / 1e9 / hbm_peak, "traffic": traffic,
                 "algorithmic_bytes_per_launch": byt, "launch_ms": per_launch_s * 1e3,
                 "peak_source": f"{peak_kind} hbm_gbs"}
-    if phase == "m2l_l2l":
+    if phase == "m2l":
+        # 3xTF32: every FP32 product is issued as three TF32 tensor-core products
         fl = 2.0 * K * K * info["n_m2l_pairs"]
-        return {"kernel": f"M2L+L2L translations ({prec})", "bound": "tensor",
-                "achieved": fl / per_launch_s / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": fl / per_launch_s / 1e12 / bf16_peak, "traffic": None,
-                "algorithmic_flops_per_launch": fl, "launch_ms": per_launch_s * 1e3,
-                "peak_source": f"{peak_kind} bf16_tflops"}
+        issued = 3 * fl
+        return {"kernel": "M2L GEMM of all levels, tcgen05 3xTF32 (fp32)", "bound": "tensor",
+                "achieved": issued / per_launch_s / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": issued / per_launch_s / 1e12 / bf16_peak, "traffic": traffic,
+                "algorithmic_flops_per_launch": fl, "issued_tf32_flops_per_launch": issued,
+                "fp32_equivalent_tflops": fl / per_launch_s / 1e12,
+                "launch_ms": per_launch_s * 1e3,
+                "peak_source": f"{peak_kind} bf16_tflops (TF32 issues at half the BF16 rate, so "
+                               "frac is at most 0.5 for this kernel)"}
     return {"kernel": f"{phase} ({prec})", "bound": "hbm", "achieved": None, "peak": hbm_peak,
-            "unit": "GB/s", "frac": None, "traffic": None, "launch_ms": per_launch_s * 1e3,
+            "unit": "GB/s", "frac": None, "traffic": traffic, "launch_ms": per_launch_s * 1e3,
             "peak_source": f"{peak_kind} hbm_gbs"}
 
 

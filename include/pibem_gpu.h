@@ -160,7 +160,9 @@ int     pibem_near_export(pibem_handle *h, int32_t *rows, int32_t *cols, double 
 /* Quadrature points of the mesh, cell-major (n_cells * nq points). */
 int pibem_quad_points(pibem_handle *h, double *pts);
 /* Phase timings of the last operator application, milliseconds, in the order
- * near, p2m, m2m, m2l+l2l, (unused), m2p, l2p (7 values); needs profiling on. */
+ * near, p2m, m2m (all levels), m2l (the batched M2L GEMM of all levels), l2l
+ * (L2L and the sums of each box's products, all levels), m2p, l2p (7 values);
+ * needs profiling on. */
 int pibem_last_phase_ms(pibem_handle *h, double *ms7);
 /* Turns CUDA-event timing of the operator phases on or off (off by default;
  * on adds event records and one stream synchronisation per application). */

@@ -20,6 +20,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "kernels.h"
@@ -162,12 +163,13 @@ struct pibem_handle
     d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
     d_down_box, d_up_q, d_down_q;
   DBuf<NearEntry> d_entries;
-  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv;
-  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg;
+  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc;
+  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg, d_Tcf;
   DBuf<float2>  d_opsff; // the FP64 operator table as (hi, lo) FP32 pairs
   DBuf<int>     d_err;
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
+  int                  max_leaf_rows = 0;
   OperatorDev<double> op64;
   OperatorDev<float>  op32;
   TreeDev             td;
@@ -216,7 +218,7 @@ struct pibem_handle
         d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
         d_up_box, d_down_box, d_up_q, d_down_q);
-    add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_S32, d_T1f, d_T2f, d_Wf,
+    add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
         d_y32, d_m2p32, d_Y32);
@@ -275,7 +277,7 @@ namespace
   // ---------------------------------------------------------------------
   template <typename T>
   void far_field(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
-                 DBuf<T> &Y, int R, const uint8_t *modes, const T *x, T *y)
+                 DBuf<T> &Y, int R, const uint8_t *modes, const T *x, T *y, bool combined = false)
   {
     Y.alloc(std::max<size_t>(1, size_t(op.n_pairs) * R * op.K));
     const int    N = int(h->N());
@@ -289,15 +291,15 @@ namespace
     op.m2p_scratch = scr.p;
     cudaStream_t s = h->stream;
     PIBEM_CUDA(cudaMemsetAsync(M.p, 0, need * sizeof(T), s));
-    launch_p2m_apply<T>(op, R, N, h->d_dir.p, modes, x, M.p, s);
+    launch_p2m_apply<T>(op, R, N, h->d_dir.p, modes, x, M.p, combined, s);
     record(h, 2);
     for (int l = h->tree.L; l >= 1; --l)
       launch_upward_level<T>(op, R, l, M.p, Y.p, s);
     record(h, 3);
     launch_m2l_gemm<T>(op, R, M.p, Y.p, s);
+    record(h, 4);
     for (int l = 1; l <= h->tree.L; ++l)
       launch_downward_level<T>(op, R, l, Lx.p, Y.p, s);
-    record(h, 4);
     record(h, 5);
     launch_m2p<T>(op, h->td, R, N, M.p, y, s);
     record(h, 6);
@@ -406,7 +408,8 @@ namespace
     record(h, 0);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_S.p, xin, y, false, s);
     record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, xin, y);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, xin, y,
+                      true);
     finish_timing(h, 0);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
@@ -422,7 +425,7 @@ namespace
                             h->stream);
     record(h, 1);
     far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, h->d_Y32, R, h->d_modes32.p,
-                     h->d_x32.p, h->d_y32.p);
+                     h->d_x32.p, h->d_y32.p, true);
   }
 
   void drop_graph(pibem_handle *h)
@@ -616,12 +619,9 @@ namespace
             // z = P^-1 V_j ; w = A z
             const double *vj = h->g_V.p + int64_t(j) * N;
             if (prec)
-              {
-                copy_cols(h->g_u.p, N, vj, ldr, N, R, s);
-                launch_block_apply(h->plan.nrows.size(), R, N, h->d_row_leaf.p, h->d_nrow_ptr.p,
-                                   h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, h->g_z.p,
-                                   s);
-              }
+              launch_block_apply(int(h->blk_ptr.size()) - 1, h->max_leaf_rows, R, N,
+                                 h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, vj, ldr,
+                                 h->g_z.p, s);
             else
               copy_cols(h->g_z.p, N, vj, ldr, N, R, s);
             A(h->g_z.p, h->g_w.p);
@@ -695,8 +695,8 @@ namespace
         launch_gemv_sub(N, R, kmax, N, ldr, h->g_V.p, h->g_y.p, m + 1, h->g_u.p, -1.0, s);
         if (prec)
           {
-            launch_block_apply(h->plan.nrows.size(), R, N, h->d_row_leaf.p, h->d_nrow_ptr.p,
-                               h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, h->g_z.p, s);
+            launch_block_apply(int(h->blk_ptr.size()) - 1, h->max_leaf_rows, R, N, h->d_nrow_ptr.p,
+                               h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, N, h->g_z.p, s);
             launch_axpby(int64_t(R) * N, 1.0, h->g_z.p, 1.0, x, s);
           }
         else
@@ -711,10 +711,12 @@ namespace
     const int     nl = int(pl.nleaf_box.size());
     cudaStream_t  s  = h->stream;
     h->blk_ptr.assign(nl + 1, 0);
+    h->max_leaf_rows = 0;
     for (int k = 0; k < nl; ++k)
       {
         int64_t nr       = pl.nrow_ptr[k + 1] - pl.nrow_ptr[k];
         h->blk_ptr[k + 1] = h->blk_ptr[k] + nr * nr;
+        h->max_leaf_rows  = std::max(h->max_leaf_rows, int(nr));
       }
     h->d_blk_ptr.upload(h->blk_ptr, s);
     DBuf<double> blocks;
@@ -777,6 +779,7 @@ namespace
       op.up_q_ptr      = h->d_up_q_ptr.p;
       op.down_q_ptr    = h->d_down_q_ptr.p;
       op.n_pairs       = int64_t(pl.q_src.size());
+      op.Tc            = nullptr; // made by set_bc
       op.max_near_cols = 0;
       for (size_t k2 = 0; k2 + 1 < pl.ncol_ptr.size(); ++k2)
         op.max_near_cols = std::max<int64_t>(op.max_near_cols, pl.ncol_ptr[k2 + 1] - pl.ncol_ptr[k2]);
@@ -897,6 +900,19 @@ namespace
       need(v >= 0 && v < t.nb, "down box");
     for (int32_t v : pl.up_q)
       need(v >= 0 && v < nq_pairs, "up pair");
+    need(pl.up_chunk_ptr.size() == size_t(t.L + 2) && pl.down_chunk_ptr.size() == size_t(t.L + 2) &&
+           pl.up_box_ptr.size() == size_t(t.L + 2) && pl.down_box_ptr.size() == size_t(t.L + 2) &&
+           pl.up_box_ptr[t.L + 1] == int(pl.up_box.size()) &&
+           pl.down_box_ptr[t.L + 1] == int(pl.down_box.size()) &&
+           pl.up_chunk_ptr[t.L + 1] <= int(pl.ch_start.size()) &&
+           pl.down_chunk_ptr[t.L + 1] <= int(pl.ch_start.size()),
+         "level range sizes");
+    for (int l = 1; l <= t.L; ++l)
+      need(pl.up_chunk_ptr[l] <= pl.up_chunk_ptr[l + 1] && pl.down_chunk_ptr[l] <= pl.down_chunk_ptr[l + 1] &&
+             pl.up_box_ptr[l] <= pl.up_box_ptr[l + 1] && pl.down_box_ptr[l] <= pl.down_box_ptr[l + 1] &&
+             pl.up_chunk_ptr[l] >= 0 && pl.down_chunk_ptr[l] >= 0 && pl.up_box_ptr[l] >= 0 &&
+             pl.down_box_ptr[l] >= 0,
+           "level ranges");
     for (int32_t v : pl.down_q)
       need(v >= 0 && v < nq_pairs, "down pair");
     need(pl.m2l_src_ptr.size() == pl.m2l_tgt.size() + 1, "m2l ptr");
@@ -1039,6 +1055,7 @@ namespace
     h->d_m2p_src_ptr.upload(pl.m2p_src_ptr, s);
     h->d_m2p_src.upload(pl.m2p_src, s);
     h->d_q_src.upload(pl.q_src, s);
+
     h->d_ch_start.upload(pl.ch_start, s);
     h->d_ch_cnt.upload(pl.ch_cnt, s);
     h->d_ch_op.upload(pl.ch_op, s);
@@ -1265,6 +1282,19 @@ namespace
                                h->d_ncol_ptr.p, h->d_nrow_ptr.p, h->d_nrows.p, h->d_ncols.p,
                                h->d_dir.p, h->d_alpha.p, h->d_N.p, h->d_D.p, h->d_S.p, h->d_S32.p,
                                s);
+    // combined-strength P2M tables of the system operator (one row read per row)
+    {
+      const int64_t nr = int64_t(pl.prow_dof.size());
+      const int     K4 = (pl.K + 3) / 4 * 4;
+      h->d_Tc.alloc(std::max<int64_t>(1, nr * K4));
+      h->d_Tcf.alloc(std::max<int64_t>(1, nr * K4));
+      launch_combine_p2m<double>(nr, K4, h->d_prow_dof.p, h->d_dir.p, h->d_T1.p, h->d_T2.p,
+                                 h->d_Tc.p, s);
+      launch_combine_p2m<float>(nr, K4, h->d_prow_dof.p, h->d_dir.p, h->d_T1f.p, h->d_T2f.p,
+                                h->d_Tcf.p, s);
+      h->op64.Tc = h->d_Tc.p;
+      h->op32.Tc = h->d_Tcf.p;
+    }
     if (h->prm.preconditioner)
       build_preconditioner(h);
     PIBEM_CUDA(cudaStreamSynchronize(s));
@@ -1832,7 +1862,7 @@ namespace
     const int    N = int(h->N());
     cudaStream_t s = h->stream;
     PIBEM_CUDA(cudaMemsetAsync(M, 0, size_t(h->tree.nb) * R * op.K * sizeof(double), s));
-    launch_p2m_apply<double>(op, R, N, dir, modes, x, M, s);
+    launch_p2m_apply<double>(op, R, N, dir, modes, x, M, false, s);
     for (int l = h->tree.L; l >= 1; --l)
       launch_upward_level<double>(op, R, l, M, Y, s);
     launch_m2l_gemm<double>(op, R, M, Y, s);

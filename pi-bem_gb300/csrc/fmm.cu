@@ -28,6 +28,10 @@ namespace pibem
       return v;
     }
 
+    // a * b + c with one rounding (no dependence on the compiler's contraction)
+    __device__ __forceinline__ float  fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    __device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
     // s + a . x for 4 values, with the rounding steps spelled out so that every
     // code path (one column or several) computes a column bit-for-bit alike.
     __device__ inline float dot4_acc(float s, const float (&a)[4], const float *x)
@@ -154,7 +158,10 @@ namespace pibem
     // combined system strengths.  Warp w of the block takes rows w, w+8, ...;
     // lane l owns coefficients 4l..4l+3 (table rows padded to 4 values); the
     // eight partial sums are added in a fixed order.
-    template <typename T>
+    // COMBINED: every column uses the combined strengths, read from the table
+    // Tc = (Dirichlet dof ? -T2 : T1) made at set_bc (one table row per row
+    // instead of two); T1 is then Tc and T2 is unused.
+    template <typename T, bool COMBINED>
     __global__ void __launch_bounds__(256)
       p2m_apply_kernel(int R, int K, int N, const int64_t *__restrict__ prow_ptr,
                        const int32_t *__restrict__ pleaf_box, const int32_t *__restrict__ prow_dof,
@@ -180,11 +187,25 @@ namespace pibem
             for (int b = 0; b < 4; ++b)
               acc[a][b] = T(0);
           if (act)
+#pragma unroll 4
             for (int64_t row = rb + warp; row < re; row += 8)
               {
                 const int dof = prow_dof[row];
                 T         t1[4], t2[4];
                 load4(T1 + row * K4 + 4 * lane, t1);
+                if constexpr (COMBINED)
+                  {
+#pragma unroll
+                    for (int rr = 0; rr < 4; ++rr)
+                      if (rr < rc)
+                        {
+                          const T xv = x[int64_t(rq + rr) * N + dof];
+#pragma unroll
+                          for (int c = 0; c < 4; ++c)
+                            acc[rr][c] += xv * t1[c];
+                        }
+                    continue;
+                  }
                 load4(T2 + row * K4 + 4 * lane, t2);
                 const bool d = dir[dof] != 0;
 #pragma unroll
@@ -257,7 +278,9 @@ namespace pibem
           sB[ki * GB_LDB + c] = M[(int64_t(q_src[q]) * R + r) * K + ki];
         }
       __syncthreads();
-      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+      // rows ko = row0 + tx + 16 i of this block (row0 > 0 when the rows are split
+      // over blockIdx.z for launches with few blocks)
+      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, row0 = blockIdx.z * 16 * KI;
       T         acc[KI][4];
 #pragma unroll
       for (int i = 0; i < KI; ++i)
@@ -270,7 +293,7 @@ namespace pibem
 #pragma unroll
           for (int i = 0; i < KI; ++i)
             {
-              const int ko = tx + 16 * i;
+              const int ko = row0 + tx + 16 * i;
               a[i]         = ko < K ? sT[ki * K + ko] : T(0);
             }
 #pragma unroll
@@ -280,7 +303,7 @@ namespace pibem
           for (int i = 0; i < KI; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-              acc[i][j] += a[i] * b[j];
+              acc[i][j] = fma_rn(a[i], b[j], acc[i][j]);
         }
 #pragma unroll
       for (int j = 0; j < 4; ++j)
@@ -294,7 +317,7 @@ namespace pibem
 #pragma unroll
           for (int i = 0; i < KI; ++i)
             {
-              const int ko = tx + 16 * i;
+              const int ko = row0 + tx + 16 * i;
               if (ko < K)
                 Y[(q * R + r) * K + ko] = acc[i][j];
             }
@@ -354,7 +377,7 @@ namespace pibem
           sB[ki * GB_LDB + c] = make_float2(hi, __double2float_rn(__dsub_rn(x, double(hi))));
         }
       __syncthreads();
-      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, row0 = blockIdx.z * 16 * KI;
       float     sh[KI][4], sl[KI][4];
 #pragma unroll
       for (int i = 0; i < KI; ++i)
@@ -367,7 +390,7 @@ namespace pibem
 #pragma unroll
           for (int i = 0; i < KI; ++i)
             {
-              const int ko = tx + 16 * i;
+              const int ko = row0 + tx + 16 * i;
               a[i]         = ko < K ? sT[ki * K + ko] : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
@@ -391,7 +414,7 @@ namespace pibem
 #pragma unroll
           for (int i = 0; i < KI; ++i)
             {
-              const int ko = tx + 16 * i;
+              const int ko = row0 + tx + 16 * i;
               if (ko < K)
                 Y[(q * R + r) * K + ko] = __dadd_rn(double(sh[i][j]), double(sl[i][j]));
             }
@@ -571,13 +594,17 @@ namespace pibem
 
   template <typename T>
   void launch_p2m_apply(const OperatorDev<T> &op, int R, int N, const uint8_t *dir,
-                        const uint8_t *modes, const T *x, T *M, cudaStream_t s)
+                        const uint8_t *modes, const T *x, T *M, bool combined, cudaStream_t s)
   {
     if (op.n_p2m_leaves == 0)
       return;
     const size_t smem = size_t(8) * 4 * ((op.K + 3) / 4 * 4) * sizeof(T);
-    p2m_apply_kernel<T><<<op.n_p2m_leaves, 256, smem, s>>>(
-      R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof, op.T1, op.T2, dir, modes, x, M);
+    if (combined && op.Tc)
+      p2m_apply_kernel<T, true><<<op.n_p2m_leaves, 256, smem, s>>>(
+        R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof, op.Tc, op.T2, dir, modes, x, M);
+    else
+      p2m_apply_kernel<T, false><<<op.n_p2m_leaves, 256, smem, s>>>(
+        R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof, op.T1, op.T2, dir, modes, x, M);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -594,9 +621,14 @@ namespace pibem
           launch_tc_gemm(op, R, c0, c1, E, Y, op.tc_err, s);
           return;
         }
-    // largest column count of the chunks in [c0, c1): R x (<= 128 pairs)
-    const dim3 grid(unsigned(c1 - c0), unsigned((op.max_chunk_pairs * R + GB_COLS - 1) / GB_COLS));
-    const int  KI = (op.K + 15) / 16;
+    // largest column count of the chunks in [c0, c1): R x (<= 128 pairs).  A
+    // launch with fewer blocks than ~2 per SM (the tree's small levels) splits
+    // each block's rows over blockIdx.z (16 rows per block) for parallelism.
+    const unsigned gx = unsigned(c1 - c0),
+                   gy = unsigned((op.max_chunk_pairs * R + GB_COLS - 1) / GB_COLS);
+    const bool     split = int64_t(gx) * gy < 256;
+    const int      KI    = split ? 1 : (op.K + 15) / 16;
+    const dim3     grid(gx, gy, split ? unsigned((op.K + 15) / 16) : 1u);
     if constexpr (std::is_same<T, double>::value)
       if (op.ops_ff)
         {
@@ -726,7 +758,7 @@ namespace pibem
   template void launch_near_spmv<T>(const OperatorDev<T> &, int, int, const T *, const T *, T *, \
                                     bool, cudaStream_t);                                         \
   template void launch_p2m_apply<T>(const OperatorDev<T> &, int, int, const uint8_t *,           \
-                                    const uint8_t *, const T *, T *, cudaStream_t);              \
+                                    const uint8_t *, const T *, T *, bool, cudaStream_t);        \
   template void launch_upward_level<T>(const OperatorDev<T> &, int, int, T *, T *, cudaStream_t); \
   template void launch_m2l_gemm<T>(const OperatorDev<T> &, int, const T *, T *, cudaStream_t);    \
   template void launch_downward_level<T>(const OperatorDev<T> &, int, int, T *, T *,             \

@@ -79,6 +79,7 @@ namespace pibem
     const int64_t *prow_ptr = nullptr;
     const int32_t *pleaf_box = nullptr, *prow_dof = nullptr;
     const T       *T1 = nullptr, *T2 = nullptr;
+    const T       *Tc = nullptr; // combined-strength table (set_bc): dir ? -T2 : T1
     // l2p (same row positions as the near field)
     const int32_t *lleaf_box = nullptr;
     const T       *W = nullptr;
@@ -112,7 +113,7 @@ namespace pibem
                         bool accumulate, cudaStream_t s);
   template <typename T>
   void launch_p2m_apply(const OperatorDev<T> &op, int R, int N, const uint8_t *dir,
-                        const uint8_t *modes, const T *x, T *M, cudaStream_t s);
+                        const uint8_t *modes, const T *x, T *M, bool combined, cudaStream_t s);
   // upward level l: M2M of the level-l children, gathered into the parents
   template <typename T>
   void launch_upward_level(const OperatorDev<T> &op, int R, int level, T *M, T *Y, cudaStream_t s);
@@ -147,6 +148,10 @@ namespace pibem
   // ---- vector kernels (krylov.cu) -------------------------------------------
   void launch_convert_d2f(int64_t n, const double *a, float *b, cudaStream_t s);
   void launch_convert_f2d(int64_t n, const float *a, double *b, cudaStream_t s);
+  // Tc[row] = dir[dof(row)] ? -T2[row] : T1[row] for the rows of the P2M tables
+  template <typename T>
+  void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,
+                          const T *T1, const T *T2, T *Tc, cudaStream_t s);
   void launch_build_system_matrix(int64_t n_vals, int n_leaves, const int64_t *val_ptr,
                                   const int64_t *col_ptr, const int64_t *row_ptr,
                                   const int32_t *rows, const int32_t *cols, const uint8_t *dir,

@@ -2,6 +2,8 @@
 // Gram-Schmidt applied twice) and of the BEMProblem wrappers (masks, rhs,
 // system matrix).  Reductions are two-stage with a fixed order, so results do
 // not depend on scheduling.
+#include <algorithm>
+
 #include "krylov.h"
 
 namespace pibem
@@ -205,32 +207,51 @@ namespace pibem
     }
 
     // z[node] = sum_c Pinv[leaf][r][c] v[rows_c]  (leaf-block Jacobi, right preconditioner)
-    __global__ void block_apply_kernel(int64_t n_rows, int R, int64_t n,
-                                       const int32_t *__restrict__ row_leaf,
+    // z = P^-1 v on every childless box's rows: one block per box; the box's
+    // entries of v are gathered into shared memory once, then warp k takes rows
+    // k, k + nw, ... with its lanes over the (row-major) inverse block -- the same
+    // products and the same reduction order as one warp per row reading v
+    // directly.
+    __global__ void block_apply_kernel(int R, int64_t n, int64_t ldv,
                                        const int64_t *__restrict__ row_ptr,
                                        const int64_t *__restrict__ blk_ptr,
                                        const int32_t *__restrict__ rows,
                                        const double *__restrict__ Pinv,
                                        const double *__restrict__ v, double *__restrict__ z)
     {
-      const int64_t row  = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-      const int     lane = threadIdx.x & 31;
-      if (row >= n_rows)
-        return;
-      const int     leaf = row_leaf[row];
+      extern __shared__ double sv[];
+      const int     leaf = blockIdx.x;
       const int64_t r0 = row_ptr[leaf], nr = row_ptr[leaf + 1] - r0;
-      const double *P    = Pinv + blk_ptr[leaf] + (row - r0) * nr;
-      const int     node = rows[row];
+      const double *P    = Pinv + blk_ptr[leaf];
+      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
       for (int rr = 0; rr < R; ++rr)
         {
-          double s = 0;
-          for (int64_t c = lane; c < nr; c += 32)
-            s += P[c] * v[int64_t(rr) * n + rows[r0 + c]];
-          for (int o = 16; o > 0; o >>= 1)
-            s += __shfl_xor_sync(0xffffffffu, s, o);
-          if (lane == 0)
-            z[int64_t(rr) * n + node] = s;
+          for (int64_t c = threadIdx.x; c < nr; c += blockDim.x)
+            sv[c] = v[int64_t(rr) * ldv + rows[r0 + c]];
+          __syncthreads();
+          for (int64_t row = warp; row < nr; row += nw)
+            {
+              double s = 0;
+              for (int64_t c = lane; c < nr; c += 32)
+                s += P[row * nr + c] * sv[c];
+              for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_xor_sync(0xffffffffu, s, o);
+              if (lane == 0)
+                z[int64_t(rr) * n + rows[r0 + row]] = s;
+            }
+          __syncthreads();
         }
+    }
+
+    template <typename T>
+    __global__ void combine_p2m_kernel(int64_t n, int K4, const int32_t *__restrict__ prow_dof,
+                                       const uint8_t *__restrict__ dir, const T *__restrict__ T1,
+                                       const T *__restrict__ T2, T *__restrict__ Tc)
+    {
+      const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i >= n)
+        return;
+      Tc[i] = dir[prow_dof[i / K4]] ? -T2[i] : T1[i];
     }
 
     inline unsigned nblocks(int64_t n, int t = 256) { return unsigned((n + t - 1) / t); }
@@ -335,15 +356,33 @@ namespace pibem
     note_launch();
   }
 
-  void launch_block_apply(int64_t n_rows, int R, int64_t n, const int32_t *row_leaf,
-                          const int64_t *row_ptr, const int64_t *blk_ptr, const int32_t *rows,
-                          const double *Pinv, const double *v, double *z, cudaStream_t s)
+  void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
+                          const int64_t *blk_ptr, const int32_t *rows, const double *Pinv,
+                          const double *v, int64_t ldv, double *z, cudaStream_t s)
   {
-    if (n_rows == 0)
+    if (n_leaves == 0)
       return;
-    block_apply_kernel<<<nblocks(n_rows * 32), 256, 0, s>>>(n_rows, R, n, row_leaf, row_ptr,
-                                                            blk_ptr, rows, Pinv, v, z);
+    const size_t smem = size_t(std::max(max_rows, 1)) * sizeof(double);
+    if (smem > 48 * 1024)
+      raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel), smem);
+    block_apply_kernel<<<n_leaves, 128, smem, s>>>(R, n, ldv, row_ptr, blk_ptr, rows, Pinv, v, z);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
+
+  template <typename T>
+  void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,
+                          const T *T1, const T *T2, T *Tc, cudaStream_t s)
+  {
+    const int64_t n = n_rows * K4;
+    if (n == 0)
+      return;
+    combine_p2m_kernel<T><<<nblocks(n), 256, 0, s>>>(n, K4, prow_dof, dir, T1, T2, Tc);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+  template void launch_combine_p2m<float>(int64_t, int, const int32_t *, const uint8_t *,
+                                          const float *, const float *, float *, cudaStream_t);
+  template void launch_combine_p2m<double>(int64_t, int, const int32_t *, const uint8_t *,
+                                           const double *, const double *, double *, cudaStream_t);
 } // namespace pibem

@@ -233,6 +233,10 @@ namespace pibem
       auto tfull  = [&](int a) { return bar0 + 8u * uint32_t(2 * TC_STAGES + a); };
       auto tempty = [&](int a) { return bar0 + 8u * uint32_t(2 * TC_STAGES + 2 + a); };
       const uint32_t drain = bar0 + 8u * uint32_t(2 * TC_STAGES + 4);
+      // each block takes a contiguous range of chunks: consecutive chunks mostly
+      // share their operator, so a stage can keep its B tile (see the producers)
+      const int ch_lo = chunk0 + int(int64_t(n_chunks) * blockIdx.x / gridDim.x);
+      const int ch_hi = chunk0 + int(int64_t(n_chunks) * (blockIdx.x + 1) / gridDim.x);
       const size_t   op_img_floats = size_t(nkc) * Np * TC_KC; // one half of an operator image
 
       if (tid == 0)
@@ -282,6 +286,15 @@ namespace pibem
           // warp w of a group owns tile rows 32 (w % 4) .. 32 (w % 4) + 31.
           const int grp = warp >> 2, gw = warp & 3, gtid = tid & (TC_GROUP - 1);
           int  it = 0;
+          // (operator, K chunk) whose B images each stage holds after the
+          // iterations so far (-1: none).  The copy decision is a function of
+          // the iteration sequence alone, which both groups walk in full, so
+          // both keep the same record, including the stages the other group
+          // fills; a copy is skipped when the stage already holds the tile.
+          int  held_op[TC_STAGES], held_kc[TC_STAGES];
+#pragma unroll
+          for (int s = 0; s < TC_STAGES; ++s)
+            held_op[s] = held_kc[s] = -1;
           bool inflight[TC_STAGES];
           int  inflight_par[TC_STAGES];
 #pragma unroll
@@ -290,10 +303,10 @@ namespace pibem
               inflight[s]     = false;
               inflight_par[s] = 0;
             }
-          for (int ch = chunk0 + blockIdx.x; ok && ch < chunk0 + n_chunks; ch += gridDim.x)
+          for (int ch = ch_lo; ok && ch < ch_hi; ++ch)
             {
-              const int    start = ch_start[ch], rows_total = ch_cnt[ch] * R;
-              const float *Bhi   = images + size_t(ch_op[ch]) * 2 * op_img_floats;
+              const int    start = ch_start[ch], rows_total = ch_cnt[ch] * R, op = ch_op[ch];
+              const float *Bhi   = images + size_t(op) * 2 * op_img_floats;
               const float *Blo   = Bhi + op_img_floats;
               for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS)
                 {
@@ -309,9 +322,13 @@ namespace pibem
                   }
                   for (int kc = 0; kc < nkc; ++kc, ++it)
                     {
-                      if ((it & 1) != grp)
-                        continue;
                       const int s = it % TC_STAGES, use = it / TC_STAGES;
+                      if ((it & 1) != grp)
+                        {
+                          held_op[s] = op; // the other group's iteration
+                          held_kc[s] = kc;
+                          continue;
+                        }
                       if (use > 0 && !mbar_wait(empty(s), uint32_t(use - 1) & 1u, &abort_flag))
                         {
                           fail();
@@ -322,14 +339,21 @@ namespace pibem
                       uint8_t       *gs = gbase + size_t(s) * lay.stage_bytes;
                       if (gtid == 0)
                         {
-                          mbar_arrive_expect_tx(full(s), 2 * lay.b_bytes);
-                          bulk_copy(st + 2 * TC_A_BYTES, Bhi + size_t(kc) * Np * TC_KC,
-                                    lay.b_bytes, full(s));
-                          bulk_copy(st + 2 * TC_A_BYTES + lay.b_bytes,
-                                    Blo + size_t(kc) * Np * TC_KC, lay.b_bytes, full(s));
-                          inflight[s]     = true;
-                          inflight_par[s] = use & 1;
+                          if (held_op[s] == op && held_kc[s] == kc)
+                            mbar_arrive(full(s)); // the stage already holds this B tile
+                          else
+                            {
+                              mbar_arrive_expect_tx(full(s), 2 * lay.b_bytes);
+                              bulk_copy(st + 2 * TC_A_BYTES, Bhi + size_t(kc) * Np * TC_KC,
+                                        lay.b_bytes, full(s));
+                              bulk_copy(st + 2 * TC_A_BYTES + lay.b_bytes,
+                                        Blo + size_t(kc) * Np * TC_KC, lay.b_bytes, full(s));
+                              inflight[s]     = true;
+                              inflight_par[s] = use & 1;
+                            }
                         }
+                      held_op[s] = op;
+                      held_kc[s] = kc;
                       // all 32 row loads of the warp in flight at once (coalesced:
                       // lane = k), then split and store
                       const int k = kc * TC_KC + lane;
@@ -368,7 +392,7 @@ namespace pibem
                                      (uint32_t(Np >> 3) << 17) | (uint32_t(TC_ROWS >> 4) << 24);
               int  it = 0, tile = 0;
               bool issued = false;
-              for (int ch = chunk0 + blockIdx.x; ok && ch < chunk0 + n_chunks; ch += gridDim.x)
+              for (int ch = ch_lo; ok && ch < ch_hi; ++ch)
                 {
                   const int rows_total = ch_cnt[ch] * R;
                   for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS, ++tile)
@@ -428,7 +452,7 @@ namespace pibem
           const int q    = warp - TC_EPI_WARP0;
           float    *stg  = reinterpret_cast<float *>(gbase + lay.epi) + q * 32 * TC_EPI_LD;
           int       tile = 0;
-          for (int ch = chunk0 + blockIdx.x; ok && ch < chunk0 + n_chunks; ch += gridDim.x)
+          for (int ch = ch_lo; ok && ch < ch_hi; ++ch)
             {
               const int start = ch_start[ch], rows_total = ch_cnt[ch] * R;
               for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS, ++tile)

@@ -374,7 +374,7 @@ class BEMSolver:
         self._check(self.L.pibem_quad_points(self.h, _d(pts)))
         return pts
 
-    PHASES = ["near", "p2m", "m2m", "m2l_l2l", "unused", "m2p", "l2p"]
+    PHASES = ["near", "p2m", "m2m", "m2l", "l2l", "m2p", "l2p"]
 
     def phase_ms(self):
         out = np.zeros(7)

@@ -26,6 +26,9 @@ def test_graph_matches_direct_launches(pibem_mod, synthetic):
     try:
         g.set_profiling(True)   # direct launches
         y_direct = g.system_matvec(x.reshape(-1))
+        l0 = pibem_mod.launch_count()
+        g.system_matvec(x.reshape(-1))
+        per_direct = pibem_mod.launch_count() - l0
         g.set_profiling(False)  # first call captures, later calls replay
         y_first = g.system_matvec(x.reshape(-1))
         l0 = pibem_mod.launch_count()
@@ -35,7 +38,7 @@ def test_graph_matches_direct_launches(pibem_mod, synthetic):
         os.environ.pop("PIBEM_MATVEC_FP32", None)
     np.testing.assert_array_equal(y_direct, y_first)
     np.testing.assert_array_equal(y_direct, y_replay)
-    assert per_call >= 20  # the graph's kernels are counted at replay
+    assert per_call == per_direct > 5  # the graph's kernels are counted at replay
     g.set_profiling(True)
     p1, d1, s1 = g.solve(tmp)
     g.set_profiling(False)
