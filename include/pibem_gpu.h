@@ -180,6 +180,23 @@ int64_t pibem_launch_count(void);
  * resident meshes inside an HBM budget. */
 int pibem_device_bytes(const pibem_handle *h, uint64_t *bytes);
 
+/* ---- L2 projections onto the continuous Q1 space of the mesh -------------
+ * The post-solve steps of BEMProblem (source/bem_problem.cc): the L2 projection
+ * of a vector field g, u = M^-1 b with the consistent Q1 mass matrix M and
+ * b_i = integral of phi_i g, per component, on the mesh's Gauss rule:
+ *   compute_normals (:1998):           g = the cell normal;
+ *   compute_surface_gradients (:1879): g = tangential gradient of the
+ *                                      interpolated u;
+ *   compute_gradients (:1747):         g = tangential gradient of phi + n dphi/dn.
+ * Output: 3 values per node (x, y, z), node-major, R columns one after another.
+ * Needs pibem_set_mesh only.  The reference solves with GMRES + AMG to its
+ * solver tolerance; here CG with a Jacobi preconditioner runs to a relative
+ * residual of 1e-13 (the same projection). */
+int pibem_compute_normals(pibem_handle *h, double *normals);
+int pibem_compute_surface_gradients(pibem_handle *h, int32_t R, const double *u, double *grad);
+int pibem_compute_gradients(pibem_handle *h, int32_t R, const double *phi, const double *dphi_dn,
+                            double *grad);
+
 /* ---- mesh ingestion (host only; no GPU needed) ---------------------------
  * UCD (.inp) surface mesh, as ComputationalDomain::read_domain reads it with
  * GridIn::read_ucd (source/computational_domain.cc:280-287).  Call once with

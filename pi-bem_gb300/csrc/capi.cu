@@ -150,7 +150,8 @@ struct pibem_handle
   size_t       bytes_resident = 0;
   // mesh
   DBuf<double>  d_xyz, d_qpts, d_qnrm, d_qjxw, d_qshape, d_gpts, d_gw;
-  DBuf<int32_t> d_cells, d_dbl_off, d_dbl_ids;
+  DBuf<int32_t> d_cells, d_dbl_off, d_dbl_ids, d_elem_off, d_elem_ids;
+  DBuf<double>  d_proj; // L2-projection work (grow-only)
   // tree
   DBuf<int32_t> d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted;
   DBuf<double>  d_center, d_delta;
@@ -208,7 +209,8 @@ struct pibem_handle
   {
     size_t t = 0;
     auto   add = [&t](const auto &...b) { ((t += b.bytes()), ...); };
-    add(d_xyz, d_qpts, d_qnrm, d_qjxw, d_qshape, d_gpts, d_gw, d_cells, d_dbl_off, d_dbl_ids);
+    add(d_xyz, d_qpts, d_qnrm, d_qjxw, d_qshape, d_gpts, d_gw, d_cells, d_dbl_off, d_dbl_ids,
+        d_elem_off, d_elem_ids, d_proj);
     add(d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted, d_center,
         d_delta);
     add(d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr, d_m2l_src_ptr,
@@ -999,6 +1001,8 @@ namespace
     h->d_dbl_off.upload(m.dbl_off, s);
     h->d_dbl_ids.upload(m.dbl_ids, s);
     h->d_gpts.upload(h->gpts, s);
+    h->d_elem_off.upload(m.elem_off, s);
+    h->d_elem_ids.upload(m.elem_ids, s);
     h->d_gw.upload(h->gw, s);
     const int64_t Q = n_cells * h->nq;
     h->d_qpts.alloc(3 * Q);
@@ -1651,6 +1655,63 @@ extern "C"
         throw Error(PIBEM_EINVAL, "bad arguments");
       solve_dev(h, R, phi, dphi, tmp, st);
     });
+  }
+
+  // L2 projections (BEMProblem::compute_normals / compute_surface_gradients /
+  // compute_gradients, source/bem_problem.cc:1747-2070)
+  static int projection(pibem_handle *h, int mode, int32_t R, const double *u, const double *dudn,
+                        double *out)
+  {
+    return guarded(h, [&] {
+      if (!h->mesh_ok)
+        throw Error(PIBEM_EINVAL, "L2 projection before pibem_set_mesh");
+      if (R < 1 || !out || (mode > 0 && !u) || (mode == 2 && !dudn))
+        throw Error(PIBEM_EINVAL, "bad arguments");
+      const int64_t N = h->N(), n = size_t(R) * N;
+      HostIO        io{h};
+      const double *du = mode > 0 ? io.in(u, n) : nullptr;
+      const double *dd = mode == 2 ? io.in(dudn, n) : nullptr;
+      double       *dout = io.scratch(size_t(3) * n);
+      h->d_proj.alloc(l2_projection_work(N, h->mesh.n_cells, R));
+      ProjectionArgs a;
+      a.mode     = mode;
+      a.n_nodes  = N;
+      a.n_cells  = h->mesh.n_cells;
+      a.nq       = h->nq;
+      a.R        = R;
+      a.cells    = h->d_cells.p;
+      a.elem_off = h->d_elem_off.p;
+      a.elem_ids = h->d_elem_ids.p;
+      a.xyz      = h->d_xyz.p;
+      a.gpts     = h->d_gpts.p;
+      a.qshape   = h->d_qshape.p;
+      a.qjxw     = h->d_qjxw.p;
+      a.qnrm     = h->d_qnrm.p;
+      a.u        = du;
+      a.dudn     = dd;
+      a.work     = h->d_proj.p;
+      a.out      = dout;
+      l2_projection(a, h->stream);
+      PIBEM_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
+                                 h->stream));
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_compute_normals(pibem_handle *h, double *normals)
+  {
+    return projection(h, 0, 1, nullptr, nullptr, normals);
+  }
+
+  int pibem_compute_surface_gradients(pibem_handle *h, int32_t R, const double *u, double *grad)
+  {
+    return projection(h, 1, R, u, nullptr, grad);
+  }
+
+  int pibem_compute_gradients(pibem_handle *h, int32_t R, const double *phi, const double *dphi_dn,
+                              double *grad)
+  {
+    return projection(h, 2, R, phi, dphi_dn, grad);
   }
 
   int pibem_device_bytes(const pibem_handle *h, uint64_t *bytes)

@@ -187,7 +187,6 @@ namespace pibem
             for (int b = 0; b < 4; ++b)
               acc[a][b] = T(0);
           if (act)
-#pragma unroll 4
             for (int64_t row = rb + warp; row < re; row += 8)
               {
                 const int dof = prow_dof[row];

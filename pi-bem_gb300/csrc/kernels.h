@@ -145,6 +145,24 @@ namespace pibem
   void launch_tc_gemm(const OperatorDev<float> &op, int R, int c0, int c1, const float *E, float *Y,
                       int *err, cudaStream_t s);
 
+  // ---- L2 projections onto the Q1 space (projection.cu) ------------------------
+  struct ProjectionArgs
+  {
+    int            mode = 0; // 0 normals, 1 surface gradient of u, 2 gradient (u = phi, dudn)
+    int64_t        n_nodes = 0, n_cells = 0;
+    int            nq = 0, R = 1;
+    const int32_t *cells = nullptr, *elem_off = nullptr, *elem_ids = nullptr;
+    const double  *xyz = nullptr, *gpts = nullptr, *qshape = nullptr, *qjxw = nullptr,
+                  *qnrm = nullptr, *u = nullptr, *dudn = nullptr;
+    double        *work = nullptr; // l2_projection_work() doubles
+    double        *out  = nullptr; // R x N x 3, node-major
+    int            max_iterations = 1000;
+    double         tolerance      = 1e-13;
+    int           *iterations     = nullptr;
+  };
+  void   l2_projection(const ProjectionArgs &a, cudaStream_t s);
+  size_t l2_projection_work(int64_t n_nodes, int64_t n_cells, int R);
+
   // ---- vector kernels (krylov.cu) -------------------------------------------
   void launch_convert_d2f(int64_t n, const double *a, float *b, cudaStream_t s);
   void launch_convert_f2d(int64_t n, const float *a, double *b, cudaStream_t s);

@@ -93,7 +93,8 @@ EXPORTS = [
     "pibem_quad_points", "pibem_last_phase_ms", "pibem_set_profiling", "pibem_phase_totals",
     "pibem_launch_count", "pibem_fmm_matvec_noalloc", "pibem_device_bytes",
     "pibem_ucd_read", "pibem_mesh_io_error", "pibem_double_nodes",
-    "pibem_dirichlet_mask_from_materials",
+    "pibem_dirichlet_mask_from_materials", "pibem_compute_normals",
+    "pibem_compute_surface_gradients", "pibem_compute_gradients",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -150,6 +151,9 @@ def load():
                                      C.POINTER(C.c_int64)]
     L.pibem_dirichlet_mask_from_materials.argtypes = [C.c_int64, C.c_int64, _ip, _ip, C.c_int32,
                                                       _ip, _u8p]
+    L.pibem_compute_normals.argtypes = [C.c_void_p, _dp]
+    L.pibem_compute_surface_gradients.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
+    L.pibem_compute_gradients.argtypes = [C.c_void_p, C.c_int32, _dp, _dp, _dp]
     _lib = L
     return L
 
@@ -380,6 +384,28 @@ class BEMSolver:
         out = np.zeros(7)
         self._check(self.L.pibem_last_phase_ms(self.h, _d(out)))
         return dict(zip(self.PHASES, out.tolist()))
+
+    # L2 projections onto the Q1 space (BEMProblem::compute_normals /
+    # compute_surface_gradients / compute_gradients): (N, 3) arrays, or (R, N, 3)
+    def normals(self):
+        out = np.zeros((self.n, 3))
+        self._check(self.L.pibem_compute_normals(self.h, _d(out)))
+        return out
+
+    def surface_gradients(self, u):
+        u = np.ascontiguousarray(u, np.float64)
+        R = u.size // self.n
+        out = np.zeros((R, self.n, 3))
+        self._check(self.L.pibem_compute_surface_gradients(self.h, R, _d(u), _d(out)))
+        return out[0] if u.ndim == 1 else out
+
+    def gradients(self, phi, dphi_dn):
+        phi = np.ascontiguousarray(phi, np.float64)
+        dphi = np.ascontiguousarray(dphi_dn, np.float64)
+        R = phi.size // self.n
+        out = np.zeros((R, self.n, 3))
+        self._check(self.L.pibem_compute_gradients(self.h, R, _d(phi), _d(dphi), _d(out)))
+        return out[0] if phi.ndim == 1 else out
 
     def device_bytes(self) -> int:
         """Device memory the handle holds now (bytes)."""
