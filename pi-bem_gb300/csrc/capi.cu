@@ -140,6 +140,8 @@ struct pibem_handle
   pibem_params prm;
   std::string  err;
   cudaStream_t stream = nullptr, own = nullptr;
+  cudaStream_t side = nullptr; // second stream of the two-branch operator
+  cudaEvent_t  ev_fork = nullptr, ev_up = nullptr, ev_side = nullptr;
   bool         mesh_ok = false, bc_ok = false;
   MeshHost     mesh;
   int          nq = 0, n_tel = 0;
@@ -275,14 +277,13 @@ namespace
   }
 
   // ---------------------------------------------------------------------
-  // Far field (P2M ... L2P) added to y for R columns.
+  // Far field (P2M ... L2P) added to y for R columns, in stages.
   // ---------------------------------------------------------------------
   template <typename T>
-  void far_field(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
-                 DBuf<T> &Y, int R, const uint8_t *modes, const T *x, T *y, bool combined = false)
+  void far_alloc(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
+                 DBuf<T> &Y, int R)
   {
     Y.alloc(std::max<size_t>(1, size_t(op.n_pairs) * R * op.K));
-    const int    N = int(h->N());
     const size_t need = size_t(h->tree.nb) * R * op.K;
     if (M.n < need)
       {
@@ -291,22 +292,84 @@ namespace
       }
     scr.alloc(std::max<size_t>(1, size_t(op.n_m2p_items) * R));
     op.m2p_scratch = scr.p;
-    cudaStream_t s = h->stream;
+  }
+
+  // P2M and the upward pass: M of every box
+  template <typename T>
+  void far_up(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Y, int R,
+              const uint8_t *modes, const T *x, bool combined, cudaStream_t s)
+  {
+    const size_t need = size_t(h->tree.nb) * R * op.K;
     PIBEM_CUDA(cudaMemsetAsync(M.p, 0, need * sizeof(T), s));
-    launch_p2m_apply<T>(op, R, N, h->d_dir.p, modes, x, M.p, combined, s);
+    launch_p2m_apply<T>(op, R, int(h->N()), h->d_dir.p, modes, x, M.p, combined, s);
     record(h, 2);
     for (int l = h->tree.L; l >= 1; --l)
       launch_upward_level<T>(op, R, l, M.p, Y.p, s);
     record(h, 3);
+  }
+
+  // M2L and the downward pass: L of every box with nodes
+  template <typename T>
+  void far_down(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &Y, int R,
+                cudaStream_t s)
+  {
     launch_m2l_gemm<T>(op, R, M.p, Y.p, s);
     record(h, 4);
     for (int l = 1; l <= h->tree.L; ++l)
       launch_downward_level<T>(op, R, l, Lx.p, Y.p, s);
     record(h, 5);
+  }
+
+  template <typename T>
+  void far_field(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
+                 DBuf<T> &Y, int R, const uint8_t *modes, const T *x, T *y, bool combined = false)
+  {
+    const int    N = int(h->N());
+    cudaStream_t s = h->stream;
+    far_alloc<T>(h, op, M, Lx, scr, Y, R);
+    far_up<T>(h, op, M, Y, R, modes, x, combined, s);
+    far_down<T>(h, op, M, Lx, Y, R, s);
     launch_m2p<T>(op, h->td, R, N, M.p, y, s);
     record(h, 6);
     launch_l2p<T>(op, R, N, Lx.p, y, s);
     record(h, 7);
+  }
+
+  // The system operator y = S x (near field + combined far field).  Without
+  // phase timing the independent branches run on two streams: the near SpMV
+  // (HBM-bound) and then M2P on the handle's side stream, beside P2M, the
+  // upward pass, M2L and the downward pass (latency-bound small GEMMs) on the
+  // main stream; L2P joins them.  y is written by the near SpMV and then added
+  // to by M2P and L2P in that order, as in the one-stream sequence, so the
+  // result is the same bit for bit.
+  template <typename T>
+  void system_operator(pibem_handle *h, OperatorDev<T> &op, const T *vals, DBuf<T> &M,
+                       DBuf<T> &Lx, DBuf<T> &scr, DBuf<T> &Y, int R, const uint8_t *modes,
+                       const T *x, T *y)
+  {
+    const int    N = int(h->N());
+    cudaStream_t s = h->stream;
+    if (h->timing || !h->side)
+      {
+        record(h, 0);
+        launch_near_spmv<T>(op, R, N, vals, x, y, false, s);
+        record(h, 1);
+        far_field<T>(h, op, M, Lx, scr, Y, R, modes, x, y, true);
+        return;
+      }
+    cudaStream_t side = h->side;
+    far_alloc<T>(h, op, M, Lx, scr, Y, R);
+    PIBEM_CUDA(cudaEventRecord(h->ev_fork, s));
+    PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_fork, 0));
+    launch_near_spmv<T>(op, R, N, vals, x, y, false, side);
+    far_up<T>(h, op, M, Y, R, modes, x, true, s);
+    PIBEM_CUDA(cudaEventRecord(h->ev_up, s));
+    PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_up, 0));
+    launch_m2p<T>(op, h->td, R, N, M.p, y, side);
+    PIBEM_CUDA(cudaEventRecord(h->ev_side, side));
+    far_down<T>(h, op, M, Lx, Y, R, s);
+    PIBEM_CUDA(cudaStreamWaitEvent(s, h->ev_side, 0));
+    launch_l2p<T>(op, R, N, Lx.p, y, s);
   }
 
   // prec: 0 FP64 operator, 1 FP32 operator
@@ -407,11 +470,8 @@ namespace
         xin = h->d_t4.p;
       }
     set_modes(h, R, MODE_COMBINED);
-    record(h, 0);
-    launch_near_spmv<double>(h->op64, R, int(N), h->d_S.p, xin, y, false, s);
-    record(h, 1);
-    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, xin, y,
-                      true);
+    system_operator<double>(h, h->op64, h->d_S.p, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R,
+                            h->d_modes.p, xin, y);
     finish_timing(h, 0);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
@@ -421,13 +481,8 @@ namespace
   // Near SpMV + far field of the FP32 system operator, d_x32 -> d_y32.
   void operator32_body(pibem_handle *h, int R)
   {
-    const int64_t N = h->N();
-    record(h, 0);
-    launch_near_spmv<float>(h->op32, R, int(N), h->d_S32.p, h->d_x32.p, h->d_y32.p, false,
-                            h->stream);
-    record(h, 1);
-    far_field<float>(h, h->op32, h->d_M32, h->d_L32, h->d_m2p32, h->d_Y32, R, h->d_modes32.p,
-                     h->d_x32.p, h->d_y32.p, true);
+    system_operator<float>(h, h->op32, h->d_S32.p, h->d_M32, h->d_L32, h->d_m2p32, h->d_Y32, R,
+                           h->d_modes32.p, h->d_x32.p, h->d_y32.p);
   }
 
   void drop_graph(pibem_handle *h)
@@ -1495,6 +1550,9 @@ extern "C"
       {
         PIBEM_CUDA(cudaSetDevice(P.device));
         PIBEM_CUDA(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
+        PIBEM_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        for (cudaEvent_t *e : {&h->ev_fork, &h->ev_up, &h->ev_side})
+          PIBEM_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
         h->stream = h->own;
         const char *env = std::getenv("PIBEM_PHASE_TIMING");
         h->timing       = env && env[0] == '1';
@@ -1522,6 +1580,14 @@ extern "C"
     for (auto &e : h->ev)
       if (e)
         cudaEventDestroy(e);
+    for (cudaEvent_t e : {h->ev_fork, h->ev_up, h->ev_side})
+      if (e)
+        cudaEventDestroy(e);
+    if (h->side)
+      {
+        cudaStreamSynchronize(h->side);
+        cudaStreamDestroy(h->side);
+      }
     cudaStream_t own = h->own;
     drop_graph(h);
     delete h;
