@@ -825,6 +825,7 @@ namespace
       op.ch_op         = h->d_ch_op.p;
       op.m2l_chunk_end = pl.m2l_chunk_end;
       op.max_chunk_pairs = pl.ch_cnt.empty() ? 0 : *std::max_element(pl.ch_cnt.begin(), pl.ch_cnt.end());
+      op.n_boxes         = h->tree.nb;
       op.up_chunk_ptr  = pl.up_chunk_ptr;
       op.down_chunk_ptr = pl.down_chunk_ptr;
       op.up_box_ptr    = pl.up_box_ptr;

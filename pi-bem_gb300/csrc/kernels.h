@@ -91,6 +91,7 @@ namespace pibem
     const float2  *ops_ff = nullptr;
     const int32_t *q_src = nullptr, *ch_start = nullptr, *ch_cnt = nullptr, *ch_op = nullptr;
     int            max_chunk_pairs = 0;
+    int            n_boxes         = 0;
     int            m2l_chunk_end = 0;
     std::vector<int> up_chunk_ptr, down_chunk_ptr, up_box_ptr, down_box_ptr;
     const int32_t *up_box = nullptr, *down_box = nullptr, *up_q = nullptr, *down_q = nullptr;

@@ -310,14 +310,15 @@ namespace pibem
               const float *Blo   = Bhi + op_img_floats;
               for (int t0 = 0; ok && t0 < rows_total; t0 += TC_ROWS)
                 {
-                  // source offset of row t0 + 32 gw + lane (-1: padding row)
-                  int64_t my_src = -1;
+                  // source offset of row t0 + 32 gw + lane (-1: padding row); the
+                  // host checks that every offset fits in 32 bits
+                  int32_t my_src = -1;
                   {
                     const int i = t0 + 32 * gw + lane;
                     if (i < rows_total)
                       {
                         const int q = start + i / R, r = i - (i / R) * R;
-                        my_src      = (int64_t(q_src[q]) * R + r) * K;
+                        my_src      = (q_src[q] * R + r) * K;
                       }
                   }
                   for (int kc = 0; kc < nkc; ++kc, ++it)
@@ -336,7 +337,6 @@ namespace pibem
                         }
                       inflight[s]       = false;
                       const uint32_t st = base + uint32_t(s) * lay.stage_bytes;
-                      uint8_t       *gs = gbase + size_t(s) * lay.stage_bytes;
                       if (gtid == 0)
                         {
                           if (held_op[s] == op && held_kc[s] == kc)
@@ -356,21 +356,27 @@ namespace pibem
                       held_kc[s] = kc;
                       // all 32 row loads of the warp in flight at once (coalesced:
                       // lane = k), then split and store
-                      const int k = kc * TC_KC + lane;
-                      float     x[32];
+                      const int   k    = kc * TC_KC + lane;
+                      const bool k_ok = k < K;
+                      float      x[32];
 #pragma unroll
                       for (int u = 0; u < 32; ++u)
                         {
-                          const int64_t src = __shfl_sync(0xffffffffu, my_src, u);
-                          x[u]              = (src >= 0 && k < K) ? E[src + k] : 0.0f;
+                          const int32_t src = __shfl_sync(0xffffffffu, my_src, u);
+                          x[u]              = (src >= 0 && k_ok) ? E[src + k] : 0.0f;
                         }
+                      // stores by shared-window address (st.shared), hi then lo
+                      const uint32_t a_hi = st + uint32_t(32 * gw) * 128u;
 #pragma unroll
                       for (int u = 0; u < 32; ++u)
                         {
-                          const uint32_t o = sw128_off(32 * gw + u, lane);
+                          const uint32_t o = a_hi + sw128_off(u, lane);
                           const float    h = tf32_hi(x[u]);
-                          *reinterpret_cast<float *>(gs + o)              = h;
-                          *reinterpret_cast<float *>(gs + TC_A_BYTES + o) = x[u] - h;
+                          asm volatile("st.shared.f32 [%0], %1;" : : "r"(o), "f"(h) : "memory");
+                          asm volatile("st.shared.f32 [%0], %1;"
+                                       :
+                                       : "r"(o + TC_A_BYTES), "f"(x[u] - h)
+                                       : "memory");
                         }
                       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                       mbar_arrive(full(s));
@@ -556,6 +562,9 @@ namespace pibem
     PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
     const TcGeometry g   = tc_geometry(op.K);
     const int        nch = c1 - c0;
+    if (int64_t(op.n_boxes) * R * op.K >= (int64_t(1) << 31))
+      throw Error(PIBEM_EINVAL, "too many right-hand sides for the tensor-core translations "
+                                "(expansion offsets exceed 32 bits); use the CUDA-core engine");
     auto fn = (c0 == 0 && c1 == op.m2l_chunk_end) ? tc_gemm_kernel<true> : tc_gemm_kernel<false>;
     raise_smem_limit(reinterpret_cast<const void *>(fn), g.smem);
     fn<<<std::min(nch, std::max(n_sm, 1)), TC_THREADS, g.smem, s>>>(
