@@ -192,6 +192,27 @@ namespace pibem
 
     __host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
+    // a[s] = v / a[s] with s a run-time stage index: the loop over the
+    // compile-time indices keeps the array in registers (no local memory)
+    template <typename V>
+    __device__ __forceinline__ void put(V (&a)[TC_STAGES], int s, V v)
+    {
+#pragma unroll
+      for (int j = 0; j < TC_STAGES; ++j)
+        if (j == s)
+          a[j] = v;
+    }
+    template <typename V>
+    __device__ __forceinline__ V get(const V (&a)[TC_STAGES], int s)
+    {
+      V v = a[0];
+#pragma unroll
+      for (int j = 1; j < TC_STAGES; ++j)
+        if (j == s)
+          v = a[j];
+      return v;
+    }
+
     // Shared-memory layout, byte offsets from the 1024-byte aligned base:
     // TC_STAGES x [A hi | A lo | B hi | B lo], epilogue staging, mbarriers.
     struct TcLayout
@@ -321,13 +342,19 @@ namespace pibem
                         my_src      = (q_src[q] * R + r) * K;
                       }
                   }
+                  // every lane holds the offsets of the warp's 32 rows for all
+                  // the tile's K chunks (one shuffle per row per tile)
+                  int32_t srcs[32];
+#pragma unroll
+                  for (int u = 0; u < 32; ++u)
+                    srcs[u] = __shfl_sync(0xffffffffu, my_src, u);
                   for (int kc = 0; kc < nkc; ++kc, ++it)
                     {
                       const int s = it % TC_STAGES, use = it / TC_STAGES;
                       if ((it & 1) != grp)
                         {
-                          held_op[s] = op; // the other group's iteration
-                          held_kc[s] = kc;
+                          put(held_op, s, op); // the other group's iteration
+                          put(held_kc, s, kc);
                           continue;
                         }
                       if (use > 0 && !mbar_wait(empty(s), uint32_t(use - 1) & 1u, &abort_flag))
@@ -335,11 +362,11 @@ namespace pibem
                           fail();
                           break;
                         }
-                      inflight[s]       = false;
+                      put(inflight, s, false);
                       const uint32_t st = base + uint32_t(s) * lay.stage_bytes;
                       if (gtid == 0)
                         {
-                          if (held_op[s] == op && held_kc[s] == kc)
+                          if (get(held_op, s) == op && get(held_kc, s) == kc)
                             mbar_arrive(full(s)); // the stage already holds this B tile
                           else
                             {
@@ -348,12 +375,12 @@ namespace pibem
                                         lay.b_bytes, full(s));
                               bulk_copy(st + 2 * TC_A_BYTES + lay.b_bytes,
                                         Blo + size_t(kc) * Np * TC_KC, lay.b_bytes, full(s));
-                              inflight[s]     = true;
-                              inflight_par[s] = use & 1;
+                              put(inflight, s, true);
+                              put(inflight_par, s, use & 1);
                             }
                         }
-                      held_op[s] = op;
-                      held_kc[s] = kc;
+                      put(held_op, s, op);
+                      put(held_kc, s, kc);
                       // all 32 row loads of the warp in flight at once (coalesced:
                       // lane = k), then split and store
                       const int   k    = kc * TC_KC + lane;
@@ -362,8 +389,7 @@ namespace pibem
 #pragma unroll
                       for (int u = 0; u < 32; ++u)
                         {
-                          const int32_t src = __shfl_sync(0xffffffffu, my_src, u);
-                          x[u]              = (src >= 0 && k_ok) ? E[src + k] : 0.0f;
+                          x[u] = (srcs[u] >= 0 && k_ok) ? E[srcs[u] + k] : 0.0f;
                         }
                       // stores by shared-window address (st.shared), hi then lo
                       const uint32_t a_hi = st + uint32_t(32 * gw) * 128u;
