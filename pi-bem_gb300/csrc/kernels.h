@@ -135,7 +135,7 @@ namespace pibem
   // ---- tensor-core translations (m2l_tc.cu) ----------------------------------
   struct TcGeometry
   {
-    int    K = 0, Kp = 0, Np = 0;
+    int    K = 0, Kp = 0, Np = 0, stages = 3;
     size_t smem = 0;
     bool   ok   = false;
   };

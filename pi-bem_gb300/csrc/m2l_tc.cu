@@ -46,7 +46,6 @@ namespace pibem
   {
     constexpr int      TC_ROWS       = 128;
     constexpr int      TC_KC         = 32;  // K values per stage: one 128-byte line of TF32
-    constexpr int      TC_STAGES     = 3;
     constexpr int      TC_GROUP      = 128; // producer group: 4 warps, one row per lane
     constexpr int      TC_EPI_WARP0  = 8;   // warps 8-11
     constexpr int      TC_MMA_WARP   = 12;
@@ -194,43 +193,49 @@ namespace pibem
 
     // a[s] = v / a[s] with s a run-time stage index: the loop over the
     // compile-time indices keeps the array in registers (no local memory)
-    template <typename V>
-    __device__ __forceinline__ void put(V (&a)[TC_STAGES], int s, V v)
+    template <typename V, int N>
+    __device__ __forceinline__ void put(V (&a)[N], int s, V v)
     {
 #pragma unroll
-      for (int j = 0; j < TC_STAGES; ++j)
+      for (int j = 0; j < N; ++j)
         if (j == s)
           a[j] = v;
     }
-    template <typename V>
-    __device__ __forceinline__ V get(const V (&a)[TC_STAGES], int s)
+    template <typename V, int N>
+    __device__ __forceinline__ V get(const V (&a)[N], int s)
     {
       V v = a[0];
 #pragma unroll
-      for (int j = 1; j < TC_STAGES; ++j)
+      for (int j = 1; j < N; ++j)
         if (j == s)
           v = a[j];
       return v;
     }
 
     // Shared-memory layout, byte offsets from the 1024-byte aligned base:
-    // TC_STAGES x [A hi | A lo | B hi | B lo], epilogue staging, mbarriers.
+    // stages x [A hi | A lo | B hi | B lo], epilogue staging (per epilogue warp
+    // the larger of a 32 x 33 column-chunk tile and its 32 rows x K, row-major,
+    // + 4 floats of alignment shift), mbarriers.
     struct TcLayout
     {
-      uint32_t b_bytes, stage_bytes, epi, bars, total;
-      __host__ __device__ explicit TcLayout(int Np)
+      uint32_t b_bytes, stage_bytes, epi, epi_warp_floats, bars, total;
+      __host__ __device__ TcLayout(int Np, int K, int stages)
       {
-        b_bytes     = uint32_t(Np) * 128;
-        stage_bytes = 2 * TC_A_BYTES + 2 * b_bytes;
-        epi         = TC_STAGES * stage_bytes;
-        bars        = epi + 4 * 32 * TC_EPI_LD * 4;
-        total       = bars + (2 * TC_STAGES + 5) * 8;
+        b_bytes         = uint32_t(Np) * 128;
+        stage_bytes     = 2 * TC_A_BYTES + 2 * b_bytes;
+        epi             = uint32_t(stages) * stage_bytes;
+        epi_warp_floats = uint32_t(round_up(32 * K + 4, 4));
+        if (epi_warp_floats < 32 * TC_EPI_LD)
+          epi_warp_floats = uint32_t(round_up(32 * TC_EPI_LD, 4));
+        bars  = epi + 4 * epi_warp_floats * 4;
+        total = bars + (2 * uint32_t(stages) + 5) * 8;
       }
     };
 
     // ALL_LEVELS_M2L only names the instantiation used for the batched M2L of all
-    // levels (so that profilers can select it); the code is the same.
-    template <bool ALL_LEVELS_M2L>
+    // levels (so that profilers can select it); the code is the same.  TC_STAGES:
+    // depth of the stage ring (3, or 2 where shared memory is short, p = 10).
+    template <bool ALL_LEVELS_M2L, int TC_STAGES>
     __global__ void __launch_bounds__(TC_THREADS, 1)
       tc_gemm_kernel(int R, int K, int Np, int nkc, int chunk0, int n_chunks,
                      const int32_t *__restrict__ ch_start, const int32_t *__restrict__ ch_cnt,
@@ -241,7 +246,7 @@ namespace pibem
       extern __shared__ uint8_t smem_raw[];
       __shared__ uint32_t       tmem_slot;
       __shared__ volatile int   abort_flag;
-      const TcLayout  lay(Np);
+      const TcLayout  lay(Np, K, TC_STAGES);
       const uint32_t  raw   = smem_u32(smem_raw);
       const uint32_t  base  = (raw + 1023u) & ~1023u;
       uint8_t        *gbase = smem_raw + (base - raw);
@@ -480,10 +485,19 @@ namespace pibem
         }
       else
         {
-          // ---------------- epilogue (warps 4-7) ----------------
-          const int q    = warp - TC_EPI_WARP0;
-          float    *stg  = reinterpret_cast<float *>(gbase + lay.epi) + q * 32 * TC_EPI_LD;
-          int       tile = 0;
+          // ---------------- epilogue (warps 8-11) ----------------
+          // Odd K (even p): the warp stages its 32 rows x K row-major in shared
+          // memory (conflict-free: lane = row, K odd) at the alignment of their
+          // place in Y, and one thread stores the 16-byte aligned middle of the
+          // contiguous block with a bulk copy (cp.async.bulk, shared -> global);
+          // the < 4 floats at either end by plain stores.  Even K: 32-column
+          // chunks through a 32 x 33 tile, one coalesced row segment per store.
+          const int      q     = warp - TC_EPI_WARP0;
+          float         *stg   = reinterpret_cast<float *>(gbase + lay.epi) + size_t(q) * lay.epi_warp_floats;
+          const uint32_t stg_s = base + lay.epi + uint32_t(q) * lay.epi_warp_floats * 4u;
+          const bool     bulk  = (K & 1) != 0;
+          bool           pending = false; // a bulk store of this warp may still read stg
+          int            tile    = 0;
           for (int ch = ch_lo; ok && ch < ch_hi; ++ch)
             {
               const int start = ch_start[ch], rows_total = ch_cnt[ch] * R;
@@ -499,24 +513,71 @@ namespace pibem
                   const int row0   = t0 + 32 * q;
                   const int nvalid = min(32, rows_total - row0);
                   float    *ybase  = Y + (int64_t(start) * R + row0) * K;
-                  for (int c0 = 0; c0 < Np; c0 += 32)
+                  if (bulk)
                     {
-                      float v[32];
-                      tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(a * TC_ACC_COLS + c0), v);
+                      if (pending)
+                        {
+                          if (lane == 0)
+                            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                          __syncwarp();
+                          pending = false;
+                        }
+                      const int shift = int((reinterpret_cast<uintptr_t>(ybase) >> 2) & 3u);
+                      for (int c0 = 0; c0 < Np; c0 += 32)
+                        {
+                          float v[32];
+                          tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(a * TC_ACC_COLS + c0), v);
 #pragma unroll
-                      for (int j = 0; j < 32; ++j)
-                        stg[lane * TC_EPI_LD + j] = v[j];
-                      __syncwarp();
-                      const int col = c0 + lane;
-                      if (col < K)
-                        for (int r = 0; r < nvalid; ++r)
-                          ybase[int64_t(r) * K + col] = stg[r * TC_EPI_LD + lane];
-                      __syncwarp();
+                          for (int j = 0; j < 32; ++j)
+                            if (c0 + j < K)
+                              stg[shift + lane * K + c0 + j] = v[j];
+                        }
+                      if (nvalid > 0)
+                        {
+                          const int nfl  = nvalid * K;
+                          const int head = min((4 - shift) & 3, nfl);
+                          const int nvec = (nfl - head) >> 2; // 16-byte units
+                          const int tl0  = head + 4 * nvec;
+                          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                          __syncwarp();
+                          if (lane < head)
+                            ybase[lane] = stg[shift + lane];
+                          if (lane < nfl - tl0)
+                            ybase[tl0 + lane] = stg[shift + tl0 + lane];
+                          if (nvec > 0 && lane == 0)
+                            {
+                              asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                                           :
+                                           : "l"(ybase + head),
+                                             "r"(stg_s + uint32_t(shift + head) * 4u),
+                                             "r"(uint32_t(nvec) * 16u)
+                                           : "memory");
+                              asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                            }
+                          pending = nvec > 0;
+                        }
                     }
+                  else
+                    for (int c0 = 0; c0 < Np; c0 += 32)
+                      {
+                        float v[32];
+                        tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(a * TC_ACC_COLS + c0), v);
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                          stg[lane * TC_EPI_LD + j] = v[j];
+                        __syncwarp();
+                        const int col = c0 + lane;
+                        if (col < K)
+                          for (int r = 0; r < nvalid; ++r)
+                            ybase[int64_t(r) * K + col] = stg[r * TC_EPI_LD + lane];
+                        __syncwarp();
+                      }
                   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                   mbar_arrive(tempty(a));
                 }
             }
+          if (lane == 0)
+            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); // bulk stores complete
         }
 
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -546,9 +607,14 @@ namespace pibem
     g.K  = K;
     g.Kp = round_up(K, TC_KC);
     g.Np = round_up(K, 16);
-    const TcLayout lay(g.Np);
-    g.smem = size_t(lay.total) + 1024; // + alignment slack of the dynamic base
-    g.ok   = K >= 1 && g.Np <= TC_ACC_COLS && g.smem <= 220 * 1024;
+    for (g.stages = 3; g.stages >= 2; --g.stages)
+      {
+        const TcLayout lay(g.Np, K, g.stages);
+        g.smem = size_t(lay.total) + 1024; // + alignment slack of the dynamic base
+        if (g.smem <= 220 * 1024)
+          break;
+      }
+    g.ok = K >= 1 && g.Np <= TC_ACC_COLS && g.stages >= 2 && g.smem <= 220 * 1024;
     return g;
   }
 
@@ -591,7 +657,9 @@ namespace pibem
     if (int64_t(op.n_boxes) * R * op.K >= (int64_t(1) << 31))
       throw Error(PIBEM_EINVAL, "too many right-hand sides for the tensor-core translations "
                                 "(expansion offsets exceed 32 bits); use the CUDA-core engine");
-    auto fn = (c0 == 0 && c1 == op.m2l_chunk_end) ? tc_gemm_kernel<true> : tc_gemm_kernel<false>;
+    const bool all = c0 == 0 && c1 == op.m2l_chunk_end;
+    auto       fn  = g.stages == 3 ? (all ? tc_gemm_kernel<true, 3> : tc_gemm_kernel<false, 3>)
+                                   : (all ? tc_gemm_kernel<true, 2> : tc_gemm_kernel<false, 2>);
     raise_smem_limit(reinterpret_cast<const void *>(fn), g.smem);
     fn<<<std::min(nch, std::max(n_sm, 1)), TC_THREADS, g.smem, s>>>(
       R, op.K, g.Np, g.Kp / TC_KC, c0, nch, op.ch_start, op.ch_cnt, op.ch_op, op.q_src,
