@@ -164,10 +164,11 @@ struct pibem_handle
   DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
     d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
-    d_down_box, d_up_q, d_down_q;
+    d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par;
+  DBuf<uint8_t> d_down_oct;
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc;
-  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg, d_Tcf;
+  DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg, d_Tcf, d_lvopsf;
   DBuf<float2>  d_opsff; // the FP64 operator table as (hi, lo) FP32 pairs
   DBuf<int>     d_err;
   bool          use_tc = true;
@@ -221,9 +222,9 @@ struct pibem_handle
     add(d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
         d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
-        d_up_box, d_down_box, d_up_q, d_down_q);
+        d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
-        d_opsf, d_opsff, d_tcimg, d_err, d_dir, d_modes, d_modes32, d_alpha);
+        d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
         d_y32, d_m2p32, d_Y32);
     add(g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
@@ -315,6 +316,7 @@ namespace
   {
     launch_m2l_gemm<T>(op, R, M.p, Y.p, s);
     record(h, 4);
+    launch_m2l_sums<T>(op, R, Lx.p, Y.p, s);
     for (int l = 1; l <= h->tree.L; ++l)
       launch_downward_level<T>(op, R, l, Lx.p, Y.p, s);
     record(h, 5);
@@ -836,6 +838,15 @@ namespace
       op.down_q        = h->d_down_q.p;
       op.up_q_ptr      = h->d_up_q_ptr.p;
       op.down_q_ptr    = h->d_down_q_ptr.p;
+      op.up_child8     = h->d_up_child8.p;
+      op.down_par      = h->d_down_par.p;
+      op.down_oct      = h->d_down_oct.p;
+      op.lv_op0        = int(pl.offsets.size() / 3);
+      op.down_l2l_level.assign(pl.down_box_ptr.size(), 0);
+      for (size_t l = 0; l + 1 < pl.down_box_ptr.size(); ++l)
+        for (int i = pl.down_box_ptr[l]; i < pl.down_box_ptr[l + 1]; ++i)
+          if (pl.down_par[i] >= 0)
+            op.down_l2l_level[l] = 1;
       op.n_pairs       = int64_t(pl.q_src.size());
       op.Tc            = nullptr; // made by set_bc
       op.max_near_cols = 0;
@@ -863,6 +874,8 @@ namespace
     h->op32.T2      = h->d_T2f.p;
     h->op32.W       = h->d_Wf.p;
     h->op32.ops     = h->d_opsf.p;
+    h->op32.lv_ops  = h->d_lvopsf.p;
+    h->op32.dev_err = h->d_err.p;
     h->op32.tc_images = h->d_tcimg.n ? h->d_tcimg.p : nullptr;
     h->op32.tc_err    = h->d_err.p;
     TreeDev &td               = h->td;
@@ -973,6 +986,15 @@ namespace
            "level ranges");
     for (int32_t v : pl.down_q)
       need(v >= 0 && v < nq_pairs, "down pair");
+    need(pl.up_child8.size() == 8 * pl.up_box.size() && pl.down_par.size() == pl.down_box.size() &&
+           pl.down_oct.size() == pl.down_box.size(),
+         "level tables");
+    for (int32_t v : pl.up_child8)
+      need(v >= -1 && v < t.nb, "up child");
+    for (size_t i = 0; i < pl.down_box.size(); ++i)
+      need(pl.down_par[i] >= -1 && pl.down_par[i] < t.nb && pl.down_oct[i] < 8 &&
+             (pl.down_par[i] < 0 || pl.down_q_ptr[i + 1] > pl.down_q_ptr[i]),
+           "down box table");
     need(pl.m2l_src_ptr.size() == pl.m2l_tgt.size() + 1, "m2l ptr");
     for (size_t i = 0; i < pl.m2l_src.size(); ++i)
       need(pl.m2l_src[i] >= 0 && pl.m2l_src[i] < t.nb && pl.m2l_off[i] >= 0 && pl.m2l_off[i] < noff,
@@ -1125,6 +1147,9 @@ namespace
     h->d_down_q.upload(pl.down_q, s);
     h->d_up_q_ptr.upload(pl.up_q_ptr, s);
     h->d_down_q_ptr.upload(pl.down_q_ptr, s);
+    h->d_up_child8.upload(pl.up_child8, s);
+    h->d_down_par.upload(pl.down_par, s);
+    h->d_down_oct.upload(pl.down_oct, s);
     // M2P work items: one per (pair, node of the pair's target box)
     {
       const size_t         nt = pl.m2p_tgt.size();
@@ -1240,11 +1265,14 @@ namespace
       launch_convert_d2f(nrows_p * K4, h->d_T1.p, h->d_T1f.p, s);
       launch_convert_d2f(nrows_p * K4, h->d_T2.p, h->d_T2f.p, s);
       const int64_t npos = int64_t(pl.lnode_ids.size());
-      h->d_W.alloc(npos * K);
-      launch_l2p_tables(npos, K, int(pl.lleaf_box.size()), h->d_nrow_ptr.p, h->d_lleaf_box.p,
-                        h->d_nrows.p, h->d_xyz.p, h->d_center.p, h->d_delta.p, h->d_W.p, s);
-      h->d_Wf.alloc(npos * K);
-      launch_convert_d2f(npos * K, h->d_W.p, h->d_Wf.p, s);
+      // rows padded to K4 values (zero beyond K): 16-byte aligned rows for L2P
+      h->d_W.alloc(npos * K4);
+      h->d_W.zero(s);
+      launch_l2p_tables(npos, K, int(K4), int(pl.lleaf_box.size()), h->d_nrow_ptr.p,
+                        h->d_lleaf_box.p, h->d_nrows.p, h->d_xyz.p, h->d_center.p, h->d_delta.p,
+                        h->d_W.p, s);
+      h->d_Wf.alloc(npos * K4);
+      launch_convert_d2f(npos * K4, h->d_W.p, h->d_Wf.p, s);
     }
     // translation operators
     {
@@ -1269,6 +1297,15 @@ namespace
       h->d_ops.upload(td, s);
       transpose_ops(all, nops, K, tf);
       h->d_opsf.upload(tf, s);
+      {
+        // the 16 level operators (8 M2M, 8 L2L), each padded to 16 bytes
+        const size_t        kk = fused_level_ops_floats(K) / 16;
+        std::vector<float> lv(16 * kk, 0.0f);
+        for (int o = 0; o < 16; ++o)
+          std::copy(tf.begin() + size_t(nof + o) * K * K, tf.begin() + size_t(nof + o + 1) * K * K,
+                    lv.begin() + o * kk);
+        h->d_lvopsf.upload(lv, s);
+      }
       {
         std::vector<float2> ff(td.size());
         for (size_t i = 0; i < td.size(); ++i)
@@ -1373,7 +1410,7 @@ namespace
     if (e)
       {
         h->d_err.zero(h->stream);
-        throw Error(PIBEM_ETIMEDOUT, "a bounded device wait timed out in the tensor-core translations");
+        throw Error(PIBEM_ETIMEDOUT, "a bounded device wait timed out in the translations");
       }
   }
 

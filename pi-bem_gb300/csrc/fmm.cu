@@ -155,87 +155,107 @@ namespace pibem
 
     // P2M apply: M^[leaf][r][k] = sum_rows w(row, r) T[row][k] x_r[dof(row)],
     // w selecting the double layer (Ker1), the single layer (Ker2) or the
-    // combined system strengths.  Warp w of the block takes rows w, w+8, ...;
-    // lane l owns coefficients 4l..4l+3 (table rows padded to 4 values); the
-    // eight partial sums are added in a fixed order.
+    // combined system strengths.  One warp per leaf, 8 leaves per block: lane l
+    // owns coefficients 4l..4l+3 (table rows padded to K4 values); the rows'
+    // weights are gathered 32 at a time (lane j: row j) and broadcast by
+    // shuffles; eight table rows in flight; the rows are summed in order.
     // COMBINED: every column uses the combined strengths, read from the table
     // Tc = (Dirichlet dof ? -T2 : T1) made at set_bc (one table row per row
     // instead of two); T1 is then Tc and T2 is unused.
-    template <typename T, bool COMBINED>
+    // RC: columns per pass (1 for one right-hand side, else 4).
+    template <typename T, bool COMBINED, int RC>
     __global__ void __launch_bounds__(256)
-      p2m_apply_kernel(int R, int K, int N, const int64_t *__restrict__ prow_ptr,
+      p2m_apply_kernel(int n_leaves, int R, int K, int N, const int64_t *__restrict__ prow_ptr,
                        const int32_t *__restrict__ pleaf_box, const int32_t *__restrict__ prow_dof,
                        const T *__restrict__ T1, const T *__restrict__ T2,
                        const uint8_t *__restrict__ dir, const uint8_t *__restrict__ modes,
                        const T *__restrict__ x, T *__restrict__ M)
     {
-      extern __shared__ __align__(16) unsigned char smem_raw[];
-      const int     K4   = (K + 3) / 4 * 4;
-      T            *part = reinterpret_cast<T *>(smem_raw); // [8][4][K4]
-      const int     leaf = blockIdx.x;
-      const int64_t box  = pleaf_box[leaf];
+      const int leaf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+      if (leaf >= n_leaves)
+        return;
+      const int     K4  = (K + 3) / 4 * 4;
+      const int64_t box = pleaf_box[leaf];
       const int64_t rb = prow_ptr[leaf], re = prow_ptr[leaf + 1];
-      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      const bool    act  = 4 * lane < K4;
-      for (int rq = 0; rq < R; rq += 4)
+      const bool    act = 4 * lane < K4;
+      for (int rq = 0; rq < R; rq += RC)
         {
-          const int rc = min(4, R - rq);
-          T         acc[4][4];
+          const int rc = min(RC, R - rq);
+          T         acc[RC][4];
 #pragma unroll
-          for (int a = 0; a < 4; ++a)
+          for (int a = 0; a < RC; ++a)
 #pragma unroll
             for (int b = 0; b < 4; ++b)
               acc[a][b] = T(0);
-          if (act)
-            for (int64_t row = rb + warp; row < re; row += 8)
-              {
-                const int dof = prow_dof[row];
-                T         t1[4], t2[4];
-                load4(T1 + row * K4 + 4 * lane, t1);
-                if constexpr (COMBINED)
-                  {
-#pragma unroll
-                    for (int rr = 0; rr < 4; ++rr)
-                      if (rr < rc)
-                        {
-                          const T xv = x[int64_t(rq + rr) * N + dof];
-#pragma unroll
-                          for (int c = 0; c < 4; ++c)
-                            acc[rr][c] += xv * t1[c];
-                        }
-                    continue;
-                  }
-                load4(T2 + row * K4 + 4 * lane, t2);
-                const bool d = dir[dof] != 0;
-#pragma unroll
-                for (int rr = 0; rr < 4; ++rr)
-                  if (rr < rc)
-                    {
-                      const uint8_t mode = modes[rq + rr];
-                      const T       xv   = x[int64_t(rq + rr) * N + dof];
-                      const T       w1   = mode == MODE_KER2 ? T(0) : (mode == MODE_KER1 ? xv : (d ? T(0) : xv));
-                      const T       w2   = mode == MODE_KER1 ? T(0) : (mode == MODE_KER2 ? xv : (d ? -xv : T(0)));
-#pragma unroll
-                      for (int c = 0; c < 4; ++c)
-                        acc[rr][c] += w1 * t1[c] + w2 * t2[c];
-                    }
-              }
-          if (act)
-#pragma unroll
-            for (int rr = 0; rr < 4; ++rr)
-#pragma unroll
-              for (int c = 0; c < 4; ++c)
-                part[(warp * 4 + rr) * K4 + 4 * lane + c] = acc[rr][c];
-          __syncthreads();
-          for (int i = threadIdx.x; i < rc * K; i += blockDim.x)
+          for (int64_t b0 = rb; b0 < re; b0 += 32)
             {
-              const int rr = i / K, k = i - rr * K;
-              T         s  = part[rr * K4 + k];
-              for (int w = 1; w < 8; ++w)
-                s += part[(w * 4 + rr) * K4 + k];
-              M[(box * R + rq + rr) * K + k] = s;
+              const int nb = re - b0 < 32 ? int(re - b0) : 32;
+              T         w1[RC], w2[RC];
+#pragma unroll
+              for (int rr = 0; rr < RC; ++rr)
+                w1[rr] = w2[rr] = T(0);
+              if (lane < nb)
+                {
+                  const int  dof = prow_dof[b0 + lane];
+                  const bool d   = dir[dof] != 0;
+#pragma unroll
+                  for (int rr = 0; rr < RC; ++rr)
+                    if (rr < rc)
+                      {
+                        const T xv = x[int64_t(rq + rr) * N + dof];
+                        if constexpr (COMBINED)
+                          w1[rr] = xv;
+                        else
+                          {
+                            const uint8_t mode = modes[rq + rr];
+                            w1[rr] = mode == MODE_KER2 ? T(0) : (mode == MODE_KER1 ? xv : (d ? T(0) : xv));
+                            w2[rr] = mode == MODE_KER1 ? T(0) : (mode == MODE_KER2 ? xv : (d ? -xv : T(0)));
+                          }
+                      }
+                }
+              for (int j0 = 0; j0 < nb; j0 += 8)
+                {
+                  T t1[8][4], t2[8][4];
+#pragma unroll
+                  for (int u = 0; u < 8; ++u)
+                    if (act && j0 + u < nb)
+                      {
+                        load4(T1 + (b0 + j0 + u) * K4 + 4 * lane, t1[u]);
+                        if constexpr (!COMBINED)
+                          load4(T2 + (b0 + j0 + u) * K4 + 4 * lane, t2[u]);
+                      }
+#pragma unroll
+                  for (int u = 0; u < 8; ++u)
+                    if (j0 + u < nb)
+#pragma unroll
+                      for (int rr = 0; rr < RC; ++rr)
+                        if (rr < rc)
+                          {
+                            const T a1 = __shfl_sync(0xffffffffu, w1[rr], j0 + u);
+                            if constexpr (COMBINED)
+                              {
+#pragma unroll
+                                for (int c = 0; c < 4; ++c)
+                                  acc[rr][c] += a1 * t1[u][c];
+                              }
+                            else
+                              {
+                                const T a2 = __shfl_sync(0xffffffffu, w2[rr], j0 + u);
+#pragma unroll
+                                for (int c = 0; c < 4; ++c)
+                                  acc[rr][c] += a1 * t1[u][c] + a2 * t2[u][c];
+                              }
+                          }
+                }
             }
-          __syncthreads();
+          if (act)
+#pragma unroll
+            for (int rr = 0; rr < RC; ++rr)
+              if (rr < rc)
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                  if (4 * lane + c < K)
+                    M[(box * R + rq + rr) * K + 4 * lane + c] = acc[rr][c];
         }
     }
 
@@ -541,29 +561,56 @@ namespace pibem
         }
     }
 
+    // L2P: y[r][node] += W[row] . L^[leaf][r] for every row (node of a
+    // childless box).  One warp per leaf, 8 leaves per block: lane l multiplies
+    // coefficients 4l..4l+3 (W rows padded to K4 values), eight rows in flight;
+    // the lanes' products are added by a fixed butterfly, and lane u updates
+    // the node of row u of each group of eight.
     template <typename T>
-    __global__ void l2p_kernel(int64_t n_rows, int R, int K, int N,
-                               const int32_t *__restrict__ row_leaf,
-                               const int32_t *__restrict__ lleaf_box,
-                               const int32_t *__restrict__ nrows, const T *__restrict__ W,
-                               const T *__restrict__ Lx, T *__restrict__ y)
+    __global__ void __launch_bounds__(256)
+      l2p_kernel(int n_leaves, int R, int K, int N, const int64_t *__restrict__ row_ptr,
+                 const int32_t *__restrict__ lleaf_box, const int32_t *__restrict__ nrows,
+                 const T *__restrict__ W, const T *__restrict__ Lx, T *__restrict__ y)
     {
-      const int64_t row  = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-      const int     lane = threadIdx.x & 31;
-      if (row >= n_rows)
+      const int leaf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+      if (leaf >= n_leaves)
         return;
-      const int64_t box  = lleaf_box[row_leaf[row]];
-      const int     node = nrows[row];
-      const T      *w    = W + row * K;
+      const int     K4  = (K + 3) / 4 * 4;
+      const int64_t box = lleaf_box[leaf];
+      const int64_t r0 = row_ptr[leaf], r1 = row_ptr[leaf + 1];
+      const bool    act = 4 * lane < K4;
       for (int r = 0; r < R; ++r)
         {
-          const T *l = Lx + (box * R + r) * K;
-          T        s = T(0);
-          for (int k = lane; k < K; k += 32)
-            s += w[k] * l[k];
-          s = warp_sum(s);
-          if (lane == 0)
-            y[int64_t(r) * N + node] += s;
+          T l[4] = {T(0), T(0), T(0), T(0)};
+          if (act)
+            {
+              const T *lp = Lx + (box * R + r) * K;
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                if (4 * lane + c < K)
+                  l[c] = lp[4 * lane + c];
+            }
+          for (int64_t i0 = r0; i0 < r1; i0 += 8)
+            {
+              T w[8][4];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                if (act && i0 + u < r1)
+                  load4(W + (i0 + u) * K4 + 4 * lane, w[u]);
+                else
+                  w[u][0] = w[u][1] = w[u][2] = w[u][3] = T(0);
+              T mine = T(0);
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                {
+                  T s = (w[u][0] * l[0] + w[u][1] * l[1]) + (w[u][2] * l[2] + w[u][3] * l[3]);
+                  s   = warp_sum(s);
+                  if (lane == u)
+                    mine = s;
+                }
+              if (lane < 8 && i0 + lane < r1)
+                y[int64_t(r) * N + nrows[i0 + lane]] += mine;
+            }
         }
     }
 
@@ -597,13 +644,16 @@ namespace pibem
   {
     if (op.n_p2m_leaves == 0)
       return;
-    const size_t smem = size_t(8) * 4 * ((op.K + 3) / 4 * 4) * sizeof(T);
-    if (combined && op.Tc)
-      p2m_apply_kernel<T, true><<<op.n_p2m_leaves, 256, smem, s>>>(
-        R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof, op.Tc, op.T2, dir, modes, x, M);
+    const unsigned grid = unsigned((op.n_p2m_leaves + 7) / 8);
+    const bool     comb = combined && op.Tc;
+    auto launch = [&](auto kern) {
+      kern<<<grid, 256, 0, s>>>(op.n_p2m_leaves, R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof,
+                                comb ? op.Tc : op.T1, op.T2, dir, modes, x, M);
+    };
+    if (comb)
+      R == 1 ? launch(p2m_apply_kernel<T, true, 1>) : launch(p2m_apply_kernel<T, true, 4>);
     else
-      p2m_apply_kernel<T, false><<<op.n_p2m_leaves, 256, smem, s>>>(
-        R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof, op.T1, op.T2, dir, modes, x, M);
+      R == 1 ? launch(p2m_apply_kernel<T, false, 1>) : launch(p2m_apply_kernel<T, false, 4>);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -689,6 +739,12 @@ namespace pibem
   template <typename T>
   void launch_upward_level(const OperatorDev<T> &op, int R, int level, T *M, T *Y, cudaStream_t s)
   {
+    if constexpr (std::is_same<T, float>::value)
+      if (op.up_child8 && fused_levels_ok(op.K, R))
+        {
+          launch_m2m_level_fused(op, R, level, M, s);
+          return;
+        }
     launch_trans_gemm<T>(op, R, op.up_chunk_ptr[level], op.up_chunk_ptr[level + 1], M, Y, s);
     const int a = op.up_box_ptr[level], b = op.up_box_ptr[level + 1];
     launch_gather<T>(R, op.K, b - a, op.up_box + a, op.up_q_ptr + a, op.up_q, Y, M, s);
@@ -701,9 +757,23 @@ namespace pibem
   }
 
   template <typename T>
+  void launch_m2l_sums(const OperatorDev<T> &op, int R, T *Lx, const T *Y, cudaStream_t s)
+  {
+    if constexpr (std::is_same<T, float>::value)
+      if (op.down_par && fused_levels_ok(op.K, R))
+        launch_m2l_sums_fused(op, R, Lx, Y, s);
+  }
+
+  template <typename T>
   void launch_downward_level(const OperatorDev<T> &op, int R, int level, T *Lx, T *Y,
                              cudaStream_t s)
   {
+    if constexpr (std::is_same<T, float>::value)
+      if (op.down_par && fused_levels_ok(op.K, R))
+        {
+          launch_l2l_level_fused(op, R, level, Lx, s);
+          return;
+        }
     launch_trans_gemm<T>(op, R, op.down_chunk_ptr[level], op.down_chunk_ptr[level + 1], Lx, Y, s);
     const int a = op.down_box_ptr[level], b = op.down_box_ptr[level + 1];
     launch_gather<T>(R, op.K, b - a, op.down_box + a, op.down_q_ptr + a, op.down_q, Y, Lx, s);
@@ -744,11 +814,10 @@ namespace pibem
   template <typename T>
   void launch_l2p(const OperatorDev<T> &op, int R, int N, const T *Lx, T *y, cudaStream_t s)
   {
-    if (op.n_rows == 0)
+    if (op.n_rows == 0 || op.n_near_leaves == 0)
       return;
-    const int64_t threads = op.n_rows * 32;
-    l2p_kernel<T><<<unsigned((threads + 255) / 256), 256, 0, s>>>(
-      op.n_rows, R, op.K, N, op.row_leaf, op.lleaf_box, op.nrows, op.W, Lx, y);
+    l2p_kernel<T><<<unsigned((op.n_near_leaves + 7) / 8), 256, 0, s>>>(
+      op.n_near_leaves, R, op.K, N, op.nrow_ptr, op.lleaf_box, op.nrows, op.W, Lx, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -760,6 +829,7 @@ namespace pibem
                                     const uint8_t *, const T *, T *, bool, cudaStream_t);        \
   template void launch_upward_level<T>(const OperatorDev<T> &, int, int, T *, T *, cudaStream_t); \
   template void launch_m2l_gemm<T>(const OperatorDev<T> &, int, const T *, T *, cudaStream_t);    \
+  template void launch_m2l_sums<T>(const OperatorDev<T> &, int, T *, const T *, cudaStream_t);    \
   template void launch_downward_level<T>(const OperatorDev<T> &, int, int, T *, T *,             \
                                          cudaStream_t);                                          \
   template void launch_m2p<T>(const OperatorDev<T> &, const TreeDev &, int, int, const T *, T *, \

@@ -42,7 +42,7 @@ namespace pibem
                          const double *box_delta, const double *qpts, const double *qnrm,
                          const double *qjxw, const double *qshape, double *T1, double *T2,
                          cudaStream_t s);
-  void launch_l2p_tables(int64_t n_pos, int K, int n_leaves, const int64_t *pos_ptr,
+  void launch_l2p_tables(int64_t n_pos, int K, int ldw, int n_leaves, const int64_t *pos_ptr,
                          const int32_t *leaf_box, const int32_t *nodes, const double *xyz,
                          const double *box_center, const double *box_delta, double *W,
                          cudaStream_t s);
@@ -96,6 +96,15 @@ namespace pibem
     std::vector<int> up_chunk_ptr, down_chunk_ptr, up_box_ptr, down_box_ptr;
     const int32_t *up_box = nullptr, *down_box = nullptr, *up_q = nullptr, *down_q = nullptr;
     const int64_t *up_q_ptr = nullptr, *down_q_ptr = nullptr;
+    // fused level passes (levels.cu): children of each up_box entry by octant,
+    // L2L parent (-1: none) and octant of each down_box entry; the M2M
+    // operators are ops[lv_op0 .. lv_op0 + 7], the L2L ones the next 8
+    const int32_t *up_child8 = nullptr, *down_par = nullptr;
+    const uint8_t *down_oct  = nullptr;
+    int            lv_op0    = 0;
+    const T       *lv_ops    = nullptr; // the 16 level operators, each padded to 16 bytes
+    int           *dev_err   = nullptr; // set by a bounded device wait that timed out
+    std::vector<char> down_l2l_level; // per level: its boxes receive L2L
     int64_t        n_pairs = 0;
     int64_t        max_near_cols = 0;
     // tensor-core path of the FP32 translations (null: CUDA-core GEMM)
@@ -122,12 +131,29 @@ namespace pibem
   template <typename T>
   void launch_m2l_gemm(const OperatorDev<T> &op, int R, const T *M, T *Y, cudaStream_t s);
   // downward level l: L2L products, then L[b] = L2L + sum of M2L products
+  // (fused passes: L[b] += L2L, the M2L sums being in place already)
   template <typename T>
   void launch_downward_level(const OperatorDev<T> &op, int R, int level, T *Lx, T *Y,
                              cudaStream_t s);
   template <typename T>
   void launch_m2p(const OperatorDev<T> &op, const TreeDev &td, int R, int N, const T *M, T *y,
                   cudaStream_t s);
+  // M2L sums of all levels into Lx (the first step of the downward pass, before
+  // the levels); does nothing unless the fused level passes apply
+  template <typename T>
+  void launch_m2l_sums(const OperatorDev<T> &op, int R, T *Lx, const T *Y, cudaStream_t s);
+  // fused level passes of the FP32 operator (levels.cu), used for R up to
+  // FUSED_LEVEL_MAX_R columns: M2L sums of all levels in one launch, then one
+  // launch per level, no gathers
+  constexpr int FUSED_LEVEL_MAX_R = 16;
+  bool          fused_levels_ok(int K, int R);
+  size_t        fused_level_ops_floats(int K); // size of OperatorDev::lv_ops
+  void launch_m2m_level_fused(const OperatorDev<float> &op, int R, int level, float *M,
+                              cudaStream_t s);
+  void launch_m2l_sums_fused(const OperatorDev<float> &op, int R, float *Lx, const float *Y,
+                             cudaStream_t s);
+  void launch_l2l_level_fused(const OperatorDev<float> &op, int R, int level, float *Lx,
+                              cudaStream_t s);
   void ensure_fmm_tables(int device, cudaStream_t s);
   template <typename T>
   void launch_l2p(const OperatorDev<T> &op, int R, int N, const T *Lx, T *y, cudaStream_t s);

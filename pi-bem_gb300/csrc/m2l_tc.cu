@@ -38,6 +38,7 @@
 #include <cstdint>
 #include <cstring>
 
+#include "async_copy.cuh"
 #include "kernels.h"
 
 namespace pibem
@@ -65,11 +66,6 @@ namespace pibem
                       (k & 3) * 4);
     }
 
-    __device__ inline uint32_t smem_u32(const void *p)
-    {
-      return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-    }
-
     // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
     // 1024 bytes apart (stride byte offset); the leading byte offset is unused
     // for swizzled K-major operands.  A K-step of 8 TF32 values inside the
@@ -92,18 +88,6 @@ namespace pibem
       return __uint_as_float(r);
     }
 
-    __device__ inline bool mbar_try(uint32_t addr, uint32_t parity)
-    {
-      uint32_t done;
-      asm volatile("{\n\t.reg .pred p;\n\t"
-                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                   "selp.u32 %0, 1, 0, p;\n\t}"
-                   : "=r"(done)
-                   : "r"(addr), "r"(parity)
-                   : "memory");
-      return done != 0;
-    }
-
     // Bounded wait; gives up early once another role has raised the abort flag.
     __device__ inline bool mbar_wait(uint32_t addr, uint32_t parity, const volatile int *abort)
     {
@@ -123,32 +107,6 @@ namespace pibem
       for (long it = 0; it < TC_SPIN_LIMIT; ++it)
         if (mbar_try(addr, parity))
           return;
-    }
-
-    __device__ inline void mbar_init(uint32_t addr, uint32_t count)
-    {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" : : "r"(addr), "r"(count) : "memory");
-    }
-
-    __device__ inline void mbar_arrive(uint32_t addr)
-    {
-      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" : : "r"(addr) : "memory");
-    }
-
-    __device__ inline void mbar_arrive_expect_tx(uint32_t addr, uint32_t bytes)
-    {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                   :
-                   : "r"(addr), "r"(bytes)
-                   : "memory");
-    }
-
-    __device__ inline void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar)
-    {
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                   :
-                   : "r"(dst), "l"(src), "r"(bytes), "r"(mbar)
-                   : "memory");
     }
 
     __device__ inline void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,

@@ -183,6 +183,11 @@ namespace pibem
     std::vector<int32_t>  up_box, down_box;
     std::vector<int64_t>  up_q_ptr, down_q_ptr;         // per listed box
     std::vector<int32_t>  up_q, down_q;
+    // fused level passes: the children of each up_box entry by octant (-1:
+    // none), 8 per entry; per down_box entry its octant and the parent whose
+    // local expansion it receives by L2L (-1: none; then down_q has no L2L entry)
+    std::vector<int32_t>  up_child8, down_par;
+    std::vector<uint8_t>  down_oct;
     // M2P pairs grouped by target
     std::vector<int32_t>  m2p_tgt;
     std::vector<int64_t>  m2p_src_ptr;

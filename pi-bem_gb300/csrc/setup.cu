@@ -330,7 +330,7 @@ namespace pibem
 
     // L2P tables: W[pos][k] such that the field at node rows[pos] of its leaf is
     // sum_k W[pos][k] L^[leaf][k] (LocalExpansion::Evaluate local_expansion.cc:252-287).
-    __global__ void l2p_table_kernel(int64_t n_pos, int K, int n_leaves,
+    __global__ void l2p_table_kernel(int64_t n_pos, int K, int ldw, int n_leaves,
                                      const int64_t *__restrict__ pos_ptr,
                                      const int32_t *__restrict__ leaf_box,
                                      const int32_t *__restrict__ nodes,
@@ -380,7 +380,7 @@ namespace pibem
         }
       else if (k == 0)
         val = 1.0;
-      W[pos * K + k] = val / h;
+      W[pos * ldw + k] = val / h;
     }
   } // namespace
 
@@ -494,7 +494,7 @@ namespace pibem
     note_launch();
   }
 
-  void launch_l2p_tables(int64_t n_pos, int K, int n_leaves, const int64_t *pos_ptr,
+  void launch_l2p_tables(int64_t n_pos, int K, int ldw, int n_leaves, const int64_t *pos_ptr,
                          const int32_t *leaf_box, const int32_t *nodes, const double *xyz,
                          const double *box_center, const double *box_delta, double *W,
                          cudaStream_t s)
@@ -502,7 +502,7 @@ namespace pibem
     int64_t n = n_pos * K;
     if (n == 0)
       return;
-    l2p_table_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n_pos, K, n_leaves, pos_ptr,
+    l2p_table_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n_pos, K, ldw, n_leaves, pos_ptr,
                                                                leaf_box, nodes, xyz, box_center,
                                                                box_delta, W);
     PIBEM_CUDA(cudaGetLastError());

@@ -621,6 +621,17 @@ namespace pibem
         }
       cut(0, np);
       pl.m2l_chunk_end = int(pl.ch_start.size());
+      // Levels whose expansions are ever read: multipoles of the boxes at or
+      // below the shallowest M2L / M2P source (M2M stops there), locals of
+      // the boxes at or below the shallowest M2L target (above it they are
+      // zero: no L2L from there, the boxes with nodes get a zero expansion).
+      int lo_src = t.L + 1, lo_tgt = t.L + 1;
+      for (int32_t b : pl.m2l_src)
+        lo_src = std::min(lo_src, t.level[b]);
+      for (int32_t b : pl.m2p_src)
+        lo_src = std::min(lo_src, t.level[b]);
+      for (int32_t b : pl.m2l_tgt)
+        lo_tgt = std::min(lo_tgt, t.level[b]);
       // M2M: children at level l -> parents at level l-1, grouped by octant
       pl.up_chunk_ptr.assign(t.L + 2, 0);
       pl.up_box_ptr.assign(t.L + 2, 0);
@@ -629,7 +640,10 @@ namespace pibem
       for (int l = 1; l <= t.L; ++l)
         {
           pl.up_chunk_ptr[l] = int(pl.ch_start.size());
-          int64_t q0         = int64_t(pl.q_src.size());
+          pl.up_box_ptr[l]   = int(pl.up_box.size());
+          if (l - 1 < lo_src)
+            continue;
+          int64_t q0 = int64_t(pl.q_src.size());
           for (int dg = 0; dg < 8; ++dg)
             for (int b = t.startLevel[l]; b <= t.endLevel[l] && t.startLevel[l] <= t.endLevel[l]; ++b)
               if (t.digit[b] == dg)
@@ -639,22 +653,28 @@ namespace pibem
                   pl.q_op.push_back(noff + dg);
                 }
           cut(q0, int64_t(pl.q_src.size()));
-          pl.up_box_ptr[l] = int(pl.up_box.size());
           // parents (level l-1) gather their children's products
-          int a = l == 1 ? 0 : t.startLevel[l - 1], e = l == 1 ? 0 : t.endLevel[l - 1];
-          for (int P = a; P <= e; ++P)
+          for (int P = t.startLevel[l - 1]; P <= t.endLevel[l - 1]; ++P)
             if (t.nchild[P] > 0)
               {
                 pl.up_box.push_back(P);
+                const size_t at = pl.up_child8.size();
+                pl.up_child8.resize(at + 8, -1);
                 for (int c = 0; c < t.nchild[P]; ++c)
-                  pl.up_q.push_back(int32_t(child_q[t.child_first[P] + c]));
+                  {
+                    const int cb = t.child_first[P] + c;
+                    pl.up_q.push_back(int32_t(child_q[cb]));
+                    pl.up_child8[at + t.digit[cb]] = cb;
+                  }
                 pl.up_q_ptr.push_back(int64_t(pl.up_q.size()));
               }
         }
       pl.up_chunk_ptr[t.L + 1] = int(pl.ch_start.size());
       pl.up_box_ptr[t.L + 1]   = int(pl.up_box.size());
-      // L2L: parent (level l-1) -> child with nodes (level l >= 2), by octant;
-      // gather per box with nodes: its L2L product, then its M2L products.
+      // L2L: parent (level l-1 >= lo_tgt) -> child with nodes (level l), by
+      // octant; gather per box with nodes, listed by octant: its L2L product,
+      // then its M2L products.  Boxes with nodes above lo_tgt are listed (with
+      // nothing to sum) at the first level that has any.
       pl.down_chunk_ptr.assign(t.L + 2, 0);
       pl.down_box_ptr.assign(t.L + 2, 0);
       pl.down_q_ptr.push_back(0);
@@ -662,24 +682,35 @@ namespace pibem
       std::vector<int64_t> m2l_first(t.nb, -1);
       for (size_t ti = 0; ti < pl.m2l_tgt.size(); ++ti)
         m2l_first[pl.m2l_tgt[ti]] = int64_t(ti);
+      const int zero_level = std::min(std::max(lo_tgt, 1), t.L);
       for (int l = 1; l <= t.L; ++l)
         {
           pl.down_chunk_ptr[l] = int(pl.ch_start.size());
-          int64_t q0           = int64_t(pl.q_src.size());
-          if (l >= 2)
-            for (int dg = 0; dg < 8; ++dg)
-              for (int b : t.dofs_filled[l])
-                if (t.digit[b] == dg)
-                  {
-                    l2l_q[b] = int64_t(pl.q_src.size());
-                    pl.q_src.push_back(t.parent[b]);
-                    pl.q_op.push_back(noff + 8 + dg);
-                  }
+          pl.down_box_ptr[l]   = int(pl.down_box.size());
+          if (l < zero_level)
+            continue;
+          std::vector<int> boxes;
+          if (l == zero_level)
+            for (int l2 = 1; l2 < l; ++l2)
+              boxes.insert(boxes.end(), t.dofs_filled[l2].begin(), t.dofs_filled[l2].end());
+          std::vector<int> here = t.dofs_filled[l];
+          std::stable_sort(here.begin(), here.end(),
+                           [&](int a, int b) { return t.digit[a] < t.digit[b]; });
+          int64_t q0 = int64_t(pl.q_src.size());
+          if (l >= 2 && l - 1 >= lo_tgt)
+            for (int b : here)
+              {
+                l2l_q[b] = int64_t(pl.q_src.size());
+                pl.q_src.push_back(t.parent[b]);
+                pl.q_op.push_back(noff + 8 + t.digit[b]);
+              }
           cut(q0, int64_t(pl.q_src.size()));
-          pl.down_box_ptr[l] = int(pl.down_box.size());
-          for (int b : t.dofs_filled[l])
+          boxes.insert(boxes.end(), here.begin(), here.end());
+          for (int b : boxes)
             {
               pl.down_box.push_back(b);
+              pl.down_oct.push_back(uint8_t(t.digit[b] & 7));
+              pl.down_par.push_back(l2l_q[b] >= 0 ? t.parent[b] : -1);
               if (l2l_q[b] >= 0)
                 pl.down_q.push_back(int32_t(l2l_q[b]));
               if (m2l_first[b] >= 0)
