@@ -140,8 +140,10 @@ struct pibem_handle
   pibem_params prm;
   std::string  err;
   cudaStream_t stream = nullptr, own = nullptr;
-  cudaStream_t side = nullptr; // second stream of the two-branch operator
-  cudaEvent_t  ev_fork = nullptr, ev_up = nullptr, ev_side = nullptr;
+  // the two branches of the operator: the tree passes (the critical path) on a
+  // stream of the highest priority, the near field and M2P on one of the lowest
+  cudaStream_t main_hp = nullptr, side = nullptr;
+  cudaEvent_t  ev_fork = nullptr, ev_up = nullptr, ev_side = nullptr, ev_main = nullptr;
   bool         mesh_ok = false, bc_ok = false;
   MeshHost     mesh;
   int          nq = 0, n_tel = 0;
@@ -164,7 +166,7 @@ struct pibem_handle
   DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
     d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
-    d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par;
+    d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_m2p_item_pair;
   DBuf<uint8_t> d_down_oct;
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc;
@@ -222,7 +224,8 @@ struct pibem_handle
     add(d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
         d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
-        d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct);
+        d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
+        d_m2p_item_pair);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
@@ -339,9 +342,10 @@ namespace
 
   // The system operator y = S x (near field + combined far field).  Without
   // phase timing the independent branches run on two streams: the near SpMV
-  // (HBM-bound) and then M2P on the handle's side stream, beside P2M, the
-  // upward pass, M2L and the downward pass (latency-bound small GEMMs) on the
-  // main stream; L2P joins them.  y is written by the near SpMV and then added
+  // (HBM-bound) and then M2P on the handle's low-priority side stream, beside
+  // P2M, the upward pass, M2L and the downward pass (latency-bound, the
+  // critical path) on its high-priority stream; L2P joins them, and the
+  // caller's stream waits for the result.  y is written by the near SpMV and then added
   // to by M2P and L2P in that order, as in the one-stream sequence, so the
   // result is the same bit for bit.
   template <typename T>
@@ -359,19 +363,22 @@ namespace
         far_field<T>(h, op, M, Lx, scr, Y, R, modes, x, y, true);
         return;
       }
-    cudaStream_t side = h->side;
+    cudaStream_t side = h->side, main = h->main_hp;
     far_alloc<T>(h, op, M, Lx, scr, Y, R);
     PIBEM_CUDA(cudaEventRecord(h->ev_fork, s));
     PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_fork, 0));
+    PIBEM_CUDA(cudaStreamWaitEvent(main, h->ev_fork, 0));
     launch_near_spmv<T>(op, R, N, vals, x, y, false, side);
-    far_up<T>(h, op, M, Y, R, modes, x, true, s);
-    PIBEM_CUDA(cudaEventRecord(h->ev_up, s));
+    far_up<T>(h, op, M, Y, R, modes, x, true, main);
+    PIBEM_CUDA(cudaEventRecord(h->ev_up, main));
     PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_up, 0));
     launch_m2p<T>(op, h->td, R, N, M.p, y, side);
     PIBEM_CUDA(cudaEventRecord(h->ev_side, side));
-    far_down<T>(h, op, M, Lx, Y, R, s);
-    PIBEM_CUDA(cudaStreamWaitEvent(s, h->ev_side, 0));
-    launch_l2p<T>(op, R, N, Lx.p, y, s);
+    far_down<T>(h, op, M, Lx, Y, R, main);
+    PIBEM_CUDA(cudaStreamWaitEvent(main, h->ev_side, 0));
+    launch_l2p<T>(op, R, N, Lx.p, y, main);
+    PIBEM_CUDA(cudaEventRecord(h->ev_main, main));
+    PIBEM_CUDA(cudaStreamWaitEvent(s, h->ev_main, 0));
   }
 
   // prec: 0 FP64 operator, 1 FP32 operator
@@ -558,7 +565,9 @@ namespace
         throw;
       }
     PIBEM_CUDA(cudaStreamEndCapture(s, &g));
-    const cudaError_t e = cudaGraphInstantiate(&h->g32_exec, g, 0);
+    // kernel nodes keep the priority of the stream they were captured from
+    const cudaError_t e =
+      cudaGraphInstantiateWithFlags(&h->g32_exec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess)
       {
@@ -794,10 +803,15 @@ namespace
     for (int k = 0; k < nl; ++k)
       {
         int n = int(pl.nrow_ptr[k + 1] - pl.nrow_ptr[k]);
-        if (!invert(n, &hb[h->blk_ptr[k]], &inv[h->blk_ptr[k]]))
+        double *b = &inv[h->blk_ptr[k]];
+        if (!invert(n, &hb[h->blk_ptr[k]], b))
           for (int i = 0; i < n; ++i)
             for (int j2 = 0; j2 < n; ++j2)
-              inv[h->blk_ptr[k] + size_t(i) * n + j2] = i == j2 ? 1.0 : 0.0;
+              b[size_t(i) * n + j2] = i == j2 ? 1.0 : 0.0;
+        // stored column by column: the apply reads a column across the rows
+        for (int i = 0; i < n; ++i)
+          for (int j2 = i + 1; j2 < n; ++j2)
+            std::swap(b[size_t(i) * n + j2], b[size_t(j2) * n + i]);
       }
     h->d_Pinv.upload(inv, s);
   }
@@ -861,6 +875,7 @@ namespace
       op.m2p_src_ptr   = h->d_m2p_src_ptr.p;
       op.m2p_pair_tgt  = h->d_m2p_pair_tgt.p;
       op.m2p_item_ptr  = h->d_m2p_item_ptr.p;
+      op.m2p_item_pair = h->d_m2p_item_pair.p;
       op.m2p_tnode_ptr = h->d_m2p_tnode_ptr.p;
     };
     fill(h->op64);
@@ -1168,6 +1183,10 @@ namespace
         }
       h->m2p_items  = item_ptr.back();
       h->m2p_tnodes = tnode_ptr.back();
+      std::vector<int32_t> item_pair(size_t(h->m2p_items));
+      for (size_t e = 0; e + 1 < item_ptr.size(); ++e)
+        std::fill(item_pair.begin() + item_ptr[e], item_pair.begin() + item_ptr[e + 1], int32_t(e));
+      h->d_m2p_item_pair.upload(item_pair, s);
       h->d_m2p_pair_tgt.upload(pair_tgt, s);
       h->d_m2p_item_ptr.upload(item_ptr, s);
       h->d_m2p_tnode_ptr.upload(tnode_ptr, s);
@@ -1588,8 +1607,11 @@ extern "C"
       {
         PIBEM_CUDA(cudaSetDevice(P.device));
         PIBEM_CUDA(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
-        PIBEM_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
-        for (cudaEvent_t *e : {&h->ev_fork, &h->ev_up, &h->ev_side})
+        int prio_lo = 0, prio_hi = 0; // least, greatest
+        PIBEM_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+        PIBEM_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_lo));
+        PIBEM_CUDA(cudaStreamCreateWithPriority(&h->main_hp, cudaStreamNonBlocking, prio_hi));
+        for (cudaEvent_t *e : {&h->ev_fork, &h->ev_up, &h->ev_side, &h->ev_main})
           PIBEM_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
         h->stream = h->own;
         const char *env = std::getenv("PIBEM_PHASE_TIMING");
@@ -1618,14 +1640,15 @@ extern "C"
     for (auto &e : h->ev)
       if (e)
         cudaEventDestroy(e);
-    for (cudaEvent_t e : {h->ev_fork, h->ev_up, h->ev_side})
+    for (cudaEvent_t e : {h->ev_fork, h->ev_up, h->ev_side, h->ev_main})
       if (e)
         cudaEventDestroy(e);
-    if (h->side)
-      {
-        cudaStreamSynchronize(h->side);
-        cudaStreamDestroy(h->side);
-      }
+    for (cudaStream_t st : {h->side, h->main_hp})
+      if (st)
+        {
+          cudaStreamSynchronize(st);
+          cudaStreamDestroy(st);
+        }
     cudaStream_t own = h->own;
     drop_graph(h);
     delete h;

@@ -153,6 +153,91 @@ namespace pibem
         }
     }
 
+    // 4-byte asynchronous global -> shared copy (cp.async, L1-allocating)
+    __device__ inline void cp_async4(void *dst, const void *src)
+    {
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+                   "l"(src)
+                   : "memory");
+    }
+    __device__ inline void cp_async8(void *dst, const void *src)
+    {
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+                   "l"(src)
+                   : "memory");
+    }
+    __device__ inline void cp_async_x(float *dst, const float *src) { cp_async4(dst, src); }
+    __device__ inline void cp_async_x(double *dst, const double *src) { cp_async8(dst, src); }
+
+    // Near-field SpMV for one column, software-pipelined: persistent blocks
+    // take leaves L, L + gridDim.x, ...; while the warps stream the rows of a
+    // leaf, the x entries of the block's next leaf are gathered into the other
+    // half of a double buffer with cp.async.  A row is computed exactly as in
+    // near_leaf_kernel (same chunks per lane, same order, same butterfly).
+    // Shared memory: 2 x ld_max values.
+    template <typename T>
+    __global__ void __launch_bounds__(256)
+      near_leaf_pipe_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ nrow_ptr,
+                            const int64_t *__restrict__ ncol_ptr,
+                            const int64_t *__restrict__ nval_ptr, const int32_t *__restrict__ nrows,
+                            const int32_t *__restrict__ ncols, const T *__restrict__ vals,
+                            const T *__restrict__ x, T *__restrict__ y, bool acc)
+    {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      T        *sxb  = reinterpret_cast<T *>(smem_raw); // [2][ld_max]
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      // gather of leaf l into buffer b: cp.async for the columns, zeros in the padding
+      auto gather = [&](int l, int b) {
+        const int64_t c0 = ncol_ptr[l], nc = ncol_ptr[l + 1] - c0;
+        const int64_t ld = (nc + 3) / 4 * 4;
+        T            *sx = sxb + int64_t(b) * ld_max;
+        for (int64_t c = threadIdx.x; c < ld; c += blockDim.x)
+          if (c < nc)
+            cp_async_x(sx + c, x + ncols[c0 + c]);
+          else
+            sx[c] = T(0);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      };
+      int leaf = blockIdx.x, buf = 0;
+      if (leaf < n_leaves)
+        gather(leaf, 0);
+      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
+        {
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
+          __syncthreads(); // this leaf's x is in place; the other buffer is free
+          const int next = leaf + gridDim.x;
+          if (next < n_leaves)
+            gather(next, buf ^ 1);
+          const T      *sx = sxb + int64_t(buf) * ld_max;
+          const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
+          const int64_t ld = (nc + 3) / 4 * 4;
+          const int     n4 = int(ld / 4);
+          const int64_t r0 = nrow_ptr[leaf], nr = nrow_ptr[leaf + 1] - r0;
+          const T      *V  = vals + nval_ptr[leaf];
+          for (int64_t row = warp; row < nr; row += nw)
+            {
+              const T *v  = V + row * ld;
+              T        s0 = T(0);
+#pragma unroll 4
+              for (int j = lane; j < n4; j += 32)
+                {
+                  T a[4];
+                  load4(v + 4 * j, a);
+                  s0 = dot4_acc(s0, a, sx + 4 * j);
+                }
+              const T t = warp_sum(s0);
+              if (lane == 0)
+                {
+                  T &o = y[nrows[r0 + row]];
+                  o    = acc ? o + t : t;
+                }
+            }
+        }
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+
     // P2M apply: M^[leaf][r][k] = sum_rows w(row, r) T[row][k] x_r[dof(row)],
     // w selecting the double layer (Ker1), the single layer (Ker2) or the
     // combined system strengths.  One warp per leaf, 8 leaves per block: lane l
@@ -474,8 +559,9 @@ namespace pibem
     // M2P phase 1: one thread per (pair, node of the pair's target box):
     // scratch[r][item] = multipole of the source box evaluated at the node.
     template <typename T>
-    __global__ void m2p_eval_kernel(int64_t n_items, int64_t n_pairs, int R, int K, int p,
+    __global__ void m2p_eval_kernel(int64_t n_items, int R, int K, int p,
                                     const int64_t *__restrict__ item_ptr,
+                                    const int32_t *__restrict__ item_pair,
                                     const int32_t *__restrict__ pair_tgt,
                                     const int32_t *__restrict__ tgt,
                                     const int32_t *__restrict__ src,
@@ -489,16 +575,7 @@ namespace pibem
       const int64_t it = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (it >= n_items)
         return;
-      int64_t lo = 0, hi = n_pairs - 1;
-      while (lo < hi)
-        {
-          int64_t mid = (lo + hi + 1) >> 1;
-          if (item_ptr[mid] <= it)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-      const int64_t e    = lo;
+      const int64_t e    = item_pair[it];
       const int64_t t    = tgt[pair_tgt[e]];
       const int64_t s    = src[e];
       const int     node = node_sorted[nbeg[t] + (it - item_ptr[e])];
@@ -512,52 +589,48 @@ namespace pibem
           eval_expansion_fast<T, T>(M + (s * R + r) * K, p, rx, ry, rz, true) * ih;
     }
 
-    // M2P phase 2: one thread per (target box node): fixed-order sum over the
-    // box's sources, added to y.
+    // M2P phase 2: one warp per target box, one lane per node of the box: the
+    // node's values over the box's sources, added in list order to y.  The
+    // items of a target box are contiguous, source-major (item_ptr[e] =
+    // item_ptr[e0] + (e - e0) nn), so a node's values sit nn apart; 16 loads
+    // in flight.
     template <typename T>
-    __global__ void m2p_sum_kernel(int64_t n_tnodes, int n_tgt, int R, int N, int64_t n_items,
-                                   const int64_t *__restrict__ tnode_ptr,
-                                   const int32_t *__restrict__ tgt,
-                                   const int64_t *__restrict__ src_ptr,
-                                   const int64_t *__restrict__ item_ptr,
-                                   const int32_t *__restrict__ nbeg,
-                                   const int32_t *__restrict__ node_sorted,
-                                   const T *__restrict__ scratch, T *__restrict__ y)
+    __global__ void __launch_bounds__(256)
+      m2p_sum_kernel(int n_tgt, int R, int N, int64_t n_items, const int64_t *__restrict__ tnode_ptr,
+                     const int32_t *__restrict__ tgt, const int64_t *__restrict__ src_ptr,
+                     const int64_t *__restrict__ item_ptr, const int32_t *__restrict__ nbeg,
+                     const int32_t *__restrict__ node_sorted, const T *__restrict__ scratch,
+                     T *__restrict__ y)
     {
-      const int64_t tn = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (tn >= n_tnodes)
+      const int ti = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+      if (ti >= n_tgt)
         return;
-      int lo = 0, hi = n_tgt - 1;
-      while (lo < hi)
+      const int64_t  nn = tnode_ptr[ti + 1] - tnode_ptr[ti];
+      const int64_t  e0 = src_ptr[ti], ns = src_ptr[ti + 1] - e0;
+      const int64_t  base = e0 < src_ptr[n_tgt] ? item_ptr[e0] : 0;
+      const int32_t *nodes = node_sorted + nbeg[tgt[ti]];
+      for (int64_t i = lane; i < nn; i += 32)
         {
-          int mid = (lo + hi + 1) >> 1;
-          if (tnode_ptr[mid] <= tn)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-      const int64_t i    = tn - tnode_ptr[lo];
-      const int     node = node_sorted[nbeg[tgt[lo]] + i];
-      const int64_t e0 = src_ptr[lo], e1 = src_ptr[lo + 1];
-      for (int r = 0; r < R; ++r)
-        {
-          // 8 loads in flight, added in list order
-          const T *sc  = scratch + int64_t(r) * n_items + i;
-          T        acc = T(0);
-          int64_t  e   = e0;
-          for (; e + 8 <= e1; e += 8)
+          const int node = nodes[i];
+          for (int r = 0; r < R; ++r)
             {
-              T v[8];
+              const T *sc  = scratch + int64_t(r) * n_items + base + i;
+              T        acc = T(0);
+              int64_t  j   = 0;
+              for (; j + 16 <= ns; j += 16)
+                {
+                  T v[16];
 #pragma unroll
-              for (int u = 0; u < 8; ++u)
-                v[u] = sc[item_ptr[e + u]];
+                  for (int u = 0; u < 16; ++u)
+                    v[u] = sc[(j + u) * nn];
 #pragma unroll
-              for (int u = 0; u < 8; ++u)
-                acc += v[u];
+                  for (int u = 0; u < 16; ++u)
+                    acc += v[u];
+                }
+              for (; j < ns; ++j)
+                acc += sc[j * nn];
+              y[int64_t(r) * N + node] += acc;
             }
-          for (; e < e1; ++e)
-            acc += sc[item_ptr[e]];
-          y[int64_t(r) * N + node] += acc;
         }
     }
 
@@ -627,9 +700,25 @@ namespace pibem
     int           rb    = int(std::max<int64_t>(1, (96 * 1024) / (maxnc * int64_t(sizeof(T)))));
     rb                  = std::min(rb, R);
     const size_t smem   = size_t(rb) * maxnc * sizeof(T);
-    // R == 1: the one-column kernel (fewer registers, more loads in flight);
-    // both compute a column with the same rounding steps in the same order
-    auto kern = R == 1 ? near_leaf_kernel<T, true> : near_leaf_kernel<T, false>;
+    if (R == 1)
+      {
+        // one column: the software-pipelined persistent kernel (a row is
+        // computed with the same rounding steps in the same order as below)
+        int dev = 0, n_sm = 1;
+        PIBEM_CUDA(cudaGetDevice(&dev));
+        PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+        const size_t smem1 = size_t(2) * maxnc * sizeof(T);
+        if (smem1 > 48 * 1024)
+          raise_smem_limit(reinterpret_cast<const void *>(near_leaf_pipe_kernel<T>), smem1);
+        const int grid = std::min(op.n_near_leaves, 6 * n_sm);
+        near_leaf_pipe_kernel<T><<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr,
+                                                         op.ncol_ptr, op.nval_ptr, op.nrows,
+                                                         op.ncols, vals, x, y, accumulate);
+        PIBEM_CUDA(cudaGetLastError());
+        note_launch();
+        return;
+      }
+    auto kern = near_leaf_kernel<T, false>;
     if (smem > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
     kern<<<op.n_near_leaves, 256, smem, s>>>(R, rb, N, op.nrow_ptr, op.ncol_ptr, op.nval_ptr,
@@ -786,13 +875,14 @@ namespace pibem
     if (op.n_m2p_tgt == 0)
       return;
     m2p_eval_kernel<T><<<unsigned((op.n_m2p_items + 127) / 128), 128, 0, s>>>(
-      op.n_m2p_items, op.n_m2p_pairs, R, op.K, op.p, op.m2p_item_ptr, op.m2p_pair_tgt, op.m2p_tgt,
-      op.m2p_src, td.nbeg, td.node_sorted, td.xyz, td.center, td.delta, M, op.m2p_scratch);
+      op.n_m2p_items, R, op.K, op.p, op.m2p_item_ptr, op.m2p_item_pair, op.m2p_pair_tgt,
+      op.m2p_tgt, op.m2p_src, td.nbeg, td.node_sorted, td.xyz, td.center, td.delta, M,
+      op.m2p_scratch);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
-    m2p_sum_kernel<T><<<unsigned((op.n_m2p_tnodes + 127) / 128), 128, 0, s>>>(
-      op.n_m2p_tnodes, op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt,
-      op.m2p_src_ptr, op.m2p_item_ptr, td.nbeg, td.node_sorted, op.m2p_scratch, y);
+    m2p_sum_kernel<T><<<unsigned((op.n_m2p_tgt + 7) / 8), 256, 0, s>>>(
+      op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt, op.m2p_src_ptr,
+      op.m2p_item_ptr, td.nbeg, td.node_sorted, op.m2p_scratch, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

@@ -33,6 +33,7 @@ namespace pibem
         {
           const double *v = Vr + int64_t(i) * ldv;
           double        s = 0;
+#pragma unroll 8
           for (int64_t t = t0 + lane; t < t1; t += 32)
             s += v[t] * wr[t];
           for (int o = 16; o > 0; o >>= 1)
@@ -70,6 +71,7 @@ namespace pibem
         return;
       int64_t r = idx / n, t = idx % n;
       double  s = 0;
+#pragma unroll 8
       for (int i = 0; i < ncols; ++i)
         s += V[r * ldr + int64_t(i) * ldv + t] * h[r * ldh + i];
       w[idx] -= sign * s;
@@ -206,40 +208,52 @@ namespace pibem
       x[idx] += shift[idx / n];
     }
 
-    // z[node] = sum_c Pinv[leaf][r][c] v[rows_c]  (leaf-block Jacobi, right preconditioner)
-    // z = P^-1 v on every childless box's rows: one block per box; the box's
-    // entries of v are gathered into shared memory once, then warp k takes rows
-    // k, k + nw, ... with its lanes over the (row-major) inverse block -- the same
-    // products and the same reduction order as one warp per row reading v
-    // directly.
-    __global__ void block_apply_kernel(int R, int64_t n, int64_t ldv,
-                                       const int64_t *__restrict__ row_ptr,
-                                       const int64_t *__restrict__ blk_ptr,
-                                       const int32_t *__restrict__ rows,
-                                       const double *__restrict__ Pinv,
-                                       const double *__restrict__ v, double *__restrict__ z)
+    // z[node] = sum_c Pinv[leaf][r][c] v[rows_c]  (leaf-block Jacobi, right
+    // preconditioner).  One warp per leaf, 8 per block: the leaf's v entries
+    // are gathered into the warp's shared slice, lane i computes rows i, i + 32,
+    // ... with c ascending; the blocks are stored column-major (entry (r, c)
+    // at c * nr + r), so a column is read across the lanes.
+    __global__ void __launch_bounds__(256)
+      block_apply_kernel(int n_leaves, int max_rows, int R, int64_t n, int64_t ldv,
+                         const int64_t *__restrict__ row_ptr, const int64_t *__restrict__ blk_ptr,
+                         const int32_t *__restrict__ rows, const double *__restrict__ Pinv,
+                         const double *__restrict__ v, double *__restrict__ z)
     {
-      extern __shared__ double sv[];
-      const int     leaf = blockIdx.x;
-      const int64_t r0 = row_ptr[leaf], nr = row_ptr[leaf + 1] - r0;
-      const double *P    = Pinv + blk_ptr[leaf];
-      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      extern __shared__ double sv_all[];
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      const int leaf = blockIdx.x * 8 + warp;
+      if (leaf >= n_leaves)
+        return;
+      double       *sv = sv_all + int64_t(warp) * max_rows;
+      const int64_t r0 = row_ptr[leaf];
+      const int     nr = int(row_ptr[leaf + 1] - r0);
+      const double *P  = Pinv + blk_ptr[leaf];
       for (int rr = 0; rr < R; ++rr)
         {
-          for (int64_t c = threadIdx.x; c < nr; c += blockDim.x)
+          for (int c = lane; c < nr; c += 32)
             sv[c] = v[int64_t(rr) * ldv + rows[r0 + c]];
-          __syncthreads();
-          for (int64_t row = warp; row < nr; row += nw)
+          __syncwarp();
+          for (int i = lane; i - lane < nr; i += 32)
             {
               double s = 0;
-              for (int64_t c = lane; c < nr; c += 32)
-                s += P[row * nr + c] * sv[c];
-              for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_xor_sync(0xffffffffu, s, o);
-              if (lane == 0)
-                z[int64_t(rr) * n + rows[r0 + row]] = s;
+              if (i < nr)
+                {
+                  int c = 0;
+                  for (; c + 4 <= nr; c += 4)
+                    {
+                      const double p0 = P[int64_t(c) * nr + i], p1 = P[int64_t(c + 1) * nr + i],
+                                   p2 = P[int64_t(c + 2) * nr + i], p3 = P[int64_t(c + 3) * nr + i];
+                      s += p0 * sv[c];
+                      s += p1 * sv[c + 1];
+                      s += p2 * sv[c + 2];
+                      s += p3 * sv[c + 3];
+                    }
+                  for (; c < nr; ++c)
+                    s += P[int64_t(c) * nr + i] * sv[c];
+                  z[int64_t(rr) * n + rows[r0 + i]] = s;
+                }
             }
-          __syncthreads();
+          __syncwarp();
         }
     }
 
@@ -362,10 +376,12 @@ namespace pibem
   {
     if (n_leaves == 0)
       return;
-    const size_t smem = size_t(std::max(max_rows, 1)) * sizeof(double);
+    const int    mr   = std::max(max_rows, 1);
+    const size_t smem = size_t(8) * mr * sizeof(double);
     if (smem > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel), smem);
-    block_apply_kernel<<<n_leaves, 128, smem, s>>>(R, n, ldv, row_ptr, blk_ptr, rows, Pinv, v, z);
+    block_apply_kernel<<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
+                                                             blk_ptr, rows, Pinv, v, z);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
