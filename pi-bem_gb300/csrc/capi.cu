@@ -166,7 +166,8 @@ struct pibem_handle
   DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
     d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
-    d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_m2p_item_pair;
+    d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_m2p_item_pair, d_m2l_yslot,
+    d_down_m2l_beg, d_down_m2l_end;
   DBuf<uint8_t> d_down_oct;
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc;
@@ -225,7 +226,7 @@ struct pibem_handle
         d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
-        d_m2p_item_pair);
+        d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
@@ -287,7 +288,9 @@ namespace
   void far_alloc(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
                  DBuf<T> &Y, int R)
   {
-    Y.alloc(std::max<size_t>(1, size_t(op.n_pairs) * R * op.K));
+    // rows of K values; the target-major M2L products of the fused level
+    // passes use rows of K rounded up to 4 (16-byte aligned rows)
+    Y.alloc(std::max<size_t>(1, size_t(op.n_pairs) * R * ((op.K + 3) / 4 * 4)));
     const size_t need = size_t(h->tree.nb) * R * op.K;
     if (M.n < need)
       {
@@ -855,6 +858,9 @@ namespace
       op.up_child8     = h->d_up_child8.p;
       op.down_par      = h->d_down_par.p;
       op.down_oct      = h->d_down_oct.p;
+      op.m2l_yslot     = h->d_m2l_yslot.p;
+      op.down_m2l_beg  = h->d_down_m2l_beg.p;
+      op.down_m2l_end  = h->d_down_m2l_end.p;
       op.lv_op0        = int(pl.offsets.size() / 3);
       op.down_l2l_level.assign(pl.down_box_ptr.size(), 0);
       for (size_t l = 0; l + 1 < pl.down_box_ptr.size(); ++l)
@@ -1006,6 +1012,21 @@ namespace
          "level tables");
     for (int32_t v : pl.up_child8)
       need(v >= -1 && v < t.nb, "up child");
+    need(pl.m2l_yslot.size() == size_t(pl.n_m2l) && pl.down_m2l_beg.size() == pl.down_box.size() &&
+           pl.down_m2l_end.size() == pl.down_box.size(),
+         "target-major M2L tables");
+    {
+      std::vector<char> seen(pl.m2l_yslot.size(), 0);
+      for (int32_t v : pl.m2l_yslot)
+        {
+          need(v >= 0 && v < int64_t(seen.size()) && !seen[v], "M2L slot");
+          seen[v] = 1;
+        }
+      for (size_t i = 0; i < pl.down_box.size(); ++i)
+        need(pl.down_m2l_beg[i] >= 0 && pl.down_m2l_beg[i] <= pl.down_m2l_end[i] &&
+               pl.down_m2l_end[i] <= int64_t(pl.m2l_yslot.size()),
+             "M2L slot range");
+    }
     for (size_t i = 0; i < pl.down_box.size(); ++i)
       need(pl.down_par[i] >= -1 && pl.down_par[i] < t.nb && pl.down_oct[i] < 8 &&
              (pl.down_par[i] < 0 || pl.down_q_ptr[i + 1] > pl.down_q_ptr[i]),
@@ -1165,6 +1186,9 @@ namespace
     h->d_up_child8.upload(pl.up_child8, s);
     h->d_down_par.upload(pl.down_par, s);
     h->d_down_oct.upload(pl.down_oct, s);
+    h->d_m2l_yslot.upload(pl.m2l_yslot, s);
+    h->d_down_m2l_beg.upload(pl.down_m2l_beg, s);
+    h->d_down_m2l_end.upload(pl.down_m2l_end, s);
     // M2P work items: one per (pair, node of the pair's target box)
     {
       const size_t         nt = pl.m2p_tgt.size();

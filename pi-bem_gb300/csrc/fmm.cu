@@ -359,7 +359,8 @@ namespace pibem
       trans_gemm_kernel(int R, int K, int chunk0, const int32_t *__restrict__ chunk_start,
                         const int32_t *__restrict__ chunk_cnt, const int32_t *__restrict__ chunk_off,
                         const int32_t *__restrict__ q_src, const T *__restrict__ ops,
-                        const T *__restrict__ M, T *__restrict__ Y)
+                        const T *__restrict__ M, T *__restrict__ Y,
+                        const int32_t *__restrict__ yslot, int ldy)
     {
       extern __shared__ unsigned char smem_raw[];
       T        *sT    = reinterpret_cast<T *>(smem_raw); // [K][K] in-major
@@ -418,12 +419,13 @@ namespace pibem
           const int     cg = c0 + c;
           const int64_t q  = start + cg / R;
           const int     r  = cg % R;
+          const int64_t yr = (yslot ? int64_t(yslot[q]) : q) * R + r; // row of (pair, rhs)
 #pragma unroll
           for (int i = 0; i < KI; ++i)
             {
               const int ko = row0 + tx + 16 * i;
               if (ko < K)
-                Y[(q * R + r) * K + ko] = acc[i][j];
+                Y[yr * ldy + ko] = acc[i][j];
             }
         }
     }
@@ -747,16 +749,26 @@ namespace pibem
     note_launch();
   }
 
+  // The downward pass of the FP32 operator as fused level passes: target-major
+  // M2L products, their sums per box, then L2L level by level.
+  static bool fused_down(const OperatorDev<float> &op, int R)
+  {
+    return op.down_par && op.down_m2l_beg && fused_levels_ok(op.K, R);
+  }
+
+  // Y row of (pair q, rhs r): (yslot ? yslot[q] : q) * R + r, rows of ldy values
   template <typename T>
   static void launch_trans_gemm(const OperatorDev<T> &op, int R, int c0, int c1, const T *E, T *Y,
-                                cudaStream_t s)
+                                cudaStream_t s, const int32_t *yslot = nullptr, int ldy = 0)
   {
     if (c1 <= c0)
       return;
+    if (ldy == 0)
+      ldy = op.K;
     if constexpr (std::is_same<T, float>::value)
       if (op.tc_images)
         {
-          launch_tc_gemm(op, R, c0, c1, E, Y, op.tc_err, s);
+          launch_tc_gemm(op, R, c0, c1, E, Y, yslot, ldy, op.tc_err, s);
           return;
         }
     // largest column count of the chunks in [c0, c1): R x (<= 128 pairs).  A
@@ -797,7 +809,7 @@ namespace pibem
       if (smem > 48 * 1024)
         raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
       kern<<<grid, 256, smem, s>>>(R, op.K, c0, op.ch_start, op.ch_cnt, op.ch_op, op.q_src, op.ops,
-                                   E, Y);
+                                   E, Y, yslot, ldy);
     };
     switch (KI)
       {
@@ -839,9 +851,18 @@ namespace pibem
     launch_gather<T>(R, op.K, b - a, op.up_box + a, op.up_q_ptr + a, op.up_q, Y, M, s);
   }
 
+  // the M2L products of all levels; for the fused level passes in the
+  // target-major order with 16-byte aligned rows (what the M2L sums read)
   template <typename T>
   void launch_m2l_gemm(const OperatorDev<T> &op, int R, const T *M, T *Y, cudaStream_t s)
   {
+    if constexpr (std::is_same<T, float>::value)
+      if (fused_down(op, R))
+        {
+          launch_trans_gemm<T>(op, R, 0, op.m2l_chunk_end, M, Y, s, op.m2l_yslot,
+                               (op.K + 3) / 4 * 4);
+          return;
+        }
     launch_trans_gemm<T>(op, R, 0, op.m2l_chunk_end, M, Y, s);
   }
 
@@ -849,7 +870,7 @@ namespace pibem
   void launch_m2l_sums(const OperatorDev<T> &op, int R, T *Lx, const T *Y, cudaStream_t s)
   {
     if constexpr (std::is_same<T, float>::value)
-      if (op.down_par && fused_levels_ok(op.K, R))
+      if (fused_down(op, R))
         launch_m2l_sums_fused(op, R, Lx, Y, s);
   }
 
@@ -858,7 +879,7 @@ namespace pibem
                              cudaStream_t s)
   {
     if constexpr (std::is_same<T, float>::value)
-      if (op.down_par && fused_levels_ok(op.K, R))
+      if (fused_down(op, R))
         {
           launch_l2l_level_fused(op, R, level, Lx, s);
           return;

@@ -105,6 +105,9 @@ namespace pibem
     const T       *lv_ops    = nullptr; // the 16 level operators, each padded to 16 bytes
     int           *dev_err   = nullptr; // set by a bounded device wait that timed out
     std::vector<char> down_l2l_level; // per level: its boxes receive L2L
+    // target-major M2L products (fused passes): slot of each M2L pair, and the
+    // slot range of each down_box entry
+    const int32_t *m2l_yslot = nullptr, *down_m2l_beg = nullptr, *down_m2l_end = nullptr;
     int64_t        n_pairs = 0;
     int64_t        max_near_cols = 0;
     // tensor-core path of the FP32 translations (null: CUDA-core GEMM)
@@ -170,8 +173,10 @@ namespace pibem
   // hi/lo TF32 images of row-major [out][in] operators in the MMA B layout
   void build_tc_images(const std::vector<double> &ops_out_in, int nops, int K,
                        std::vector<float> &img);
+  // Y row of (pair q, rhs r): (yslot ? yslot[q] : q) * R + r, rows of ldy
+  // values (ldy a multiple of 4 when yslot is given)
   void launch_tc_gemm(const OperatorDev<float> &op, int R, int c0, int c1, const float *E, float *Y,
-                      int *err, cudaStream_t s);
+                      const int32_t *yslot, int ldy, int *err, cudaStream_t s);
 
   // ---- L2 projections onto the Q1 space (projection.cu) ------------------------
   struct ProjectionArgs

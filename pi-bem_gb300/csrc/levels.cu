@@ -126,49 +126,59 @@ namespace pibem
             }
     }
 
-    // M2L sums of the boxes of the downward lists, all levels: one warp per
-    // task (column c = i * R + r, slice of 32 output coefficients), summing
-    // the pair list (the entries of q[q_ptr[i] .. q_ptr[i+1]) after the L2L
-    // entry, which comes first when par[i] >= 0) in order, 32 rows in flight.
-    // Y rows are (pair, rhs) of K values.
+    // M2L sums of the boxes of the downward lists, all levels.  The M2L
+    // products are target-major: the rows (slot, rhs) of a box's pairs are the
+    // slots [beg, end) in list order, rows of Kx = round_up(K, 4) values.  One
+    // warp per column c = i * R + r; lane l adds coefficients 4l..4l+3 over
+    // the box's rows in order, 16 rows in flight.
     __global__ void __launch_bounds__(256)
-      m2l_sum_kernel(int R, int K, int nslice, int64_t ntasks, const int32_t *__restrict__ box,
-                     const int32_t *__restrict__ par, const int64_t *__restrict__ q_ptr,
-                     const int32_t *__restrict__ q, const float *__restrict__ Y,
-                     float *__restrict__ Lx)
+      m2l_sum_kernel(int R, int K, int64_t ncols, const int32_t *__restrict__ box,
+                     const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
+                     const float *__restrict__ Y, float *__restrict__ Lx)
     {
-      const int64_t task = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-      if (task >= ntasks)
+      const int64_t col = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+      if (col >= ncols)
         return;
       const int     lane = threadIdx.x & 31;
-      const int64_t col = task / nslice;
-      const int     sl  = int(task - col * nslice);
       const int     bi = int(col / R), r = int(col - int64_t(bi) * R);
-      const int     ko  = sl * 32 + lane;
-      const int     kc  = ko < K ? ko : K - 1; // idle lanes read a valid element
-      const float  *Yk  = Y + (int64_t(r) * K + kc);
-      const int64_t e0 = q_ptr[bi] + (par[bi] >= 0 ? 1 : 0), e1 = q_ptr[bi + 1];
-      float         s  = 0.0f;
-      for (int64_t eb = e0; eb < e1; eb += 32)
+      const int     n4 = lv_kx(K) / 4;
+      const int     e0 = beg[bi], e1 = end[bi];
+      float4        s  = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane < n4)
         {
-          const int cnt = e1 - eb < 32 ? int(e1 - eb) : 32;
-          const int qr  = lane < cnt ? q[eb + lane] * R : 0; // row of (pair, rhs 0)
-          if (cnt == 32)
+          const float4 *y      = reinterpret_cast<const float4 *>(Y) + (int64_t(e0) * R + r) * n4 + lane;
+          const int64_t stride = int64_t(R) * n4;
+          int           e      = e0;
+          for (; e + 16 <= e1; e += 16)
             {
-              float v[32];
+              float4 v[16];
 #pragma unroll
-              for (int u = 0; u < 32; ++u)
-                v[u] = __ldg(Yk + int64_t(__shfl_sync(0xffffffffu, qr, u)) * K);
+              for (int u = 0; u < 16; ++u)
+                v[u] = __ldg(y + int64_t(e - e0 + u) * stride);
 #pragma unroll
-              for (int u = 0; u < 32; ++u)
-                s += v[u];
+              for (int u = 0; u < 16; ++u)
+                {
+                  s.x += v[u].x;
+                  s.y += v[u].y;
+                  s.z += v[u].z;
+                  s.w += v[u].w;
+                }
             }
-          else
-            for (int u = 0; u < cnt; ++u)
-              s += __ldg(Yk + int64_t(__shfl_sync(0xffffffffu, qr, u)) * K);
+          for (; e < e1; ++e)
+            {
+              const float4 v = __ldg(y + int64_t(e - e0) * stride);
+              s.x += v.x;
+              s.y += v.y;
+              s.z += v.z;
+              s.w += v.w;
+            }
+          float *o = Lx + (int64_t(box[bi]) * R + r) * K + 4 * lane;
+          const float sv[4] = {s.x, s.y, s.z, s.w};
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+            if (4 * lane + c < K)
+              o[c] = sv[c];
         }
-      if (ko < K)
-        Lx[(int64_t(box[bi]) * R + r) * K + ko] = s;
     }
 
     // One level of the downward pass after the M2L sums: L[b] += T_oct L[parent]
@@ -546,11 +556,9 @@ namespace pibem
     const int b = op.down_box_ptr.empty() ? 0 : op.down_box_ptr.back();
     if (b <= a)
       return;
-    const int     K      = op.K;
-    const int     nslice = (K + 31) / 32;
-    const int64_t ntasks = int64_t(b - a) * R * nslice;
-    m2l_sum_kernel<<<unsigned((ntasks + 7) / 8), 256, 0, s>>>(
-      R, K, nslice, ntasks, op.down_box + a, op.down_par + a, op.down_q_ptr + a, op.down_q, Y, Lx);
+    const int64_t ncols = int64_t(b - a) * R;
+    m2l_sum_kernel<<<unsigned((ncols + 7) / 8), 256, 0, s>>>(
+      R, op.K, ncols, op.down_box + a, op.down_m2l_beg + a, op.down_m2l_end + a, Y, Lx);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

@@ -172,8 +172,8 @@ namespace pibem
 
     // Shared-memory layout, byte offsets from the 1024-byte aligned base:
     // stages x [A hi | A lo | B hi | B lo], epilogue staging (per epilogue warp
-    // the larger of a 32 x 33 column-chunk tile and its 32 rows x K, row-major,
-    // + 4 floats of alignment shift), mbarriers.
+    // the largest of a 32 x 33 column-chunk tile, its 32 rows x K row-major + 4
+    // floats of alignment shift, and 32 rows of round_up(K, 4)), mbarriers.
     struct TcLayout
     {
       uint32_t b_bytes, stage_bytes, epi, epi_warp_floats, bars, total;
@@ -185,6 +185,8 @@ namespace pibem
         epi_warp_floats = uint32_t(round_up(32 * K + 4, 4));
         if (epi_warp_floats < 32 * TC_EPI_LD)
           epi_warp_floats = uint32_t(round_up(32 * TC_EPI_LD, 4));
+        if (epi_warp_floats < uint32_t(32 * round_up(K, 4))) // scattered rows of round_up(K, 4)
+          epi_warp_floats = uint32_t(32 * round_up(K, 4));
         bars  = epi + 4 * epi_warp_floats * 4;
         total = bars + (2 * uint32_t(stages) + 5) * 8;
       }
@@ -199,7 +201,8 @@ namespace pibem
                      const int32_t *__restrict__ ch_start, const int32_t *__restrict__ ch_cnt,
                      const int32_t *__restrict__ ch_op, const int32_t *__restrict__ q_src,
                      const float *__restrict__ images, const float *__restrict__ E,
-                     float *__restrict__ Y, int *__restrict__ err)
+                     float *__restrict__ Y, const int32_t *__restrict__ yslot, int ldy,
+                     int *__restrict__ err)
     {
       extern __shared__ uint8_t smem_raw[];
       __shared__ uint32_t       tmem_slot;
@@ -471,7 +474,36 @@ namespace pibem
                   const int row0   = t0 + 32 * q;
                   const int nvalid = min(32, rows_total - row0);
                   float    *ybase  = Y + (int64_t(start) * R + row0) * K;
-                  if (bulk)
+                  if (yslot)
+                    {
+                      // rows to their slots: lane i stages row i (ldy values,
+                      // zero beyond K) and copies it with one bulk store
+                      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                      __syncwarp();
+                      for (int c0 = 0; c0 < Np; c0 += 32)
+                        {
+                          float v[32];
+                          tmem_ld32(tmem + (uint32_t(32 * q) << 16) + uint32_t(a * TC_ACC_COLS + c0), v);
+#pragma unroll
+                          for (int j = 0; j < 32; ++j)
+                            if (c0 + j < ldy)
+                              stg[lane * ldy + c0 + j] = c0 + j < K ? v[j] : 0.0f;
+                        }
+                      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                      __syncwarp();
+                      if (lane < nvalid)
+                        {
+                          const int row = row0 + lane, pq = start + row / R, r = row - (row / R) * R;
+                          float    *dst = Y + (int64_t(yslot[pq]) * R + r) * ldy;
+                          asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                                       :
+                                       : "l"(dst), "r"(stg_s + uint32_t(lane * ldy) * 4u),
+                                         "r"(uint32_t(ldy) * 4u)
+                                       : "memory");
+                          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                        }
+                    }
+                  else if (bulk)
                     {
                       if (pending)
                         {
@@ -534,8 +566,7 @@ namespace pibem
                   mbar_arrive(tempty(a));
                 }
             }
-          if (lane == 0)
-            asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); // bulk stores complete
+          asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); // bulk stores complete
         }
 
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -603,8 +634,10 @@ namespace pibem
   }
 
   void launch_tc_gemm(const OperatorDev<float> &op, int R, int c0, int c1, const float *E, float *Y,
-                      int *err, cudaStream_t s)
+                      const int32_t *yslot, int ldy, int *err, cudaStream_t s)
   {
+    if (yslot && ldy != round_up(op.K, 4))
+      throw Error(PIBEM_EINVAL, "tensor-core translations: slot rows must hold round_up(K, 4) values");
     if (c1 <= c0)
       return;
     int dev = 0, n_sm = 0;
@@ -621,7 +654,7 @@ namespace pibem
     raise_smem_limit(reinterpret_cast<const void *>(fn), g.smem);
     fn<<<std::min(nch, std::max(n_sm, 1)), TC_THREADS, g.smem, s>>>(
       R, op.K, g.Np, g.Kp / TC_KC, c0, nch, op.ch_start, op.ch_cnt, op.ch_op, op.q_src,
-      op.tc_images, E, Y, err);
+      op.tc_images, E, Y, yslot, ldy, err);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

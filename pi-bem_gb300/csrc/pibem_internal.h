@@ -188,6 +188,9 @@ namespace pibem
     // local expansion it receives by L2L (-1: none; then down_q has no L2L entry)
     std::vector<int32_t>  up_child8, down_par;
     std::vector<uint8_t>  down_oct;
+    // target-major M2L products: slot of each M2L pair q (its index in
+    // m2l_src), and per down_box entry the range of its slots
+    std::vector<int32_t>  m2l_yslot, down_m2l_beg, down_m2l_end;
     // M2P pairs grouped by target
     std::vector<int32_t>  m2p_tgt;
     std::vector<int64_t>  m2p_src_ptr;

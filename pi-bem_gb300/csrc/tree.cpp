@@ -621,6 +621,10 @@ namespace pibem
         }
       cut(0, np);
       pl.m2l_chunk_end = int(pl.ch_start.size());
+      // target-major slot of each M2L pair (its place in m2l_src)
+      pl.m2l_yslot.assign(np, 0);
+      for (int64_t e = 0; e < np; ++e)
+        pl.m2l_yslot[qof[e]] = int32_t(e);
       // Levels whose expansions are ever read: multipoles of the boxes at or
       // below the shallowest M2L / M2P source (M2M stops there), locals of
       // the boxes at or below the shallowest M2L target (above it they are
@@ -711,6 +715,8 @@ namespace pibem
               pl.down_box.push_back(b);
               pl.down_oct.push_back(uint8_t(t.digit[b] & 7));
               pl.down_par.push_back(l2l_q[b] >= 0 ? t.parent[b] : -1);
+              pl.down_m2l_beg.push_back(m2l_first[b] >= 0 ? int32_t(pl.m2l_src_ptr[m2l_first[b]]) : 0);
+              pl.down_m2l_end.push_back(m2l_first[b] >= 0 ? int32_t(pl.m2l_src_ptr[m2l_first[b] + 1]) : 0);
               if (l2l_q[b] >= 0)
                 pl.down_q.push_back(int32_t(l2l_q[b]));
               if (m2l_first[b] >= 0)
