@@ -170,7 +170,11 @@ struct pibem_handle
     d_down_m2l_beg, d_down_m2l_end;
   DBuf<uint8_t> d_down_oct;
   DBuf<NearEntry> d_entries;
-  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc;
+  DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Tc;
+  // leaf-block Jacobi inverses, column-major: FP32 for the mixed path, FP64
+  // for the plain FP64 path
+  DBuf<float>   d_Pinv;
+  DBuf<double>  d_Pinv64;
   DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg, d_Tcf, d_lvopsf;
   DBuf<float2>  d_opsff; // the FP64 operator table as (hi, lo) FP32 pairs
   DBuf<int>     d_err;
@@ -227,7 +231,7 @@ struct pibem_handle
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
         d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end);
-    add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
+    add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
         d_y32, d_m2p32, d_Y32);
@@ -631,6 +635,21 @@ namespace
                                  size_t(n) * sizeof(double), size_t(R), cudaMemcpyDeviceToDevice, s));
   }
 
+  // z = P^-1 v for R columns (v column stride ldv): the FP64 inverses where the
+  // handle keeps them (GMRES on an FP64-accurate operator), else the FP32 ones
+  void apply_block_jacobi(pibem_handle *h, int R, const double *v, int64_t ldv, double *z,
+                          cudaStream_t s)
+  {
+    const int     nl = int(h->blk_ptr.size()) - 1;
+    const int64_t N  = h->N();
+    if (h->d_Pinv64.p)
+      launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
+                         h->d_Pinv64.p, v, ldv, z, s);
+    else
+      launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
+                         h->d_Pinv.p, v, ldv, z, s);
+  }
+
   GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
                     const std::vector<double> &tol, int maxit, int m,
                     const std::function<void(const double *, double *)> &A, bool prec)
@@ -690,9 +709,7 @@ namespace
             // z = P^-1 V_j ; w = A z
             const double *vj = h->g_V.p + int64_t(j) * N;
             if (prec)
-              launch_block_apply(int(h->blk_ptr.size()) - 1, h->max_leaf_rows, R, N,
-                                 h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, vj, ldr,
-                                 h->g_z.p, s);
+              apply_block_jacobi(h, R, vj, ldr, h->g_z.p, s);
             else
               copy_cols(h->g_z.p, N, vj, ldr, N, R, s);
             A(h->g_z.p, h->g_w.p);
@@ -766,8 +783,7 @@ namespace
         launch_gemv_sub(N, R, kmax, N, ldr, h->g_V.p, h->g_y.p, m + 1, h->g_u.p, -1.0, s);
         if (prec)
           {
-            launch_block_apply(int(h->blk_ptr.size()) - 1, h->max_leaf_rows, R, N, h->d_nrow_ptr.p,
-                               h->d_blk_ptr.p, h->d_nrows.p, h->d_Pinv.p, h->g_u.p, N, h->g_z.p, s);
+            apply_block_jacobi(h, R, h->g_u.p, N, h->g_z.p, s);
             launch_axpby(int64_t(R) * N, 1.0, h->g_z.p, 1.0, x, s);
           }
         else
@@ -816,7 +832,11 @@ namespace
           for (int j2 = i + 1; j2 < n; ++j2)
             std::swap(b[size_t(i) * n + j2], b[size_t(j2) * n + i]);
       }
-    h->d_Pinv.upload(inv, s);
+    std::vector<float> inv32(inv.begin(), inv.end());
+    h->d_Pinv.upload(inv32, s);
+    h->d_Pinv64.release();
+    if (h->prm.precision_mode != PIBEM_PRECISION_MIXED) // solves on an FP64-accurate operator
+      h->d_Pinv64.upload(inv, s);
   }
 
   void fill_operator_views(pibem_handle *h)

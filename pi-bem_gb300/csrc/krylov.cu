@@ -209,48 +209,55 @@ namespace pibem
     }
 
     // z[node] = sum_c Pinv[leaf][r][c] v[rows_c]  (leaf-block Jacobi, right
-    // preconditioner).  One warp per leaf, 8 per block: the leaf's v entries
-    // are gathered into the warp's shared slice, lane i computes rows i, i + 32,
-    // ... with c ascending; the blocks are stored column-major (entry (r, c)
-    // at c * nr + r), so a column is read across the lanes.
+    // preconditioner), in the precision P of the stored inverses: FP32 for the
+    // mixed path's inner solves (GB300's FP64 rate is 1/58 of its FP32 rate),
+    // FP64 for the plain FP64 path (whose GMRES would otherwise see the FP32
+    // rounding as a nonlinearity near its 1e-8 target).  One warp per leaf, 8
+    // per block: the leaf's v entries are gathered into the warp's shared
+    // slice, lane i computes rows i, i + 32, ... with c ascending; the blocks
+    // are stored column-major (entry (r, c) at c * nr + r), so a column is read
+    // across the lanes.
+    template <typename P>
     __global__ void __launch_bounds__(256)
       block_apply_kernel(int n_leaves, int max_rows, int R, int64_t n, int64_t ldv,
                          const int64_t *__restrict__ row_ptr, const int64_t *__restrict__ blk_ptr,
-                         const int32_t *__restrict__ rows, const double *__restrict__ Pinv,
+                         const int32_t *__restrict__ rows, const P *__restrict__ Pinv,
                          const double *__restrict__ v, double *__restrict__ z)
     {
-      extern __shared__ double sv_all[];
+      extern __shared__ __align__(8) unsigned char sv_raw[];
+      P        *sv_all = reinterpret_cast<P *>(sv_raw);
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int leaf = blockIdx.x * 8 + warp;
       if (leaf >= n_leaves)
         return;
-      double       *sv = sv_all + int64_t(warp) * max_rows;
+      P            *sv = sv_all + int64_t(warp) * max_rows;
       const int64_t r0 = row_ptr[leaf];
       const int     nr = int(row_ptr[leaf + 1] - r0);
-      const double *P  = Pinv + blk_ptr[leaf];
+      const P      *B  = Pinv + blk_ptr[leaf];
       for (int rr = 0; rr < R; ++rr)
         {
           for (int c = lane; c < nr; c += 32)
-            sv[c] = v[int64_t(rr) * ldv + rows[r0 + c]];
+            sv[c] = P(v[int64_t(rr) * ldv + rows[r0 + c]]);
           __syncwarp();
           for (int i = lane; i - lane < nr; i += 32)
             {
-              double s = 0;
+              P s = P(0);
               if (i < nr)
                 {
                   int c = 0;
-                  for (; c + 4 <= nr; c += 4)
+                  for (; c + 8 <= nr; c += 8)
                     {
-                      const double p0 = P[int64_t(c) * nr + i], p1 = P[int64_t(c + 1) * nr + i],
-                                   p2 = P[int64_t(c + 2) * nr + i], p3 = P[int64_t(c + 3) * nr + i];
-                      s += p0 * sv[c];
-                      s += p1 * sv[c + 1];
-                      s += p2 * sv[c + 2];
-                      s += p3 * sv[c + 3];
+                      P p[8];
+#pragma unroll
+                      for (int u = 0; u < 8; ++u)
+                        p[u] = B[int64_t(c + u) * nr + i];
+#pragma unroll
+                      for (int u = 0; u < 8; ++u)
+                        s = fma(p[u], sv[c + u], s);
                     }
                   for (; c < nr; ++c)
-                    s += P[int64_t(c) * nr + i] * sv[c];
-                  z[int64_t(rr) * n + rows[r0 + i]] = s;
+                    s = fma(B[int64_t(c) * nr + i], sv[c], s);
+                  z[int64_t(rr) * n + rows[r0 + i]] = double(s);
                 }
             }
           __syncwarp();
@@ -370,21 +377,28 @@ namespace pibem
     note_launch();
   }
 
+  template <typename P>
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
-                          const int64_t *blk_ptr, const int32_t *rows, const double *Pinv,
+                          const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,
                           const double *v, int64_t ldv, double *z, cudaStream_t s)
   {
     if (n_leaves == 0)
       return;
     const int    mr   = std::max(max_rows, 1);
-    const size_t smem = size_t(8) * mr * sizeof(double);
+    const size_t smem = size_t(8) * mr * sizeof(P);
     if (smem > 48 * 1024)
-      raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel), smem);
-    block_apply_kernel<<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
-                                                             blk_ptr, rows, Pinv, v, z);
+      raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel<P>), smem);
+    block_apply_kernel<P><<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
+                                                                blk_ptr, rows, Pinv, v, z);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
+  template void launch_block_apply<float>(int, int, int, int64_t, const int64_t *, const int64_t *,
+                                          const int32_t *, const float *, const double *, int64_t,
+                                          double *, cudaStream_t);
+  template void launch_block_apply<double>(int, int, int, int64_t, const int64_t *, const int64_t *,
+                                           const int32_t *, const double *, const double *, int64_t,
+                                           double *, cudaStream_t);
 
   template <typename T>
   void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,

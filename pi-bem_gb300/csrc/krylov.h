@@ -20,7 +20,8 @@ namespace pibem
   void launch_scatter(int64_t n, int R, const double *sol, const uint8_t *dir, double *phi,
                       double *dphi, cudaStream_t s);
   void launch_add_scalar(int64_t n, int R, const double *shift, double *x, cudaStream_t s);
+  template <typename P>
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
-                          const int64_t *blk_ptr, const int32_t *rows, const double *Pinv,
+                          const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,
                           const double *v, int64_t ldv, double *z, cudaStream_t s);
 } // namespace pibem
