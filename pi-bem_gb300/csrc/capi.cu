@@ -193,6 +193,7 @@ struct pibem_handle
   // work
   DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64;
   DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32, d_Y32;
+  DBuf<float2> d_Mff, d_Lff; // (hi, lo) expansions of the float-float tree passes
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
@@ -234,7 +235,7 @@ struct pibem_handle
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
-        d_y32, d_m2p32, d_Y32);
+        d_y32, d_m2p32, d_Y32, d_Mff, d_Lff);
     add(g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
         sv_part, sv_nrm);
     for (const auto &b : io_buf)
@@ -303,6 +304,12 @@ namespace
       }
     scr.alloc(std::max<size_t>(1, size_t(op.n_m2p_items) * R));
     op.m2p_scratch = scr.p;
+    if constexpr (std::is_same<T, double>::value)
+      if (op.ops_ff)
+        {
+          h->d_Mff.alloc(need);
+          h->d_Lff.alloc(need);
+        }
   }
 
   // P2M and the upward pass: M of every box
@@ -314,6 +321,18 @@ namespace
     PIBEM_CUDA(cudaMemsetAsync(M.p, 0, need * sizeof(T), s));
     launch_p2m_apply<T>(op, R, int(h->N()), h->d_dir.p, modes, x, M.p, combined, s);
     record(h, 2);
+    if constexpr (std::is_same<T, double>::value)
+      if (op.ops_ff)
+        {
+          // float-float passes on (hi, lo) expansions; M back in FP64 for M2P
+          float2 *Mff = h->d_Mff.p, *Yff = reinterpret_cast<float2 *>(Y.p);
+          launch_convert_d2ff(int64_t(need), M.p, Mff, s);
+          for (int l = h->tree.L; l >= 1; --l)
+            launch_upward_level_ff(op, R, l, Mff, Yff, s);
+          launch_convert_ff2d(int64_t(need), Mff, M.p, s);
+          record(h, 3);
+          return;
+        }
     for (int l = h->tree.L; l >= 1; --l)
       launch_upward_level<T>(op, R, l, M.p, Y.p, s);
     record(h, 3);
@@ -324,6 +343,20 @@ namespace
   void far_down(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &Y, int R,
                 cudaStream_t s)
   {
+    if constexpr (std::is_same<T, double>::value)
+      if (op.ops_ff)
+        {
+          // float-float passes on (hi, lo) expansions; L back in FP64 for L2P
+          const size_t need = size_t(h->tree.nb) * R * op.K;
+          float2      *Mff = h->d_Mff.p, *Lff = h->d_Lff.p, *Yff = reinterpret_cast<float2 *>(Y.p);
+          launch_m2l_ff(op, R, Mff, Yff, s);
+          record(h, 4);
+          for (int l = 1; l <= h->tree.L; ++l)
+            launch_downward_level_ff(op, R, l, Lff, Yff, s);
+          launch_convert_ff2d(int64_t(need), Lff, Lx.p, s);
+          record(h, 5);
+          return;
+        }
     launch_m2l_gemm<T>(op, R, M.p, Y.p, s);
     record(h, 4);
     launch_m2l_sums<T>(op, R, Lx.p, Y.p, s);

@@ -12,6 +12,7 @@
 #include <type_traits>
 
 #include "devmath.cuh"
+#include "ffmath.cuh"
 #include "kernels.h"
 
 namespace pibem
@@ -430,35 +431,24 @@ namespace pibem
         }
     }
 
-    // s + c += a * b in FP32-pair ("float-float") arithmetic: a = (hi, lo),
-    // b = (hi, lo) with hi = fl32(x), lo = fl32(x - hi).  The leading product
-    // is split exactly with an FMA (Dekker's TwoProduct), the cross terms are
-    // added to its error, and the leading sum is carried exactly with Knuth's
-    // TwoSum; the lo * lo term (2^-48 relative) is dropped.  Relative error of a
-    // K-term dot product ~ K 2^-47.  Round-to-nearest intrinsics throughout, so
-    // the compiler cannot contract or reassociate the steps.
-    __device__ __forceinline__ void ff_mac(float &s, float &c, float2 a, float2 b)
-    {
-      const float p = __fmul_rn(a.x, b.x);
-      float       e = __fmaf_rn(a.x, b.x, -p);
-      e             = __fmaf_rn(a.x, b.y, e);
-      e             = __fmaf_rn(a.y, b.x, e);
-      const float t = __fadd_rn(s, p);
-      const float z = __fsub_rn(t, s);
-      const float d = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
-      c             = __fadd_rn(c, __fadd_rn(d, e));
-      s             = t;
-    }
+    __device__ __forceinline__ float2 ff_load(const double *p) { return ff_split(*p); }
+    __device__ __forceinline__ float2 ff_load(const float2 *p) { return *p; }
+    __device__ __forceinline__ void   ff_store(double *p, float h, float l) { *p = __dadd_rn(double(h), double(l)); }
+    __device__ __forceinline__ void   ff_store(float2 *p, float h, float l) { *p = ff_norm(h, l); }
 
     // The translation GEMM of the FP64 operator in float-float arithmetic on
-    // the FP32 pipes (FP64 in, FP64 out): same tiling as trans_gemm_kernel,
-    // operator pre-split into (hi, lo) pairs, expansions split on load.
-    template <int KI>
-    __global__ void __launch_bounds__(256, 1)
-      ff_gemm_kernel(int R, int K, int chunk0, const int32_t *__restrict__ chunk_start,
+    // the FP32 pipes: operator pre-split into (hi, lo) pairs; expansions and
+    // products either FP64 (split on load, joined on store) or already in
+    // (hi, lo) form (IO = float2: no FP64 instruction at all).  Thread (tx, ty)
+    // of TX x (64 / CJ) computes rows row0 + tx + TX i (i < RI) and columns
+    // ty + (64 / CJ) j (j < CJ) of a 64-column block of chunk c; TX RI >= K
+    // rows with TX = ceil(K / RI), so at most RI - 1 rows are padding.
+    template <int RI, int CJ, typename IO>
+    __global__ void __launch_bounds__(256, 2)
+      ff_gemm_kernel(int R, int K, int TX, int chunk0, const int32_t *__restrict__ chunk_start,
                      const int32_t *__restrict__ chunk_cnt, const int32_t *__restrict__ chunk_off,
                      const int32_t *__restrict__ q_src, const float2 *__restrict__ ops,
-                     const double *__restrict__ M, double *__restrict__ Y)
+                     const IO *__restrict__ M, IO *__restrict__ Y)
     {
       extern __shared__ __align__(16) unsigned char smem_raw[];
       float2   *sT    = reinterpret_cast<float2 *>(smem_raw); // [K][K] in-major
@@ -478,53 +468,97 @@ namespace pibem
           const int     cg = c0 + c;
           const int64_t q  = start + cg / R;
           const int     r  = cg % R;
-          const double  x  = M[(int64_t(q_src[q]) * R + r) * K + ki];
-          const float   hi = __double2float_rn(x);
-          sB[ki * GB_LDB + c] = make_float2(hi, __double2float_rn(__dsub_rn(x, double(hi))));
+          sB[ki * GB_LDB + c] = ff_load(M + (int64_t(q_src[q]) * R + r) * K + ki);
         }
       __syncthreads();
-      const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, row0 = blockIdx.z * 16 * KI;
-      float     sh[KI][4], sl[KI][4];
+      constexpr int TY = 64 / CJ;
+      const int     tx = threadIdx.x % TX, ty = threadIdx.x / TX, row0 = blockIdx.z * TX * RI;
+      if (ty >= TY)
+        return;
+      float sh[RI][CJ], sl[RI][CJ];
 #pragma unroll
-      for (int i = 0; i < KI; ++i)
+      for (int i = 0; i < RI; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < CJ; ++j)
           sh[i][j] = sl[i][j] = 0.0f;
       for (int ki = 0; ki < K; ++ki)
         {
-          float2 a[KI], b[4];
+          float2 a[RI], b[CJ];
 #pragma unroll
-          for (int i = 0; i < KI; ++i)
+          for (int i = 0; i < RI; ++i)
             {
-              const int ko = row0 + tx + 16 * i;
+              const int ko = row0 + tx + TX * i;
               a[i]         = ko < K ? sT[ki * K + ko] : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
-            b[j] = sB[ki * GB_LDB + ty + 16 * j];
+          for (int j = 0; j < CJ; ++j)
+            b[j] = sB[ki * GB_LDB + ty + TY * j];
 #pragma unroll
-          for (int i = 0; i < KI; ++i)
+          for (int i = 0; i < RI; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+            for (int j = 0; j < CJ; ++j)
               ff_mac(sh[i][j], sl[i][j], a[i], b[j]);
         }
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int j = 0; j < CJ; ++j)
         {
-          const int c = ty + 16 * j;
+          const int c = ty + TY * j;
           if (c >= nc)
             continue;
           const int     cg = c0 + c;
           const int64_t q  = start + cg / R;
           const int     r  = cg % R;
 #pragma unroll
-          for (int i = 0; i < KI; ++i)
+          for (int i = 0; i < RI; ++i)
             {
-              const int ko = row0 + tx + 16 * i;
+              const int ko = row0 + tx + TX * i;
               if (ko < K)
-                Y[(q * R + r) * K + ko] = __dadd_rn(double(sh[i][j]), double(sl[i][j]));
+                ff_store(Y + (q * R + r) * K + ko, sh[i][j], sl[i][j]);
             }
         }
+    }
+
+    // out[box] = sum of the box's (hi, lo) translation products, in list order,
+    // in float-float arithmetic; 8 loads in flight.
+    __global__ void gather_ff_kernel(int R, int K, const int32_t *__restrict__ boxes,
+                                     const int64_t *__restrict__ q_ptr,
+                                     const int32_t *__restrict__ q, const float2 *__restrict__ Y,
+                                     float2 *__restrict__ out)
+    {
+      const int64_t b  = boxes[blockIdx.x];
+      const int64_t e0 = q_ptr[blockIdx.x], e1 = q_ptr[blockIdx.x + 1];
+      const int64_t RK = int64_t(R) * K;
+      for (int i = threadIdx.x; i < R * K; i += blockDim.x)
+        {
+          float2  acc = make_float2(0.0f, 0.0f);
+          int64_t e   = e0;
+          for (; e + 8 <= e1; e += 8)
+            {
+              float2 v[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                v[u] = Y[int64_t(q[e + u]) * RK + i];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                acc = ff_add(acc, v[u]);
+            }
+          for (; e < e1; ++e)
+            acc = ff_add(acc, Y[int64_t(q[e]) * RK + i]);
+          out[b * RK + i] = acc;
+        }
+    }
+
+    __global__ void d2ff_kernel(int64_t n, const double *__restrict__ a, float2 *__restrict__ b)
+    {
+      const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i < n)
+        b[i] = ff_split(a[i]);
+    }
+    __global__ void ff2d_kernel(int64_t n, const float2 *__restrict__ a, double *__restrict__ b)
+    {
+      const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (i < n)
+        b[i] = ff_join(a[i]);
     }
 
     // out[box] = sum of the box's translation products Y[q], in list order.  The
@@ -756,6 +790,98 @@ namespace pibem
     return op.down_par && op.down_m2l_beg && fused_levels_ok(op.K, R);
   }
 
+  // The float-float translation GEMM for chunks [c0, c1); IO = double (FP64
+  // expansions) or float2 ((hi, lo) expansions).  A launch with fewer blocks
+  // than ~2 per SM splits the rows over blockIdx.z (16 per block).
+  template <typename IO>
+  void launch_ff_gemm(const OperatorDev<double> &op, int R, int c0, int c1, const IO *E, IO *Y,
+                      cudaStream_t s)
+  {
+    if (c1 <= c0)
+      return;
+    const int      K  = op.K;
+    const unsigned gx = unsigned(c1 - c0),
+                   gy = unsigned((op.max_chunk_pairs * R + GB_COLS - 1) / GB_COLS);
+    const bool     split = int64_t(gx) * gy < 256;
+    const int      RI    = split ? 1 : std::min(4, (K + 31) / 32);
+    const int      TX    = split ? 16 : (K + RI - 1) / RI;
+    const int      CJ    = split ? 4 : 8; // columns per thread (split: 16 x 16 threads)
+    const dim3     grid(gx, gy, split ? unsigned((K + 15) / 16) : 1u);
+    const size_t   smem = (size_t(K) * K + size_t(K) * GB_LDB) * sizeof(float2);
+    if (K > 128)
+      throw Error(PIBEM_EINVAL, "float-float translations: K = (p+1)^2 above 128");
+    auto launch = [&](auto kern) {
+      if (smem > 48 * 1024)
+        raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
+      kern<<<grid, (64 / CJ) * TX, smem, s>>>(R, K, TX, c0, op.ch_start, op.ch_cnt, op.ch_op,
+                                              op.q_src, op.ops_ff, E, Y);
+    };
+    if (CJ == 4)
+      launch(ff_gemm_kernel<1, 4, IO>);
+    else
+      switch (RI)
+        {
+          case 1: launch(ff_gemm_kernel<1, 8, IO>); break;
+          case 2: launch(ff_gemm_kernel<2, 8, IO>); break;
+          case 3: launch(ff_gemm_kernel<3, 8, IO>); break;
+          default: launch(ff_gemm_kernel<4, 8, IO>); break;
+        }
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+  template void launch_ff_gemm<double>(const OperatorDev<double> &, int, int, int, const double *,
+                                       double *, cudaStream_t);
+  template void launch_ff_gemm<float2>(const OperatorDev<double> &, int, int, int, const float2 *,
+                                       float2 *, cudaStream_t);
+
+  // the FP64-accurate tree passes on (hi, lo) expansions
+  void launch_upward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *M, float2 *Y,
+                              cudaStream_t s)
+  {
+    launch_ff_gemm<float2>(op, R, op.up_chunk_ptr[level], op.up_chunk_ptr[level + 1], M, Y, s);
+    const int a = op.up_box_ptr[level], b = op.up_box_ptr[level + 1];
+    if (b > a)
+      {
+        gather_ff_kernel<<<b - a, R * op.K >= 128 ? 128 : 96, 0, s>>>(
+          R, op.K, op.up_box + a, op.up_q_ptr + a, op.up_q, Y, M);
+        PIBEM_CUDA(cudaGetLastError());
+        note_launch();
+      }
+  }
+  void launch_m2l_ff(const OperatorDev<double> &op, int R, const float2 *M, float2 *Y, cudaStream_t s)
+  {
+    launch_ff_gemm<float2>(op, R, 0, op.m2l_chunk_end, M, Y, s);
+  }
+  void launch_downward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *Lx,
+                                float2 *Y, cudaStream_t s)
+  {
+    launch_ff_gemm<float2>(op, R, op.down_chunk_ptr[level], op.down_chunk_ptr[level + 1], Lx, Y, s);
+    const int a = op.down_box_ptr[level], b = op.down_box_ptr[level + 1];
+    if (b > a)
+      {
+        gather_ff_kernel<<<b - a, R * op.K >= 128 ? 128 : 96, 0, s>>>(
+          R, op.K, op.down_box + a, op.down_q_ptr + a, op.down_q, Y, Lx);
+        PIBEM_CUDA(cudaGetLastError());
+        note_launch();
+      }
+  }
+  void launch_convert_d2ff(int64_t n, const double *a, float2 *b, cudaStream_t s)
+  {
+    if (n == 0)
+      return;
+    d2ff_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, a, b);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+  void launch_convert_ff2d(int64_t n, const float2 *a, double *b, cudaStream_t s)
+  {
+    if (n == 0)
+      return;
+    ff2d_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, a, b);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
   // Y row of (pair q, rhs r): (yslot ? yslot[q] : q) * R + r, rows of ldy values
   template <typename T>
   static void launch_trans_gemm(const OperatorDev<T> &op, int R, int c0, int c1, const T *E, T *Y,
@@ -782,26 +908,7 @@ namespace pibem
     if constexpr (std::is_same<T, double>::value)
       if (op.ops_ff)
         {
-          const size_t smem = (size_t(op.K) * op.K + size_t(op.K) * GB_LDB) * sizeof(float2);
-          auto launch = [&](auto kern) {
-            if (smem > 48 * 1024)
-              raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
-            kern<<<grid, 256, smem, s>>>(R, op.K, c0, op.ch_start, op.ch_cnt, op.ch_op, op.q_src,
-                                         op.ops_ff, E, Y);
-          };
-          switch (KI)
-            {
-              case 1: launch(ff_gemm_kernel<1>); break;
-              case 2: launch(ff_gemm_kernel<2>); break;
-              case 3: launch(ff_gemm_kernel<3>); break;
-              case 4: launch(ff_gemm_kernel<4>); break;
-              case 5: launch(ff_gemm_kernel<5>); break;
-              case 6: launch(ff_gemm_kernel<6>); break;
-              case 7: launch(ff_gemm_kernel<7>); break;
-              default: launch(ff_gemm_kernel<8>); break;
-            }
-          PIBEM_CUDA(cudaGetLastError());
-          note_launch();
+          launch_ff_gemm<double>(op, R, c0, c1, E, Y, s);
           return;
         }
     const size_t smem = (size_t(op.K) * op.K + size_t(op.K) * GB_LDB) * sizeof(T);

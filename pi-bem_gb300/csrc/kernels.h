@@ -142,6 +142,19 @@ namespace pibem
   template <typename T>
   void launch_m2p(const OperatorDev<T> &op, const TreeDev &td, int R, int N, const T *M, T *y,
                   cudaStream_t s);
+  // FP64-accurate tree passes on (hi, lo) float-float expansions (fmm.cu):
+  // the translation GEMM, per-level passes with float-float sums, conversions
+  template <typename IO>
+  void launch_ff_gemm(const OperatorDev<double> &op, int R, int c0, int c1, const IO *E, IO *Y,
+                      cudaStream_t s);
+  void launch_upward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *M, float2 *Y,
+                              cudaStream_t s);
+  void launch_m2l_ff(const OperatorDev<double> &op, int R, const float2 *M, float2 *Y,
+                     cudaStream_t s);
+  void launch_downward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *Lx,
+                                float2 *Y, cudaStream_t s);
+  void launch_convert_d2ff(int64_t n, const double *a, float2 *b, cudaStream_t s);
+  void launch_convert_ff2d(int64_t n, const float2 *a, double *b, cudaStream_t s);
   // M2L sums of all levels into Lx (the first step of the downward pass, before
   // the levels); does nothing unless the fused level passes apply
   template <typename T>
