@@ -159,10 +159,9 @@ namespace pibem
   // the levels); does nothing unless the fused level passes apply
   template <typename T>
   void launch_m2l_sums(const OperatorDev<T> &op, int R, T *Lx, const T *Y, cudaStream_t s);
-  // fused level passes of the FP32 operator (levels.cu), used for R up to
-  // FUSED_LEVEL_MAX_R columns: M2L sums of all levels in one launch, then one
-  // launch per level, no gathers
-  constexpr int FUSED_LEVEL_MAX_R = 16;
+  // fused level passes of the FP32 operator (levels.cu), for every column
+  // count (so that a column's result never depends on the batch it is in):
+  // M2L sums of all levels in one launch, then one launch per level, no gathers
   bool          fused_levels_ok(int K, int R);
   size_t        fused_level_ops_floats(int K); // size of OperatorDev::lv_ops
   void launch_m2m_level_fused(const OperatorDev<float> &op, int R, int level, float *M,

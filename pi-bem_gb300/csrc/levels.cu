@@ -497,7 +497,7 @@ namespace pibem
 
   bool fused_levels_ok(int K, int R)
   {
-    return R >= 1 && R <= FUSED_LEVEL_MAX_R && size_t(16) * lv_kx(K) * sizeof(float) <= 48 * 1024;
+    return R >= 1 && size_t(16) * lv_kx(K) * sizeof(float) <= 48 * 1024;
   }
 
   size_t fused_level_ops_floats(int K) { return size_t(16) * lv_kk(K); }
