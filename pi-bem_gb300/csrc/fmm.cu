@@ -217,22 +217,33 @@ namespace pibem
           const int     n4 = int(ld / 4);
           const int64_t r0 = nrow_ptr[leaf], nr = nrow_ptr[leaf + 1] - r0;
           const T      *V  = vals + nval_ptr[leaf];
-          for (int64_t row = warp; row < nr; row += nw)
+          // two rows per warp at a time (rows row and row + nw), four 16-byte
+          // loads of each in flight per lane
+          for (int64_t row = warp; row < nr; row += 2 * nw)
             {
-              const T *v  = V + row * ld;
-              T        s0 = T(0);
+              const bool two = row + nw < nr;
+              const T   *v0  = V + row * ld;
+              const T   *v1  = V + (two ? row + nw : row) * ld;
+              T          s0 = T(0), s1 = T(0);
 #pragma unroll 4
               for (int j = lane; j < n4; j += 32)
                 {
-                  T a[4];
-                  load4(v + 4 * j, a);
-                  s0 = dot4_acc(s0, a, sx + 4 * j);
+                  T a0[4], a1[4];
+                  load4(v0 + 4 * j, a0);
+                  load4(v1 + 4 * j, a1);
+                  s0 = dot4_acc(s0, a0, sx + 4 * j);
+                  s1 = dot4_acc(s1, a1, sx + 4 * j);
                 }
-              const T t = warp_sum(s0);
+              const T t0 = warp_sum(s0), t1 = warp_sum(s1);
               if (lane == 0)
                 {
-                  T &o = y[nrows[r0 + row]];
-                  o    = acc ? o + t : t;
+                  T &o0 = y[nrows[r0 + row]];
+                  o0    = acc ? o0 + t0 : t0;
+                  if (two)
+                    {
+                      T &o1 = y[nrows[r0 + row + nw]];
+                      o1    = acc ? o1 + t1 : t1;
+                    }
                 }
             }
         }
@@ -616,10 +627,23 @@ namespace pibem
       const int64_t s    = src[e];
       const int     node = node_sorted[nbeg[t] + (it - item_ptr[e])];
       const double  h    = delta[s];
-      const T       rx   = T((xyz[3 * int64_t(node)] - center[3 * s]) / h);
-      const T       ry   = T((xyz[3 * int64_t(node) + 1] - center[3 * s + 1]) / h);
-      const T       rz   = T((xyz[3 * int64_t(node) + 2] - center[3 * s + 2]) / h);
-      const T       ih   = T(1.0 / h);
+      T             rx, ry, rz, ih;
+      if constexpr (std::is_same<T, float>::value)
+        {
+          // FP32 operator: the offset from the centre in FP64 (no cancellation),
+          // scaled in FP32 (GB300's FP64 divide would dominate this kernel)
+          ih = __frcp_rn(float(h));
+          rx = float(xyz[3 * int64_t(node)] - center[3 * s]) * ih;
+          ry = float(xyz[3 * int64_t(node) + 1] - center[3 * s + 1]) * ih;
+          rz = float(xyz[3 * int64_t(node) + 2] - center[3 * s + 2]) * ih;
+        }
+      else
+        {
+          rx = (xyz[3 * int64_t(node)] - center[3 * s]) / h;
+          ry = (xyz[3 * int64_t(node) + 1] - center[3 * s + 1]) / h;
+          rz = (xyz[3 * int64_t(node) + 2] - center[3 * s + 2]) / h;
+          ih = 1.0 / h;
+        }
       for (int r = 0; r < R; ++r)
         scratch[int64_t(r) * n_items + it] =
           eval_expansion_fast<T, T>(M + (s * R + r) * K, p, rx, ry, rz, true) * ih;
