@@ -194,6 +194,11 @@ struct pibem_handle
   DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64;
   DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32, d_Y32;
   DBuf<float2> d_Mff, d_Lff; // (hi, lo) expansions of the float-float tree passes
+  // tensor-core FP64-accurate M2L: operator digit images and row exponents,
+  // expansion digits and row exponents (work)
+  DBuf<uint16_t> d_ozimg, d_ozslc;
+  DBuf<int16_t>  d_ozecol;
+  DBuf<int>      d_ozerow;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
@@ -235,7 +240,7 @@ struct pibem_handle
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
-        d_y32, d_m2p32, d_Y32, d_Mff, d_Lff);
+        d_y32, d_m2p32, d_Y32, d_Mff, d_Lff, d_ozimg, d_ozslc, d_ozecol, d_ozerow);
     add(g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
         sv_part, sv_nrm);
     for (const auto &b : io_buf)
@@ -349,7 +354,18 @@ namespace
           // float-float passes on (hi, lo) expansions; L back in FP64 for L2P
           const size_t need = size_t(h->tree.nb) * R * op.K;
           float2      *Mff = h->d_Mff.p, *Lff = h->d_Lff.p, *Yff = reinterpret_cast<float2 *>(Y.p);
-          launch_m2l_ff(op, R, Mff, Yff, s);
+          if (op.oz_images && op.dev_err)
+            {
+              // tensor-core FP64-accurate M2L from the digits of the multipoles
+              const int64_t rows = int64_t(h->tree.nb) * R;
+              h->d_ozslc.alloc(size_t(6) * rows * 128);
+              h->d_ozerow.alloc(size_t(rows));
+              launch_ozaki_slices(rows, op.K, Mff, h->d_ozslc.p, h->d_ozerow.p, s);
+              launch_ozaki_gemm(op, R, 0, op.m2l_chunk_end, h->d_ozslc.p, h->d_ozerow.p, rows, Yff,
+                                s);
+            }
+          else
+            launch_m2l_ff(op, R, Mff, Yff, s);
           record(h, 4);
           for (int l = 1; l <= h->tree.L; ++l)
             launch_downward_level_ff(op, R, l, Lff, Yff, s);
@@ -943,6 +959,9 @@ namespace
     h->op64.T2      = h->d_T2.p;
     h->op64.W       = h->d_W.p;
     h->op64.ops     = h->d_ops.p;
+    h->op64.oz_images = h->d_ozimg.n ? h->d_ozimg.p : nullptr;
+    h->op64.oz_ecol   = h->d_ozecol.n ? h->d_ozecol.p : nullptr;
+    h->op64.dev_err   = h->d_err.p;
     h->op64.ops_ff  = h->prm.precision_mode == PIBEM_PRECISION_FLOAT_FLOAT ? h->d_opsff.p : nullptr;
     h->op32.T1      = h->d_T1f.p;
     h->op32.T2      = h->d_T2f.p;
@@ -1417,6 +1436,16 @@ namespace
           std::vector<float> img;
           build_tc_images(all, nops, K, img);
           h->d_tcimg.upload(img, s);
+        }
+      h->d_ozimg.release();
+      h->d_ozecol.release();
+      if (h->use_tc && h->prm.precision_mode != PIBEM_PRECISION_FP64 && ozaki_ok(K))
+        {
+          std::vector<uint16_t> oimg;
+          std::vector<int16_t>  ecol;
+          build_ozaki_images(all, nops, K, oimg, ecol);
+          h->d_ozimg.upload(oimg, s);
+          h->d_ozecol.upload(ecol, s);
         }
       h->d_err.alloc(1);
       h->d_err.zero(s);

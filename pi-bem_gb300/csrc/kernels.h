@@ -112,6 +112,10 @@ namespace pibem
     int64_t        max_near_cols = 0;
     // tensor-core path of the FP32 translations (null: CUDA-core GEMM)
     const float   *tc_images = nullptr;
+    // FP64-accurate operator only: BF16 digit images of the operators and
+    // their row exponents for the tensor-core FP64-accurate GEMM (ozaki_tc.cu)
+    const uint16_t *oz_images = nullptr;
+    const int16_t  *oz_ecol   = nullptr;
     int           *tc_err    = nullptr;
     // M2P per target CSR, evaluated per (pair, target node) item
     int            n_m2p_tgt = 0;
@@ -142,6 +146,17 @@ namespace pibem
   template <typename T>
   void launch_m2p(const OperatorDev<T> &op, const TreeDev &td, int R, int N, const T *M, T *y,
                   cudaStream_t s);
+  // FP64-accurate translation GEMM on the tensor cores (ozaki_tc.cu): digits of
+  // the operators (host, once) and of the expansions (device, per product),
+  // then Y = T E as (hi, lo) pairs; for K <= 96 (p <= 8)
+  bool ozaki_ok(int K);
+  void build_ozaki_images(const std::vector<double> &ops_out_in, int nops, int K,
+                          std::vector<uint16_t> &img, std::vector<int16_t> &e_col);
+  void launch_ozaki_slices(int64_t nrows, int K, const float2 *E, uint16_t *slices, int *e_row,
+                           cudaStream_t s);
+  void launch_ozaki_gemm(const OperatorDev<double> &op, int R, int c0, int c1,
+                         const uint16_t *aslc, const int *e_row, int64_t a_rows, float2 *Y,
+                         cudaStream_t s);
   // FP64-accurate tree passes on (hi, lo) float-float expansions (fmm.cu):
   // the translation GEMM, per-level passes with float-float sums, conversions
   template <typename IO>
