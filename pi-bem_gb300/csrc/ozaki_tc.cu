@@ -261,31 +261,40 @@ namespace pibem
                       const int q = start + row / R, r = row - (row / R) * R;
                       src         = int64_t(a.q_src[q]) * R + r;
                     }
+                  // stage s = (K chunk s / 6, slice s % 6); the loads of stage s + 2
+                  // are issued before stage s is stored (three stages of the row in
+                  // registers), so the L2 latency overlaps the ring waits
+                  uint4 buf[3][8];
+                  auto  load = [&](int s, uint4(&v)[8]) {
+                    const int kc = s / OZ_S, i = s % OZ_S;
+                    if (src >= 0)
+                      {
+                        const uint4 *p = reinterpret_cast<const uint4 *>(
+                          a.aslc + (int64_t(i) * a.a_rows + src) * 128 + kc * OZ_KC);
+#pragma unroll
+                        for (int c = 0; c < 8; ++c)
+                          v[c] = __ldg(p + c);
+                      }
+                    else
+#pragma unroll
+                      for (int c = 0; c < 8; ++c)
+                        v[c] = make_uint4(0u, 0u, 0u, 0u);
+                  };
+                  load(0, buf[0]);
+                  load(1, buf[1]);
+#pragma unroll
                   for (int s = 0; s < OZ_NKC * OZ_S; ++s)
                     {
+                      if (s + 2 < OZ_NKC * OZ_S)
+                        load(s + 2, buf[(s + 2) % 3]);
                       const long g_st = stage + s;
                       const int  slot = int(g_st % OZ_RING);
                       if (g_st >= OZ_RING)
                         oz_wait(a_empty(slot), uint32_t(g_st / OZ_RING - 1) & 1u, a.err, &abort_flag);
-                      const int      kc = s / OZ_S, i = s % OZ_S;
-                      uint4          v[8];
-                      const uint4    z = make_uint4(0u, 0u, 0u, 0u);
-                      if (src >= 0)
-                        {
-                          const uint4 *p = reinterpret_cast<const uint4 *>(
-                            a.aslc + (int64_t(i) * a.a_rows + src) * 128 + kc * OZ_KC);
-#pragma unroll
-                          for (int c = 0; c < 8; ++c)
-                            v[c] = __ldg(p + c);
-                        }
-                      else
-#pragma unroll
-                        for (int c = 0; c < 8; ++c)
-                          v[c] = z;
                       uint8_t *at = smem_raw + (base - raw) + OZ_OFF_A + size_t(slot) * OZ_A_BYTES;
 #pragma unroll
                       for (int c = 0; c < 8; ++c)
-                        *reinterpret_cast<uint4 *>(at + sw128_off_b16(tid, 8 * c)) = v[c];
+                        *reinterpret_cast<uint4 *>(at + sw128_off_b16(tid, 8 * c)) = buf[s % 3][c];
                       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                       mbar_arrive(a_full(slot));
                     }
@@ -300,37 +309,47 @@ namespace pibem
                       const int q = start + q_row / R, r = q_row - (q_row / R) * R;
                       er          = a.e_row[int64_t(a.q_src[q]) * R + r];
                     }
-                  float2   *yrow = a.Y + (int64_t(start) * R + q_row) * K;
-                  const int16_t *ec = a.e_col + size_t(op) * OZ_NP;
+                  const int16_t *ec   = a.e_col + size_t(op) * OZ_NP;
+                  float2        *yrow = a.Y + (int64_t(start) * R + q_row) * K;
                   for (int c0 = 0; c0 < OZ_NP; c0 += 32)
                     {
-                      float h[32], l[32];
-                      tmem_ld32(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c0), h);
+                      // the five group sums of 32 columns (five loads, one wait):
+                      // g0, g1 and g2, g3 pairwise by TwoSum, the two pairs by
+                      // TwoSum, the errors and g4 added last (each below 2^-40 of
+                      // the result), one renormalisation
+                      uint32_t g[5][32];
 #pragma unroll
-                      for (int jj = 0; jj < 32; ++jj)
-                        l[jj] = 0.0f;
-                      for (int g = 1; g < OZ_G; ++g)
-                        {
-                          float v[32];
-                          tmem_ld32(tmem + (uint32_t(32 * warp) << 16) + uint32_t(g * OZ_NP + c0), v);
-#pragma unroll
-                          for (int jj = 0; jj < 32; ++jj)
-                            {
-                              const float2 s2 = ff_add(make_float2(h[jj], l[jj]), make_float2(v[jj], 0.0f));
-                              h[jj]           = s2.x;
-                              l[jj]           = s2.y;
-                            }
-                        }
+                      for (int q = 0; q < OZ_G; ++q)
+                        tmem_ld32_nowait(tmem + (uint32_t(32 * warp) << 16) + uint32_t(q * OZ_NP + c0), g[q]);
+                      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                       if (valid)
 #pragma unroll
                         for (int jj = 0; jj < 32; ++jj)
                           {
                             const int n = c0 + jj;
-                            if (n < K)
+                            if (n >= K)
+                              continue;
+                            const float g0 = __uint_as_float(g[0][jj]), g1 = __uint_as_float(g[1][jj]);
+                            const float g2 = __uint_as_float(g[2][jj]), g3 = __uint_as_float(g[3][jj]);
+                            const float g4 = __uint_as_float(g[4][jj]);
+                            const float t1 = __fadd_rn(g0, g1), z1 = __fsub_rn(t1, g0);
+                            const float e1 = __fadd_rn(__fsub_rn(g0, __fsub_rn(t1, z1)), __fsub_rn(g1, z1));
+                            const float t2 = __fadd_rn(g2, g3), z2 = __fsub_rn(t2, g2);
+                            const float e2 = __fadd_rn(__fsub_rn(g2, __fsub_rn(t2, z2)), __fsub_rn(g3, z2));
+                            const float t  = __fadd_rn(t1, t2), z = __fsub_rn(t, t1);
+                            const float d  = __fadd_rn(__fsub_rn(t1, __fsub_rn(t, z)), __fsub_rn(t2, z));
+                            const float lo = __fadd_rn(__fadd_rn(e1, __fadd_rn(e2, d)), g4);
+                            const float2 r = ff_norm(t, lo);
+                            // times 2^(e_r + e_n): a power of two built from its bits
+                            // when it is a normal float, else ldexpf
+                            const int e = er + ec[n];
+                            if (e > -127 && e < 128)
                               {
-                                const int e = er + ec[n];
-                                yrow[n]     = make_float2(ldexpf(h[jj], e), ldexpf(l[jj], e));
+                                const float sc = __int_as_float((e + 127) << 23);
+                                yrow[n] = make_float2(__fmul_rn(r.x, sc), __fmul_rn(r.y, sc));
                               }
+                            else
+                              yrow[n] = make_float2(ldexpf(r.x, e), ldexpf(r.y, e));
                           }
                     }
                 }
