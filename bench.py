@@ -670,7 +670,7 @@ def run_served(args, w, rank, world, local):
 # DRAM traffic per launch of the roofline kernels, from one ncu capture each of
 # `bench.py --mode profile` on the workload (dram__bytes_read.sum +
 # dram__bytes_write.sum); the summaries are in profiles/.
-NCU_TRAFFIC_MB = {("spheroid98k", "m2l"): 58.2, ("spheroid98k", "near"): 251.2}
+NCU_TRAFFIC_MB = {("spheroid98k", "m2l"): 66.6, ("spheroid98k", "near"): 250.9}
 
 
 def roofline(info, n, prec, phase, ms, cnt, hbm_peak, bf16_peak, peak_kind, p, workload):
