@@ -53,6 +53,7 @@ typedef struct pibem_handle pibem_handle;
  *   BEMProblem<3>/Quadrature rules/Singular quadrature order             (5)
  *   BEMProblem<3>/Solver/Max steps, Tolerance
  *   BEMProblem<3>/Is external flow
+ *   BEMProblem<3>/Symmetry plane z level                                 (0.0)
  * (source/bem_fma.cc:65-103, source/bem_problem.cc:247-312), plus the keys of
  * the added subsection "GB300 Params". */
 typedef struct pibem_params
@@ -72,6 +73,13 @@ typedef struct pibem_params
   double  inner_tolerance;               /* mixed mode: inner FP32 GMRES tolerance */
   double  hbm_budget_gb;                 /* 0 = unlimited */
   int32_t m2l_engine;                    /* FP32 translations: PIBEM_M2L_* */
+  /* Double body (BEMProblem::_assemble_system_double_body, bem_problem.cc:958-1135):
+   * 1 adds to every collocation row the integrals over the mesh reflected in the
+   * plane z = symmetry_plane_z_level (points z -> 2 z0 - z, normals n_z -> -n_z,
+   * regular Gauss rule, values of the reflected node taken from its original).
+   * 0 (default) is the one-body operator of the FMA branch. */
+  int32_t double_body;
+  double  symmetry_plane_z_level;
 } pibem_params;
 
 typedef struct pibem_solve_stats

@@ -51,6 +51,7 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_mesh.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, _ip, _ip]
         L.orc_set_bc.argtypes = [C.c_void_p, _ucp]
+        L.orc_set_double_body.argtypes = [C.c_void_p, C.c_int, C.c_double]
         for f in ("orc_fmm_matvec", "orc_dense_matvec"):
             getattr(L, f).argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_compute_alpha.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -89,6 +90,34 @@ def lib():
     return _lib
 
 
+def mirror_mesh(xyz, cells, z0=0.0, double_offsets=None, double_ids=None):
+    """The closed geometry of a double body: the mesh followed by its reflection
+    in z = z0 (node n + k is the image of node k; cell C + c the image of cell c
+    with vertices (v0, v2, v1, v3), which reverses its orientation so that its
+    normal is the reflected normal (n_x, n_y, -n_z) of bem_problem.cc:1048-1052).
+    Double-node sets are copied onto the images (no node shares a set with an
+    image).  Returns (xyz2, cells2, offsets2, ids2).  Fed to the oracle's FMM
+    with the values [x, x], rows 0..n-1 are the FMM form of the double-body
+    operator."""
+    xyz = np.asarray(xyz, np.float64).reshape(-1, 3)
+    cells = np.asarray(cells, np.int32).reshape(-1, 4)
+    n = xyz.shape[0]
+    im = xyz.copy()
+    im[:, 2] = 2.0 * z0 - im[:, 2]
+    xyz2 = np.vstack([xyz, im])
+    cells2 = np.vstack([cells, cells[:, [0, 2, 1, 3]] + n]).astype(np.int32)
+    if double_offsets is None:
+        sets = [[i] for i in range(n)]
+    else:
+        sets = [sorted(set([i] + list(double_ids[double_offsets[i]:double_offsets[i + 1]])))
+                for i in range(n)]
+    sets2 = sets + [[d + n for d in s_] for s_ in sets]
+    off = np.zeros(2 * n + 1, np.int32)
+    off[1:] = np.cumsum([len(s_) for s_ in sets2])
+    ids = np.asarray([d for s_ in sets2 for d in s_], np.int32)
+    return xyz2, cells2, off, ids
+
+
 def ncoef(p):
     return (p + 1) * (p + 2) // 2
 
@@ -119,6 +148,10 @@ class Oracle:
         self._keep = (do, di)
         self.L.orc_set_mesh(self.h, self.n, _d(self.xyz), self.cells.shape[0], _i(self.cells),
                             _i(do) if do is not None else None, _i(di) if di is not None else None)
+
+    def set_double_body(self, on, z0=0.0):
+        """Dense operator of the double body (bem_problem.cc:958-1135)."""
+        self.L.orc_set_double_body(self.h, int(on), float(z0))
 
     def set_bc(self, mask):
         self.mask = np.ascontiguousarray(mask, dtype=np.uint8)

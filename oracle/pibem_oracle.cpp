@@ -559,6 +559,9 @@ struct orc_handle
   std::vector<Expansion>         M1, M2, L1, L2;
   // dense
   std::vector<double>            denseN, denseD;
+  // double body: the dense matrices add the mesh reflected in z = z0
+  int                            double_body = 0;
+  double                         z0 = 0.0;
   // Telles rules per singular vertex, Gauss rule
   std::vector<double>            gpts, gw;
   std::vector<double>            tpts[4], tw[4];
@@ -1082,6 +1085,33 @@ namespace
       }
   }
 
+  // The reflected cell of BEMProblem::_assemble_system_double_body
+  // (bem_problem.cc:1036-1062 for a regular pair, :1100-1121 for a singular
+  // one: the same regular rule either way): the quadrature points mirrored in
+  // z = z0, the normal's z component negated, the cell's own shape values and
+  // JxW.  The row's cell part is added by the caller.
+  void integrate_reflected_cell(const orc_handle *h, int i, int c, double Nr[4], double Dr[4])
+  {
+    for (int j = 0; j < 4; ++j)
+      Nr[j] = Dr[j] = 0;
+    const P3 &xi = h->xyz[i];
+    for (int q = 0; q < h->nq; ++q)
+      {
+        size_t k = size_t(c) * h->nq + q;
+        P3     R{h->qpts[k].x - xi.x, h->qpts[k].y - xi.y, 2.0 * h->z0 - h->qpts[k].z - xi.z};
+        P3     nr{h->qnrm[k].x, h->qnrm[k].y, -h->qnrm[k].z};
+        P3     D;
+        double s;
+        kernels(R, D, s);
+        double dn = D.x * nr.x + D.y * nr.y + D.z * nr.z;
+        for (int j = 0; j < 4; ++j)
+          {
+            Nr[j] += (dn * h->qshape[k * 4 + j] * h->qjxw[k]);
+            Dr[j] += (s * h->qshape[k * 4 + j] * h->qjxw[k]);
+          }
+      }
+  }
+
   // Dense one-body collocation matrices (bem_problem.cc:478-950, without the
   // matrix print), with the same regular and singular rules as the FMM near
   // field.
@@ -1099,6 +1129,16 @@ namespace
         {
           double Nr[4], Dr[4];
           integrate_cell(h, i, c, &all, singular_vertex(h, i, c), Nr, Dr);
+          if (h->double_body)
+            {
+              double Nm[4], Dm[4];
+              integrate_reflected_cell(h, i, c, Nm, Dm);
+              for (int j = 0; j < 4; ++j)
+                {
+                  Nr[j] += Nm[j];
+                  Dr[j] += Dm[j];
+                }
+            }
           for (int j = 0; j < 4; ++j)
             {
               h->denseN[size_t(i) * n + h->cells[4 * c + j]] += Nr[j];
@@ -1222,6 +1262,15 @@ extern "C"
     build_tree(h);
     build_near(h);
     build_p2m(h);
+    return 0;
+  }
+
+  int orc_set_double_body(orc_handle *h, int on, double z0)
+  {
+    h->double_body = on ? 1 : 0;
+    h->z0          = z0;
+    h->denseN.clear();
+    h->denseD.clear();
     return 0;
   }
 

@@ -26,6 +26,11 @@ void        orc_set_threads(int n);
 int orc_set_mesh(orc_handle *h, int n_nodes, const double *xyz, int n_cells, const int *cells,
                  const int *double_offsets, const int *double_ids);
 int orc_set_bc(orc_handle *h, const unsigned char *dirichlet_mask);
+/* Double body for the dense operator (BEMProblem::_assemble_system_double_body,
+ * bem_problem.cc:958-1135): every row adds the integrals over the mesh
+ * reflected in z = z0.  The FMM functions keep the one-body operator of the
+ * mesh they were given. */
+int orc_set_double_body(orc_handle *h, int on, double z0);
 
 /* BEMFMA::generate_multipole_expansions + multipole_matr_vect_products. */
 void orc_fmm_matvec(orc_handle *h, const double *phi, const double *dphi_dn, double *outN,

@@ -167,7 +167,7 @@ struct pibem_handle
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
     d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
     d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_m2p_item_pair, d_m2l_yslot,
-    d_down_m2l_beg, d_down_m2l_end;
+    d_down_m2l_beg, d_down_m2l_end, d_m2p_tnodes;
   DBuf<uint8_t> d_down_oct;
   DBuf<NearEntry> d_entries;
   DBuf<double>  d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Tc;
@@ -218,7 +218,9 @@ struct pibem_handle
   int         cnt64 = 0, cnt32 = 0;
   int64_t     m2p_items = 0, m2p_tnodes = 0;
 
-  int64_t N() const { return mesh.n_nodes; }
+  // unknowns per column: the collocation nodes (the mesh's own nodes; a
+  // double body's reflected nodes carry no unknowns)
+  int64_t N() const { return mesh.n_dofs; }
 
   // Device memory held by the handle (every buffer above, at its capacity).
   size_t device_bytes() const
@@ -236,7 +238,7 @@ struct pibem_handle
         d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
-        d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end);
+        d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end, d_m2p_tnodes);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
@@ -952,6 +954,7 @@ namespace
       op.m2p_item_ptr  = h->d_m2p_item_ptr.p;
       op.m2p_item_pair = h->d_m2p_item_pair.p;
       op.m2p_tnode_ptr = h->d_m2p_tnode_ptr.p;
+      op.m2p_tnodes    = h->d_m2p_tnodes.p;
     };
     fill(h->op64);
     fill(h->op32);
@@ -995,7 +998,7 @@ namespace
       if (!ok)
         throw Error(PIBEM_EINVAL, std::string("internal plan check failed: ") + what);
     };
-    const int64_t N = m.n_nodes, Q = m.n_cells * nq;
+    const int64_t N = m.n_dofs, Q = m.n_cells * nq;
     const int     nl = int(pl.nleaf_box.size());
     need(pl.nrow_ptr.size() == size_t(nl + 1) && pl.ncol_ptr.size() == size_t(nl + 1) &&
            pl.nent_ptr.size() == size_t(nl + 1) && pl.nval_ptr.size() == size_t(nl + 1),
@@ -1135,22 +1138,17 @@ namespace
     const pibem_params &P = h->prm;
     cudaStream_t        s = h->stream;
     h->mesh_ok = h->bc_ok = false;
-    MeshHost &m = h->mesh;
-    m.n_nodes   = n_nodes;
-    m.n_cells   = n_cells;
-    m.xyz.assign(xyz, xyz + 3 * n_nodes);
-    m.cells.assign(cells, cells + 4 * n_cells);
     for (int64_t i = 0; i < 4 * n_cells; ++i)
       if (cells[i] < 0 || cells[i] >= n_nodes)
         throw Error(PIBEM_EINVAL, "cell node id out of range");
     for (int64_t i = 0; i < 3 * n_nodes; ++i)
       if (!std::isfinite(xyz[i]))
         throw Error(PIBEM_EINVAL, "non-finite node coordinate");
-    m.dbl_off.assign(n_nodes + 1, 0);
-    m.dbl_ids.clear();
+    std::vector<std::vector<int32_t>> sets(static_cast<size_t>(n_nodes));
     for (int64_t i = 0; i < n_nodes; ++i)
       {
-        std::vector<int32_t> set = {int32_t(i)};
+        std::vector<int32_t> &set = sets[size_t(i)];
+        set.push_back(int32_t(i));
         if (doff)
           for (int32_t k = doff[i]; k < doff[i + 1]; ++k)
             {
@@ -1160,12 +1158,14 @@ namespace
             }
         std::sort(set.begin(), set.end());
         set.erase(std::unique(set.begin(), set.end()), set.end());
-        m.dbl_ids.insert(m.dbl_ids.end(), set.begin(), set.end());
-        m.dbl_off[i + 1] = int32_t(m.dbl_ids.size());
       }
+    MeshHost &m = h->mesh;
+    mirror_mesh(n_nodes, xyz, n_cells, cells, sets, P.double_body != 0, P.symmetry_plane_z_level, m);
+    n_nodes = m.n_nodes;
+    n_cells = m.n_cells;
     m.elem_off.assign(n_nodes + 1, 0);
     for (int64_t i = 0; i < 4 * n_cells; ++i)
-      m.elem_off[cells[i] + 1]++;
+      m.elem_off[m.cells[i] + 1]++;
     for (int64_t i = 0; i < n_nodes; ++i)
       m.elem_off[i + 1] += m.elem_off[i];
     m.elem_ids.assign(m.elem_off[n_nodes], 0);
@@ -1173,7 +1173,7 @@ namespace
       std::vector<int32_t> fillp(m.elem_off.begin(), m.elem_off.end() - 1);
       for (int64_t c = 0; c < n_cells; ++c)
         for (int j = 0; j < 4; ++j)
-          m.elem_ids[fillp[cells[4 * c + j]]++] = int32_t(c);
+          m.elem_ids[fillp[m.cells[4 * c + j]]++] = int32_t(c);
     }
     // quadrature rules
     gauss_rule_2d(P.quadrature_order, h->gpts, h->gw);
@@ -1264,13 +1264,18 @@ namespace
     // M2P work items: one per (pair, node of the pair's target box)
     {
       const size_t         nt = pl.m2p_tgt.size();
-      std::vector<int32_t> pair_tgt(pl.m2p_src.size());
+      std::vector<int32_t> pair_tgt(pl.m2p_src.size()), tnodes;
       std::vector<int64_t> item_ptr(pl.m2p_src.size() + 1, 0), tnode_ptr(nt + 1, 0);
       for (size_t ti = 0; ti < nt; ++ti)
         {
-          const int     b  = pl.m2p_tgt[ti];
-          const int64_t nn = t.nend[b] - t.nbeg[b];
-          tnode_ptr[ti + 1] = tnode_ptr[ti] + nn;
+          const int b = pl.m2p_tgt[ti];
+          for (int k = t.nbeg[b]; k < t.nend[b]; ++k)
+            if (t.node_sorted[k] < m.n_dofs)
+              tnodes.push_back(t.node_sorted[k]);
+          tnode_ptr[ti + 1] = int64_t(tnodes.size());
+          const int64_t nn  = tnode_ptr[ti + 1] - tnode_ptr[ti];
+          if (nn == 0)
+            throw Error(PIBEM_EINVAL, "internal plan check failed: M2P target without collocation nodes");
           for (int64_t e = pl.m2p_src_ptr[ti]; e < pl.m2p_src_ptr[ti + 1]; ++e)
             {
               pair_tgt[e]     = int32_t(ti);
@@ -1286,6 +1291,7 @@ namespace
       h->d_m2p_pair_tgt.upload(pair_tgt, s);
       h->d_m2p_item_ptr.upload(item_ptr, s);
       h->d_m2p_tnode_ptr.upload(tnode_ptr, s);
+      h->d_m2p_tnodes.upload(tnodes, s);
     }
     ensure_fmm_tables(P.device, s);
     // diagonal column of every row inside its leaf (block-Jacobi)
@@ -1905,11 +1911,11 @@ extern "C"
       const double *du = mode > 0 ? io.in(u, n) : nullptr;
       const double *dd = mode == 2 ? io.in(dudn, n) : nullptr;
       double       *dout = io.scratch(size_t(3) * n);
-      h->d_proj.alloc(l2_projection_work(N, h->mesh.n_cells, R));
+      h->d_proj.alloc(l2_projection_work(N, h->mesh.n_cells_body, R));
       ProjectionArgs a;
       a.mode     = mode;
       a.n_nodes  = N;
-      a.n_cells  = h->mesh.n_cells;
+      a.n_cells  = h->mesh.n_cells_body; // a double body's reflected cells come after these
       a.nq       = h->nq;
       a.R        = R;
       a.cells    = h->d_cells.p;

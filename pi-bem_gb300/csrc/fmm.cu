@@ -603,8 +603,9 @@ namespace pibem
         }
     }
 
-    // M2P phase 1: one thread per (pair, node of the pair's target box):
-    // scratch[r][item] = multipole of the source box evaluated at the node.
+    // M2P phase 1: one thread per (pair, collocation node of the pair's target
+    // box): scratch[r][item] = multipole of the source box evaluated at the
+    // node.  tnodes lists each target box's collocation nodes (tnode_ptr).
     template <typename T>
     __global__ void m2p_eval_kernel(int64_t n_items, int R, int K, int p,
                                     const int64_t *__restrict__ item_ptr,
@@ -612,8 +613,8 @@ namespace pibem
                                     const int32_t *__restrict__ pair_tgt,
                                     const int32_t *__restrict__ tgt,
                                     const int32_t *__restrict__ src,
-                                    const int32_t *__restrict__ nbeg,
-                                    const int32_t *__restrict__ node_sorted,
+                                    const int64_t *__restrict__ tnode_ptr,
+                                    const int32_t *__restrict__ tnodes,
                                     const double *__restrict__ xyz,
                                     const double *__restrict__ center,
                                     const double *__restrict__ delta, const T *__restrict__ M,
@@ -623,9 +624,8 @@ namespace pibem
       if (it >= n_items)
         return;
       const int64_t e    = item_pair[it];
-      const int64_t t    = tgt[pair_tgt[e]];
       const int64_t s    = src[e];
-      const int     node = node_sorted[nbeg[t] + (it - item_ptr[e])];
+      const int     node = tnodes[tnode_ptr[pair_tgt[e]] + (it - item_ptr[e])];
       const double  h    = delta[s];
       T             rx, ry, rz, ih;
       if constexpr (std::is_same<T, float>::value)
@@ -658,9 +658,8 @@ namespace pibem
     __global__ void __launch_bounds__(256)
       m2p_sum_kernel(int n_tgt, int R, int N, int64_t n_items, const int64_t *__restrict__ tnode_ptr,
                      const int32_t *__restrict__ tgt, const int64_t *__restrict__ src_ptr,
-                     const int64_t *__restrict__ item_ptr, const int32_t *__restrict__ nbeg,
-                     const int32_t *__restrict__ node_sorted, const T *__restrict__ scratch,
-                     T *__restrict__ y)
+                     const int64_t *__restrict__ item_ptr, const int32_t *__restrict__ tnodes,
+                     const T *__restrict__ scratch, T *__restrict__ y)
     {
       const int ti = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
       if (ti >= n_tgt)
@@ -668,7 +667,7 @@ namespace pibem
       const int64_t  nn = tnode_ptr[ti + 1] - tnode_ptr[ti];
       const int64_t  e0 = src_ptr[ti], ns = src_ptr[ti + 1] - e0;
       const int64_t  base = e0 < src_ptr[n_tgt] ? item_ptr[e0] : 0;
-      const int32_t *nodes = node_sorted + nbeg[tgt[ti]];
+      const int32_t *nodes = tnodes + tnode_ptr[ti];
       for (int64_t i = lane; i < nn; i += 32)
         {
           const int node = nodes[i];
@@ -1028,13 +1027,13 @@ namespace pibem
       return;
     m2p_eval_kernel<T><<<unsigned((op.n_m2p_items + 127) / 128), 128, 0, s>>>(
       op.n_m2p_items, R, op.K, op.p, op.m2p_item_ptr, op.m2p_item_pair, op.m2p_pair_tgt,
-      op.m2p_tgt, op.m2p_src, td.nbeg, td.node_sorted, td.xyz, td.center, td.delta, M,
+      op.m2p_tgt, op.m2p_src, op.m2p_tnode_ptr, op.m2p_tnodes, td.xyz, td.center, td.delta, M,
       op.m2p_scratch);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
     m2p_sum_kernel<T><<<unsigned((op.n_m2p_tgt + 7) / 8), 256, 0, s>>>(
       op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt, op.m2p_src_ptr,
-      op.m2p_item_ptr, td.nbeg, td.node_sorted, op.m2p_scratch, y);
+      op.m2p_item_ptr, op.m2p_tnodes, op.m2p_scratch, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

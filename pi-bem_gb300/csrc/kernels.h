@@ -123,6 +123,7 @@ namespace pibem
     const int32_t *m2p_tgt = nullptr, *m2p_src = nullptr, *m2p_pair_tgt = nullptr;
     const int64_t *m2p_src_ptr = nullptr, *m2p_item_ptr = nullptr, *m2p_tnode_ptr = nullptr;
     const int32_t *m2p_item_pair = nullptr; // pair of each item
+    const int32_t *m2p_tnodes = nullptr;    // collocation nodes of each target (m2p_tnode_ptr)
     T             *m2p_scratch = nullptr; // n_m2p_items * R
   };
 

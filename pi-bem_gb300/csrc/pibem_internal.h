@@ -118,14 +118,33 @@ namespace pibem
     }
   };
 
+  // The geometry the operator integrates over.  One body: the mesh itself.
+  // Double body: the mesh (nodes 0..n_dofs-1, cells 0..n_cells_body-1)
+  // followed by its reflection in the symmetry plane: node n_dofs + k is the
+  // image of node k, cell n_cells_body + c the image of cell c with its
+  // orientation reversed, so that its normal is the reflected normal.  Only
+  // the mesh's own nodes are collocation points and unknowns; an image node
+  // takes the value of its original (dof()).
   struct MeshHost
   {
     int64_t              n_nodes = 0, n_cells = 0;
+    int64_t              n_dofs = 0, n_cells_body = 0;
     std::vector<double>  xyz;
     std::vector<int32_t> cells;
     std::vector<int32_t> dbl_off, dbl_ids; // always filled (each set includes the node)
-    std::vector<int32_t> elem_off, elem_ids; // dof -> cells CSR
+    std::vector<int32_t> elem_off, elem_ids; // node -> cells CSR
+    int32_t dof(int32_t v) const { return v < n_dofs ? v : int32_t(v - n_dofs); }
   };
+
+  // Fills m (nodes, cells, double-node sets) from the mesh; with double_body
+  // appends the reflection in z = z0 (source/bem_problem.cc:958-1135: points
+  // z -> 2 z0 - z, normals n_z -> -n_z).  An image node's double-node set is
+  // its original's set moved to the images: a node never shares a set with
+  // an image, so reflected cells always take the regular Gauss rule, as in
+  // the reference.
+  void mirror_mesh(int64_t n_nodes, const double *xyz, int64_t n_cells, const int32_t *cells,
+                   const std::vector<std::vector<int32_t>> &sets, bool double_body, double z0,
+                   MeshHost &m);
 
   // Builds the octree and the near / interaction / non-interaction lists with
   // the reference semantics (bem_fma.cc:3615-4801).

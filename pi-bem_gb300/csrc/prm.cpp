@@ -55,6 +55,8 @@ extern "C" int pibem_params_default(pibem_params *p)
   p->inner_tolerance               = 1e-4;
   p->hbm_budget_gb                 = 0.0;
   p->m2l_engine                    = PIBEM_M2L_TENSOR_CORE;
+  p->double_body                   = 0;
+  p->symmetry_plane_z_level        = 0.0;
   return PIBEM_OK;
 }
 
@@ -111,6 +113,8 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
         p->solver_tolerance = std::atof(v);
       else if (sec == "BEMProblem<3>" && key == "Is external flow")
         p->is_external_flow = as_bool(val) ? 1 : 0;
+      else if (sec == "BEMProblem<3>" && key == "Symmetry plane z level")
+        p->symmetry_plane_z_level = std::atof(v);
       else if (sec == "GB300 Params")
         {
           if (key == "Precision mode")
@@ -129,6 +133,8 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
             p->hbm_budget_gb = std::atof(v);
           else if (key == "Device")
             p->device = std::atoi(v);
+          else if (key == "Double body")
+            p->double_body = as_bool(val) ? 1 : 0;
           else if (key == "M2L engine")
             p->m2l_engine = (val == "CUDA cores" || val == "cuda" || val == "1")
                               ? PIBEM_M2L_CUDA_CORE

@@ -348,12 +348,68 @@ namespace pibem
       }
   }
 
+  void mirror_mesh(int64_t n_nodes, const double *xyz, int64_t n_cells, const int32_t *cells,
+                   const std::vector<std::vector<int32_t>> &sets, bool double_body, double z0,
+                   MeshHost &m)
+  {
+    const int64_t f = double_body ? 2 : 1;
+    m.n_dofs        = n_nodes;
+    m.n_cells_body  = n_cells;
+    m.n_nodes       = f * n_nodes;
+    m.n_cells       = f * n_cells;
+    m.xyz.assign(xyz, xyz + 3 * n_nodes);
+    m.cells.assign(cells, cells + 4 * n_cells);
+    m.dbl_off.assign(m.n_nodes + 1, 0);
+    m.dbl_ids.clear();
+    for (int64_t i = 0; i < n_nodes; ++i)
+      {
+        m.dbl_ids.insert(m.dbl_ids.end(), sets[i].begin(), sets[i].end());
+        m.dbl_off[i + 1] = int32_t(m.dbl_ids.size());
+      }
+    if (!double_body)
+      return;
+    const int32_t o = int32_t(n_nodes);
+    for (int64_t i = 0; i < n_nodes; ++i)
+      {
+        m.xyz.push_back(xyz[3 * i]);
+        m.xyz.push_back(xyz[3 * i + 1]);
+        m.xyz.push_back(2.0 * z0 - xyz[3 * i + 2]);
+      }
+    // lexicographic (v0, v1, v2, v3) -> (v0, v2, v1, v3): the reference
+    // coordinates swap, which turns the normal of the reflected cell around
+    for (int64_t c = 0; c < n_cells; ++c)
+      {
+        const int32_t *v = cells + 4 * c;
+        m.cells.push_back(v[0] + o);
+        m.cells.push_back(v[2] + o);
+        m.cells.push_back(v[1] + o);
+        m.cells.push_back(v[3] + o);
+      }
+    for (int64_t i = 0; i < n_nodes; ++i)
+      {
+        for (int32_t d : sets[i])
+          m.dbl_ids.push_back(d + o);
+        m.dbl_off[n_nodes + i + 1] = int32_t(m.dbl_ids.size());
+      }
+  }
+
   void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &pl)
   {
     pl     = Plan();
     pl.p   = p;
     pl.K   = (p + 1) * (p + 1);
     const int64_t Q = int64_t(t.qbox.size() / (t.L + 1));
+    // Target boxes: boxes holding collocation nodes (every box with nodes for
+    // one body; a double body's boxes of image nodes only are sources only).
+    std::vector<char> tgt(t.nb, 0);
+    for (int b = 0; b < t.nb; ++b)
+      for (int k = t.nbeg[b]; k < t.nend[b] && !tgt[b]; ++k)
+        tgt[b] = t.node_sorted[k] < mesh.n_dofs;
+    std::vector<std::vector<int>> tfill(t.L + 1);
+    for (int l = 0; l <= t.L; ++l)
+      for (int b : t.dofs_filled[l])
+        if (tgt[b])
+          tfill[l].push_back(b);
 
     // cell -> quad mask of a set of boxes
     auto collect = [&](const std::vector<int> &boxes, std::vector<std::pair<int, uint64_t>> &out) {
@@ -372,7 +428,7 @@ namespace pibem
     std::vector<std::vector<std::pair<int, uint64_t>>> coarse(t.nb);
     for (int l = 1; l <= t.L; ++l)
       {
-        const std::vector<int> &fl = t.dofs_filled[l];
+        const std::vector<int> &fl = tfill[l];
 #pragma omp parallel for schedule(dynamic, 16)
         for (int k = 0; k < int(fl.size()); ++k)
           {
@@ -391,7 +447,7 @@ namespace pibem
     // ---- near field per childless box with nodes
     std::vector<int> nleaves;
     for (int b : t.childless)
-      if (t.nend[b] > t.nbeg[b])
+      if (tgt[b])
         nleaves.push_back(b);
     const int nl = int(nleaves.size());
     std::vector<std::vector<int>>       rows(nl), cols(nl);
@@ -414,14 +470,16 @@ namespace pibem
         for (int a : chain)
           for (auto &cm : coarse[a])
             E.push_back(NearEntry{cm.first, 0, cm.second, {0, 0, 0, 0}});
+        // columns: the unknowns (an image node's column is its original's)
         std::vector<int> c;
         for (auto &e : E)
           for (int j = 0; j < 4; ++j)
-            c.push_back(mesh.cells[4 * size_t(e.cell) + j]);
+            c.push_back(mesh.dof(mesh.cells[4 * size_t(e.cell) + j]));
         sort_unique(c);
         for (auto &e : E)
           for (int j = 0; j < 4; ++j)
-            e.lcol[j] = int(std::lower_bound(c.begin(), c.end(), mesh.cells[4 * size_t(e.cell) + j]) -
+            e.lcol[j] = int(std::lower_bound(c.begin(), c.end(),
+                                             mesh.dof(mesh.cells[4 * size_t(e.cell) + j])) -
                             c.begin());
         std::vector<std::vector<int>> g(c.size());
         for (size_t ei = 0; ei < E.size(); ++ei)
@@ -433,7 +491,10 @@ namespace pibem
             gi.insert(gi.end(), v.begin(), v.end());
             gp.push_back(int(gi.size()));
           }
-        std::vector<int> r(t.node_sorted.begin() + t.nbeg[b], t.node_sorted.begin() + t.nend[b]);
+        std::vector<int> r;
+        for (int s = t.nbeg[b]; s < t.nend[b]; ++s)
+          if (t.node_sorted[s] < mesh.n_dofs)
+            r.push_back(t.node_sorted[s]);
         std::sort(r.begin(), r.end());
         rows[k] = r;
         cols[k] = c;
@@ -487,7 +548,7 @@ namespace pibem
             int qid = t.quad_sorted[s];
             int c   = qid / nq;
             for (int j = 0; j < 4; ++j)
-              dq.push_back({mesh.cells[4 * size_t(c) + j], qid * 4 + j});
+              dq.push_back({mesh.dof(mesh.cells[4 * size_t(c) + j]), qid * 4 + j});
           }
         std::sort(dq.begin(), dq.end());
         std::vector<int> rws, cp(1, 0), cq;
@@ -536,7 +597,7 @@ namespace pibem
       {
         pl.m2l_tgt_ptr_level[l] = int(pl.m2l_tgt.size());
         const int sL = t.startLevel[l], eL = t.endLevel[l];
-        for (int b : t.dofs_filled[l])
+        for (int b : tfill[l])
           {
             std::vector<int> ms, mp;
             for (size_t sub = 0; sub < t.nn[b].size(); ++sub)
@@ -696,8 +757,8 @@ namespace pibem
           std::vector<int> boxes;
           if (l == zero_level)
             for (int l2 = 1; l2 < l; ++l2)
-              boxes.insert(boxes.end(), t.dofs_filled[l2].begin(), t.dofs_filled[l2].end());
-          std::vector<int> here = t.dofs_filled[l];
+              boxes.insert(boxes.end(), tfill[l2].begin(), tfill[l2].end());
+          std::vector<int> here = tfill[l];
           std::stable_sort(here.begin(), here.end(),
                            [&](int a, int b) { return t.digit[a] < t.digit[b]; });
           int64_t q0 = int64_t(pl.q_src.size());
@@ -738,7 +799,7 @@ namespace pibem
       {
         pl.l2l_ptr_level[l] = int(pl.l2l_box.size());
         if (l >= 2)
-          for (int b : t.dofs_filled[l])
+          for (int b : tfill[l])
             pl.l2l_box.push_back(b);
       }
     pl.l2l_ptr_level[t.L + 1] = int(pl.l2l_box.size());

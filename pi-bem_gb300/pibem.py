@@ -43,6 +43,8 @@ class Params(C.Structure):
         ("inner_tolerance", C.c_double),
         ("hbm_budget_gb", C.c_double),
         ("m2l_engine", C.c_int32),
+        ("double_body", C.c_int32),
+        ("symmetry_plane_z_level", C.c_double),
     ]
 
 

@@ -153,11 +153,12 @@ def _nodal_normals(xyz, cells):
     return out
 
 
-def wigley_hull(nx: int, nz: int, ny_lid: int, L=1.0, B=0.1, T=0.0625) -> Mesh:
+def wigley_hull(nx: int, nz: int, ny_lid: int, L=1.0, B=0.1, T=0.0625, lid: bool = True) -> Mesh:
     """Closed Wigley-type hull y = +-(B/2)(1-(2x/L)^2)(1-(z/T)^2), z in [-T,0],
     closed by the lid z = 0.  Port and starboard sides are nx x nz grids, the lid
     an nx x ny_lid grid; the keel (z=-T, y=0) and the bow/stern lines (y=0) are
-    single shared node rows.  Outward cell orientation."""
+    single shared node rows.  Outward cell orientation.  lid=False leaves the
+    lid out: the wetted surface, open along the waterline z = 0."""
     xs = np.linspace(-L / 2, L / 2, nx + 1)
     zs = np.linspace(-T, 0.0, nz + 1)
     index = {}
@@ -194,7 +195,7 @@ def wigley_hull(nx: int, nz: int, ny_lid: int, L=1.0, B=0.1, T=0.0625) -> Mesh:
                     q = [q[0], q[2], q[1], q[3]]
                 cells.append(q)
     # lid: z = 0, grid over x and eta in [-1,1] with y = eta * half_beam(x, 0)
-    for j in range(ny_lid):
+    for j in range(ny_lid if lid else 0):
         for i in range(nx):
             quad = []
             for dj in (0, 1):
@@ -340,6 +341,33 @@ def wigley_mixed_case(nx: int, nz: int, ny_lid: int, seed: int = 3, n_sources: i
     S = sources_in_wigley(rng, n_sources)
     mask = mixed_bc_by_cell_centroid(mesh, z_split=-0.5 * 0.0625)
     tmp, ph, dn = point_source_data(mesh, mask, S, q)
+    return mesh, mask, tmp, ph, dn
+
+
+def wigley_double_body_case(nx: int, nz: int, seed: int = 5, n_sources: int = 6,
+                            z0: float = 0.0):
+    """Double body: the wetted Wigley hull (no lid, waterline z = z0 = 0) and
+    data from n_sources point sources of strength U(-1,1) inside the hull plus
+    their images in the waterline (the field is symmetric about z = z0, so the
+    doubled body sees it exactly).  Exterior problem; cells with centroid
+    z > -T/2 Dirichlet, the rest Neumann.  Nodal normals on the waterline are
+    the horizontal normals of the doubled body.
+
+    Returns mesh, dirichlet mask, tmp_rhs, exact phi, exact dphi/dn."""
+    T = 0.0625
+    mesh = wigley_hull(nx, nz, 2, lid=False)
+    on_plane = np.abs(mesh.xyz[:, 2] - z0) < 1e-12
+    nrm = mesh.normals.copy()
+    nrm[on_plane, 2] = 0.0
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    mesh = Mesh(mesh.xyz, mesh.cells, nrm)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    q = rng.uniform(-1.0, 1.0, n_sources)
+    S = sources_in_wigley(rng, n_sources)
+    Sm = S.copy()
+    Sm[:, 2] = 2.0 * z0 - Sm[:, 2]
+    mask = mixed_bc_by_cell_centroid(mesh, z_split=-0.5 * T)
+    tmp, ph, dn = point_source_data(mesh, mask, np.vstack([S, Sm]), np.concatenate([q, q]))
     return mesh, mask, tmp, ph, dn
 
 

@@ -35,6 +35,8 @@ def test_defaults_are_the_reference_defaults(pibem_mod):
     assert p.singular_quadrature_order == 5
     assert p.gmres_restart == 100
     assert p.is_external_flow == 0
+    assert p.double_body == 0
+    assert p.symmetry_plane_z_level == 0.0
 
 
 PRM = """
@@ -51,6 +53,7 @@ end
 subsection BEMProblem<3>
   set Is external flow = true
   set Solution method  = FMA
+  set Symmetry plane z level = -0.25
   subsection Quadrature rules
     set Quadrature order          = 3
     set Singular quadrature order = 7
@@ -64,6 +67,7 @@ subsection BEMProblem<3>
     set GMRES restart  = 60
     set HBM budget GB  = 150
     set M2L engine     = CUDA cores
+    set Double body    = true
   end
 end
 subsection Other
@@ -89,6 +93,8 @@ def test_prm_reader(pibem_mod):
     assert p.hbm_budget_gb == pytest.approx(150)
     assert p.m2l_engine == pibem_mod.M2L_CUDA_CORE
     assert pibem_mod.default_params().m2l_engine == pibem_mod.M2L_TENSOR_CORE
+    assert p.symmetry_plane_z_level == pytest.approx(-0.25)
+    assert p.double_body == 1
 
 
 def test_create_rejects_bad_parameters(pibem_mod):

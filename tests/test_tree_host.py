@@ -79,3 +79,28 @@ def test_perturbed_sphere_shallow_tree(th, oracle_mod, synthetic):
 
 def test_wigley_hull(th, oracle_mod, synthetic):
     _compare(th, oracle_mod, synthetic.wigley_hull(40, 8, 6), leaf=20)
+
+
+def test_double_body_tree_and_plan(th, oracle_mod, synthetic):
+    """Double body: the octree of the mirrored geometry equals the oracle's
+    for that geometry, and the plan's rows, columns and targets are the mesh's
+    own nodes only (image nodes are sources whose values are their
+    originals')."""
+    mesh = synthetic.wigley_double_body_case(40, 8)[0]
+    n = mesh.n_nodes
+    x2, c2, _, _ = oracle_mod.mirror_mesh(mesh.xyz, mesh.cells, 0.0)
+    geo = synthetic.Mesh(x2, c2, np.zeros_like(x2))
+    _compare(th, oracle_mod, geo, leaf=20)
+    o = oracle_mod.Oracle(p=4, levels=10, max_nodes=20)
+    o.set_mesh(x2, c2)
+    pts = np.ascontiguousarray(o.quad_data()[0])
+    st = np.zeros(11, np.int64)
+    th.th_plan_mirrored.argtypes = [C.c_int, dp, C.c_int, ip, C.c_double, dp, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.POINTER(C.c_long)]
+    cells = np.ascontiguousarray(mesh.cells, np.int32)
+    th.th_plan_mirrored(n, mesh.xyz.ctypes.data_as(dp), mesh.n_cells, cells.ctypes.data_as(ip), 0.0,
+                        pts.ctypes.data_as(dp), 16, 10, 20, 4, st.ctypes.data_as(C.POINTER(C.c_long)))
+    assert st[0] == n and st[9] == 0          # every collocation node is one near row
+    assert st[1] < n and st[2] < n and st[3] < n
+    assert st[4] == n
+    assert st[5] > 0 and st[6] == 0 and st[8] == 0 and st[10] == 0
