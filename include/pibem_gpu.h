@@ -54,6 +54,7 @@ typedef struct pibem_handle pibem_handle;
  *   BEMProblem<3>/Solver/Max steps, Tolerance
  *   BEMProblem<3>/Is external flow
  *   BEMProblem<3>/Symmetry plane z level                                 (0.0)
+ *   BEMProblem<3>/Continuos gradient across edges                        (true)
  * (source/bem_fma.cc:65-103, source/bem_problem.cc:247-312), plus the keys of
  * the added subsection "GB300 Params". */
 typedef struct pibem_params
@@ -80,6 +81,9 @@ typedef struct pibem_params
    * 0 (default) is the one-body operator of the FMA branch. */
   int32_t double_body;
   double  symmetry_plane_z_level;
+  /* "Continuos gradient across edges" (bem_problem.cc:277, default 1): the
+   * constraint lines of Dirichlet-Dirichlet double nodes (see pibem_solve). */
+  int32_t continuous_gradient;
 } pibem_params;
 
 typedef struct pibem_solve_stats
@@ -144,7 +148,17 @@ int pibem_compute_rhs(pibem_handle *h, int32_t nrhs, const double *tmp_rhs, doub
 
 /* BEMProblem::solve_system (bem_problem.cc:1267): rhs, GMRES from x0 = rhs,
  * scatter phi(i) = sol(i) on Neumann nodes, dphi_dn(i) = sol(i) on Dirichlet
- * nodes; the other entries of phi / dphi_dn are left as given. */
+ * nodes; the other entries of phi / dphi_dn are left as given.  With double
+ * nodes the solve runs on the constrained system of compute_constraints
+ * (bem_problem.cc:1377-1579) and ConstrainedOperator (constrained_matrix.h):
+ * per double-node set, with i its first Dirichlet node (else its smallest id),
+ *   i Neumann:            x_d = x_i for the set's other nodes d;
+ *   i Dirichlet, d Neumann:   x_d = tmp_rhs_i;
+ *   i, d Dirichlet (continuous_gradient): x_i and x_d are the normal
+ *   derivatives given by the L2-projected normals and surface gradients of
+ *   tmp_rhs (pibem_compute_normals / _surface_gradients).
+ * pibem_system_matvec and pibem_compute_rhs stay unconstrained, as vmult and
+ * compute_rhs are. */
 int pibem_solve(pibem_handle *h, int32_t nrhs, double *phi, double *dphi_dn,
                 const double *tmp_rhs, pibem_solve_stats *stats);
 

@@ -52,6 +52,7 @@ def lib():
         L.orc_set_mesh.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, _ip, _ip, _ip]
         L.orc_set_bc.argtypes = [C.c_void_p, _ucp]
         L.orc_set_double_body.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        L.orc_set_constraints.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _dp]
         for f in ("orc_fmm_matvec", "orc_dense_matvec"):
             getattr(L, f).argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_compute_alpha.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -152,6 +153,13 @@ class Oracle:
     def set_double_body(self, on, z0=0.0):
         """Dense operator of the double body (bem_problem.cc:958-1135)."""
         self.L.orc_set_double_body(self.h, int(on), float(z0))
+
+    def set_constraints(self, rows, cols, g):
+        """Constraint lines of solve() (oracle/constraints.py)."""
+        self._con = (np.ascontiguousarray(rows, np.int32), np.ascontiguousarray(cols, np.int32),
+                     np.ascontiguousarray(g, np.float64))
+        r, c, v = self._con
+        self.L.orc_set_constraints(self.h, len(r), _i(r), _i(c), _d(v))
 
     def set_bc(self, mask):
         self.mask = np.ascontiguousarray(mask, dtype=np.uint8)

@@ -562,6 +562,9 @@ struct orc_handle
   // double body: the dense matrices add the mesh reflected in z = z0
   int                            double_body = 0;
   double                         z0 = 0.0;
+  // constraint lines of the solve: x[row] - (col >= 0 ? x[col] : 0) = g
+  std::vector<int>               con_row, con_col;
+  std::vector<double>            con_g;
   // Telles rules per singular vertex, Gauss rule
   std::vector<double>            gpts, gw;
   std::vector<double>            tpts[4], tw[4];
@@ -1354,6 +1357,28 @@ extern "C"
 
   // BEMProblem::solve_system, bem_problem.cc:1267-1347, with an own restarted
   // GMRES (modified Gram-Schmidt, Givens rotations) on the true residual.
+  // ConstrainedOperator::vmult (include/constrained_matrix.h:100-125): the
+  // system operator, then every constrained row replaced by its constraint
+  // x[row] - w x[col].
+  static void constrained_matvec(orc_handle *h, int dense, const double *alpha, const double *x,
+                                 double *y)
+  {
+    orc_system_matvec(h, dense, alpha, x, y);
+    for (size_t k = 0; k < h->con_row.size(); ++k)
+      {
+        const int i = h->con_row[k];
+        y[i]        = x[i] - (h->con_col[k] >= 0 ? x[h->con_col[k]] : 0.0);
+      }
+  }
+
+  int orc_set_constraints(orc_handle *h, int n, const int *rows, const int *cols, const double *g)
+  {
+    h->con_row.assign(rows, rows + n);
+    h->con_col.assign(cols, cols + n);
+    h->con_g.assign(g, g + n);
+    return 0;
+  }
+
   int orc_solve(orc_handle *h, int dense, double *phi, double *dphi, const double *tmp, double tol,
                 int max_steps, int restart, double *final_res)
   {
@@ -1361,6 +1386,9 @@ extern "C"
     std::vector<double> alpha(n), b(n), x(n), r(n), w(n);
     orc_compute_alpha(h, dense, alpha.data());
     orc_compute_rhs(h, dense, alpha.data(), tmp, b.data());
+    // ConstrainedOperator::distribute_rhs (include/constrained_matrix.h:172-181)
+    for (size_t k = 0; k < h->con_row.size(); ++k)
+      b[h->con_row[k]] = h->con_g[k];
     x           = b; // initial guess = rhs (bem_problem.cc:1295)
     double bn   = norm2(b);
     int    its  = 0;
@@ -1369,7 +1397,7 @@ extern "C"
       bn = 1;
     while (its < max_steps)
       {
-        orc_system_matvec(h, dense, alpha.data(), x.data(), w.data());
+        constrained_matvec(h, dense, alpha.data(), x.data(), w.data());
         for (size_t i = 0; i < n; ++i)
           r[i] = b[i] - w[i];
         double beta = norm2(r);
@@ -1387,7 +1415,7 @@ extern "C"
         for (; k < m && its < max_steps; ++k)
           {
             ++its;
-            orc_system_matvec(h, dense, alpha.data(), V[k].data(), w.data());
+            constrained_matvec(h, dense, alpha.data(), V[k].data(), w.data());
             for (int i = 0; i <= k; ++i)
               {
                 double s = 0;
@@ -1431,7 +1459,7 @@ extern "C"
           for (size_t t = 0; t < n; ++t)
             x[t] += y[i] * V[i][t];
       }
-    orc_system_matvec(h, dense, alpha.data(), x.data(), w.data());
+    constrained_matvec(h, dense, alpha.data(), x.data(), w.data());
     for (size_t i = 0; i < n; ++i)
       r[i] = b[i] - w[i];
     rel = norm2(r) / bn;

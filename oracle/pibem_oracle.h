@@ -31,6 +31,11 @@ int orc_set_bc(orc_handle *h, const unsigned char *dirichlet_mask);
  * reflected in z = z0.  The FMM functions keep the one-body operator of the
  * mesh they were given. */
 int orc_set_double_body(orc_handle *h, int on, double z0);
+/* Constraint lines applied by orc_solve as deal.II's ConstrainedOperator in
+ * BEMProblem::solve_system (include/constrained_matrix.h, bem_problem.cc:1275-1283):
+ * row rows[k] of the operator becomes x[rows[k]] - x[cols[k]] (cols[k] = -1: no
+ * entry) and of the right-hand side g[k].  n = 0 clears them. */
+int orc_set_constraints(orc_handle *h, int n, const int *rows, const int *cols, const double *g);
 
 /* BEMFMA::generate_multipole_expansions + multipole_matr_vect_products. */
 void orc_fmm_matvec(orc_handle *h, const double *phi, const double *dphi_dn, double *outN,

@@ -21,6 +21,7 @@
 #include <mutex>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "kernels.h"
@@ -190,6 +191,15 @@ struct pibem_handle
   int                  modes32_R = 0; // d_modes32 holds MODE_COMBINED for this many columns
   DBuf<double>         d_alpha;
   bool                 have_dirichlet = true;
+  // double-node constraint lines of the solve (made by set_bc): row, entry
+  // column (-1: none), kind (0: x_row = x_col; 1: x_row = tmp_rhs[p]; 2: the
+  // Dirichlet-Dirichlet normal derivative of the pair (p, q))
+  std::vector<int32_t> con_row, con_col, con_p, con_q;
+  std::vector<uint8_t> con_kind;
+  bool                 con_proj = false; // some line needs normals and surface gradients
+  DBuf<int32_t>        d_con_row, d_con_col, d_con_p, d_con_q;
+  DBuf<uint8_t>        d_con_kind;
+  DBuf<double>         d_con_nrm, d_con_sg; // nodal normals (kept per mesh), surface gradients
   // work
   DBuf<double> d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64;
   DBuf<float>  d_M32, d_L32, d_x32, d_y32, d_m2p32, d_Y32;
@@ -239,6 +249,7 @@ struct pibem_handle
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
         d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end, d_m2p_tnodes);
+    add(d_con_row, d_con_col, d_con_p, d_con_q, d_con_kind, d_con_nrm, d_con_sg);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
@@ -523,8 +534,17 @@ namespace
     launch_add_scalar(N, R, h->g_u.p, v, h->stream);
   }
 
-  // BEMProblem::vmult for R columns, FP64 (device in/out).
-  void system_apply64(pibem_handle *h, int R, const double *x, double *y)
+  // ConstrainedOperator::vmult (include/constrained_matrix.h:100-125): every
+  // constrained row of y replaced by its line x[row] - x[col].
+  void constrain_rows(pibem_handle *h, int R, const double *x, double *y)
+  {
+    launch_constrain_rows(int(h->con_row.size()), R, h->N(), h->d_con_row.p, h->d_con_col.p, x, y,
+                          h->stream);
+  }
+
+  // BEMProblem::vmult for R columns, FP64 (device in/out); constrained: the
+  // solve's operator (the constraint lines of its double nodes).
+  void system_apply64(pibem_handle *h, int R, const double *x, double *y, bool constrained = false)
   {
     const int64_t N = h->N();
     cudaStream_t  s = h->stream;
@@ -542,6 +562,8 @@ namespace
     finish_timing(h, 0);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
+    if (constrained)
+      constrain_rows(h, R, x, y);
     h->cnt64 += R;
   }
 
@@ -640,7 +662,7 @@ namespace
   }
 
   // Same operator in FP32 (input and output FP64).
-  void system_apply32(pibem_handle *h, int R, const double *x, double *y)
+  void system_apply32(pibem_handle *h, int R, const double *x, double *y, bool constrained = false)
   {
     const int64_t N = h->N();
     cudaStream_t  s = h->stream;
@@ -660,6 +682,8 @@ namespace
     launch_convert_f2d(int64_t(R) * N, h->d_y32.p, y, s);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
+    if (constrained)
+      constrain_rows(h, R, x, y);
     h->cnt32 += R;
   }
 
@@ -843,6 +867,89 @@ namespace
     return res;
   }
 
+  // The double-node constraint lines of BEMProblem::compute_constraints
+  // (bem_problem.cc:1405-1579) for the current Dirichlet mask.  Per set, with
+  // i its first Dirichlet node in ascending order (else its smallest id), made
+  // once, when the loop reaches i:
+  //   i Neumann:               x_d - x_i = 0 for the other nodes d;
+  //   i Dirichlet, d Neumann:  x_d = tmp_rhs[i];
+  //   i, d Dirichlet:          with continuous_gradient, x_i and x_d are the
+  //     normal derivatives from the normals and surface gradients (the
+  //     reference's flat-edge branch, normal_distance / normal_distance < 1e-4,
+  //     is never taken); a line made again keeps its place and takes the new
+  //     value, so with several Dirichlet doubles x_i follows the last one.
+  // Hanging-node lines do not arise on the conforming meshes taken here.
+  void build_constraints(pibem_handle *h)
+  {
+    const MeshHost &m = h->mesh;
+    const int64_t   N = h->N();
+    h->con_row.clear();
+    h->con_col.clear();
+    h->con_p.clear();
+    h->con_q.clear();
+    h->con_kind.clear();
+    std::unordered_map<int32_t, size_t> at;
+    auto line = [&](int32_t row) {
+      auto it = at.find(row);
+      if (it != at.end())
+        return it->second;
+      at[row] = h->con_row.size();
+      h->con_row.push_back(row);
+      h->con_col.push_back(-1);
+      h->con_p.push_back(-1);
+      h->con_q.push_back(-1);
+      h->con_kind.push_back(0);
+      return h->con_row.size() - 1;
+    };
+    for (int32_t i = 0; i < int32_t(N); ++i)
+      {
+        const int32_t *b = m.dbl_ids.data() + m.dbl_off[i], *e = m.dbl_ids.data() + m.dbl_off[i + 1];
+        if (e - b < 2)
+          continue;
+        int32_t first = *b;
+        for (const int32_t *d = b; d != e; ++d)
+          if (h->dir[*d])
+            {
+              first = *d;
+              break;
+            }
+        if (i != first)
+          continue;
+        for (const int32_t *d = b; d != e; ++d)
+          {
+            if (*d == i)
+              continue;
+            if (h->dir[i] && h->dir[*d])
+              {
+                if (!h->prm.continuous_gradient)
+                  continue;
+                const size_t kd = line(*d), ki = line(i);
+                h->con_kind[ki] = 2;
+                h->con_p[ki]    = i;
+                h->con_q[ki]    = *d;
+                h->con_kind[kd] = 2;
+                h->con_p[kd]    = *d;
+                h->con_q[kd]    = i;
+              }
+            else if (h->dir[i])
+              {
+                const size_t kd = line(*d);
+                h->con_kind[kd] = 1;
+                h->con_p[kd]    = i;
+              }
+            else
+              h->con_col[line(*d)] = i;
+          }
+      }
+    h->con_proj = std::find(h->con_kind.begin(), h->con_kind.end(), uint8_t(2)) != h->con_kind.end();
+    cudaStream_t s = h->stream;
+    h->d_con_row.upload(h->con_row, s);
+    h->d_con_col.upload(h->con_col, s);
+    h->d_con_p.upload(h->con_p, s);
+    h->d_con_q.upload(h->con_q, s);
+    h->d_con_kind.upload(h->con_kind, s);
+  }
+
   void build_preconditioner(pibem_handle *h)
   {
     const Plan   &pl = h->plan;
@@ -869,6 +976,29 @@ namespace
     std::vector<double> hb(h->blk_ptr[nl]), inv(h->blk_ptr[nl]);
     blocks.download(hb.data(), hb.size(), s);
     PIBEM_CUDA(cudaStreamSynchronize(s));
+    // a constrained row of the solve's operator is its constraint line: the
+    // same line in the row's block (its entry where the column is in the block)
+    if (!h->con_row.empty())
+      {
+        std::vector<int64_t> pos(h->N(), -1); // node -> near row position
+        for (size_t r = 0; r < pl.nrows.size(); ++r)
+          pos[pl.nrows[r]] = int64_t(r);
+        for (size_t k = 0; k < h->con_row.size(); ++k)
+          {
+            const int64_t r = pos[h->con_row[k]];
+            const int     lf = pl.row_leaf[r];
+            const int64_t r0 = pl.nrow_ptr[lf], n = pl.nrow_ptr[lf + 1] - r0;
+            double       *row = &hb[h->blk_ptr[lf] + (r - r0) * n];
+            std::fill(row, row + n, 0.0);
+            row[r - r0] = 1.0;
+            if (h->con_col[k] >= 0)
+              {
+                const int64_t c = pos[h->con_col[k]];
+                if (c >= r0 && c < r0 + n)
+                  row[c - r0] = -1.0;
+              }
+          }
+      }
 #pragma omp parallel for schedule(dynamic, 16)
     for (int k = 0; k < nl; ++k)
       {
@@ -1129,6 +1259,7 @@ namespace
   {
     auto t0 = std::chrono::steady_clock::now();
     drop_graph(h); // its kernels carry the previous mesh's sizes
+    h->d_con_nrm.release();
     if (n_nodes <= 0 || n_cells <= 0 || !xyz || !cells)
       throw Error(PIBEM_EINVAL, "empty mesh");
     if ((doff == nullptr) != (dids == nullptr))
@@ -1523,6 +1654,7 @@ namespace
       h->op64.Tc = h->d_Tc.p;
       h->op32.Tc = h->d_Tcf.p;
     }
+    build_constraints(h);
     if (h->prm.preconditioner)
       build_preconditioner(h);
     PIBEM_CUDA(cudaStreamSynchronize(s));
@@ -1558,6 +1690,57 @@ namespace
                        rhs, s);
   }
 
+  // L2 projection of R columns onto the Q1 space of the mesh (device in/out):
+  // mode 0 normals, 1 surface gradients of u, 2 gradients of (u, dudn).
+  void projection_dev(pibem_handle *h, int mode, int R, const double *du, const double *dd,
+                      double *dout)
+  {
+    const int64_t N = h->N();
+    h->d_proj.alloc(l2_projection_work(N, h->mesh.n_cells_body, R));
+    ProjectionArgs a;
+    a.mode     = mode;
+    a.n_nodes  = N;
+    a.n_cells  = h->mesh.n_cells_body; // a double body's reflected cells come after these
+    a.nq       = h->nq;
+    a.R        = R;
+    a.cells    = h->d_cells.p;
+    a.elem_off = h->d_elem_off.p;
+    a.elem_ids = h->d_elem_ids.p;
+    a.xyz      = h->d_xyz.p;
+    a.gpts     = h->d_gpts.p;
+    a.qshape   = h->d_qshape.p;
+    a.qjxw     = h->d_qjxw.p;
+    a.qnrm     = h->d_qnrm.p;
+    a.u        = du;
+    a.dudn     = dd;
+    a.work     = h->d_proj.p;
+    a.out      = dout;
+    l2_projection(a, h->stream);
+  }
+
+  // ConstrainedOperator::distribute_rhs (include/constrained_matrix.h:172-181):
+  // the constrained rows of b take their lines' values.
+  void constrain_rhs(pibem_handle *h, int R, const double *tmp, double *b)
+  {
+    const int nc = int(h->con_row.size());
+    if (nc == 0)
+      return;
+    const int64_t N = h->N();
+    if (h->con_proj)
+      {
+        if (!h->d_con_nrm.p)
+          {
+            h->d_con_nrm.alloc(3 * N);
+            projection_dev(h, 0, 1, nullptr, nullptr, h->d_con_nrm.p);
+          }
+        h->d_con_sg.alloc(size_t(3) * R * N);
+        projection_dev(h, 1, R, tmp, nullptr, h->d_con_sg.p);
+      }
+    launch_constraint_rhs(nc, R, N, h->d_con_row.p, h->d_con_kind.p, h->d_con_p.p, h->d_con_q.p, tmp,
+                          h->con_proj ? h->d_con_nrm.p : nullptr,
+                          h->con_proj ? h->d_con_sg.p : nullptr, b, h->stream);
+  }
+
   void solve_dev(pibem_handle *h, int R, double *phi, double *dphi, const double *tmp,
                  pibem_solve_stats *st)
   {
@@ -1581,11 +1764,12 @@ namespace
     b.alloc(size_t(R) * N);
     x.alloc(size_t(R) * N);
     compute_rhs_dev(h, R, tmp, b.p);
+    constrain_rhs(h, R, tmp, b.p);
     PIBEM_CUDA(cudaMemcpyAsync(x.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
     const pibem_params &P    = h->prm;
     const bool          prec = P.preconditioner != 0;
-    auto A64 = [h, R](const double *in, double *out) { system_apply64(h, R, in, out); };
-    auto A32 = [h, R](const double *in, double *out) { system_apply32(h, R, in, out); };
+    auto A64 = [h, R](const double *in, double *out) { system_apply64(h, R, in, out, true); };
+    auto A32 = [h, R](const double *in, double *out) { system_apply32(h, R, in, out, true); };
     int                 iters = 0, refine = 0;
     std::vector<double> rel;
     if (P.precision_mode != PIBEM_PRECISION_MIXED)
@@ -1911,26 +2095,7 @@ extern "C"
       const double *du = mode > 0 ? io.in(u, n) : nullptr;
       const double *dd = mode == 2 ? io.in(dudn, n) : nullptr;
       double       *dout = io.scratch(size_t(3) * n);
-      h->d_proj.alloc(l2_projection_work(N, h->mesh.n_cells_body, R));
-      ProjectionArgs a;
-      a.mode     = mode;
-      a.n_nodes  = N;
-      a.n_cells  = h->mesh.n_cells_body; // a double body's reflected cells come after these
-      a.nq       = h->nq;
-      a.R        = R;
-      a.cells    = h->d_cells.p;
-      a.elem_off = h->d_elem_off.p;
-      a.elem_ids = h->d_elem_ids.p;
-      a.xyz      = h->d_xyz.p;
-      a.gpts     = h->d_gpts.p;
-      a.qshape   = h->d_qshape.p;
-      a.qjxw     = h->d_qjxw.p;
-      a.qnrm     = h->d_qnrm.p;
-      a.u        = du;
-      a.dudn     = dd;
-      a.work     = h->d_proj.p;
-      a.out      = dout;
-      l2_projection(a, h->stream);
+      projection_dev(h, mode, R, du, dd, dout);
       PIBEM_CUDA(cudaMemcpyAsync(out, dout, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
                                  h->stream));
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));

@@ -276,6 +276,56 @@ namespace pibem
     }
 
     inline unsigned nblocks(int64_t n, int t = 256) { return unsigned((n + t - 1) / t); }
+
+    // Double-node constraint lines (deal.II ConstrainedOperator::vmult,
+    // include/constrained_matrix.h:100-125): row rows[k] of y becomes
+    // x[row] - x[cols[k]] (cols[k] < 0: x[row]).  One thread per (line, column).
+    __global__ void constrain_rows_kernel(int n_con, int R, int64_t n, const int32_t *__restrict__ rows,
+                                          const int32_t *__restrict__ cols,
+                                          const double *__restrict__ x, double *__restrict__ y)
+    {
+      const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (t >= int64_t(n_con) * R)
+        return;
+      const int64_t r = t / n_con, k = t - r * n_con;
+      const double *xr = x + r * n;
+      const int32_t c  = cols[k];
+      y[r * n + rows[k]] = xr[rows[k]] - (c >= 0 ? xr[c] : 0.0);
+    }
+
+    // Right-hand side of the constraint lines (bem_problem.cc:1405-1579), per
+    // (line, column): kind 0 -> 0 (x_row = x_col); kind 1 -> tmp[p] (the
+    // potential given at the set's Dirichlet node); kind 2 -> the normal
+    // derivative of a Dirichlet-Dirichlet pair (p, q) from the nodal normals
+    // nrm (3 per node) and the surface gradients sg of tmp (3 per node, column
+    // after column): c = n_p.n_q, (s_q.n_p + (s_p.n_q) c) / (1 - c^2).  Then
+    // b[row] = that value (ConstrainedOperator::distribute_rhs).
+    __global__ void constraint_rhs_kernel(int n_con, int R, int64_t n, const int32_t *__restrict__ rows,
+                                          const uint8_t *__restrict__ kind,
+                                          const int32_t *__restrict__ p, const int32_t *__restrict__ q,
+                                          const double *__restrict__ tmp,
+                                          const double *__restrict__ nrm,
+                                          const double *__restrict__ sg, double *__restrict__ b)
+    {
+      const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (t >= int64_t(n_con) * R)
+        return;
+      const int64_t r = t / n_con, k = t - r * n_con;
+      double        g = 0.0;
+      if (kind[k] == 1)
+        g = tmp[r * n + p[k]];
+      else if (kind[k] == 2)
+        {
+          const double *np_ = nrm + 3 * int64_t(p[k]), *nq = nrm + 3 * int64_t(q[k]);
+          const double *sp_ = sg + 3 * (r * n + p[k]), *sq = sg + 3 * (r * n + q[k]);
+          const double  c   = np_[0] * nq[0] + np_[1] * nq[1] + np_[2] * nq[2];
+          const double  sqnp = sq[0] * np_[0] + sq[1] * np_[1] + sq[2] * np_[2];
+          const double  spnq = sp_[0] * nq[0] + sp_[1] * nq[1] + sp_[2] * nq[2];
+          g = (1.0 / (1.0 - c * c)) * (sqnp + spnq * c);
+        }
+      b[r * n + rows[k]] = g;
+    }
+
   } // namespace
 
   void launch_dots(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
@@ -366,6 +416,28 @@ namespace pibem
                       double *dphi, cudaStream_t s)
   {
     scatter_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, sol, dir, phi, dphi);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_constrain_rows(int n_con, int R, int64_t n, const int32_t *rows, const int32_t *cols,
+                             const double *x, double *y, cudaStream_t s)
+  {
+    if (n_con == 0 || R == 0)
+      return;
+    constrain_rows_kernel<<<nblocks(int64_t(n_con) * R), 256, 0, s>>>(n_con, R, n, rows, cols, x, y);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_constraint_rhs(int n_con, int R, int64_t n, const int32_t *rows, const uint8_t *kind,
+                             const int32_t *p, const int32_t *q, const double *tmp,
+                             const double *nrm, const double *sg, double *b, cudaStream_t s)
+  {
+    if (n_con == 0 || R == 0)
+      return;
+    constraint_rhs_kernel<<<nblocks(int64_t(n_con) * R), 256, 0, s>>>(n_con, R, n, rows, kind, p, q,
+                                                                      tmp, nrm, sg, b);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

@@ -20,6 +20,12 @@ namespace pibem
   void launch_scatter(int64_t n, int R, const double *sol, const uint8_t *dir, double *phi,
                       double *dphi, cudaStream_t s);
   void launch_add_scalar(int64_t n, int R, const double *shift, double *x, cudaStream_t s);
+  // double-node constraint lines: operator rows and right-hand side
+  void launch_constrain_rows(int n_con, int R, int64_t n, const int32_t *rows, const int32_t *cols,
+                             const double *x, double *y, cudaStream_t s);
+  void launch_constraint_rhs(int n_con, int R, int64_t n, const int32_t *rows, const uint8_t *kind,
+                             const int32_t *p, const int32_t *q, const double *tmp,
+                             const double *nrm, const double *sg, double *b, cudaStream_t s);
   template <typename P>
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
                           const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,

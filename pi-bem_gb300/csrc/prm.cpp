@@ -57,6 +57,7 @@ extern "C" int pibem_params_default(pibem_params *p)
   p->m2l_engine                    = PIBEM_M2L_TENSOR_CORE;
   p->double_body                   = 0;
   p->symmetry_plane_z_level        = 0.0;
+  p->continuous_gradient           = 1;
   return PIBEM_OK;
 }
 
@@ -115,6 +116,8 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
         p->is_external_flow = as_bool(val) ? 1 : 0;
       else if (sec == "BEMProblem<3>" && key == "Symmetry plane z level")
         p->symmetry_plane_z_level = std::atof(v);
+      else if (sec == "BEMProblem<3>" && key == "Continuos gradient across edges")
+        p->continuous_gradient = as_bool(val) ? 1 : 0;
       else if (sec == "GB300 Params")
         {
           if (key == "Precision mode")

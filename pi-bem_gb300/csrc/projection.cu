@@ -267,12 +267,18 @@ namespace pibem
     PIBEM_CUDA(cudaMemcpyAsync(rz.data(), dots, sizeof(double) * ncol, cudaMemcpyDeviceToHost, s));
     PIBEM_CUDA(cudaStreamSynchronize(s));
     note_launch(1);
-    int it = 0;
+    // A column that has converged takes no further steps (alpha = 0 leaves its
+    // x and r as they are), so its result does not depend on the other columns.
+    int               it = 0;
+    std::vector<char> active(ncol, 1);
     for (; it < a.max_iterations; ++it)
       {
         bool done = true;
         for (int k = 0; k < ncol; ++k)
-          done = done && (rz[k] == 0 || (it > 0 && std::sqrt(rn[k]) <= a.tolerance * std::sqrt(bn[k])));
+          {
+            active[k] = !(rz[k] == 0 || (it > 0 && std::sqrt(rn[k]) <= a.tolerance * std::sqrt(bn[k])));
+            done      = done && !active[k];
+          }
         if (done)
           break;
         proj_mass_kernel<<<grid_for(N), 256, 0, s>>>(N, ncol, a.elem_off, a.elem_ids, a.cells,
@@ -282,7 +288,7 @@ namespace pibem
         PIBEM_CUDA(cudaMemcpyAsync(pq.data(), dots, sizeof(double) * ncol, cudaMemcpyDeviceToHost, s));
         PIBEM_CUDA(cudaStreamSynchronize(s));
         for (int k = 0; k < ncol; ++k)
-          al[k] = pq[k] != 0 ? rz[k] / pq[k] : 0.0;
+          al[k] = active[k] && pq[k] != 0 ? rz[k] / pq[k] : 0.0;
         PIBEM_CUDA(cudaMemcpyAsync(dots, al.data(), sizeof(double) * ncol, cudaMemcpyHostToDevice, s));
         proj_update_kernel<<<grid_for(n), 256, 0, s>>>(N, ncol, dots, p, q, x, r);
         proj_precond_kernel<<<grid_for(n), 256, 0, s>>>(N, ncol, diag, r, z);

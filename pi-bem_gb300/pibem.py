@@ -45,6 +45,7 @@ class Params(C.Structure):
         ("m2l_engine", C.c_int32),
         ("double_body", C.c_int32),
         ("symmetry_plane_z_level", C.c_double),
+        ("continuous_gradient", C.c_int32),
     ]
 
 

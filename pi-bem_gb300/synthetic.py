@@ -97,6 +97,79 @@ def _cube_surface(n: int):
     return p, np.asarray(cells, dtype=np.int32)
 
 
+def sharp_cube(n: int, half: float = 1.0):
+    """Cube [-half, half]^3 with sharp edges: every face is its own uniform n x n
+    grid with its own nodes, so nodes on the edges and corners are double
+    (triple) nodes, as CAD meshes with sharp edges give them.  Outward cells
+    (the cube-sphere's orientation).
+
+    Returns (mesh with face normals as nodal normals, double-node CSR offsets,
+    ids (every node's set includes itself), face id of every cell: 0..5 for
+    +x, -x, +y, -y, +z, -z)."""
+    ticks = np.linspace(-half, half, n + 1)
+    pts, nrm, cells, face = [], [], [], []
+    index = {}
+    f = 0
+    for a in range(3):
+        b, c = (a + 1) % 3, (a + 2) % 3
+        for sign in (1, -1):
+            s_ax, t_ax = (b, c) if sign > 0 else (c, b)
+            fixed = n if sign > 0 else 0
+            normal = [0.0, 0.0, 0.0]
+            normal[a] = float(sign)
+            for j in range(n):
+                for i in range(n):
+                    quad = []
+                    for dj in (0, 1):
+                        for di in (0, 1):
+                            ijk = [0, 0, 0]
+                            ijk[a] = fixed
+                            ijk[s_ax] = i + di
+                            ijk[t_ax] = j + dj
+                            key = (f, *ijk)
+                            k = index.get(key)
+                            if k is None:
+                                k = len(pts)
+                                index[key] = k
+                                pts.append([ticks[ijk[0]], ticks[ijk[1]], ticks[ijk[2]]])
+                                nrm.append(normal)
+                            quad.append(k)
+                    cells.append(quad)
+                    face.append(f)
+            f += 1
+    xyz = np.asarray(pts, dtype=np.float64)
+    groups = {}
+    for i, x in enumerate(np.round(xyz / half * n).astype(np.int64)):
+        groups.setdefault(tuple(x), []).append(i)
+    sets = [None] * len(xyz)
+    for g in groups.values():
+        for i in g:
+            sets[i] = sorted(g)
+    off = np.zeros(len(xyz) + 1, np.int32)
+    off[1:] = np.cumsum([len(v) for v in sets])
+    ids = np.asarray([d for v in sets for d in v], np.int32)
+    return (Mesh(xyz, np.asarray(cells, np.int32), np.asarray(nrm)), off, ids,
+            np.asarray(face, np.int32))
+
+
+def sharp_cube_case(n: int, seed: int = 7, n_sources: int = 6, dirichlet_faces=(0, 4)):
+    """Sharp cube (double nodes on every edge) with mixed data from n_sources
+    point sources of strength U(-1,1) in |s| < 0.5 (exterior problem): the nodes
+    of the faces in dirichlet_faces (default +x and +z, which share an edge)
+    are Dirichlet, the rest Neumann.
+
+    Returns mesh, dirichlet mask, tmp_rhs, exact phi, exact dphi/dn, double
+    offsets, double ids."""
+    mesh, off, ids, face = sharp_cube(n)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    q = rng.uniform(-1.0, 1.0, n_sources)
+    S = sources_in_ball(rng, n_sources)
+    mask = np.zeros(mesh.n_nodes, np.uint8)
+    mask[np.unique(mesh.cells[np.isin(face, dirichlet_faces)])] = 1
+    tmp, ph, dn = point_source_data(mesh, mask, S, q)
+    return mesh, mask, tmp, ph, dn, off, ids
+
+
 def cube_sphere(n: int, radius: float = 1.0) -> Mesh:
     p, cells = _cube_surface(n)
     return Mesh(radius * p, cells, p.copy())

@@ -37,6 +37,7 @@ def test_defaults_are_the_reference_defaults(pibem_mod):
     assert p.is_external_flow == 0
     assert p.double_body == 0
     assert p.symmetry_plane_z_level == 0.0
+    assert p.continuous_gradient == 1
 
 
 PRM = """
@@ -54,6 +55,7 @@ subsection BEMProblem<3>
   set Is external flow = true
   set Solution method  = FMA
   set Symmetry plane z level = -0.25
+  set Continuos gradient across edges = false
   subsection Quadrature rules
     set Quadrature order          = 3
     set Singular quadrature order = 7
@@ -95,6 +97,7 @@ def test_prm_reader(pibem_mod):
     assert pibem_mod.default_params().m2l_engine == pibem_mod.M2L_TENSOR_CORE
     assert p.symmetry_plane_z_level == pytest.approx(-0.25)
     assert p.double_body == 1
+    assert p.continuous_gradient == 0
 
 
 def test_create_rejects_bad_parameters(pibem_mod):
