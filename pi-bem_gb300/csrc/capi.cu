@@ -210,6 +210,7 @@ struct pibem_handle
   DBuf<int16_t>  d_ozecol;
   DBuf<int>      d_ozerow;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
+  DBuf<int>    g_ticket; // Arnoldi pass tickets (zero between launches)
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
   DBuf<double> sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm;
@@ -738,8 +739,10 @@ namespace
     h->g_z.alloc(size_t(R) * N);
     h->g_u.alloc(size_t(R) * std::max<int64_t>(N, m + 2));
     h->g_partial.alloc(size_t(R) * nblk * (m + 2));
-    h->g_h.alloc(size_t(R) * (m + 2));
-    h->g_h2.alloc(size_t(R) * (m + 2));
+    // [h (R (j+1)) | h2 (R (j+1)) | |w|^2 (R)] of the current step, one download
+    h->g_h.alloc(size_t(R) * (2 * (m + 2) + 1));
+    h->g_ticket.alloc(R);
+    h->g_ticket.zero(s);
     h->g_nrm.alloc(R);
     h->g_bn.alloc(R);
     GmresResult res;
@@ -788,17 +791,24 @@ namespace
             else
               copy_cols(h->g_z.p, N, vj, ldr, N, R, s);
             A(h->g_z.p, h->g_w.p);
-            // CGS2
-            launch_dots(N, R, j + 1, N, ldr, h->g_V.p, h->g_w.p, h->g_partial.p, nblk, h->g_h.p, s);
-            launch_gemv_sub(N, R, j + 1, N, ldr, h->g_V.p, h->g_h.p, j + 1, h->g_w.p, 1.0, s);
-            launch_dots(N, R, j + 1, N, ldr, h->g_V.p, h->g_w.p, h->g_partial.p, nblk, h->g_h2.p, s);
-            launch_gemv_sub(N, R, j + 1, N, ldr, h->g_V.p, h->g_h2.p, j + 1, h->g_w.p, 1.0, s);
-            launch_dots(N, R, 1, N, N, h->g_w.p, h->g_w.p, h->g_partial.p, nblk, h->g_nrm.p, s);
-            launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p + int64_t(j + 1) * N, ldr, s);
-            h->g_h.download(hh.data(), size_t(R) * (j + 1), s);
-            h->g_h2.download(h2.data(), size_t(R) * (j + 1), s);
-            h->g_nrm.download(nr.data(), R, s);
-            PIBEM_CUDA(cudaStreamSynchronize(s));
+            // CGS2: h = V^T w; w -= V h, h2 = V^T w; w -= V h2, |w|^2; V_{j+1} = w / |w|
+            double *d_h1 = h->g_h.p, *d_h2 = d_h1 + size_t(R) * (j + 1),
+                   *d_nr = d_h2 + size_t(R) * (j + 1);
+            launch_cgs_step(0, N, R, j + 1, N, ldr, h->g_V.p, nullptr, 0, h->g_w.p, nblk,
+                            h->g_partial.p, h->g_ticket.p, d_h1, s);
+            launch_cgs_step(1, N, R, j + 1, N, ldr, h->g_V.p, d_h1, j + 1, h->g_w.p, nblk,
+                            h->g_partial.p, h->g_ticket.p, d_h2, s);
+            launch_cgs_step(2, N, R, j + 1, N, ldr, h->g_V.p, d_h2, j + 1, h->g_w.p, nblk,
+                            h->g_partial.p, h->g_ticket.p, d_nr, s);
+            launch_normalize(N, R, h->g_w.p, d_nr, h->g_V.p + int64_t(j + 1) * N, ldr, s);
+            {
+              const size_t nh = size_t(R) * (j + 1);
+              hh.resize(2 * nh + R);
+              h->g_h.download(hh.data(), 2 * nh + R, s);
+              PIBEM_CUDA(cudaStreamSynchronize(s));
+              std::copy(hh.begin() + nh, hh.begin() + 2 * nh, h2.begin());
+              std::copy(hh.begin() + 2 * nh, hh.begin() + 2 * nh + R, nr.begin());
+            }
             ++res.iterations;
             bool all = true;
             for (int r = 0; r < R; ++r)
@@ -1677,6 +1687,11 @@ namespace
       }
   }
 
+  // BEMProblem::compute_rhs (bem_problem.cc:1220-1260): rhs = -(alpha + N) phi_D + D dphi_N
+  // with phi_D = tmp on Dirichlet nodes, dphi_N = tmp on Neumann nodes.  The
+  // near field applies N and D to the masked columns; the far field takes
+  // both layers in one expansion per column, with strengths N on Dirichlet and
+  // -D on Neumann DoFs (MODE_SWAPPED): R columns of far field instead of 2R.
   void compute_rhs_dev(pibem_handle *h, int R, const double *tmp, double *rhs)
   {
     const int64_t N = h->N();
@@ -1685,9 +1700,17 @@ namespace
     h->d_t2.alloc(size_t(R) * N);
     h->d_t3.alloc(size_t(2 * R) * N);
     launch_split_masks(N, R, tmp, h->d_dir.p, h->d_t1.p, h->d_t2.p, s);
-    fmm_apply64(h, R, h->d_t1.p, h->d_t2.p, h->d_t3.p, h->d_t3.p + int64_t(R) * N);
-    launch_rhs_combine(N, R, tmp, h->d_dir.p, h->d_alpha.p, h->d_t3.p, h->d_t3.p + int64_t(R) * N,
-                       rhs, s);
+    double *yN = h->d_t3.p, *yD = h->d_t3.p + int64_t(R) * N;
+    set_modes(h, R, MODE_SWAPPED);
+    record(h, 0);
+    launch_near_spmv<double>(h->op64, R, int(N), h->d_N.p, h->d_t1.p, yN, false, s);
+    launch_near_spmv<double>(h->op64, R, int(N), h->d_D.p, h->d_t2.p, yD, false, s);
+    record(h, 1);
+    far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, tmp, yN);
+    finish_timing(h, 0);
+    h->cnt64 += R;
+    // yN = N phi_D + far (N phi_D - D dphi_N), yD = near D dphi_N
+    launch_rhs_combine(N, R, tmp, h->d_dir.p, h->d_alpha.p, yN, yD, rhs, s);
   }
 
   // L2 projection of R columns onto the Q1 space of the mesh (device in/out):

@@ -305,8 +305,9 @@ namespace pibem
                         else
                           {
                             const uint8_t mode = modes[rq + rr];
-                            w1[rr] = mode == MODE_KER2 ? T(0) : (mode == MODE_KER1 ? xv : (d ? T(0) : xv));
-                            w2[rr] = mode == MODE_KER1 ? T(0) : (mode == MODE_KER2 ? xv : (d ? -xv : T(0)));
+                            const bool    dd   = mode == MODE_SWAPPED ? !d : d;
+                            w1[rr] = mode == MODE_KER2 ? T(0) : (mode == MODE_KER1 ? xv : (dd ? T(0) : xv));
+                            w2[rr] = mode == MODE_KER1 ? T(0) : (mode == MODE_KER2 ? xv : (dd ? -xv : T(0)));
                           }
                       }
                 }

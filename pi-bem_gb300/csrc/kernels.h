@@ -53,7 +53,8 @@ namespace pibem
   {
     MODE_COMBINED = 0, // strengths (1-dir) Ker1 - dir Ker2 (system operator)
     MODE_KER1     = 1, // double layer only (N)
-    MODE_KER2     = 2  // single layer only (D)
+    MODE_KER2     = 2, // single layer only (D)
+    MODE_SWAPPED  = 3  // strengths dir Ker1 - (1-dir) Ker2 (right-hand side: N phi_D - D dphi_N)
   };
 
   struct TreeDev

@@ -77,6 +77,81 @@ namespace pibem
       w[idx] -= sign * s;
     }
 
+    // One Gram-Schmidt step of the Arnoldi process in one launch per pass, with
+    // the same arithmetic as dots_partial + dots_final and gemv_sub:
+    //   MODE 0: out[r][i]  = V[r][i] . w[r]                      (i < ncols)
+    //   MODE 1: w[r] -= sum_i V[r][i] hin[r][i], then out[r][i] = V[r][i] . w[r]
+    //   MODE 2: w[r] -= sum_i V[r][i] hin[r][i], then out[r][0] = w[r] . w[r]
+    // Block blk of row r owns rows [blk chunk, (blk + 1) chunk) of every vector:
+    // it updates them (threads stride over the rows, the sum over i in order),
+    // then forms its partial dots (warp k takes outputs k, k + 8, ...; lanes
+    // stride over the rows; fixed shuffle tree).  The last block of row r to
+    // finish (a ticket taken after a fence) adds the nblk partials of each
+    // output in the fixed order of dots_final and resets the ticket, so the
+    // result does not depend on which block is last.
+    template <int MODE>
+    __global__ void __launch_bounds__(256)
+      cgs_step_kernel(int64_t n, int ncols, int64_t ldv, int64_t ldr, const double *__restrict__ V,
+                      const double *__restrict__ hin, int ldh, double *__restrict__ w, int nblk,
+                      double *__restrict__ partial, int *__restrict__ ticket,
+                      double *__restrict__ out)
+    {
+      const int     r     = blockIdx.y;
+      const int     blk   = blockIdx.x;
+      const double *Vr    = V + int64_t(r) * ldr;
+      double       *wr    = w + int64_t(r) * n;
+      const int64_t chunk = (n + nblk - 1) / nblk;
+      const int64_t t0 = int64_t(blk) * chunk, t1 = min(n, t0 + chunk);
+      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      if constexpr (MODE > 0)
+        {
+          const double *hr = hin + int64_t(r) * ldh;
+          for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x)
+            {
+              double s = 0;
+#pragma unroll 8
+              for (int i = 0; i < ncols; ++i)
+                s += Vr[int64_t(i) * ldv + t] * hr[i];
+              wr[t] -= s;
+            }
+          __syncthreads(); // the block's w rows are updated (visible to the block)
+        }
+      const int nout = MODE == 2 ? 1 : ncols;
+      for (int i = warp; i < nout; i += nw)
+        {
+          const double *v = MODE == 2 ? wr : Vr + int64_t(i) * ldv;
+          double        s = 0;
+#pragma unroll 8
+          for (int64_t t = t0 + lane; t < t1; t += 32)
+            s += v[t] * wr[t];
+          for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+          if (lane == 0)
+            partial[(int64_t(r) * nblk + blk) * nout + i] = s;
+        }
+      __threadfence();
+      __syncthreads();
+      __shared__ int last;
+      if (threadIdx.x == 0)
+        last = atomicAdd(ticket + r, 1) == nblk - 1;
+      __syncthreads();
+      if (!last)
+        return;
+      __threadfence();
+      for (int i = warp; i < nout; i += nw)
+        {
+          double s = 0;
+          for (int b = lane; b < nblk; b += 32)
+            s += __ldcg(partial + (int64_t(r) * nblk + b) * nout + i);
+          for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+          if (lane == 0)
+            out[int64_t(r) * nout + i] = s;
+        }
+      if (threadIdx.x == 0)
+        ticket[r] = 0;
+    }
+
     // V[r][j+1] = w[r] / hn[r]  (hn > 0), else 0
     __global__ void normalize_kernel(int64_t n, int R, const double *__restrict__ w,
                                      const double *__restrict__ nrm, double *__restrict__ out,
@@ -336,6 +411,24 @@ namespace pibem
     dots_final_kernel<<<nblocks(int64_t(R) * ncols * 32, 256), 256, 0, s>>>(R, ncols, nblk, partial, out);
     PIBEM_CUDA(cudaGetLastError());
     note_launch(2);
+  }
+
+  void launch_cgs_step(int mode, int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
+                       const double *V, const double *hin, int ldh, double *w, int nblk,
+                       double *partial, int *ticket, double *out, cudaStream_t s)
+  {
+    dim3 grid(nblk, R);
+    if (mode == 0)
+      cgs_step_kernel<0><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
+                                                     ticket, out);
+    else if (mode == 1)
+      cgs_step_kernel<1><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
+                                                     ticket, out);
+    else
+      cgs_step_kernel<2><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
+                                                     ticket, out);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
   }
 
   void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,

@@ -9,6 +9,11 @@ namespace pibem
                    const double *w, double *partial, int nblk, double *out, cudaStream_t s);
   void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
                        const double *h, int ldh, double *w, double sign, cudaStream_t s);
+  // one Arnoldi Gram-Schmidt pass in one launch (mode 0: dots; 1: subtract then
+  // dots; 2: subtract then the squared norm); ticket: R ints, zero between calls
+  void launch_cgs_step(int mode, int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
+                       const double *V, const double *hin, int ldh, double *w, int nblk,
+                       double *partial, int *ticket, double *out, cudaStream_t s);
   void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
                         int64_t ldr, cudaStream_t s);
   void launch_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s);
