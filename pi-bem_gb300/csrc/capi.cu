@@ -178,6 +178,10 @@ struct pibem_handle
   DBuf<double>  d_Pinv64;
   DBuf<float>   d_S32, d_T1f, d_T2f, d_Wf, d_opsf, d_tcimg, d_Tcf, d_lvopsf;
   DBuf<float2>  d_opsff; // the FP64 operator table as (hi, lo) FP32 pairs
+  // FP64-accurate near field as (hi, lo) FP32 pairs (modes other than FP64):
+  // the system matrix S and the right-hand side's matrix (S of the
+  // complementary mask), and the pair copy of x
+  DBuf<float2>  d_Sff, d_Srff, d_xff;
   DBuf<int>     d_err;
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
@@ -251,6 +255,7 @@ struct pibem_handle
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
         d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end, d_m2p_tnodes);
     add(d_con_row, d_con_col, d_con_p, d_con_q, d_con_kind, d_con_nrm, d_con_sg);
+    add(d_Sff, d_Srff, d_xff);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
@@ -418,17 +423,34 @@ namespace
   // caller's stream waits for the result.  y is written by the near SpMV and then added
   // to by M2P and L2P in that order, as in the one-stream sequence, so the
   // result is the same bit for bit.
+  // y = near x: with vals_ff (FP64-accurate operator) on (hi, lo) FP32 pairs
+  template <typename T>
+  void near_apply(pibem_handle *h, const OperatorDev<T> &op, int R, const T *vals,
+                  const float2 *vals_ff, const T *x, T *y, cudaStream_t st)
+  {
+    const int N = int(h->N());
+    if constexpr (std::is_same<T, double>::value)
+      if (vals_ff)
+        {
+          h->d_xff.alloc(size_t(R) * N);
+          launch_convert_d2ff(int64_t(R) * N, x, h->d_xff.p, st);
+          launch_near_spmv_ff(op, R, N, vals_ff, h->d_xff.p, y, false, st);
+          return;
+        }
+    launch_near_spmv<T>(op, R, N, vals, x, y, false, st);
+  }
+
   template <typename T>
   void system_operator(pibem_handle *h, OperatorDev<T> &op, const T *vals, DBuf<T> &M,
                        DBuf<T> &Lx, DBuf<T> &scr, DBuf<T> &Y, int R, const uint8_t *modes,
-                       const T *x, T *y)
+                       const T *x, T *y, const float2 *vals_ff = nullptr)
   {
     const int    N = int(h->N());
     cudaStream_t s = h->stream;
     if (h->timing || !h->side)
       {
         record(h, 0);
-        launch_near_spmv<T>(op, R, N, vals, x, y, false, s);
+        near_apply<T>(h, op, R, vals, vals_ff, x, y, s);
         record(h, 1);
         far_field<T>(h, op, M, Lx, scr, Y, R, modes, x, y, true);
         return;
@@ -438,7 +460,7 @@ namespace
     PIBEM_CUDA(cudaEventRecord(h->ev_fork, s));
     PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_fork, 0));
     PIBEM_CUDA(cudaStreamWaitEvent(main, h->ev_fork, 0));
-    launch_near_spmv<T>(op, R, N, vals, x, y, false, side);
+    near_apply<T>(h, op, R, vals, vals_ff, x, y, side);
     far_up<T>(h, op, M, Y, R, modes, x, true, main);
     PIBEM_CUDA(cudaEventRecord(h->ev_up, main));
     PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_up, 0));
@@ -559,7 +581,7 @@ namespace
       }
     set_modes(h, R, MODE_COMBINED);
     system_operator<double>(h, h->op64, h->d_S.p, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R,
-                            h->d_modes.p, xin, y);
+                            h->d_modes.p, xin, y, h->op64.ops_ff ? h->d_Sff.p : nullptr);
     finish_timing(h, 0);
     if (!h->have_dirichlet)
       shift_by_norm(h, R, y);
@@ -1610,7 +1632,8 @@ namespace
     h->bytes_resident = h->d_N.bytes() * 3 + h->d_S32.bytes() + h->d_T1.bytes() * 2 +
                         h->d_T1f.bytes() * 2 + h->d_W.bytes() + h->d_Wf.bytes() +
                         h->d_ops.bytes() + h->d_opsf.bytes() + h->d_qpts.bytes() * 2 +
-                        h->d_qshape.bytes() + h->d_qjxw.bytes();
+                        h->d_qshape.bytes() + h->d_qjxw.bytes() +
+                        (P.precision_mode != PIBEM_PRECISION_FP64 ? 2 * h->d_N.bytes() : 0);
     if (P.hbm_budget_gb > 0 && double(h->bytes_resident) > P.hbm_budget_gb * 1e9)
       throw Error(PIBEM_ENOMEM_HBM, "resident operator exceeds the HBM budget");
     h->mesh_ok       = true;
@@ -1651,6 +1674,29 @@ namespace
                                h->d_ncol_ptr.p, h->d_nrow_ptr.p, h->d_nrows.p, h->d_ncols.p,
                                h->d_dir.p, h->d_alpha.p, h->d_N.p, h->d_D.p, h->d_S.p, h->d_S32.p,
                                s);
+    // FP64-accurate near field as FP32 pairs: S, and S of the complementary mask
+    // for the right-hand side (not needed by the plain FP64 path)
+    h->d_Sff.release();
+    h->d_Srff.release();
+    if (h->prm.precision_mode != PIBEM_PRECISION_FP64 && pl.nval_ptr.back() > 0)
+      {
+        const int64_t nval = pl.nval_ptr.back();
+        h->d_Sff.alloc(nval);
+        launch_convert_d2ff(nval, h->d_S.p, h->d_Sff.p, s);
+        std::vector<uint8_t> dirc(h->dir.size());
+        for (size_t i = 0; i < dirc.size(); ++i)
+          dirc[i] = h->dir[i] ? 0 : 1;
+        DBuf<uint8_t> d_dirc;
+        d_dirc.upload(dirc, s);
+        DBuf<double> Sr;
+        Sr.alloc(nval);
+        launch_build_system_matrix(nval, int(pl.nleaf_box.size()), h->d_nval_ptr.p, h->d_ncol_ptr.p,
+                                   h->d_nrow_ptr.p, h->d_nrows.p, h->d_ncols.p, d_dirc.p,
+                                   h->d_alpha.p, h->d_N.p, h->d_D.p, Sr.p, nullptr, s);
+        h->d_Srff.alloc(nval);
+        launch_convert_d2ff(nval, Sr.p, h->d_Srff.p, s);
+        PIBEM_CUDA(cudaStreamSynchronize(s));
+      }
     // combined-strength P2M tables of the system operator (one row read per row)
     {
       const int64_t nr = int64_t(pl.prow_dof.size());
@@ -1700,8 +1746,23 @@ namespace
     h->d_t2.alloc(size_t(R) * N);
     h->d_t3.alloc(size_t(2 * R) * N);
     launch_split_masks(N, R, tmp, h->d_dir.p, h->d_t1.p, h->d_t2.p, s);
-    double *yN = h->d_t3.p, *yD = h->d_t3.p + int64_t(R) * N;
     set_modes(h, R, MODE_SWAPPED);
+    if (h->op64.ops_ff && h->d_Srff.p)
+      {
+        // FP64-accurate operator: the near part is one SpMV with the matrix of
+        // the complementary mask (N on Dirichlet, -D on Neumann columns, alpha
+        // on Dirichlet rows) on float-float pairs; rhs = -(near + far)
+        record(h, 0);
+        near_apply<double>(h, h->op64, R, nullptr, h->d_Srff.p, tmp, rhs, s);
+        record(h, 1);
+        far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, tmp,
+                          rhs);
+        finish_timing(h, 0);
+        h->cnt64 += R;
+        launch_axpby(int64_t(R) * N, 0.0, rhs, -1.0, rhs, s);
+        return;
+      }
+    double *yN = h->d_t3.p, *yD = h->d_t3.p + int64_t(R) * N;
     record(h, 0);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_N.p, h->d_t1.p, yN, false, s);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_D.p, h->d_t2.p, yD, false, s);

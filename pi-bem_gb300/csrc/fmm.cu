@@ -250,6 +250,97 @@ namespace pibem
       asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
 
+    // FP64-accurate near-field SpMV for one column on the FP32 pipes: the
+    // values and x as (hi, lo) FP32 pairs (8 bytes a value, as FP64), every
+    // product split exactly (TwoProduct) with its cross terms, the row sums
+    // carried with TwoSum; about 11 FP32 instructions per value, so the kernel
+    // streams at HBM speed where FP64 FMA (1/58 of the FP32 rate) could not.
+    // Same structure as near_leaf_pipe_kernel: persistent blocks, the next
+    // leaf's x gathered with cp.async while the warps stream two rows each.
+    // y[row] = hi + lo in FP64 (acc: added).
+    __global__ void __launch_bounds__(256)
+      near_leaf_ff_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ nrow_ptr,
+                          const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
+                          const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
+                          const float2 *__restrict__ vals, const float2 *__restrict__ x,
+                          double *__restrict__ y, bool acc)
+    {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      float2   *sxb  = reinterpret_cast<float2 *>(smem_raw); // [2][ld_max]
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      auto gather = [&](int l, int b) {
+        const int64_t c0 = ncol_ptr[l], nc = ncol_ptr[l + 1] - c0;
+        const int64_t ld = (nc + 3) / 4 * 4;
+        float2       *sx = sxb + int64_t(b) * ld_max;
+        for (int64_t c = threadIdx.x; c < ld; c += blockDim.x)
+          if (c < nc)
+            cp_async8(reinterpret_cast<double *>(sx + c), reinterpret_cast<const double *>(x + ncols[c0 + c]));
+          else
+            sx[c] = make_float2(0.f, 0.f);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      };
+      int leaf = blockIdx.x, buf = 0;
+      if (leaf < n_leaves)
+        gather(leaf, 0);
+      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
+        {
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
+          __syncthreads();
+          const int next = leaf + gridDim.x;
+          if (next < n_leaves)
+            gather(next, buf ^ 1);
+          const float2 *sx = sxb + int64_t(buf) * ld_max;
+          const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
+          const int64_t ld = (nc + 3) / 4 * 4;
+          const int     n4 = int(ld / 4);
+          const int64_t r0 = nrow_ptr[leaf], nr = nrow_ptr[leaf + 1] - r0;
+          const float2 *V  = vals + nval_ptr[leaf];
+          for (int64_t row = warp; row < nr; row += 2 * nw)
+            {
+              const bool    two = row + nw < nr;
+              const float2 *v0  = V + row * ld;
+              const float2 *v1  = V + (two ? row + nw : row) * ld;
+              float         h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+#pragma unroll 2
+              for (int j = lane; j < n4; j += 32)
+                {
+                  const float4 a0 = *reinterpret_cast<const float4 *>(v0 + 4 * j);
+                  const float4 b0 = *reinterpret_cast<const float4 *>(v0 + 4 * j + 2);
+                  const float4 a1 = *reinterpret_cast<const float4 *>(v1 + 4 * j);
+                  const float4 b1 = *reinterpret_cast<const float4 *>(v1 + 4 * j + 2);
+                  const float2 x0 = sx[4 * j], x1 = sx[4 * j + 1], x2 = sx[4 * j + 2], x3 = sx[4 * j + 3];
+                  ff_mac(h0, l0, make_float2(a0.x, a0.y), x0);
+                  ff_mac(h0, l0, make_float2(a0.z, a0.w), x1);
+                  ff_mac(h0, l0, make_float2(b0.x, b0.y), x2);
+                  ff_mac(h0, l0, make_float2(b0.z, b0.w), x3);
+                  ff_mac(h1, l1, make_float2(a1.x, a1.y), x0);
+                  ff_mac(h1, l1, make_float2(a1.z, a1.w), x1);
+                  ff_mac(h1, l1, make_float2(b1.x, b1.y), x2);
+                  ff_mac(h1, l1, make_float2(b1.z, b1.w), x3);
+                }
+              float2 t0 = ff_norm(h0, l0), t1 = ff_norm(h1, l1);
+              for (int o = 16; o > 0; o >>= 1)
+                {
+                  t0 = ff_add(t0, make_float2(__shfl_xor_sync(0xffffffffu, t0.x, o),
+                                              __shfl_xor_sync(0xffffffffu, t0.y, o)));
+                  t1 = ff_add(t1, make_float2(__shfl_xor_sync(0xffffffffu, t1.x, o),
+                                              __shfl_xor_sync(0xffffffffu, t1.y, o)));
+                }
+              if (lane == 0)
+                {
+                  double &o0 = y[nrows[r0 + row]];
+                  o0         = acc ? __dadd_rn(o0, ff_join(t0)) : ff_join(t0);
+                  if (two)
+                    {
+                      double &o1 = y[nrows[r0 + row + nw]];
+                      o1         = acc ? __dadd_rn(o1, ff_join(t1)) : ff_join(t1);
+                    }
+                }
+            }
+        }
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+
     // P2M apply: M^[leaf][r][k] = sum_rows w(row, r) T[row][k] x_r[dof(row)],
     // w selecting the double layer (Ker1), the single layer (Ker2) or the
     // combined system strengths.  One warp per leaf, 8 leaves per block: lane l
@@ -785,6 +876,31 @@ namespace pibem
                                              op.nrows, op.ncols, vals, x, y, accumulate);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
+  }
+
+  void launch_near_spmv_ff(const OperatorDev<double> &op, int R, int N, const float2 *vals,
+                           const float2 *xff, double *y, bool accumulate, cudaStream_t s)
+  {
+    if (op.n_near_leaves == 0)
+      return;
+    const int64_t maxnc = (std::max<int64_t>(op.max_near_cols, 1) + 3) / 4 * 4;
+    int           dev = 0, n_sm = 1;
+    PIBEM_CUDA(cudaGetDevice(&dev));
+    PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t smem1 = size_t(2) * maxnc * sizeof(float2);
+    if (smem1 > 48 * 1024)
+      raise_smem_limit(reinterpret_cast<const void *>(near_leaf_ff_kernel), smem1);
+    const int grid = std::min(op.n_near_leaves, 6 * n_sm);
+    // one launch per column: a column's result does not depend on R
+    for (int r = 0; r < R; ++r)
+      {
+        near_leaf_ff_kernel<<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr,
+                                                     op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols,
+                                                     vals, xff + int64_t(r) * N,
+                                                     y + int64_t(r) * N, accumulate);
+        PIBEM_CUDA(cudaGetLastError());
+        note_launch();
+      }
   }
 
   template <typename T>

@@ -171,6 +171,10 @@ namespace pibem
   void launch_downward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *Lx,
                                 float2 *Y, cudaStream_t s);
   void launch_convert_d2ff(int64_t n, const double *a, float2 *b, cudaStream_t s);
+  // FP64-accurate near SpMV on (hi, lo) FP32 pairs, one launch per column:
+  // y[r] (=|+=) vals x[r], x given as pairs, y in FP64
+  void launch_near_spmv_ff(const OperatorDev<double> &op, int R, int N, const float2 *vals,
+                           const float2 *xff, double *y, bool accumulate, cudaStream_t s);
   void launch_convert_ff2d(int64_t n, const float2 *a, double *b, cudaStream_t s);
   // M2L sums of all levels into Lx (the first step of the downward pass, before
   // the levels); does nothing unless the fused level passes apply

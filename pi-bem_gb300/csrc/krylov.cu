@@ -218,8 +218,9 @@ namespace pibem
       const int64_t loc = vi - val_ptr[lo];
       if (loc % ld >= nc)
         {
-          S[vi]   = 0.0;
-          S32[vi] = 0.0f;
+          S[vi] = 0.0;
+          if (S32)
+            S32[vi] = 0.0f;
           return;
         }
       const int row = rows[row_ptr[lo] + loc / ld];
@@ -227,8 +228,9 @@ namespace pibem
       double        v   = dir[col] ? -Dv[vi] : Nv[vi];
       if (row == col && !dir[row])
         v += alpha[row];
-      S[vi]   = v;
-      S32[vi] = float(v);
+      S[vi] = v;
+      if (S32)
+        S32[vi] = float(v);
     }
 
     // rhs = -(outN + alpha*(tmp.dir)) + outD  (BEMProblem::compute_rhs, bem_problem.cc:1240-1258)
