@@ -348,12 +348,11 @@ namespace
     if constexpr (std::is_same<T, double>::value)
       if (op.ops_ff)
         {
-          // float-float passes on (hi, lo) expansions; M back in FP64 for M2P
+          // float-float passes on (hi, lo) expansions (M2P reads them too)
           float2 *Mff = h->d_Mff.p, *Yff = reinterpret_cast<float2 *>(Y.p);
           launch_convert_d2ff(int64_t(need), M.p, Mff, s);
           for (int l = h->tree.L; l >= 1; --l)
             launch_upward_level_ff(op, R, l, Mff, Yff, s);
-          launch_convert_ff2d(int64_t(need), Mff, M.p, s);
           record(h, 3);
           return;
         }
@@ -400,6 +399,20 @@ namespace
     record(h, 5);
   }
 
+  // M2P into y: the FP64-accurate operator evaluates from the (hi, lo)
+  // multipoles in float-float
+  template <typename T>
+  void m2p_apply(pibem_handle *h, const OperatorDev<T> &op, int R, const T *M, T *y, cudaStream_t st)
+  {
+    if constexpr (std::is_same<T, double>::value)
+      if (op.ops_ff)
+        {
+          launch_m2p_ff(op, h->td, R, int(h->N()), h->d_Mff.p, y, st);
+          return;
+        }
+    launch_m2p<T>(op, h->td, R, int(h->N()), M, y, st);
+  }
+
   template <typename T>
   void far_field(pibem_handle *h, OperatorDev<T> &op, DBuf<T> &M, DBuf<T> &Lx, DBuf<T> &scr,
                  DBuf<T> &Y, int R, const uint8_t *modes, const T *x, T *y, bool combined = false)
@@ -409,7 +422,7 @@ namespace
     far_alloc<T>(h, op, M, Lx, scr, Y, R);
     far_up<T>(h, op, M, Y, R, modes, x, combined, s);
     far_down<T>(h, op, M, Lx, Y, R, s);
-    launch_m2p<T>(op, h->td, R, N, M.p, y, s);
+    m2p_apply<T>(h, op, R, M.p, y, s);
     record(h, 6);
     launch_l2p<T>(op, R, N, Lx.p, y, s);
     record(h, 7);
@@ -464,7 +477,7 @@ namespace
     far_up<T>(h, op, M, Y, R, modes, x, true, main);
     PIBEM_CUDA(cudaEventRecord(h->ev_up, main));
     PIBEM_CUDA(cudaStreamWaitEvent(side, h->ev_up, 0));
-    launch_m2p<T>(op, h->td, R, N, M.p, y, side);
+    m2p_apply<T>(h, op, R, M.p, y, side);
     PIBEM_CUDA(cudaEventRecord(h->ev_side, side));
     far_down<T>(h, op, M, Lx, Y, R, main);
     PIBEM_CUDA(cudaStreamWaitEvent(main, h->ev_side, 0));

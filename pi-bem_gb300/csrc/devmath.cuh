@@ -79,6 +79,7 @@ namespace pibem
   {
     double cmm[21], cm1[21], ra[21][21], rb[21][21];
     float  fcmm[21], fcm1[21], fra[21][21], frb[21][21];
+    float2 ffcmm[21], ffcm1[21], ffra[21][21], ffrb[21][21]; // (hi, lo) pairs
   };
   // One copy per translation unit that evaluates expansions; filled by
   // fill_legendre_tables() + cudaMemcpyToSymbol from that unit.
@@ -86,6 +87,10 @@ namespace pibem
 
   inline void fill_legendre_tables(LegendreTables &t)
   {
+    auto pair = [](double v) {
+      const float hi = float(v);
+      return make_float2(hi, float(v - double(hi)));
+    };
     for (int m = 0; m <= 20; ++m)
       {
         t.cmm[m] = m > 0 ? std::sqrt((2.0 * m - 1.0) / (2.0 * m)) : 0.0;
@@ -97,9 +102,13 @@ namespace pibem
             t.rb[n][m] = ok ? std::sqrt(double((n - 1) * (n - 1) - m * m)) / std::sqrt(double(n * n - m * m)) : 0.0;
             t.fra[n][m] = float(t.ra[n][m]);
             t.frb[n][m] = float(t.rb[n][m]);
+            t.ffra[n][m] = pair(t.ra[n][m]);
+            t.ffrb[n][m] = pair(t.rb[n][m]);
           }
         t.fcmm[m] = float(t.cmm[m]);
         t.fcm1[m] = float(t.cm1[m]);
+        t.ffcmm[m] = pair(t.cmm[m]);
+        t.ffcm1[m] = pair(t.cm1[m]);
       }
   }
 

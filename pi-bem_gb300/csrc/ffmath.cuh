@@ -55,4 +55,36 @@ namespace pibem
   }
 
   __device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+  __device__ __forceinline__ float2 ff_sub(float2 a, float2 b) { return ff_add(a, ff_neg(b)); }
+
+  // a * b: TwoProduct of the leading parts plus the cross terms, renormalised
+  __device__ __forceinline__ float2 ff_mul(float2 a, float2 b)
+  {
+    const float p = __fmul_rn(a.x, b.x);
+    float       e = __fmaf_rn(a.x, b.x, -p);
+    e             = __fmaf_rn(a.x, b.y, e);
+    e             = __fmaf_rn(a.y, b.x, e);
+    const float h = __fadd_rn(p, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, p)));
+  }
+
+  // 1 / a: the FP32 reciprocal r refined by one Newton step in float-float,
+  // r + r (1 - a r)
+  __device__ __forceinline__ float2 ff_recip(float2 a)
+  {
+    const float2 r = make_float2(__frcp_rn(a.x), 0.f);
+    const float2 e = ff_sub(make_float2(1.f, 0.f), ff_mul(a, r));
+    return ff_add(r, ff_mul(r, e));
+  }
+
+  // sqrt(a), a >= 0: the FP32 root s refined by one Newton step,
+  // s + (a - s^2) / (2 s) (the correction needs FP32 accuracy only)
+  __device__ __forceinline__ float2 ff_sqrt(float2 a)
+  {
+    if (!(a.x > 0.f))
+      return make_float2(0.f, 0.f);
+    const float  s = __fsqrt_rn(a.x);
+    const float2 t = ff_sub(a, ff_mul(make_float2(s, 0.f), make_float2(s, 0.f)));
+    return ff_add(make_float2(s, 0.f), make_float2(__fmul_rn(t.x, __frcp_rn(__fmul_rn(2.f, s))), 0.f));
+  }
 } // namespace pibem

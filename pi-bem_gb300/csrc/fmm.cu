@@ -741,6 +741,100 @@ namespace pibem
           eval_expansion_fast<T, T>(M + (s * R + r) * K, p, rx, ry, rz, true) * ih;
     }
 
+    // The table-driven evaluation of eval_expansion_fast (same recurrences, same
+    // order of terms) in float-float arithmetic for the FP64-accurate operator:
+    // r is the offset from the box centre in box units (pairs), coef the
+    // expansion as pairs.  About 90 FP32 instructions per term against the
+    // FP64 pipe's 1/58 rate.
+    __device__ float2 eval_multipole_ff(const float2 *__restrict__ coef, int p, float2 rx, float2 ry,
+                                        float2 rz)
+    {
+      const float2 rxy2 = ff_add(ff_mul(rx, rx), ff_mul(ry, ry));
+      const float2 rho  = ff_sqrt(ff_add(rxy2, ff_mul(rz, rz)));
+      const float2 inv  = ff_recip(rho);
+      const float2 x    = ff_mul(rz, inv);
+      const float2 s    = ff_sqrt(ff_sub(make_float2(1.f, 0.f), ff_mul(x, x)));
+      const float2 rxy  = ff_sqrt(rxy2);
+      float2       cb = make_float2(1.f, 0.f), sb = make_float2(0.f, 0.f);
+      if (rxy.x > 0.f)
+        {
+          const float2 ir = ff_recip(rxy);
+          cb              = ff_mul(rx, ir);
+          sb              = ff_mul(ry, ir);
+        }
+      const float2 step = inv;
+      float2       acc = make_float2(0.f, 0.f), pmm = make_float2(1.f, 0.f), rpm = inv;
+      float2       cm = make_float2(1.f, 0.f), sm = make_float2(0.f, 0.f);
+      for (int m = 0; m <= p; ++m)
+        {
+          if (m > 0)
+            {
+              pmm             = ff_mul(pmm, ff_mul(ff_neg(c_leg.ffcmm[m]), s));
+              rpm             = ff_mul(rpm, step);
+              const float2 c2 = ff_sub(ff_mul(cm, cb), ff_mul(sm, sb));
+              sm              = ff_add(ff_mul(sm, cb), ff_mul(cm, sb));
+              cm              = c2;
+            }
+          // 2 cm and -2 sm: exact scalings
+          const float2 cr = m == 0 ? make_float2(1.f, 0.f) : make_float2(2.f * cm.x, 2.f * cm.y);
+          const float2 ci = m == 0 ? make_float2(0.f, 0.f) : make_float2(-2.f * sm.x, -2.f * sm.y);
+          auto term = [&](int n) {
+            const int    k0 = n * n + (m == 0 ? 0 : 2 * m - 1);
+            const float2 v  = m > 0 ? ff_add(ff_mul(coef[k0], cr), ff_mul(coef[k0 + 1], ci))
+                                    : ff_mul(coef[k0], cr);
+            return v;
+          };
+          float2 p0 = pmm, rp = rpm;
+          acc       = ff_add(acc, ff_mul(ff_mul(term(m), p0), rp));
+          if (m + 1 <= p)
+            {
+              float2 p1 = ff_mul(ff_mul(x, c_leg.ffcm1[m]), pmm);
+              rp        = ff_mul(rp, step);
+              acc       = ff_add(acc, ff_mul(ff_mul(term(m + 1), p1), rp));
+              for (int n = m + 2; n <= p; ++n)
+                {
+                  const float2 p2 = ff_sub(ff_mul(ff_mul(c_leg.ffra[n][m], x), p1),
+                                           ff_mul(c_leg.ffrb[n][m], p0));
+                  p0 = p1;
+                  p1 = p2;
+                  rp = ff_mul(rp, step);
+                  acc = ff_add(acc, ff_mul(ff_mul(term(n), p1), rp));
+                }
+            }
+        }
+      return acc;
+    }
+
+    // M2P phase 1 of the FP64-accurate operator: as m2p_eval_kernel, from the
+    // (hi, lo) multipoles; the offset from the centre is formed in FP64 and
+    // split, the scaling by 1 / h in float-float; the value stored in FP64.
+    __global__ void m2p_eval_ff_kernel(int64_t n_items, int R, int K, int p,
+                                       const int64_t *__restrict__ item_ptr,
+                                       const int32_t *__restrict__ item_pair,
+                                       const int32_t *__restrict__ pair_tgt,
+                                       const int32_t *__restrict__ src,
+                                       const int64_t *__restrict__ tnode_ptr,
+                                       const int32_t *__restrict__ tnodes,
+                                       const double *__restrict__ xyz,
+                                       const double *__restrict__ center,
+                                       const double *__restrict__ delta,
+                                       const float2 *__restrict__ M, double *__restrict__ scratch)
+    {
+      const int64_t it = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (it >= n_items)
+        return;
+      const int64_t e    = item_pair[it];
+      const int64_t s    = src[e];
+      const int     node = tnodes[tnode_ptr[pair_tgt[e]] + (it - item_ptr[e])];
+      const float2  ih   = ff_recip(ff_split(delta[s]));
+      const float2  rx   = ff_mul(ff_split(__dsub_rn(xyz[3 * int64_t(node)], center[3 * s])), ih);
+      const float2  ry   = ff_mul(ff_split(__dsub_rn(xyz[3 * int64_t(node) + 1], center[3 * s + 1])), ih);
+      const float2  rz   = ff_mul(ff_split(__dsub_rn(xyz[3 * int64_t(node) + 2], center[3 * s + 2])), ih);
+      for (int r = 0; r < R; ++r)
+        scratch[int64_t(r) * n_items + it] =
+          ff_join(ff_mul(eval_multipole_ff(M + (s * R + r) * K, p, rx, ry, rz), ih));
+    }
+
     // M2P phase 2: one warp per target box, one lane per node of the box: the
     // node's values over the box's sources, added in list order to y.  The
     // items of a target box are contiguous, source-major (item_ptr[e] =
@@ -1149,6 +1243,23 @@ namespace pibem
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
     m2p_sum_kernel<T><<<unsigned((op.n_m2p_tgt + 7) / 8), 256, 0, s>>>(
+      op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt, op.m2p_src_ptr,
+      op.m2p_item_ptr, op.m2p_tnodes, op.m2p_scratch, y);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_m2p_ff(const OperatorDev<double> &op, const TreeDev &td, int R, int N, const float2 *Mff,
+                     double *y, cudaStream_t s)
+  {
+    if (op.n_m2p_tgt == 0)
+      return;
+    m2p_eval_ff_kernel<<<unsigned((op.n_m2p_items + 127) / 128), 128, 0, s>>>(
+      op.n_m2p_items, R, op.K, op.p, op.m2p_item_ptr, op.m2p_item_pair, op.m2p_pair_tgt, op.m2p_src,
+      op.m2p_tnode_ptr, op.m2p_tnodes, td.xyz, td.center, td.delta, Mff, op.m2p_scratch);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+    m2p_sum_kernel<double><<<unsigned((op.n_m2p_tgt + 7) / 8), 256, 0, s>>>(
       op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt, op.m2p_src_ptr,
       op.m2p_item_ptr, op.m2p_tnodes, op.m2p_scratch, y);
     PIBEM_CUDA(cudaGetLastError());

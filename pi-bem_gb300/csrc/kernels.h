@@ -171,6 +171,9 @@ namespace pibem
   void launch_downward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *Lx,
                                 float2 *Y, cudaStream_t s);
   void launch_convert_d2ff(int64_t n, const double *a, float2 *b, cudaStream_t s);
+  // FP64-accurate M2P from (hi, lo) multipoles (float-float evaluation)
+  void launch_m2p_ff(const OperatorDev<double> &op, const TreeDev &td, int R, int N, const float2 *Mff,
+                     double *y, cudaStream_t s);
   // FP64-accurate near SpMV on (hi, lo) FP32 pairs, one launch per column:
   // y[r] (=|+=) vals x[r], x given as pairs, y in FP64
   void launch_near_spmv_ff(const OperatorDev<double> &op, int R, int N, const float2 *vals,
