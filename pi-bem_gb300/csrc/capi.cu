@@ -443,7 +443,7 @@ namespace
   {
     const int N = int(h->N());
     if constexpr (std::is_same<T, double>::value)
-      if (vals_ff)
+      if (vals_ff && near_ff_fits(op))
         {
           h->d_xff.alloc(size_t(R) * N);
           launch_convert_d2ff(int64_t(R) * N, x, h->d_xff.p, st);
@@ -1760,7 +1760,7 @@ namespace
     h->d_t3.alloc(size_t(2 * R) * N);
     launch_split_masks(N, R, tmp, h->d_dir.p, h->d_t1.p, h->d_t2.p, s);
     set_modes(h, R, MODE_SWAPPED);
-    if (h->op64.ops_ff && h->d_Srff.p)
+    if (h->op64.ops_ff && h->d_Srff.p && near_ff_fits(h->op64))
       {
         // FP64-accurate operator: the near part is one SpMV with the matrix of
         // the complementary mask (N on Dirichlet, -D on Neumann columns, alpha

@@ -972,6 +972,12 @@ namespace pibem
     note_launch();
   }
 
+  bool near_ff_fits(const OperatorDev<double> &op)
+  {
+    const int64_t maxnc = (std::max<int64_t>(op.max_near_cols, 1) + 3) / 4 * 4;
+    return size_t(2) * maxnc * sizeof(float2) <= 227 * 1024;
+  }
+
   void launch_near_spmv_ff(const OperatorDev<double> &op, int R, int N, const float2 *vals,
                            const float2 *xff, double *y, bool accumulate, cudaStream_t s)
   {

@@ -174,6 +174,8 @@ namespace pibem
   // FP64-accurate M2P from (hi, lo) multipoles (float-float evaluation)
   void launch_m2p_ff(const OperatorDev<double> &op, const TreeDev &td, int R, int N, const float2 *Mff,
                      double *y, cudaStream_t s);
+  // whether the leaf blocks' x pairs (two buffers) fit in shared memory
+  bool near_ff_fits(const OperatorDev<double> &op);
   // FP64-accurate near SpMV on (hi, lo) FP32 pairs, one launch per column:
   // y[r] (=|+=) vals x[r], x given as pairs, y in FP64
   void launch_near_spmv_ff(const OperatorDev<double> &op, int R, int N, const float2 *vals,
