@@ -749,16 +749,17 @@ namespace
   // z = P^-1 v for R columns (v column stride ldv): the FP64 inverses where the
   // handle keeps them (GMRES on an FP64-accurate operator), else the FP32 ones
   void apply_block_jacobi(pibem_handle *h, int R, const double *v, int64_t ldv, double *z,
-                          cudaStream_t s)
+                          cudaStream_t s, const double *nrm2 = nullptr, double *vout = nullptr,
+                          int64_t ldo = 0)
   {
     const int     nl = int(h->blk_ptr.size()) - 1;
     const int64_t N  = h->N();
     if (h->d_Pinv64.p)
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
-                         h->d_Pinv64.p, v, ldv, z, s);
+                         h->d_Pinv64.p, v, ldv, z, s, nrm2, vout, ldo);
     else
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
-                         h->d_Pinv.p, v, ldv, z, s);
+                         h->d_Pinv.p, v, ldv, z, s, nrm2, vout, ldo);
   }
 
   GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
@@ -816,15 +817,17 @@ namespace
         std::fill(g.begin(), g.end(), 0.0);
         for (int r = 0; r < R; ++r)
           g[size_t(r) * (m + 1)] = beta[r];
-        int j = 0;
+        int  j      = 0;
+        bool z_next = false; // z = P^-1 V_j already formed with the normalisation of V_j
         for (; j < m; ++j)
           {
             // z = P^-1 V_j ; w = A z
             const double *vj = h->g_V.p + int64_t(j) * N;
-            if (prec)
+            if (prec && !z_next)
               apply_block_jacobi(h, R, vj, ldr, h->g_z.p, s);
-            else
+            else if (!prec)
               copy_cols(h->g_z.p, N, vj, ldr, N, R, s);
+            z_next = false;
             A(h->g_z.p, h->g_w.p);
             // CGS2: h = V^T w; w -= V h, h2 = V^T w; w -= V h2, |w|^2; V_{j+1} = w / |w|
             double *d_h1 = h->g_h.p, *d_h2 = d_h1 + size_t(R) * (j + 1),
@@ -835,7 +838,16 @@ namespace
                             h->g_partial.p, h->g_ticket.p, d_h2, s);
             launch_cgs_step(2, N, R, j + 1, N, ldr, h->g_V.p, d_h2, j + 1, h->g_w.p, nblk,
                             h->g_partial.p, h->g_ticket.p, d_nr, s);
-            launch_normalize(N, R, h->g_w.p, d_nr, h->g_V.p + int64_t(j + 1) * N, ldr, s);
+            if (prec)
+              {
+                // V_{j+1} = w / |w| and the next step's z = P^-1 V_{j+1} in one
+                // pass (formed even if the next step does not come)
+                apply_block_jacobi(h, R, h->g_w.p, N, h->g_z.p, s, d_nr, h->g_V.p + int64_t(j + 1) * N,
+                                   ldr);
+                z_next = true;
+              }
+            else
+              launch_normalize(N, R, h->g_w.p, d_nr, h->g_V.p + int64_t(j + 1) * N, ldr, s);
             {
               const size_t nh = size_t(R) * (j + 1);
               hh.resize(2 * nh + R);

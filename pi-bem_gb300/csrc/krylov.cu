@@ -299,7 +299,8 @@ namespace pibem
       block_apply_kernel(int n_leaves, int max_rows, int R, int64_t n, int64_t ldv,
                          const int64_t *__restrict__ row_ptr, const int64_t *__restrict__ blk_ptr,
                          const int32_t *__restrict__ rows, const P *__restrict__ Pinv,
-                         const double *__restrict__ v, double *__restrict__ z)
+                         const double *__restrict__ v, double *__restrict__ z,
+                         const double *__restrict__ nrm2, double *__restrict__ vout, int64_t ldo)
     {
       extern __shared__ __align__(8) unsigned char sv_raw[];
       P        *sv_all = reinterpret_cast<P *>(sv_raw);
@@ -313,8 +314,22 @@ namespace pibem
       const P      *B  = Pinv + blk_ptr[leaf];
       for (int rr = 0; rr < R; ++rr)
         {
-          for (int c = lane; c < nr; c += 32)
-            sv[c] = P(v[int64_t(rr) * ldv + rows[r0 + c]]);
+          if (nrm2)
+            {
+              // the Arnoldi normalisation fused in (as normalize_kernel):
+              // vout = v / |v|, then z = P^-1 vout
+              const double h = sqrt(nrm2[rr]);
+              for (int c = lane; c < nr; c += 32)
+                {
+                  const int64_t row = rows[r0 + c];
+                  const double  vn  = h > 0 ? v[int64_t(rr) * ldv + row] / h : 0.0;
+                  vout[int64_t(rr) * ldo + row] = vn;
+                  sv[c]                         = P(vn);
+                }
+            }
+          else
+            for (int c = lane; c < nr; c += 32)
+              sv[c] = P(v[int64_t(rr) * ldv + rows[r0 + c]]);
           __syncwarp();
           for (int i = lane; i - lane < nr; i += 32)
             {
@@ -547,7 +562,8 @@ namespace pibem
   template <typename P>
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
                           const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,
-                          const double *v, int64_t ldv, double *z, cudaStream_t s)
+                          const double *v, int64_t ldv, double *z, cudaStream_t s,
+                          const double *nrm2, double *vout, int64_t ldo)
   {
     if (n_leaves == 0)
       return;
@@ -556,16 +572,17 @@ namespace pibem
     if (smem > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel<P>), smem);
     block_apply_kernel<P><<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
-                                                                blk_ptr, rows, Pinv, v, z);
+                                                                blk_ptr, rows, Pinv, v, z, nrm2,
+                                                                vout, ldo);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
   template void launch_block_apply<float>(int, int, int, int64_t, const int64_t *, const int64_t *,
                                           const int32_t *, const float *, const double *, int64_t,
-                                          double *, cudaStream_t);
+                                          double *, cudaStream_t, const double *, double *, int64_t);
   template void launch_block_apply<double>(int, int, int, int64_t, const int64_t *, const int64_t *,
                                            const int32_t *, const double *, const double *, int64_t,
-                                           double *, cudaStream_t);
+                                           double *, cudaStream_t, const double *, double *, int64_t);
 
   template <typename T>
   void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,

@@ -31,8 +31,11 @@ namespace pibem
   void launch_constraint_rhs(int n_con, int R, int64_t n, const int32_t *rows, const uint8_t *kind,
                              const int32_t *p, const int32_t *q, const double *tmp,
                              const double *nrm, const double *sg, double *b, cudaStream_t s);
+  // z = P^-1 v (leaf-block Jacobi); with nrm2: v is first normalised, column
+  // r by sqrt(nrm2[r]), and written to vout (column stride ldo)
   template <typename P>
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
                           const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,
-                          const double *v, int64_t ldv, double *z, cudaStream_t s);
+                          const double *v, int64_t ldv, double *z, cudaStream_t s,
+                          const double *nrm2 = nullptr, double *vout = nullptr, int64_t ldo = 0);
 } // namespace pibem
