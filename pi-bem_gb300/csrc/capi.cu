@@ -215,6 +215,7 @@ struct pibem_handle
   DBuf<int>      d_ozerow;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
   DBuf<int>    g_ticket; // Arnoldi pass tickets (zero between launches)
+  PinnedBuf<double> g_hpin; // host copy of [h | h2 | |w|^2] of an Arnoldi step
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
   DBuf<double> sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm;
@@ -850,11 +851,14 @@ namespace
               launch_normalize(N, R, h->g_w.p, d_nr, h->g_V.p + int64_t(j + 1) * N, ldr, s);
             {
               const size_t nh = size_t(R) * (j + 1);
-              hh.resize(2 * nh + R);
-              h->g_h.download(hh.data(), 2 * nh + R, s);
+              h->g_hpin.alloc(size_t(R) * (2 * (m + 2) + 1));
+              PIBEM_CUDA(cudaMemcpyAsync(h->g_hpin.p, h->g_h.p, sizeof(double) * (2 * nh + R),
+                                         cudaMemcpyDeviceToHost, s));
               PIBEM_CUDA(cudaStreamSynchronize(s));
-              std::copy(hh.begin() + nh, hh.begin() + 2 * nh, h2.begin());
-              std::copy(hh.begin() + 2 * nh, hh.begin() + 2 * nh + R, nr.begin());
+              const double *hp = h->g_hpin.p;
+              std::copy(hp, hp + nh, hh.begin());
+              std::copy(hp + nh, hp + 2 * nh, h2.begin());
+              std::copy(hp + 2 * nh, hp + 2 * nh + R, nr.begin());
             }
             ++res.iterations;
             bool all = true;

@@ -87,6 +87,35 @@ namespace pibem
     size_t bytes() const { return n * sizeof(T); }
   };
 
+  // Page-locked host buffer (grow-only): small device -> host reads that the
+  // host waits for (the Arnoldi step's Hessenberg column) skip the driver's
+  // staging copy of pageable memory.
+  template <typename T>
+  struct PinnedBuf
+  {
+    T     *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() {}
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf()
+    {
+      if (p)
+        cudaFreeHost(p);
+    }
+    void alloc(size_t count)
+    {
+      if (count <= n && p)
+        return;
+      if (p)
+        cudaFreeHost(p);
+      p = nullptr;
+      n = 0;
+      PIBEM_CUDA(cudaMallocHost((void **)&p, count * sizeof(T)));
+      n = count;
+    }
+  };
+
   // ---------------------------------------------------------------------
   // Octree and interaction lists (host, built once per mesh).
   // Box ids follow the reference's numbering: level by level, parents in
