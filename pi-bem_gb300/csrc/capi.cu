@@ -215,7 +215,8 @@ struct pibem_handle
   DBuf<int>      d_ozerow;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
   DBuf<int>    g_ticket; // Arnoldi pass tickets (zero between launches)
-  PinnedBuf<double> g_hpin; // host copy of [h | h2 | |w|^2] of an Arnoldi step
+  PinnedBuf<double> g_hpin;  // host copy of [h | h2 | |w|^2] of an Arnoldi step
+  PinnedBuf<double> g_small; // other small reads the host waits for (norms)
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
   DBuf<double> sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm;
@@ -763,6 +764,16 @@ namespace
                          h->d_Pinv.p, v, ldv, z, s, nrm2, vout, ldo);
   }
 
+  // n values from the device into out, through the handle's page-locked buffer
+  // (stream-ordered, then synchronised)
+  void read_small(pibem_handle *h, double *out, const double *dev, size_t n, cudaStream_t s)
+  {
+    h->g_small.alloc(std::max<size_t>(n, 64));
+    PIBEM_CUDA(cudaMemcpyAsync(h->g_small.p, dev, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    std::copy(h->g_small.p, h->g_small.p + n, out);
+  }
+
   GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
                     const std::vector<double> &tol, int maxit, int m,
                     const std::function<void(const double *, double *)> &A, bool prec)
@@ -786,8 +797,7 @@ namespace
     res.rel.assign(R, 1.0);
     std::vector<double> bn(R);
     launch_dots(N, R, 1, N, N, b, b, h->g_partial.p, nblk, h->g_bn.p, s);
-    h->g_bn.download(bn.data(), R, s);
-    PIBEM_CUDA(cudaStreamSynchronize(s));
+    read_small(h, bn.data(), h->g_bn.p, R, s);
     for (auto &v : bn)
       v = v > 0 ? std::sqrt(v) : 1.0;
     std::vector<double> H(size_t(R) * (m + 1) * m), cs(size_t(R) * m), sn(size_t(R) * m),
@@ -802,8 +812,7 @@ namespace
         copy_cols(h->g_V.p, ldr, h->g_w.p, N, N, R, s);
         std::vector<double> b2(R);
         launch_dots(N, R, 1, N, N, h->g_w.p, h->g_w.p, h->g_partial.p, nblk, h->g_nrm.p, s);
-        h->g_nrm.download(b2.data(), R, s);
-        PIBEM_CUDA(cudaStreamSynchronize(s));
+        read_small(h, b2.data(), h->g_nrm.p, R, s);
         bool any = false;
         for (int r = 0; r < R; ++r)
           {
@@ -1913,8 +1922,7 @@ namespace
         std::vector<double> bn(R), rn(R), itol(R);
         auto norms = [&](const double *v, std::vector<double> &out) {
           launch_dots(N, R, 1, N, N, v, v, h->sv_part.p, 64, h->sv_nrm.p, s);
-          h->sv_nrm.download(out.data(), R, s);
-          PIBEM_CUDA(cudaStreamSynchronize(s));
+          read_small(h, out.data(), h->sv_nrm.p, R, s);
           for (auto &v2 : out)
             v2 = std::sqrt(v2);
         };
