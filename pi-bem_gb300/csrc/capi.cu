@@ -182,6 +182,8 @@ struct pibem_handle
   // the system matrix S and the right-hand side's matrix (S of the
   // complementary mask), and the pair copy of x
   DBuf<float2>  d_Sff, d_Srff, d_xff;
+  DBuf<float2>  d_Wff;  // L2P rows as pairs (modes other than FP64)
+  DBuf<double>  d_Tcr;  // P2M strengths of the right-hand side: dir ? T1 : -T2
   DBuf<int>     d_err;
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
@@ -257,7 +259,7 @@ struct pibem_handle
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
         d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end, d_m2p_tnodes);
     add(d_con_row, d_con_col, d_con_p, d_con_q, d_con_kind, d_con_nrm, d_con_sg);
-    add(d_Sff, d_Srff, d_xff);
+    add(d_Sff, d_Srff, d_xff, d_Wff, d_Tcr);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
@@ -389,7 +391,8 @@ namespace
           record(h, 4);
           for (int l = 1; l <= h->tree.L; ++l)
             launch_downward_level_ff(op, R, l, Lff, Yff, s);
-          launch_convert_ff2d(int64_t(need), Lff, Lx.p, s);
+          if (!op.Wff) // L2P reads the pairs when it has pair rows
+            launch_convert_ff2d(int64_t(need), Lff, Lx.p, s);
           record(h, 5);
           return;
         }
@@ -399,6 +402,19 @@ namespace
     for (int l = 1; l <= h->tree.L; ++l)
       launch_downward_level<T>(op, R, l, Lx.p, Y.p, s);
     record(h, 5);
+  }
+
+  // L2P into y: the FP64-accurate operator reads the (hi, lo) locals
+  template <typename T>
+  void l2p_apply(pibem_handle *h, const OperatorDev<T> &op, int R, const T *Lx, T *y, cudaStream_t st)
+  {
+    if constexpr (std::is_same<T, double>::value)
+      if (op.ops_ff && op.Wff)
+        {
+          launch_l2p_ff(op, R, int(h->N()), h->d_Lff.p, y, st);
+          return;
+        }
+    launch_l2p<T>(op, R, int(h->N()), Lx, y, st);
   }
 
   // M2P into y: the FP64-accurate operator evaluates from the (hi, lo)
@@ -426,7 +442,7 @@ namespace
     far_down<T>(h, op, M, Lx, Y, R, s);
     m2p_apply<T>(h, op, R, M.p, y, s);
     record(h, 6);
-    launch_l2p<T>(op, R, N, Lx.p, y, s);
+    l2p_apply<T>(h, op, R, Lx.p, y, s);
     record(h, 7);
   }
 
@@ -483,7 +499,7 @@ namespace
     PIBEM_CUDA(cudaEventRecord(h->ev_side, side));
     far_down<T>(h, op, M, Lx, Y, R, main);
     PIBEM_CUDA(cudaStreamWaitEvent(main, h->ev_side, 0));
-    launch_l2p<T>(op, R, N, Lx.p, y, main);
+    l2p_apply<T>(h, op, R, Lx.p, y, main);
     PIBEM_CUDA(cudaEventRecord(h->ev_main, main));
     PIBEM_CUDA(cudaStreamWaitEvent(s, h->ev_main, 0));
   }
@@ -1161,6 +1177,7 @@ namespace
     h->op64.T1      = h->d_T1.p;
     h->op64.T2      = h->d_T2.p;
     h->op64.W       = h->d_W.p;
+    h->op64.Wff     = h->d_Wff.n ? h->d_Wff.p : nullptr;
     h->op64.ops     = h->d_ops.p;
     h->op64.oz_images = h->d_ozimg.n ? h->d_ozimg.p : nullptr;
     h->op64.oz_ecol   = h->d_ozecol.n ? h->d_ozecol.p : nullptr;
@@ -1595,6 +1612,12 @@ namespace
                         h->d_W.p, s);
       h->d_Wf.alloc(npos * K4);
       launch_convert_d2f(npos * K4, h->d_W.p, h->d_Wf.p, s);
+      h->d_Wff.release();
+      if (P.precision_mode != PIBEM_PRECISION_FP64 && npos > 0)
+        {
+          h->d_Wff.alloc(npos * K4);
+          launch_convert_d2ff(npos * K4, h->d_W.p, h->d_Wff.p, s);
+        }
     }
     // translation operators
     {
@@ -1716,6 +1739,7 @@ namespace
     // for the right-hand side (not needed by the plain FP64 path)
     h->d_Sff.release();
     h->d_Srff.release();
+    h->d_Tcr.release();
     if (h->prm.precision_mode != PIBEM_PRECISION_FP64 && pl.nval_ptr.back() > 0)
       {
         const int64_t nval = pl.nval_ptr.back();
@@ -1733,6 +1757,14 @@ namespace
                                    h->d_alpha.p, h->d_N.p, h->d_D.p, Sr.p, nullptr, s);
         h->d_Srff.alloc(nval);
         launch_convert_d2ff(nval, Sr.p, h->d_Srff.p, s);
+        // P2M strengths of the right-hand side, one table row per row:
+        // N on Dirichlet, -D on Neumann DoFs (the combined table of the
+        // complementary mask)
+        const int64_t nr = int64_t(pl.prow_dof.size());
+        const int     K4 = (pl.K + 3) / 4 * 4;
+        h->d_Tcr.alloc(std::max<int64_t>(1, nr * K4));
+        launch_combine_p2m<double>(nr, K4, h->d_prow_dof.p, d_dirc.p, h->d_T1.p, h->d_T2.p,
+                                   h->d_Tcr.p, s);
         PIBEM_CUDA(cudaStreamSynchronize(s));
       }
     // combined-strength P2M tables of the system operator (one row read per row)
@@ -1793,8 +1825,18 @@ namespace
         record(h, 0);
         near_apply<double>(h, h->op64, R, nullptr, h->d_Srff.p, tmp, rhs, s);
         record(h, 1);
-        far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p, tmp,
-                          rhs);
+        {
+          // P2M from the right-hand side's combined table (one row read per row)
+          struct TcSwap
+          {
+            OperatorDev<double> &op;
+            const double        *saved;
+            ~TcSwap() { op.Tc = saved; }
+          } swap{h->op64, h->op64.Tc};
+          h->op64.Tc = h->d_Tcr.p;
+          far_field<double>(h, h->op64, h->d_M64, h->d_L64, h->d_m2p64, h->d_Y64, R, h->d_modes.p,
+                            tmp, rhs, true);
+        }
         finish_timing(h, 0);
         h->cnt64 += R;
         launch_axpby(int64_t(R) * N, 0.0, rhs, -1.0, rhs, s);

@@ -932,8 +932,90 @@ namespace pibem
         }
     }
 
+    // L2P of the FP64-accurate operator in float-float: as l2p_kernel, from
+    // the (hi, lo) locals and (hi, lo) rows of W, products by TwoProduct, the
+    // row sums carried with TwoSum and reduced by the same butterfly; y += the
+    // sum in FP64.
+    __global__ void __launch_bounds__(256)
+      l2p_ff_kernel(int n_leaves, int R, int K, int N, const int64_t *__restrict__ row_ptr,
+                    const int32_t *__restrict__ lleaf_box, const int32_t *__restrict__ nrows,
+                    const float2 *__restrict__ W, const float2 *__restrict__ Lx,
+                    double *__restrict__ y)
+    {
+      const int leaf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+      if (leaf >= n_leaves)
+        return;
+      const int     K4  = (K + 3) / 4 * 4;
+      const int64_t box = lleaf_box[leaf];
+      const int64_t r0 = row_ptr[leaf], r1 = row_ptr[leaf + 1];
+      const bool    act = 4 * lane < K4;
+      for (int r = 0; r < R; ++r)
+        {
+          float2 l[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+            l[c] = make_float2(0.f, 0.f);
+          if (act)
+            {
+              const float2 *lp = Lx + (box * R + r) * K;
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                if (4 * lane + c < K)
+                  l[c] = lp[4 * lane + c];
+            }
+          for (int64_t i0 = r0; i0 < r1; i0 += 8)
+            {
+              float2 w[8][4];
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                if (act && i0 + u < r1)
+                  {
+                    const float4 a = *reinterpret_cast<const float4 *>(W + (i0 + u) * K4 + 4 * lane);
+                    const float4 b = *reinterpret_cast<const float4 *>(W + (i0 + u) * K4 + 4 * lane + 2);
+                    w[u][0] = make_float2(a.x, a.y);
+                    w[u][1] = make_float2(a.z, a.w);
+                    w[u][2] = make_float2(b.x, b.y);
+                    w[u][3] = make_float2(b.z, b.w);
+                  }
+                else
+                  w[u][0] = w[u][1] = w[u][2] = w[u][3] = make_float2(0.f, 0.f);
+              double mine = 0.0;
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                {
+                  float h = 0.f, lo = 0.f;
+#pragma unroll
+                  for (int c = 0; c < 4; ++c)
+                    ff_mac(h, lo, w[u][c], l[c]);
+                  float2 t = ff_norm(h, lo);
+                  for (int o = 16; o > 0; o >>= 1)
+                    t = ff_add(t, make_float2(__shfl_xor_sync(0xffffffffu, t.x, o),
+                                              __shfl_xor_sync(0xffffffffu, t.y, o)));
+                  if (lane == u)
+                    mine = ff_join(t);
+                }
+              if (lane < 8 && i0 + lane < r1)
+                {
+                  double &o = y[int64_t(r) * N + nrows[i0 + lane]];
+                  o         = __dadd_rn(o, mine);
+                }
+            }
+        }
+    }
+
     inline int tpb_for(int RK) { return RK >= 256 ? 256 : (RK >= 128 ? 128 : 64); }
   } // namespace
+
+  void launch_l2p_ff(const OperatorDev<double> &op, int R, int N, const float2 *Lff, double *y,
+                     cudaStream_t s)
+  {
+    if (op.n_rows == 0 || op.n_near_leaves == 0)
+      return;
+    l2p_ff_kernel<<<unsigned((op.n_near_leaves + 7) / 8), 256, 0, s>>>(
+      op.n_near_leaves, R, op.K, N, op.nrow_ptr, op.lleaf_box, op.nrows, op.Wff, Lff, y);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
 
   template <typename T>
   void launch_near_spmv(const OperatorDev<T> &op, int R, int N, const T *vals, const T *x, T *y,

@@ -80,6 +80,7 @@ namespace pibem
     const int64_t *prow_ptr = nullptr;
     const int32_t *pleaf_box = nullptr, *prow_dof = nullptr;
     const T       *T1 = nullptr, *T2 = nullptr;
+    const float2  *Wff = nullptr; // L2P rows as (hi, lo) pairs (FP64-accurate operator)
     const T       *Tc = nullptr; // combined-strength table (set_bc): dir ? -T2 : T1
     // l2p (same row positions as the near field)
     const int32_t *lleaf_box = nullptr;
@@ -171,6 +172,9 @@ namespace pibem
   void launch_downward_level_ff(const OperatorDev<double> &op, int R, int level, float2 *Lx,
                                 float2 *Y, cudaStream_t s);
   void launch_convert_d2ff(int64_t n, const double *a, float2 *b, cudaStream_t s);
+  // FP64-accurate L2P from (hi, lo) locals (float-float), op.Wff rows
+  void launch_l2p_ff(const OperatorDev<double> &op, int R, int N, const float2 *Lff, double *y,
+                     cudaStream_t s);
   // FP64-accurate M2P from (hi, lo) multipoles (float-float evaluation)
   void launch_m2p_ff(const OperatorDev<double> &op, const TreeDev &td, int R, int N, const float2 *Mff,
                      double *y, cudaStream_t s);
