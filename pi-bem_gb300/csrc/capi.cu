@@ -1694,7 +1694,9 @@ namespace
                         h->d_T1f.bytes() * 2 + h->d_W.bytes() + h->d_Wf.bytes() +
                         h->d_ops.bytes() + h->d_opsf.bytes() + h->d_qpts.bytes() * 2 +
                         h->d_qshape.bytes() + h->d_qjxw.bytes() +
-                        (P.precision_mode != PIBEM_PRECISION_FP64 ? 2 * h->d_N.bytes() : 0);
+                        (P.precision_mode != PIBEM_PRECISION_FP64
+                           ? 2 * h->d_N.bytes() + h->d_T1.bytes() + h->d_W.bytes()
+                           : 0);
     if (P.hbm_budget_gb > 0 && double(h->bytes_resident) > P.hbm_budget_gb * 1e9)
       throw Error(PIBEM_ENOMEM_HBM, "resident operator exceeds the HBM budget");
     h->mesh_ok       = true;

@@ -35,10 +35,10 @@ def estimate_bytes(n_nodes: int, nrhs: int = 1, restart: int = 100) -> int:
     """Device bytes a handle is expected to hold for an n-node mesh, before it is
     set up (the near field dominates: a few hundred entries per row in five
     8-byte matrices (N, D, S and the two float-float pair matrices of the
-    FP64-accurate operator) and one FP32 matrix; Krylov basis (restart + 1) x N
-    per RHS).  The measured size (pibem_device_bytes) replaces it once the mesh
-    is resident."""
-    return int(n_nodes * (33_000 + 8 * (restart + 8) * max(1, nrhs)) + 64 * 2**20)
+    FP64-accurate operator) and one FP32 matrix; P2M and L2P tables; Krylov
+    basis (restart + 1) x N per RHS).  The measured size (pibem_device_bytes)
+    replaces it once the mesh is resident."""
+    return int(n_nodes * (36_000 + 8 * (restart + 8) * max(1, nrhs)) + 64 * 2**20)
 
 
 class Request:
