@@ -215,7 +215,7 @@ struct pibem_handle
   DBuf<uint16_t> d_ozimg, d_ozslc;
   DBuf<int16_t>  d_ozecol;
   DBuf<int>      d_ozerow;
-  DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn;
+  DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_y, g_nrm, g_u, g_bn;
   DBuf<int>    g_ticket; // Arnoldi pass tickets (zero between launches)
   PinnedBuf<double> g_hpin;  // host copy of [h | h2 | |w|^2] of an Arnoldi step
   PinnedBuf<double> g_small; // other small reads the host waits for (norms)
@@ -264,7 +264,7 @@ struct pibem_handle
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
         d_y32, d_m2p32, d_Y32, d_Mff, d_Lff, d_ozimg, d_ozslc, d_ozecol, d_ozerow);
-    add(g_V, g_w, g_z, g_partial, g_h, g_h2, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
+    add(g_V, g_w, g_z, g_partial, g_h, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
         sv_part, sv_nrm);
     for (const auto &b : io_buf)
       t += b.bytes();
