@@ -68,3 +68,31 @@ def test_plane_mask_and_sources(synthetic):
     assert (np.abs(src[:, 1]) < hb).all() and (src[:, 2] < 0).all() and (src[:, 2] > -0.0625).all()
     src = S.sources_in_ball(rng, 200, 0.5)
     assert (np.linalg.norm(src, axis=1) < 0.5).all()
+
+
+def test_sharp_cube_double_nodes(synthetic):
+    """Faces with their own nodes: every double-node set holds nodes at one point;
+    edge nodes come in pairs, corners in threes; cells face outward."""
+    mesh, off, ids, face = synthetic.sharp_cube(5)
+    sizes = np.diff(off)
+    assert set(sizes.tolist()) == {1, 2, 3}
+    assert (sizes == 3).sum() == 8 * 3
+    for i in range(mesh.n_nodes):
+        g = ids[off[i]:off[i + 1]]
+        assert i in g and np.abs(mesh.xyz[g] - mesh.xyz[i]).max() < 1e-12
+    v = mesh.xyz[mesh.cells]
+    nrm = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    assert ((nrm * v.mean(axis=1)).sum(axis=1) > 0).all()
+    assert np.bincount(face).tolist() == [25] * 6
+
+
+def test_wetted_wigley_is_open_at_the_waterline(synthetic):
+    """lid=False keeps the two sides only; the waterline nodes lie in z = 0 and
+    the double-body case's normals there are horizontal."""
+    closed = synthetic.wigley_hull(12, 3, 2)
+    wet = synthetic.wigley_hull(12, 3, 2, lid=False)
+    assert wet.n_cells == 2 * 12 * 3 and closed.n_cells == wet.n_cells + 12 * 2
+    case = synthetic.wigley_double_body_case(12, 3)
+    mesh = case[0]
+    top = np.abs(mesh.xyz[:, 2]) < 1e-12
+    assert top.sum() > 0 and np.abs(mesh.normals[top, 2]).max() < 1e-12
