@@ -92,7 +92,9 @@ typedef struct pibem_solve_stats
   int32_t refinement_steps;  /* outer FP64 residual evaluations (mixed mode) */
   int32_t fp64_matvecs;      /* FP64 operator applications */
   int32_t fp32_matvecs;      /* FP32 operator applications */
-  double  relative_residual; /* final ||b - A x|| / ||b||, FP64 operator */
+  double  relative_residual; /* final ||b - A x|| / ||b|| (worst column), formed with the
+                                FP64 operator (FP64-accurate one in mixed mode) after the
+                                last correction */
   double  seconds;           /* wall time of the call */
 } pibem_solve_stats;
 
@@ -248,8 +250,11 @@ int pibem_dirichlet_mask_from_materials(int64_t n_nodes, int64_t n_cells,
                                         uint8_t *mask);
 
 /* Allocation-free FMM matvec.  No counterpart in the reference.
- * Same result as pibem_fmm_matvec (outN = N phi, outD = D dphi_dn), but with
- * device pointers and without allocating any device memory during the call:
+ * Same result as pibem_fmm_matvec (outN = N phi, outD = D dphi_dn) in the FP64
+ * and mixed precision modes -- its far field is always the plain FP64 one, so
+ * in PIBEM_PRECISION_FLOAT_FLOAT mode (float-float translations) the two agree
+ * to about 1e-12 relative instead -- but with device pointers and without
+ * allocating any device memory during the call:
  * every temporary of the call lives in one file-scope device array of
  * PIBEM_NOALLOC_SCRATCH_BYTES that each GPU holds from library load to exit.
  * For callers that must not allocate at call time: applications that reserve

@@ -60,6 +60,7 @@ def lib():
         L.orc_compute_rhs.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp]
         L.orc_solve.restype = C.c_int
         L.orc_solve.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, _dp]
+        L.orc_set_preconditioner.argtypes = [C.c_void_p, C.c_int]
         L.orc_num_blocks.argtypes = [C.c_void_p]
         L.orc_num_levels.argtypes = [C.c_void_p]
         L.orc_level_range.argtypes = [C.c_void_p, _ip, _ip]
@@ -200,7 +201,11 @@ class Oracle:
         self.L.orc_compute_rhs(self.h, int(dense), _d(alpha), _d(tmp), _d(b))
         return b
 
-    def solve(self, tmp, tol=1e-8, max_steps=1000, restart=100, dense=False, phi=None, dphi=None):
+    def solve(self, tmp, tol=1e-8, max_steps=1000, restart=100, dense=False, phi=None, dphi=None,
+              block_jacobi=False):
+        """GMRES(restart) from x0 = rhs to relative true residual tol; with
+        block_jacobi, right-preconditioned by the leaf-block Jacobi inverses."""
+        self.L.orc_set_preconditioner(self.h, int(block_jacobi))
         tmp = np.ascontiguousarray(tmp, np.float64)
         phi = np.where(self.mask == 1, tmp, 0.0) if phi is None else phi.copy()
         dphi = np.where(self.mask == 0, tmp, 0.0) if dphi is None else dphi.copy()

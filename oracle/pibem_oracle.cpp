@@ -565,6 +565,9 @@ struct orc_handle
   // constraint lines of the solve: x[row] - (col >= 0 ? x[col] : 0) = g
   std::vector<int>               con_row, con_col;
   std::vector<double>            con_g;
+  // preconditioner of orc_solve: 0 none, 1 leaf-block Jacobi (right)
+  int                            prec = 0;
+  std::vector<std::vector<double>> blk_inv; // per childless block, row-major m x m
   // Telles rules per singular vertex, Gauss rule
   std::vector<double>            gpts, gw;
   std::vector<double>            tpts[4], tw[4];
@@ -1379,6 +1382,108 @@ extern "C"
     return 0;
   }
 
+  // Leaf-block Jacobi, the GPU library's preconditioner (not the reference's:
+  // its FMA branch defines an ILU of the near field, bem_fma.cc:3080-3411, whose
+  // use in solve_system is commented out, bem_problem.cc:1300-1304).  Per
+  // childless block, the dense inverse of the near-field system matrix
+  // (BEMProblem::vmult's near part: N on Neumann columns, -D on Dirichlet
+  // columns, alpha on the diagonal of Neumann rows) restricted to the block's
+  // own nodes; a constrained row is its constraint line.
+  static void build_block_jacobi(orc_handle *h, const double *alpha)
+  {
+    const int           nc = int(h->childless.size());
+    std::vector<int>    con(h->n_nodes, -2); // -2: free row, else the line's column (-1: none)
+    for (size_t k = 0; k < h->con_row.size(); ++k)
+      con[h->con_row[k]] = h->con_col[k];
+    h->blk_inv.assign(nc, {});
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int kb = 0; kb < nc; ++kb)
+      {
+        const std::vector<int> &nodes = h->blocks[h->childless[kb]].nodes;
+        const int               m     = int(nodes.size());
+        std::vector<double>     a(size_t(m) * m, 0.0), inv(size_t(m) * m, 0.0);
+        for (int r = 0; r < m; ++r)
+          {
+            const int i = nodes[r];
+            if (con[i] != -2)
+              {
+                a[size_t(r) * m + r] = 1.0;
+                for (int c = 0; c < m; ++c)
+                  if (nodes[c] == con[i] && c != r)
+                    a[size_t(r) * m + c] -= 1.0;
+                continue;
+              }
+            const Row &row = h->near[i];
+            for (int c = 0; c < m; ++c)
+              {
+                const int j  = nodes[c];
+                auto      it = std::lower_bound(row.cols.begin(), row.cols.end(), j);
+                if (it != row.cols.end() && *it == j)
+                  {
+                    size_t e = size_t(it - row.cols.begin());
+                    a[size_t(r) * m + c] = h->dir[j] ? -row.D[e] : row.N[e];
+                  }
+              }
+            if (!h->dir[i])
+              a[size_t(r) * m + r] += alpha[i];
+          }
+        // Gauss-Jordan with partial pivoting
+        for (int r = 0; r < m; ++r)
+          inv[size_t(r) * m + r] = 1.0;
+        for (int c = 0; c < m; ++c)
+          {
+            int piv = c;
+            for (int r = c + 1; r < m; ++r)
+              if (std::fabs(a[size_t(r) * m + c]) > std::fabs(a[size_t(piv) * m + c]))
+                piv = r;
+            if (piv != c)
+              for (int t = 0; t < m; ++t)
+                {
+                  std::swap(a[size_t(c) * m + t], a[size_t(piv) * m + t]);
+                  std::swap(inv[size_t(c) * m + t], inv[size_t(piv) * m + t]);
+                }
+            const double d = a[size_t(c) * m + c];
+            for (int t = 0; t < m; ++t)
+              {
+                a[size_t(c) * m + t] /= d;
+                inv[size_t(c) * m + t] /= d;
+              }
+            for (int r = 0; r < m; ++r)
+              if (r != c && a[size_t(r) * m + c] != 0.0)
+                {
+                  const double f = a[size_t(r) * m + c];
+                  for (int t = 0; t < m; ++t)
+                    {
+                      a[size_t(r) * m + t] -= f * a[size_t(c) * m + t];
+                      inv[size_t(r) * m + t] -= f * inv[size_t(c) * m + t];
+                    }
+                }
+          }
+        h->blk_inv[kb].swap(inv);
+      }
+  }
+
+  static void apply_block_jacobi(const orc_handle *h, const double *v, double *z)
+  {
+    const int nc = int(h->childless.size());
+#pragma omp parallel for schedule(static)
+    for (int kb = 0; kb < nc; ++kb)
+      {
+        const std::vector<int> &nodes = h->blocks[h->childless[kb]].nodes;
+        const int               m     = int(nodes.size());
+        const double           *inv   = h->blk_inv[kb].data();
+        for (int r = 0; r < m; ++r)
+          {
+            double s = 0;
+            for (int c = 0; c < m; ++c)
+              s += inv[size_t(r) * m + c] * v[nodes[c]];
+            z[nodes[r]] = s;
+          }
+      }
+  }
+
+  void orc_set_preconditioner(orc_handle *h, int kind) { h->prec = kind; }
+
   int orc_solve(orc_handle *h, int dense, double *phi, double *dphi, const double *tmp, double tol,
                 int max_steps, int restart, double *final_res)
   {
@@ -1386,6 +1491,8 @@ extern "C"
     std::vector<double> alpha(n), b(n), x(n), r(n), w(n);
     orc_compute_alpha(h, dense, alpha.data());
     orc_compute_rhs(h, dense, alpha.data(), tmp, b.data());
+    if (h->prec)
+      build_block_jacobi(h, alpha.data());
     // ConstrainedOperator::distribute_rhs (include/constrained_matrix.h:172-181)
     for (size_t k = 0; k < h->con_row.size(); ++k)
       b[h->con_row[k]] = h->con_g[k];
@@ -1407,7 +1514,7 @@ extern "C"
         int                              m = restart;
         std::vector<std::vector<double>> V(m + 1, std::vector<double>(n));
         std::vector<std::vector<double>> H(m + 1, std::vector<double>(m, 0.0));
-        std::vector<double>              cs(m), sn(m), g(m + 1, 0.0);
+        std::vector<double>              cs(m), sn(m), g(m + 1, 0.0), z(n);
         for (size_t i = 0; i < n; ++i)
           V[0][i] = r[i] / beta;
         g[0]  = beta;
@@ -1415,7 +1522,13 @@ extern "C"
         for (; k < m && its < max_steps; ++k)
           {
             ++its;
-            constrained_matvec(h, dense, alpha.data(), V[k].data(), w.data());
+            if (h->prec)
+              {
+                apply_block_jacobi(h, V[k].data(), z.data());
+                constrained_matvec(h, dense, alpha.data(), z.data(), w.data());
+              }
+            else
+              constrained_matvec(h, dense, alpha.data(), V[k].data(), w.data());
             for (int i = 0; i <= k; ++i)
               {
                 double s = 0;
@@ -1455,9 +1568,17 @@ extern "C"
               s -= H[i][j] * y[j];
             y[i] = s / H[i][i];
           }
+        std::vector<double> u(n, 0.0);
         for (int i = 0; i < k; ++i)
           for (size_t t = 0; t < n; ++t)
-            x[t] += y[i] * V[i][t];
+            u[t] += y[i] * V[i][t];
+        if (h->prec)
+          {
+            apply_block_jacobi(h, u.data(), z.data());
+            u.swap(z);
+          }
+        for (size_t t = 0; t < n; ++t)
+          x[t] += u[t];
       }
     constrained_matvec(h, dense, alpha.data(), x.data(), w.data());
     for (size_t i = 0; i < n; ++i)

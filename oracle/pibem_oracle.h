@@ -50,6 +50,10 @@ void orc_system_matvec(orc_handle *h, int use_dense, const double *alpha, const 
 void orc_compute_rhs(orc_handle *h, int use_dense, const double *alpha, const double *tmp_rhs,
                      double *rhs);
 /* BEMProblem::solve_system semantics with an own GMRES(restart); returns iterations. */
+/* Preconditioner of orc_solve: 0 none (default), 1 right leaf-block Jacobi
+ * (dense inverses of the near-field system matrix on each childless block's
+ * own nodes, the GPU library's preconditioner). */
+void orc_set_preconditioner(orc_handle *h, int kind);
 int orc_solve(orc_handle *h, int use_dense, double *phi, double *dphi_dn, const double *tmp_rhs,
               double tol, int max_steps, int restart, double *final_rel_res);
 

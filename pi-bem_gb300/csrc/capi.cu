@@ -161,6 +161,7 @@ struct pibem_handle
   DBuf<int32_t> d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted;
   DBuf<double>  d_center, d_delta;
   // plan
+  DBuf<int32_t> d_near_part; // one-column near SpMV: leaf range of each block
   DBuf<int64_t> d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr,
     d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr,
     d_up_q_ptr, d_down_q_ptr;
@@ -235,6 +236,7 @@ struct pibem_handle
   double      phase_tot[2][7] = {};
   int64_t     phase_cnt[2] = {0, 0};
   int         cnt64 = 0, cnt32 = 0;
+  int         near_nblk = 0, near_nblk_wide = 0; // one-column near SpMV blocks (d_near_part)
   int64_t     m2p_items = 0, m2p_tnodes = 0;
 
   // unknowns per column: the collocation nodes (the mesh's own nodes; a
@@ -250,6 +252,7 @@ struct pibem_handle
         d_elem_off, d_elem_ids, d_proj);
     add(d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted, d_center,
         d_delta);
+    add(d_near_part);
     add(d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr, d_m2l_src_ptr,
         d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr, d_up_q_ptr,
         d_down_q_ptr);
@@ -1120,6 +1123,11 @@ namespace
       op.nrow_ptr      = h->d_nrow_ptr.p;
       op.ncol_ptr      = h->d_ncol_ptr.p;
       op.nval_ptr      = h->d_nval_ptr.p;
+      op.near_part     = h->d_near_part.p;
+      op.near_nblk     = h->near_nblk;
+      op.near_part_wide = h->d_near_part.p + h->near_nblk + 1;
+      op.near_nblk_wide = h->near_nblk_wide;
+      op.ncols_end16   = int64_t(pl.ncols.size()) * 4 / 16 * 16;
       op.n_p2m_leaves  = int(pl.pleaf_box.size());
       op.prow_ptr      = h->d_prow_ptr.p;
       op.pleaf_box     = h->d_pleaf_box.p;
@@ -1442,6 +1450,32 @@ namespace
     h->d_nrow_ptr.upload(pl.nrow_ptr, s);
     h->d_ncol_ptr.upload(pl.ncol_ptr, s);
     h->d_nval_ptr.upload(pl.nval_ptr, s);
+    {
+      // one-column near SpMVs: per SM as many blocks as are resident (FP32 and
+      // 8-byte values), each a contiguous range of leaves of about equal value bytes
+      int dev = 0, n_sm = 1;
+      PIBEM_CUDA(cudaGetDevice(&dev));
+      PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+      const int            nl  = int(pl.nval_ptr.size()) - 1;
+      const int64_t        tot = pl.nval_ptr.back();
+      std::vector<int32_t> part;
+      auto split = [&](int per_sm) {
+        const int nblk = std::max(1, std::min(nl, per_sm * n_sm));
+        int       leaf = 0;
+        for (int b = 0; b < nblk; ++b)
+          {
+            const int64_t target = tot / nblk * b + tot % nblk * b / nblk;
+            while (leaf < nl && pl.nval_ptr[leaf] < target)
+              ++leaf;
+            part.push_back(b == 0 ? 0 : leaf);
+          }
+        part.push_back(nl);
+        return nblk;
+      };
+      h->near_nblk      = split(NEAR_BLOCKS_PER_SM_F32);
+      h->near_nblk_wide = split(NEAR_BLOCKS_PER_SM_WIDE);
+      h->d_near_part.upload(part, s);
+    }
     h->d_nent_ptr.upload(pl.nent_ptr, s);
     h->d_row_leaf.upload(pl.row_leaf, s);
     h->d_nrows.upload(pl.nrows, s);
@@ -1952,7 +1986,10 @@ namespace
         // the whole solution, so its residual is formed with the FP64 operator;
         // every later correction d_k is small (|d_k| <= tol_inner^k |x|), so the
         // residual is updated as r <- r - A32 d_k, whose rounding error
-        // eps32 * |A| |d_k| stays far below the target.  Each column has its own
+        // eps32 * |A| |d_k| stays far below the target.  When the updated
+        // residuals of all columns meet the tolerance, b - A64 x is formed once
+        // more and the solve returns only if that exact residual meets it too, so
+        // the reported residual is always an FP64 one.  Each column has its own
         // inner tolerance and stops refining once it meets the target (its later
         // corrections are zero), so a column's solution is the same alone or in a
         // batch.
@@ -1975,17 +2012,38 @@ namespace
           v = v > 0 ? v : 1.0;
         PIBEM_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * R * N, s));
         PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+        // r_exact: r holds b - A64 x (x0 = 0, or just recomputed) rather than
+        // the A32-updated estimate
+        bool r_exact = true;
+        auto true_residual = [&] {
+          A64(x.p, w.p);
+          PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+          launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
+          r_exact = true;
+        };
+        bool ok = false;
+        auto assess = [&] {
+          norms(r.p, rn);
+          ok = true;
+          for (int c = 0; c < R; ++c)
+            {
+              rel[c]  = rn[c] / bn[c];
+              itol[c] = rel[c] <= P.solver_tolerance
+                          ? std::numeric_limits<double>::infinity()
+                          : std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / rel[c]);
+              ok = ok && rel[c] <= P.solver_tolerance;
+            }
+        };
         for (; refine <= max_refine; ++refine)
           {
-            norms(r.p, rn);
-            bool ok = true;
-            for (int c = 0; c < R; ++c)
+            assess();
+            // the stopping test is an FP64 claim: an estimate that meets the
+            // tolerance is confirmed with the FP64-accurate operator, and
+            // refinement goes on from the exact residual if it does not hold
+            if (ok && !r_exact)
               {
-                rel[c]  = rn[c] / bn[c];
-                itol[c] = rel[c] <= P.solver_tolerance
-                            ? std::numeric_limits<double>::infinity()
-                            : std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / rel[c]);
-                ok = ok && rel[c] <= P.solver_tolerance;
+                true_residual();
+                assess();
               }
             if (ok || refine == max_refine || iters >= P.solver_max_steps)
               break;
@@ -1995,14 +2053,19 @@ namespace
             iters += gr.iterations;
             launch_axpby(int64_t(R) * N, 1.0, d.p, 1.0, x.p, s);
             if (refine == 0)
-              {
-                A64(x.p, w.p); // r = b - A64 x
-                PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N,
-                                           cudaMemcpyDeviceToDevice, s));
-              }
+              true_residual(); // r = b - A64 x
             else
-              A32(d.p, w.p); // r = r - A32 d
-            launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
+              {
+                A32(d.p, w.p); // r = r - A32 d
+                launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
+                r_exact = false;
+              }
+          }
+        // a solve that stopped on its step limits also reports the exact residual
+        if (!r_exact)
+          {
+            true_residual();
+            assess();
           }
       }
     launch_scatter(N, R, x.p, h->d_dir.p, phi, dphi, s);
@@ -2528,17 +2591,12 @@ extern "C" int pibem_fmm_matvec_noalloc(pibem_handle *h, int32_t R, const double
     uint8_t     *dir   = reinterpret_cast<uint8_t *>(S + nS);
     uint8_t     *modes = dir + N;
     cudaStream_t s     = h->stream;
-    // the handle's operator view, with the M2P scratch pointed into the array
-    // for the duration of the call (no host-side copy of the view)
-    OperatorDev<double> &op    = h->op64;
-    double *const        saved = op.m2p_scratch;
-    struct Restore
-    {
-      OperatorDev<double> &op;
-      double              *p;
-      ~Restore() { op.m2p_scratch = p; }
-    } restore{op, saved};
-    op.m2p_scratch = S;
+    // a copy of the handle's operator view (host memory only) with the M2P
+    // scratch pointed into the array; the handle itself is not modified.  The
+    // far field is the plain FP64 one whatever the precision mode: ops_ff and
+    // the tensor-core images of the view are not used by this call.
+    OperatorDev<double> op = h->op64;
+    op.m2p_scratch         = S;
     PIBEM_CUDA(cudaMemsetAsync(dir, 0, size_t(N), s));
     launch_near_spmv<double>(op, R, int(N), h->d_N.p, d_phi, d_outN, false, s);
     launch_near_spmv<double>(op, R, int(N), h->d_D.p, d_dphi, d_outD, false, s);
@@ -2546,5 +2604,6 @@ extern "C" int pibem_fmm_matvec_noalloc(pibem_handle *h, int32_t R, const double
     far_field_on(h, op, R, dir, modes, d_phi, d_outN, M, Lx, Y);
     PIBEM_CUDA(cudaMemsetAsync(modes, MODE_KER2, size_t(R), s));
     far_field_on(h, op, R, dir, modes, d_dphi, d_outD, M, Lx, Y);
+    h->cnt64 += R;
   });
 }

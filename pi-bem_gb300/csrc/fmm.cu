@@ -8,6 +8,8 @@
 //   M2P for deeper non-interaction boxes (bem_fma.cc:2664-2704)
 //   L2P at the nodes of childless boxes (bem_fma.cc:2959-2986)
 // Expansions are laid out [box][rhs][k] with K = (p+1)^2 scaled reals.
+#include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <type_traits>
 
@@ -172,15 +174,54 @@ namespace pibem
     __device__ inline void cp_async_x(float *dst, const float *src) { cp_async4(dst, src); }
     __device__ inline void cp_async_x(double *dst, const double *src) { cp_async8(dst, src); }
 
-    // Near-field SpMV for one column, software-pipelined: persistent blocks
-    // take leaves L, L + gridDim.x, ...; while the warps stream the rows of a
-    // leaf, the x entries of the block's next leaf are gathered into the other
-    // half of a double buffer with cp.async.  A row is computed exactly as in
+    // L2 prefetch (a hint) of leaf l's value block, 16 KB per lane of the calling
+    // warp (the first 512 KB of a block), and of its column ids (lane 31, the
+    // ids rounded out to 16 bytes within the first ids_end16 bytes of the array,
+    // at most 16 KB).  Value blocks start on 16 bytes and are multiples of 16
+    // bytes long (rows of 4 values).
+    template <typename V>
+    __device__ inline void prefetch_leaf(int l, const int64_t *__restrict__ ncol_ptr,
+                                         const int64_t *__restrict__ nval_ptr,
+                                         const int32_t *__restrict__ ncols, const V *__restrict__ vals,
+                                         int64_t ids_end16, int lane)
+    {
+      const int64_t v0 = nval_ptr[l], vb = (nval_ptr[l + 1] - v0) * int64_t(sizeof(V));
+      const int64_t o  = int64_t(lane) * 16384;
+      if (o < vb)
+        {
+          const uint32_t n = uint32_t(vb - o < 16384 ? vb - o : 16384);
+          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                         reinterpret_cast<const char *>(vals + v0) + o),
+                       "r"(n)
+                       : "memory");
+        }
+      if (lane == 31)
+        {
+          const int64_t b0 = ncol_ptr[l] * 4 / 16 * 16;
+          int64_t       b1 = (ncol_ptr[l + 1] * 4 + 15) / 16 * 16;
+          b1               = b1 < ids_end16 ? b1 : ids_end16;
+          b1               = b1 < b0 + 16384 ? b1 : b0 + 16384;
+          if (b1 > b0)
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                           reinterpret_cast<const char *>(ncols) + b0),
+                         "r"(uint32_t(b1 - b0))
+                         : "memory");
+        }
+    }
+
+    // Near-field SpMV for one column, software-pipelined: block b takes the
+    // contiguous leaves part[b] .. part[b + 1] - 1 (ranges of about equal value
+    // bytes), so its value blocks are one contiguous stream; the last warp
+    // prefetches the value blocks and column ids of the leaves pf leaves ahead
+    // into L2 (cp.async.bulk.prefetch), and while the warps stream the rows of a
+    // leaf, the x entries of the next leaf are gathered into the other half of a
+    // double buffer with cp.async.  A row is computed exactly as in
     // near_leaf_kernel (same chunks per lane, same order, same butterfly).
     // Shared memory: 2 x ld_max values.
-    template <typename T>
-    __global__ void __launch_bounds__(256)
-      near_leaf_pipe_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ nrow_ptr,
+    template <typename T, int MINB>
+    __global__ void __launch_bounds__(256, MINB)
+      near_leaf_pipe_kernel(const int32_t *__restrict__ part, int pf, int ld_max, int64_t ids_end16,
+                            const int64_t *__restrict__ nrow_ptr,
                             const int64_t *__restrict__ ncol_ptr,
                             const int64_t *__restrict__ nval_ptr, const int32_t *__restrict__ nrows,
                             const int32_t *__restrict__ ncols, const T *__restrict__ vals,
@@ -189,6 +230,17 @@ namespace pibem
       extern __shared__ __align__(16) unsigned char smem_raw[];
       T        *sxb  = reinterpret_cast<T *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      // the block's leaf range, kept in shared memory (registers are short)
+      __shared__ int range[2];
+      if (threadIdx.x == 0)
+        {
+          range[0] = part[blockIdx.x];
+          range[1] = part[blockIdx.x + 1];
+        }
+      __syncthreads();
+      const int lb = range[0];
+      if (lb >= range[1])
+        return;
       // gather of leaf l into buffer b: cp.async for the columns, zeros in the padding
       auto gather = [&](int l, int b) {
         const int64_t c0 = ncol_ptr[l], nc = ncol_ptr[l + 1] - c0;
@@ -201,16 +253,20 @@ namespace pibem
             sx[c] = T(0);
         asm volatile("cp.async.commit_group;" ::: "memory");
       };
-      int leaf = blockIdx.x, buf = 0;
-      if (leaf < n_leaves)
-        gather(leaf, 0);
-      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
+      if (pf > 0 && warp == nw - 1)
+        for (int l = lb + 1; l < range[1] && l <= lb + pf; ++l)
+          prefetch_leaf(l, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
+      int buf = 0;
+      gather(lb, 0);
+      for (int leaf = lb; leaf < range[1]; ++leaf, buf ^= 1)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncthreads(); // this leaf's x is in place; the other buffer is free
-          const int next = leaf + gridDim.x;
-          if (next < n_leaves)
+          const int next = leaf + 1;
+          if (next < range[1])
             gather(next, buf ^ 1);
+          if (pf > 0 && warp == nw - 1 && leaf + pf + 1 < range[1])
+            prefetch_leaf(leaf + pf + 1, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
           const T      *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -255,11 +311,13 @@ namespace pibem
     // product split exactly (TwoProduct) with its cross terms, the row sums
     // carried with TwoSum; about 11 FP32 instructions per value, so the kernel
     // streams at HBM speed where FP64 FMA (1/58 of the FP32 rate) could not.
-    // Same structure as near_leaf_pipe_kernel: persistent blocks, the next
-    // leaf's x gathered with cp.async while the warps stream two rows each.
+    // Same structure as near_leaf_pipe_kernel: contiguous leaf ranges per block
+    // with L2 prefetch ahead, the next leaf's x gathered with cp.async while the
+    // warps stream two rows each.
     // y[row] = hi + lo in FP64 (acc: added).
-    __global__ void __launch_bounds__(256)
-      near_leaf_ff_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ nrow_ptr,
+    __global__ void __launch_bounds__(256, NEAR_BLOCKS_PER_SM_WIDE)
+      near_leaf_ff_kernel(const int32_t *__restrict__ part, int pf, int ld_max, int64_t ids_end16,
+                          const int64_t *__restrict__ nrow_ptr,
                           const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
                           const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
                           const float2 *__restrict__ vals, const float2 *__restrict__ x,
@@ -268,6 +326,9 @@ namespace pibem
       extern __shared__ __align__(16) unsigned char smem_raw[];
       float2   *sxb  = reinterpret_cast<float2 *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      const int lb = part[blockIdx.x], le = part[blockIdx.x + 1];
+      if (lb >= le)
+        return;
       auto gather = [&](int l, int b) {
         const int64_t c0 = ncol_ptr[l], nc = ncol_ptr[l + 1] - c0;
         const int64_t ld = (nc + 3) / 4 * 4;
@@ -279,16 +340,20 @@ namespace pibem
             sx[c] = make_float2(0.f, 0.f);
         asm volatile("cp.async.commit_group;" ::: "memory");
       };
-      int leaf = blockIdx.x, buf = 0;
-      if (leaf < n_leaves)
-        gather(leaf, 0);
-      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
+      if (pf > 0 && warp == nw - 1)
+        for (int l = lb + 1; l < le && l <= lb + pf; ++l)
+          prefetch_leaf(l, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
+      int buf = 0;
+      gather(lb, 0);
+      for (int leaf = lb; leaf < le; ++leaf, buf ^= 1)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncthreads();
-          const int next = leaf + gridDim.x;
-          if (next < n_leaves)
+          const int next = leaf + 1;
+          if (next < le)
             gather(next, buf ^ 1);
+          if (pf > 0 && warp == nw - 1 && leaf + pf + 1 < le)
+            prefetch_leaf(leaf + pf + 1, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
           const float2 *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -1004,6 +1069,16 @@ namespace pibem
     }
 
     inline int tpb_for(int RK) { return RK >= 256 ? 256 : (RK >= 128 ? 128 : 64); }
+
+    // leaves of L2 prefetch ahead in the one-column near SpMVs
+    int near_prefetch_leaves()
+    {
+      static const int pf = [] {
+        const char *e = std::getenv("PIBEM_NEAR_PREFETCH");
+        return e ? std::max(0, std::min(8, std::atoi(e))) : 2;
+      }();
+      return pf;
+    }
   } // namespace
 
   void launch_l2p_ff(const OperatorDev<double> &op, int R, int N, const float2 *Lff, double *y,
@@ -1031,16 +1106,18 @@ namespace pibem
       {
         // one column: the software-pipelined persistent kernel (a row is
         // computed with the same rounding steps in the same order as below)
-        int dev = 0, n_sm = 1;
-        PIBEM_CUDA(cudaGetDevice(&dev));
-        PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-        const size_t smem1 = size_t(2) * maxnc * sizeof(T);
+        // FP32: 6 blocks per SM (40 registers); FP64: 4 (64 registers) -- each
+        // with its own leaf partition
+        constexpr int MINB  = sizeof(T) == 4 ? NEAR_BLOCKS_PER_SM_F32 : NEAR_BLOCKS_PER_SM_WIDE;
+        auto          kern  = near_leaf_pipe_kernel<T, MINB>;
+        const size_t  smem1 = size_t(2) * maxnc * sizeof(T);
         if (smem1 > 48 * 1024)
-          raise_smem_limit(reinterpret_cast<const void *>(near_leaf_pipe_kernel<T>), smem1);
-        const int grid = std::min(op.n_near_leaves, 6 * n_sm);
-        near_leaf_pipe_kernel<T><<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr,
-                                                         op.ncol_ptr, op.nval_ptr, op.nrows,
-                                                         op.ncols, vals, x, y, accumulate);
+          raise_smem_limit(reinterpret_cast<const void *>(kern), smem1);
+        const int32_t *part = sizeof(T) == 4 ? op.near_part : op.near_part_wide;
+        const int      nblk = sizeof(T) == 4 ? op.near_nblk : op.near_nblk_wide;
+        kern<<<nblk, 256, smem1, s>>>(part, near_prefetch_leaves(), int(maxnc), op.ncols_end16,
+                                      op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols, vals, x,
+                                      y, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
         return;
@@ -1066,20 +1143,15 @@ namespace pibem
     if (op.n_near_leaves == 0)
       return;
     const int64_t maxnc = (std::max<int64_t>(op.max_near_cols, 1) + 3) / 4 * 4;
-    int           dev = 0, n_sm = 1;
-    PIBEM_CUDA(cudaGetDevice(&dev));
-    PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem1 = size_t(2) * maxnc * sizeof(float2);
     if (smem1 > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(near_leaf_ff_kernel), smem1);
-    const int grid = std::min(op.n_near_leaves, 6 * n_sm);
     // one launch per column: a column's result does not depend on R
     for (int r = 0; r < R; ++r)
       {
-        near_leaf_ff_kernel<<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr,
-                                                     op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols,
-                                                     vals, xff + int64_t(r) * N,
-                                                     y + int64_t(r) * N, accumulate);
+        near_leaf_ff_kernel<<<op.near_nblk_wide, 256, smem1, s>>>(
+          op.near_part_wide, near_prefetch_leaves(), int(maxnc), op.ncols_end16, op.nrow_ptr, op.ncol_ptr,
+          op.nval_ptr, op.nrows, op.ncols, vals, xff + int64_t(r) * N, y + int64_t(r) * N, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
       }

@@ -39,6 +39,19 @@ def synthetic():
     return synthetic
 
 
+def reference_dir():
+    """The reference checkout, where this machine has one: $PIBEM_REFERENCE, else
+    the directory the oracle's recipe compiled the reference classes from
+    (oracle/_ref/reference_dir.txt); None when neither exists."""
+    d = os.environ.get("PIBEM_REFERENCE")
+    if not d:
+        rec = os.path.join(REPO, "oracle", "_ref", "reference_dir.txt")
+        if os.path.exists(rec):
+            with open(rec) as f:
+                d = f.read().strip()
+    return d if d and os.path.isdir(d) else None
+
+
 def rel(a, b):
     a = np.asarray(a)
     b = np.asarray(b)

@@ -174,6 +174,9 @@ def test_solve_mixed_matches_fp64(case, pibem_mod):
     p, d, st = mix.solve(case["tmp"])
     assert st["relative_residual"] <= 1e-8
     assert rel(_sol(case, p, d), _sol(case, p64, d64)) < 1e-5
+    # the reported residual is the FP64 one: b - A x with the oracle-pinned FP64 operator
+    true_res = rel(case["gpu"].system_matvec(_sol(case, p, d)), case["gpu"].rhs(case["tmp"]))
+    assert true_res <= 1.001e-8 and abs(true_res - st["relative_residual"]) <= 1e-3 * true_res
     for g in (ref, mix_t, mix):
         g.close()
 

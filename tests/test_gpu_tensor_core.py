@@ -1,8 +1,9 @@
 """The tensor-core (tcgen05, 3xTF32) translation GEMM of the FP32 operator
-against the CUDA-core FP32 GEMM and the FP64 operator, through the C ABI.
+against the CUDA-core FP32 GEMM, the FP64 operator and the oracle's operator
+(BEMProblem::vmult restated on the CPU), through the C ABI.
 
 Tolerance: both FP32 operators agree to 2e-6 relative (2-norm); the FP32
-operator is within 2e-5 of the FP64 operator."""
+operator is within 2e-5 of the FP64 operator and of the oracle."""
 import os
 
 import numpy as np
@@ -40,7 +41,7 @@ def _handle(pibem, c, mesh, mask, mode, tc):
 
 
 @pytest.mark.parametrize("name,c", CASES, ids=[n for n, _ in CASES])
-def test_tensor_core_translations(name, c, pibem_mod, synthetic):
+def test_tensor_core_translations(name, c, pibem_mod, synthetic, oracle_mod):
     mesh, mask = _mesh(synthetic, c)
     x = np.random.Generator(np.random.PCG64(5)).normal(size=mesh.n_nodes)
     os.environ["PIBEM_MATVEC_FP32"] = "1"
@@ -55,6 +56,11 @@ def test_tensor_core_translations(name, c, pibem_mod, synthetic):
     y64 = g64.system_matvec(x)
     assert rel(y_tc, y_cc) < 2e-6, rel(y_tc, y_cc)
     assert rel(y_tc, y64) < 2e-5, rel(y_tc, y64)
+    o = oracle_mod.Oracle(p=c["p"], levels=10, max_nodes=c["leaf"], external=c["ext"])
+    o.set_mesh(mesh.xyz, mesh.cells)
+    o.set_bc(mask)
+    y_o = o.system_matvec(o.alpha(), x)
+    assert rel(y_tc, y_o) < 2e-5, rel(y_tc, y_o)
     # the solve through the tensor-core operator meets the FP64 residual
     tmp = np.where(mask == 1, 1.0, 0.5) * np.cos(mesh.xyz[:, 0])
     _, _, st = g_tc.solve(tmp)

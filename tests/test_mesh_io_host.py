@@ -7,7 +7,10 @@ import os
 import numpy as np
 import pytest
 
-REF_GRIDS = "/root/reference/grids"
+from conftest import reference_dir
+
+_REF = reference_dir()
+REF_GRIDS = os.path.join(_REF, "grids") if _REF else ""
 
 
 def _write_ucd(path, xyz, cells_lex, material):

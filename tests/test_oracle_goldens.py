@@ -17,7 +17,9 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
-REF = "/root/reference"
+from conftest import reference_dir
+
+REF = reference_dir()
 
 
 @pytest.fixture(scope="module")
@@ -124,7 +126,7 @@ def test_expansion_operators_match_reference(prims, vectors, p, case):
     assert prims.l2p(p, v["target"], v["m2l"], v["x"]) == pytest.approx(float(v["l2p"]), rel=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference checkout not present")
+@pytest.mark.skipif(REF is None, reason="reference checkout not present")
 def test_compiled_reference_reproduces_output_files():
     repo = os.path.dirname(HERE)
     subprocess.run(["make", "-s", "-C", os.path.join(repo, "oracle"), "ref", f"REF={REF}"], check=True)
