@@ -161,7 +161,6 @@ struct pibem_handle
   DBuf<int32_t> d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted;
   DBuf<double>  d_center, d_delta;
   // plan
-  DBuf<int32_t> d_near_part; // one-column near SpMV: leaf range of each block
   DBuf<int64_t> d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr,
     d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr,
     d_up_q_ptr, d_down_q_ptr;
@@ -218,8 +217,14 @@ struct pibem_handle
   DBuf<int>      d_ozerow;
   DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_y, g_nrm, g_u, g_bn;
   DBuf<int>    g_ticket; // Arnoldi pass tickets (zero between launches)
-  PinnedBuf<double> g_hpin;  // host copy of [h | h2 | |w|^2] of an Arnoldi step
-  PinnedBuf<double> g_small; // other small reads the host waits for (norms)
+  // device state of a GMRES restart cycle (krylov.cu): Hessenberg matrices,
+  // rotations, right-hand sides g, tolerances, per-column step of stopping,
+  // control words [step, iterations, limit, go on]
+  DBuf<double> g_H, g_cs, g_sn, g_g, g_tol;
+  DBuf<int>    g_kdone, g_ctl;
+  PinnedBuf<double> g_small; // small reads the host waits for (norms)
+  PinnedBuf<int>    g_ctlpin; // host copy of the cycle's control words
+  DBuf<double> sh_part, sh_nrm; // pure-Neumann shift of the operator input / output
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
   DBuf<double> sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm;
@@ -229,6 +234,17 @@ struct pibem_handle
   cudaGraphExec_t g32_exec = nullptr;
   uintptr_t       g32_key[8] = {};
   int64_t         g32_kernels = 0;
+  // one GMRES restart cycle as a CUDA graph: a conditional while node around
+  // one Arnoldi step, captured for the key's buffers, column count, Krylov
+  // dimension, operator and preconditioner; per step: kernels and operator
+  // applications (FP32, FP64) it makes
+  cudaGraphExec_t gm_exec = nullptr;
+  uintptr_t       gm_key[32] = {};
+  int64_t         gm_kernels = 0;
+  int             gm_c32 = 0, gm_c64 = 0;
+  // d_modes holds this mode for modes_R columns (-1: other contents)
+  int             modes_R = -1;
+  uint8_t         modes_val = 0;
   // timing
   bool        timing = false;
   cudaEvent_t ev[8] = {};
@@ -236,7 +252,6 @@ struct pibem_handle
   double      phase_tot[2][7] = {};
   int64_t     phase_cnt[2] = {0, 0};
   int         cnt64 = 0, cnt32 = 0;
-  int         near_nblk = 0, near_nblk_wide = 0; // one-column near SpMV blocks (d_near_part)
   int64_t     m2p_items = 0, m2p_tnodes = 0;
 
   // unknowns per column: the collocation nodes (the mesh's own nodes; a
@@ -252,7 +267,6 @@ struct pibem_handle
         d_elem_off, d_elem_ids, d_proj);
     add(d_parent, d_child_first, d_nchild, d_digit, d_nbeg, d_nend, d_node_sorted, d_center,
         d_delta);
-    add(d_near_part);
     add(d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr, d_m2l_src_ptr,
         d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr, d_up_q_ptr,
         d_down_q_ptr);
@@ -269,6 +283,7 @@ struct pibem_handle
         d_y32, d_m2p32, d_Y32, d_Mff, d_Lff, d_ozimg, d_ozslc, d_ozecol, d_ozerow);
     add(g_V, g_w, g_z, g_partial, g_h, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
         sv_part, sv_nrm);
+    add(g_H, g_cs, g_sn, g_g, g_tol, g_kdone, g_ctl, sh_part, sh_nrm);
     for (const auto &b : io_buf)
       t += b.bytes();
     return t;
@@ -541,6 +556,7 @@ namespace
         modes[R + r] = MODE_KER2;
       }
     h->d_modes.upload(modes, s);
+    h->modes_R = -1;
     record(h, 0);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_N.p, h->d_x64.p, h->d_y64.p, false, s);
     launch_near_spmv<double>(h->op64, R, int(N), h->d_D.p, h->d_x64.p + R * N,
@@ -561,6 +577,7 @@ namespace
     const int64_t        N = h->N();
     std::vector<uint8_t> modes(1, MODE_KER1);
     h->d_modes.upload(modes, h->stream);
+    h->modes_R = -1;
     record(h, 0);
     launch_near_spmv<double>(h->op64, 1, int(N), h->d_N.p, x, y, false, h->stream);
     record(h, 1);
@@ -568,27 +585,28 @@ namespace
     finish_timing(h, 0);
   }
 
+  // d_modes = mode for R columns (uploaded only when it changes, so that the
+  // operator can be captured into a graph)
   void set_modes(pibem_handle *h, int R, uint8_t mode)
   {
+    if (h->modes_R == R && h->modes_val == mode)
+      return;
     std::vector<uint8_t> modes(R, mode);
     h->d_modes.upload(modes, h->stream);
+    h->modes_R   = R;
+    h->modes_val = mode;
   }
 
   // Pure-Neumann shift of bem_problem.cc:1169-1172 / 1214-1215: v -= ||v||_2.
+  // (on the device, without a host round trip, so that it can be captured)
   void shift_by_norm(pibem_handle *h, int R, double *v)
   {
     const int64_t N    = h->N();
     const int     nblk = 64;
-    h->g_partial.alloc(size_t(R) * nblk * 4);
-    h->g_nrm.alloc(R);
-    launch_dots(N, R, 1, N, N, v, v, h->g_partial.p, nblk, h->g_nrm.p, h->stream);
-    std::vector<double> nr(R);
-    h->g_nrm.download(nr.data(), R, h->stream);
-    PIBEM_CUDA(cudaStreamSynchronize(h->stream));
-    for (auto &x : nr)
-      x = -std::sqrt(x);
-    h->g_u.upload(nr, h->stream);
-    launch_add_scalar(N, R, h->g_u.p, v, h->stream);
+    h->sh_part.alloc(size_t(R) * nblk);
+    h->sh_nrm.alloc(R);
+    launch_dots(N, R, 1, N, N, v, v, h->sh_part.p, nblk, h->sh_nrm.p, h->stream);
+    launch_sub_norm(N, R, h->sh_nrm.p, v, h->stream);
   }
 
   // ConstrainedOperator::vmult (include/constrained_matrix.h:100-125): every
@@ -636,6 +654,9 @@ namespace
     if (h->g32_exec)
       cudaGraphExecDestroy(h->g32_exec);
     h->g32_exec = nullptr;
+    if (h->gm_exec)
+      cudaGraphExecDestroy(h->gm_exec);
+    h->gm_exec = nullptr;
   }
 
   // The FP32 operator is applied once per GMRES iteration with the same buffers,
@@ -746,12 +767,21 @@ namespace
 
   // ---------------------------------------------------------------------
   // Restarted GMRES(m) for R right-hand sides in lockstep, right leaf-block
-  // Jacobi preconditioning, CGS2 Arnoldi in FP64 on the device, Givens
-  // rotations and the small least-squares problem on the host.  Stops column r
+  // Jacobi preconditioning, CGS2 Arnoldi in FP64 on the device.  Stops column r
   // at ||b - A x|| / ||b|| <= tol[r] (true residual at every restart); a column
   // with tol[r] = +inf is left unchanged.  The columns share the operator
   // applications but no arithmetic, so a column's iterates do not depend on the
   // other columns of the batch.
+  //
+  // A restart cycle runs on the device without the host: each Arnoldi step is
+  // followed by gmres_givens_kernel (the Hessenberg column, its Givens rotation,
+  // the stopping test), and the cycle's least-squares solution and update of x
+  // are kernels too.  The cycle is one CUDA graph -- a conditional while node
+  // around one step, captured once per handle, column count, Krylov dimension,
+  // operator and buffer set -- so the host waits only at restarts.  While phase
+  // timing is on, or the caller's stream is itself being captured, the same
+  // launches are issued step by step with a read of the continue flag after
+  // each (the same arithmetic).
   // ---------------------------------------------------------------------
   struct GmresResult
   {
@@ -771,16 +801,16 @@ namespace
   // handle keeps them (GMRES on an FP64-accurate operator), else the FP32 ones
   void apply_block_jacobi(pibem_handle *h, int R, const double *v, int64_t ldv, double *z,
                           cudaStream_t s, const double *nrm2 = nullptr, double *vout = nullptr,
-                          int64_t ldo = 0)
+                          int64_t ldo = 0, const int *jctl = nullptr)
   {
     const int     nl = int(h->blk_ptr.size()) - 1;
     const int64_t N  = h->N();
     if (h->d_Pinv64.p)
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
-                         h->d_Pinv64.p, v, ldv, z, s, nrm2, vout, ldo);
+                         h->d_Pinv64.p, v, ldv, z, s, nrm2, vout, ldo, jctl);
     else
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
-                         h->d_Pinv.p, v, ldv, z, s, nrm2, vout, ldo);
+                         h->d_Pinv.p, v, ldv, z, s, nrm2, vout, ldo, jctl);
   }
 
   // n values from the device into out, through the handle's page-locked buffer
@@ -793,25 +823,173 @@ namespace
     std::copy(h->g_small.p, h->g_small.p + n, out);
   }
 
-  GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
-                    const std::vector<double> &tol, int maxit, int m,
-                    const std::function<void(const double *, double *)> &A, bool prec)
+  // One Arnoldi step j (j read on the device from g_ctl[0]): z holds P^-1 V_j
+  // (V_j itself without preconditioner); w = A z; CGS2 coefficients into
+  // g_h; V_{j+1} = w / |w| and the next z; then the Givens step, which also
+  // advances j and decides whether the cycle goes on.
+  void gmres_step(pibem_handle *h, int R, int m, bool prec,
+                  const std::function<void(const double *, double *)> &A,
+                  cudaGraphConditionalHandle cond, bool use_cond)
   {
     const int64_t N    = h->N();
     cudaStream_t  s    = h->stream;
     const int     nblk = 2 * 152;
-    const int64_t ldr  = int64_t(m + 1) * N;
-    h->g_V.alloc(size_t(R) * (m + 1) * N);
+    const int     L    = m + 1;
+    const int64_t ldr  = int64_t(L) * N;
+    const int    *jc   = h->g_ctl.p;
+    double       *h1 = h->g_h.p, *h2 = h1 + size_t(R) * L, *nr = h2 + size_t(R) * L;
+    A(h->g_z.p, h->g_w.p);
+    launch_cgs_step(0, N, R, 0, N, ldr, h->g_V.p, nullptr, 0, h->g_w.p, nblk, h->g_partial.p,
+                    h->g_ticket.p, h1, s, jc, L);
+    launch_cgs_step(1, N, R, 0, N, ldr, h->g_V.p, h1, L, h->g_w.p, nblk, h->g_partial.p,
+                    h->g_ticket.p, h2, s, jc, L);
+    launch_cgs_step(2, N, R, 0, N, ldr, h->g_V.p, h2, L, h->g_w.p, nblk, h->g_partial.p,
+                    h->g_ticket.p, nr, s, jc, 1);
+    if (prec) // V_{j+1} = w / |w| and the next step's z = P^-1 V_{j+1} in one pass
+      apply_block_jacobi(h, R, h->g_w.p, N, h->g_z.p, s, nr, h->g_V.p, ldr, jc);
+    else
+      launch_normalize(N, R, h->g_w.p, nr, h->g_V.p, ldr, s, jc, h->g_z.p);
+    launch_gmres_givens(R, m, h1, h->g_H.p, h->g_cs.p, h->g_sn.p, h->g_g.p, h->g_kdone.p,
+                        h->g_bn.p, h->g_tol.p, h->g_ctl.p, cond, use_cond, s);
+  }
+
+  // The restart cycle: steps until every column has stopped, the cycle has m
+  // steps or the iteration limit is reached (all decided on the device).
+  // Returns true when it ran as the cycle graph.
+  bool gmres_cycle(pibem_handle *h, int R, int m, bool prec, int op_tag,
+                   const std::function<void(const double *, double *)> &A)
+  {
+    cudaStream_t s     = h->stream;
+    bool         graph = !h->timing;
+    if (graph)
+      {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        PIBEM_CUDA(cudaStreamIsCapturing(s, &cs));
+        graph = cs == cudaStreamCaptureStatusNone;
+      }
+    if (!graph)
+      {
+        h->g_ctlpin.alloc(4);
+        while (true)
+          {
+            gmres_step(h, R, m, prec, A, 0, false);
+            PIBEM_CUDA(cudaMemcpyAsync(h->g_ctlpin.p, h->g_ctl.p, 4 * sizeof(int),
+                                       cudaMemcpyDeviceToHost, s));
+            PIBEM_CUDA(cudaStreamSynchronize(s));
+            if (!h->g_ctlpin.p[3])
+              break;
+          }
+        return false;
+      }
+    // every buffer a step touches (a reallocation changes an address)
+    const void *bufs[] = {h->g_V.p,    h->g_w.p,     h->g_z.p,      h->g_h.p,      h->g_partial.p,
+                          h->g_ticket.p, h->g_H.p,   h->g_cs.p,     h->g_sn.p,     h->g_g.p,
+                          h->g_kdone.p, h->g_bn.p,   h->g_tol.p,    h->g_ctl.p,    h->d_x32.p,
+                          h->d_y32.p,  h->d_M32.p,   h->d_L32.p,    h->d_Y32.p,    h->d_m2p32.p,
+                          h->d_M64.p,  h->d_L64.p,   h->d_Y64.p,    h->d_m2p64.p,  h->d_t4.p,
+                          h->d_Mff.p,  h->d_Lff.p,   h->d_xff.p,    h->d_ozslc.p};
+    constexpr int nb = int(sizeof(bufs) / sizeof(bufs[0]));
+    static_assert(nb + 3 <= 32, "graph key");
+    uintptr_t key[32] = {};
+    key[0]            = uintptr_t(R) | (uintptr_t(m) << 16) | (uintptr_t(prec) << 40) |
+             (uintptr_t(op_tag) << 48);
+    key[1] = uintptr_t(s);
+    for (int i = 0; i < nb; ++i)
+      key[2 + i] = uintptr_t(bufs[i]);
+    if (!h->gm_exec || !std::equal(key, key + 32, h->gm_key))
+      {
+        if (h->gm_exec)
+          cudaGraphExecDestroy(h->gm_exec);
+        h->gm_exec = nullptr;
+        cudaGraph_t                g = nullptr;
+        cudaGraphConditionalHandle cond{};
+        PIBEM_CUDA(cudaGraphCreate(&g, 0));
+        struct GraphGuard
+        {
+          cudaGraph_t &g;
+          ~GraphGuard()
+          {
+            if (g)
+              cudaGraphDestroy(g);
+          }
+        } guard{g};
+        PIBEM_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {};
+        np.type                = cudaGraphNodeTypeConditional;
+        np.conditional.handle  = cond;
+        np.conditional.type    = cudaGraphCondTypeWhile;
+        np.conditional.size    = 1;
+        cudaGraphNode_t node   = nullptr;
+        PIBEM_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+        cudaGraph_t   body = np.conditional.phGraph_out[0];
+        const int64_t l0   = t_launches;
+        const int     c32 = h->cnt32, c64 = h->cnt64;
+        PIBEM_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeRelaxed));
+        try
+          {
+            gmres_step(h, R, m, prec, A, cond, true);
+          }
+        catch (...)
+          {
+            cudaGraph_t tmp = nullptr;
+            cudaStreamEndCapture(s, &tmp);
+            throw;
+          }
+        PIBEM_CUDA(cudaStreamEndCapture(s, &body));
+        // the captured kernels did not run: they are counted per executed step
+        h->gm_kernels = t_launches - l0;
+        g_launches.fetch_sub(h->gm_kernels, std::memory_order_relaxed);
+        t_launches = l0;
+        h->gm_c32  = h->cnt32 - c32;
+        h->gm_c64  = h->cnt64 - c64;
+        h->cnt32   = c32;
+        h->cnt64   = c64;
+        const cudaError_t e =
+          cudaGraphInstantiateWithFlags(&h->gm_exec, g, cudaGraphInstantiateFlagUseNodePriority);
+        if (e != cudaSuccess)
+          {
+            h->gm_exec = nullptr;
+            throw Error(PIBEM_ECUDA, std::string("GMRES cycle graph instantiation: ") +
+                                       cudaGetErrorString(e));
+          }
+        std::copy(key, key + 32, h->gm_key);
+      }
+    PIBEM_CUDA(cudaGraphLaunch(h->gm_exec, s));
+    return true;
+  }
+
+  GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
+                    const std::vector<double> &tol, int maxit, int m,
+                    const std::function<void(const double *, double *)> &A, bool prec, int op_tag)
+  {
+    const int64_t N    = h->N();
+    cudaStream_t  s    = h->stream;
+    const int     nblk = 2 * 152;
+    const int     L    = m + 1;
+    const int64_t ldr  = int64_t(L) * N;
+    if (m < 1)
+      throw Error(PIBEM_EINVAL, "GMRES restart length must be at least 1");
+    h->g_V.alloc(size_t(R) * L * N);
     h->g_w.alloc(size_t(R) * N);
     h->g_z.alloc(size_t(R) * N);
-    h->g_u.alloc(size_t(R) * std::max<int64_t>(N, m + 2));
-    h->g_partial.alloc(size_t(R) * nblk * (m + 2));
-    // [h (R (j+1)) | h2 (R (j+1)) | |w|^2 (R)] of the current step, one download
-    h->g_h.alloc(size_t(R) * (2 * (m + 2) + 1));
+    h->g_u.alloc(size_t(R) * N);
+    h->g_partial.alloc(size_t(R) * nblk * L);
+    h->g_h.alloc(size_t(R) * (2 * L + 1));
     h->g_ticket.alloc(R);
     h->g_ticket.zero(s);
     h->g_nrm.alloc(R);
     h->g_bn.alloc(R);
+    h->g_H.alloc(size_t(R) * L * m);
+    h->g_cs.alloc(size_t(R) * m);
+    h->g_sn.alloc(size_t(R) * m);
+    h->g_g.alloc(size_t(R) * L);
+    h->g_y.alloc(size_t(R) * L);
+    h->g_tol.alloc(R);
+    h->g_kdone.alloc(R);
+    h->g_ctl.alloc(4);
+    h->g_ctlpin.alloc(4);
+    h->g_tol.upload(tol, s);
     GmresResult res;
     res.rel.assign(R, 1.0);
     std::vector<double> bn(R);
@@ -819,132 +997,54 @@ namespace
     read_small(h, bn.data(), h->g_bn.p, R, s);
     for (auto &v : bn)
       v = v > 0 ? std::sqrt(v) : 1.0;
-    std::vector<double> H(size_t(R) * (m + 1) * m), cs(size_t(R) * m), sn(size_t(R) * m),
-      g(size_t(R) * (m + 1)), hh(size_t(R) * (m + 2)), h2(size_t(R) * (m + 2)), nr(R), beta(R);
-    std::vector<int>    kdone(R);
+    h->g_bn.upload(bn, s);
+    std::vector<double> b2(R);
+    int                 pending     = -1; // iterations before the cycle whose count is in g_ctlpin
+    bool                graph_cycle = false;
+    auto settle = [&] {
+      // the last cycle's control words have arrived (the stream was synchronised)
+      if (pending < 0)
+        return;
+      const int done = h->g_ctlpin.p[1] - pending;
+      res.iterations = h->g_ctlpin.p[1];
+      if (graph_cycle)
+        {
+          note_launch(h->gm_kernels * done);
+          h->cnt32 += h->gm_c32 * done;
+          h->cnt64 += h->gm_c64 * done;
+        }
+      pending = -1;
+    };
     while (true)
       {
         // true residual r = b - A x into V[:,0]
         A(x, h->g_w.p);
-        // w <- b - w, then V[r][0] <- w[r]
         launch_axpby(int64_t(R) * N, 1.0, b, -1.0, h->g_w.p, s);
         copy_cols(h->g_V.p, ldr, h->g_w.p, N, N, R, s);
-        std::vector<double> b2(R);
         launch_dots(N, R, 1, N, N, h->g_w.p, h->g_w.p, h->g_partial.p, nblk, h->g_nrm.p, s);
         read_small(h, b2.data(), h->g_nrm.p, R, s);
+        if (graph_cycle)
+          settle();
         bool any = false;
         for (int r = 0; r < R; ++r)
           {
-            beta[r]    = std::sqrt(b2[r]);
-            res.rel[r] = beta[r] / bn[r];
-            kdone[r]   = res.rel[r] <= tol[r] ? 0 : -1;
-            any        = any || kdone[r] < 0;
+            res.rel[r] = std::sqrt(b2[r]) / bn[r];
+            any        = any || !(res.rel[r] <= tol[r]);
           }
         if (!any || res.iterations >= maxit)
           break;
-        launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p, ldr, s); // V[r][0] = r_r / beta_r
-        std::fill(g.begin(), g.end(), 0.0);
-        for (int r = 0; r < R; ++r)
-          g[size_t(r) * (m + 1)] = beta[r];
-        int  j      = 0;
-        bool z_next = false; // z = P^-1 V_j already formed with the normalisation of V_j
-        for (; j < m; ++j)
-          {
-            // z = P^-1 V_j ; w = A z
-            const double *vj = h->g_V.p + int64_t(j) * N;
-            if (prec && !z_next)
-              apply_block_jacobi(h, R, vj, ldr, h->g_z.p, s);
-            else if (!prec)
-              copy_cols(h->g_z.p, N, vj, ldr, N, R, s);
-            z_next = false;
-            A(h->g_z.p, h->g_w.p);
-            // CGS2: h = V^T w; w -= V h, h2 = V^T w; w -= V h2, |w|^2; V_{j+1} = w / |w|
-            double *d_h1 = h->g_h.p, *d_h2 = d_h1 + size_t(R) * (j + 1),
-                   *d_nr = d_h2 + size_t(R) * (j + 1);
-            launch_cgs_step(0, N, R, j + 1, N, ldr, h->g_V.p, nullptr, 0, h->g_w.p, nblk,
-                            h->g_partial.p, h->g_ticket.p, d_h1, s);
-            launch_cgs_step(1, N, R, j + 1, N, ldr, h->g_V.p, d_h1, j + 1, h->g_w.p, nblk,
-                            h->g_partial.p, h->g_ticket.p, d_h2, s);
-            launch_cgs_step(2, N, R, j + 1, N, ldr, h->g_V.p, d_h2, j + 1, h->g_w.p, nblk,
-                            h->g_partial.p, h->g_ticket.p, d_nr, s);
-            if (prec)
-              {
-                // V_{j+1} = w / |w| and the next step's z = P^-1 V_{j+1} in one
-                // pass (formed even if the next step does not come)
-                apply_block_jacobi(h, R, h->g_w.p, N, h->g_z.p, s, d_nr, h->g_V.p + int64_t(j + 1) * N,
-                                   ldr);
-                z_next = true;
-              }
-            else
-              launch_normalize(N, R, h->g_w.p, d_nr, h->g_V.p + int64_t(j + 1) * N, ldr, s);
-            {
-              const size_t nh = size_t(R) * (j + 1);
-              h->g_hpin.alloc(size_t(R) * (2 * (m + 2) + 1));
-              PIBEM_CUDA(cudaMemcpyAsync(h->g_hpin.p, h->g_h.p, sizeof(double) * (2 * nh + R),
-                                         cudaMemcpyDeviceToHost, s));
-              PIBEM_CUDA(cudaStreamSynchronize(s));
-              const double *hp = h->g_hpin.p;
-              std::copy(hp, hp + nh, hh.begin());
-              std::copy(hp + nh, hp + 2 * nh, h2.begin());
-              std::copy(hp + 2 * nh, hp + 2 * nh + R, nr.begin());
-            }
-            ++res.iterations;
-            bool all = true;
-            for (int r = 0; r < R; ++r)
-              {
-                if (kdone[r] >= 0)
-                  continue;
-                double *Hc = &H[size_t(r) * (m + 1) * m];
-                for (int i = 0; i <= j; ++i)
-                  Hc[size_t(i) * m + j] = hh[size_t(r) * (j + 1) + i] + h2[size_t(r) * (j + 1) + i];
-                Hc[size_t(j + 1) * m + j] = std::sqrt(nr[r]);
-                double *c = &cs[size_t(r) * m], *sv = &sn[size_t(r) * m], *gg = &g[size_t(r) * (m + 1)];
-                for (int i = 0; i < j; ++i)
-                  {
-                    double t1 = c[i] * Hc[size_t(i) * m + j] + sv[i] * Hc[size_t(i + 1) * m + j];
-                    Hc[size_t(i + 1) * m + j] = -sv[i] * Hc[size_t(i) * m + j] + c[i] * Hc[size_t(i + 1) * m + j];
-                    Hc[size_t(i) * m + j]     = t1;
-                  }
-                double a = Hc[size_t(j) * m + j], bb = Hc[size_t(j + 1) * m + j];
-                double d = std::hypot(a, bb);
-                c[j]     = d > 0 ? a / d : 1.0;
-                sv[j]    = d > 0 ? bb / d : 0.0;
-                Hc[size_t(j) * m + j]     = d;
-                Hc[size_t(j + 1) * m + j] = 0;
-                gg[j + 1] = -sv[j] * gg[j];
-                gg[j]     = c[j] * gg[j];
-                if (std::fabs(gg[j + 1]) / bn[r] <= tol[r] || bb == 0.0)
-                  kdone[r] = j + 1;
-                else
-                  all = false;
-              }
-            if (all || res.iterations >= maxit)
-              {
-                ++j;
-                break;
-              }
-          }
-        // x += P^-1 V y
-        std::vector<double> y(size_t(R) * (m + 1), 0.0);
-        for (int r = 0; r < R; ++r)
-          {
-            int k = kdone[r] < 0 ? j : kdone[r];
-            if (kdone[r] == 0)
-              k = 0;
-            const double *Hc = &H[size_t(r) * (m + 1) * m];
-            const double *gg = &g[size_t(r) * (m + 1)];
-            for (int i = k - 1; i >= 0; --i)
-              {
-                double sum = gg[i];
-                for (int jj = i + 1; jj < k; ++jj)
-                  sum -= Hc[size_t(i) * m + jj] * y[size_t(r) * (m + 1) + jj];
-                y[size_t(r) * (m + 1) + i] = sum / Hc[size_t(i) * m + i];
-              }
-          }
-        int kmax = j;
-        h->g_y.upload(y.data(), y.size(), s);
+        // V[r][0] = r_r / beta_r (and z = V_0 without preconditioner)
+        launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p, ldr, s, nullptr,
+                         prec ? nullptr : h->g_z.p);
+        if (prec)
+          apply_block_jacobi(h, R, h->g_V.p, ldr, h->g_z.p, s);
+        launch_gmres_cycle_init(R, m, h->g_nrm.p, h->g_bn.p, h->g_tol.p, h->g_g.p, h->g_kdone.p,
+                                h->g_ctl.p, res.iterations, maxit, s);
+        graph_cycle = gmres_cycle(h, R, m, prec, op_tag, A);
+        // x += P^-1 V y, y from the cycle's triangular systems
+        launch_gmres_lsq(R, m, h->g_H.p, h->g_g.p, h->g_kdone.p, h->g_ctl.p, h->g_y.p, s);
         PIBEM_CUDA(cudaMemsetAsync(h->g_u.p, 0, sizeof(double) * R * N, s));
-        launch_gemv_sub(N, R, kmax, N, ldr, h->g_V.p, h->g_y.p, m + 1, h->g_u.p, -1.0, s);
+        launch_gemv_sub(N, R, 0, N, ldr, h->g_V.p, h->g_y.p, L, h->g_u.p, -1.0, s, h->g_ctl.p);
         if (prec)
           {
             apply_block_jacobi(h, R, h->g_u.p, N, h->g_z.p, s);
@@ -952,6 +1052,15 @@ namespace
           }
         else
           launch_axpby(int64_t(R) * N, 1.0, h->g_u.p, 1.0, x, s);
+        // the cycle's iteration count arrives with the next synchronisation
+        PIBEM_CUDA(cudaMemcpyAsync(h->g_ctlpin.p, h->g_ctl.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        pending = res.iterations;
+        if (!graph_cycle)
+          {
+            PIBEM_CUDA(cudaStreamSynchronize(s));
+            res.iterations = h->g_ctlpin.p[1];
+            pending        = -1;
+          }
       }
     return res;
   }
@@ -1123,10 +1232,6 @@ namespace
       op.nrow_ptr      = h->d_nrow_ptr.p;
       op.ncol_ptr      = h->d_ncol_ptr.p;
       op.nval_ptr      = h->d_nval_ptr.p;
-      op.near_part     = h->d_near_part.p;
-      op.near_nblk     = h->near_nblk;
-      op.near_part_wide = h->d_near_part.p + h->near_nblk + 1;
-      op.near_nblk_wide = h->near_nblk_wide;
       op.ncols_end16   = int64_t(pl.ncols.size()) * 4 / 16 * 16;
       op.n_p2m_leaves  = int(pl.pleaf_box.size());
       op.prow_ptr      = h->d_prow_ptr.p;
@@ -1450,32 +1555,6 @@ namespace
     h->d_nrow_ptr.upload(pl.nrow_ptr, s);
     h->d_ncol_ptr.upload(pl.ncol_ptr, s);
     h->d_nval_ptr.upload(pl.nval_ptr, s);
-    {
-      // one-column near SpMVs: per SM as many blocks as are resident (FP32 and
-      // 8-byte values), each a contiguous range of leaves of about equal value bytes
-      int dev = 0, n_sm = 1;
-      PIBEM_CUDA(cudaGetDevice(&dev));
-      PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-      const int            nl  = int(pl.nval_ptr.size()) - 1;
-      const int64_t        tot = pl.nval_ptr.back();
-      std::vector<int32_t> part;
-      auto split = [&](int per_sm) {
-        const int nblk = std::max(1, std::min(nl, per_sm * n_sm));
-        int       leaf = 0;
-        for (int b = 0; b < nblk; ++b)
-          {
-            const int64_t target = tot / nblk * b + tot % nblk * b / nblk;
-            while (leaf < nl && pl.nval_ptr[leaf] < target)
-              ++leaf;
-            part.push_back(b == 0 ? 0 : leaf);
-          }
-        part.push_back(nl);
-        return nblk;
-      };
-      h->near_nblk      = split(NEAR_BLOCKS_PER_SM_F32);
-      h->near_nblk_wide = split(NEAR_BLOCKS_PER_SM_WIDE);
-      h->d_near_part.upload(part, s);
-    }
     h->d_nent_ptr.upload(pl.nent_ptr, s);
     h->d_row_leaf.upload(pl.row_leaf, s);
     h->d_nrows.upload(pl.nrows, s);
@@ -1975,7 +2054,7 @@ namespace
     if (P.precision_mode != PIBEM_PRECISION_MIXED)
       {
         GmresResult gr = gmres(h, R, b.p, x.p, std::vector<double>(R, P.solver_tolerance),
-                               P.solver_max_steps, P.gmres_restart, A64, prec);
+                               P.solver_max_steps, P.gmres_restart, A64, prec, 64);
         iters          = gr.iterations;
         rel            = gr.rel;
       }
@@ -2049,7 +2128,7 @@ namespace
               break;
             PIBEM_CUDA(cudaMemsetAsync(d.p, 0, sizeof(double) * R * N, s));
             GmresResult gr = gmres(h, R, r.p, d.p, itol, P.solver_max_steps - iters,
-                                   P.gmres_restart, A32, prec);
+                                   P.gmres_restart, A32, prec, 32);
             iters += gr.iterations;
             launch_axpby(int64_t(R) * N, 1.0, d.p, 1.0, x.p, s);
             if (refine == 0)

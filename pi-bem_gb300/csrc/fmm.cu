@@ -209,18 +209,19 @@ namespace pibem
         }
     }
 
-    // Near-field SpMV for one column, software-pipelined: block b takes the
-    // contiguous leaves part[b] .. part[b + 1] - 1 (ranges of about equal value
-    // bytes), so its value blocks are one contiguous stream; the last warp
-    // prefetches the value blocks and column ids of the leaves pf leaves ahead
-    // into L2 (cp.async.bulk.prefetch), and while the warps stream the rows of a
-    // leaf, the x entries of the next leaf are gathered into the other half of a
-    // double buffer with cp.async.  A row is computed exactly as in
+    // Near-field SpMV for one column, software-pipelined: persistent blocks
+    // take leaves L, L + gridDim.x, ... (the blocks of the grid stream one
+    // window of consecutive leaves at a time, which keeps the DRAM accesses of
+    // the whole grid close together); the last warp prefetches into L2
+    // (cp.async.bulk.prefetch) the value blocks and column ids of the block's
+    // leaves pf windows ahead, and while the warps stream the rows of a leaf,
+    // the x entries of the block's next leaf are gathered into the other half
+    // of a double buffer with cp.async.  A row is computed exactly as in
     // near_leaf_kernel (same chunks per lane, same order, same butterfly).
     // Shared memory: 2 x ld_max values.
     template <typename T, int MINB>
     __global__ void __launch_bounds__(256, MINB)
-      near_leaf_pipe_kernel(const int32_t *__restrict__ part, int pf, int ld_max, int64_t ids_end16,
+      near_leaf_pipe_kernel(int n_leaves, int pf, int ld_max, int64_t ids_end16,
                             const int64_t *__restrict__ nrow_ptr,
                             const int64_t *__restrict__ ncol_ptr,
                             const int64_t *__restrict__ nval_ptr, const int32_t *__restrict__ nrows,
@@ -230,17 +231,6 @@ namespace pibem
       extern __shared__ __align__(16) unsigned char smem_raw[];
       T        *sxb  = reinterpret_cast<T *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-      // the block's leaf range, kept in shared memory (registers are short)
-      __shared__ int range[2];
-      if (threadIdx.x == 0)
-        {
-          range[0] = part[blockIdx.x];
-          range[1] = part[blockIdx.x + 1];
-        }
-      __syncthreads();
-      const int lb = range[0];
-      if (lb >= range[1])
-        return;
       // gather of leaf l into buffer b: cp.async for the columns, zeros in the padding
       auto gather = [&](int l, int b) {
         const int64_t c0 = ncol_ptr[l], nc = ncol_ptr[l + 1] - c0;
@@ -253,20 +243,24 @@ namespace pibem
             sx[c] = T(0);
         asm volatile("cp.async.commit_group;" ::: "memory");
       };
+      int leaf = blockIdx.x, buf = 0;
+      if (leaf >= n_leaves)
+        return;
       if (pf > 0 && warp == nw - 1)
-        for (int l = lb + 1; l < range[1] && l <= lb + pf; ++l)
-          prefetch_leaf(l, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
-      int buf = 0;
-      gather(lb, 0);
-      for (int leaf = lb; leaf < range[1]; ++leaf, buf ^= 1)
+        for (int k = 1; k <= pf; ++k)
+          if (leaf + k * gridDim.x < n_leaves)
+            prefetch_leaf(leaf + k * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
+      gather(leaf, 0);
+      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncthreads(); // this leaf's x is in place; the other buffer is free
-          const int next = leaf + 1;
-          if (next < range[1])
+          const int next = leaf + gridDim.x;
+          if (next < n_leaves)
             gather(next, buf ^ 1);
-          if (pf > 0 && warp == nw - 1 && leaf + pf + 1 < range[1])
-            prefetch_leaf(leaf + pf + 1, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
+          if (pf > 0 && warp == nw - 1 && leaf + (pf + 1) * gridDim.x < n_leaves)
+            prefetch_leaf(leaf + (pf + 1) * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16,
+                          lane);
           const T      *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -311,12 +305,12 @@ namespace pibem
     // product split exactly (TwoProduct) with its cross terms, the row sums
     // carried with TwoSum; about 11 FP32 instructions per value, so the kernel
     // streams at HBM speed where FP64 FMA (1/58 of the FP32 rate) could not.
-    // Same structure as near_leaf_pipe_kernel: contiguous leaf ranges per block
-    // with L2 prefetch ahead, the next leaf's x gathered with cp.async while the
-    // warps stream two rows each.
+    // Same structure as near_leaf_pipe_kernel: persistent blocks with L2
+    // prefetch ahead, the next leaf's x gathered with cp.async while the warps
+    // stream two rows each.
     // y[row] = hi + lo in FP64 (acc: added).
     __global__ void __launch_bounds__(256, NEAR_BLOCKS_PER_SM_WIDE)
-      near_leaf_ff_kernel(const int32_t *__restrict__ part, int pf, int ld_max, int64_t ids_end16,
+      near_leaf_ff_kernel(int n_leaves, int pf, int ld_max, int64_t ids_end16,
                           const int64_t *__restrict__ nrow_ptr,
                           const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
                           const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
@@ -326,9 +320,6 @@ namespace pibem
       extern __shared__ __align__(16) unsigned char smem_raw[];
       float2   *sxb  = reinterpret_cast<float2 *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-      const int lb = part[blockIdx.x], le = part[blockIdx.x + 1];
-      if (lb >= le)
-        return;
       auto gather = [&](int l, int b) {
         const int64_t c0 = ncol_ptr[l], nc = ncol_ptr[l + 1] - c0;
         const int64_t ld = (nc + 3) / 4 * 4;
@@ -340,20 +331,24 @@ namespace pibem
             sx[c] = make_float2(0.f, 0.f);
         asm volatile("cp.async.commit_group;" ::: "memory");
       };
+      int leaf = blockIdx.x, buf = 0;
+      if (leaf >= n_leaves)
+        return;
       if (pf > 0 && warp == nw - 1)
-        for (int l = lb + 1; l < le && l <= lb + pf; ++l)
-          prefetch_leaf(l, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
-      int buf = 0;
-      gather(lb, 0);
-      for (int leaf = lb; leaf < le; ++leaf, buf ^= 1)
+        for (int k = 1; k <= pf; ++k)
+          if (leaf + k * gridDim.x < n_leaves)
+            prefetch_leaf(leaf + k * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
+      gather(leaf, 0);
+      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncthreads();
-          const int next = leaf + 1;
-          if (next < le)
+          const int next = leaf + gridDim.x;
+          if (next < n_leaves)
             gather(next, buf ^ 1);
-          if (pf > 0 && warp == nw - 1 && leaf + pf + 1 < le)
-            prefetch_leaf(leaf + pf + 1, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
+          if (pf > 0 && warp == nw - 1 && leaf + (pf + 1) * gridDim.x < n_leaves)
+            prefetch_leaf(leaf + (pf + 1) * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16,
+                          lane);
           const float2 *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -1070,7 +1065,15 @@ namespace pibem
 
     inline int tpb_for(int RK) { return RK >= 256 ? 256 : (RK >= 128 ? 128 : 64); }
 
-    // leaves of L2 prefetch ahead in the one-column near SpMVs
+    int near_sm_count()
+    {
+      int dev = 0, n_sm = 1;
+      PIBEM_CUDA(cudaGetDevice(&dev));
+      PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+      return n_sm;
+    }
+
+    // windows of L2 prefetch ahead in the one-column near SpMVs
     int near_prefetch_leaves()
     {
       static const int pf = [] {
@@ -1113,11 +1116,10 @@ namespace pibem
         const size_t  smem1 = size_t(2) * maxnc * sizeof(T);
         if (smem1 > 48 * 1024)
           raise_smem_limit(reinterpret_cast<const void *>(kern), smem1);
-        const int32_t *part = sizeof(T) == 4 ? op.near_part : op.near_part_wide;
-        const int      nblk = sizeof(T) == 4 ? op.near_nblk : op.near_nblk_wide;
-        kern<<<nblk, 256, smem1, s>>>(part, near_prefetch_leaves(), int(maxnc), op.ncols_end16,
-                                      op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols, vals, x,
-                                      y, accumulate);
+        const int grid = std::min(op.n_near_leaves, MINB * near_sm_count());
+        kern<<<grid, 256, smem1, s>>>(op.n_near_leaves, near_prefetch_leaves(), int(maxnc),
+                                      op.ncols_end16, op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows,
+                                      op.ncols, vals, x, y, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
         return;
@@ -1149,8 +1151,9 @@ namespace pibem
     // one launch per column: a column's result does not depend on R
     for (int r = 0; r < R; ++r)
       {
-        near_leaf_ff_kernel<<<op.near_nblk_wide, 256, smem1, s>>>(
-          op.near_part_wide, near_prefetch_leaves(), int(maxnc), op.ncols_end16, op.nrow_ptr, op.ncol_ptr,
+        near_leaf_ff_kernel<<<std::min(op.n_near_leaves, NEAR_BLOCKS_PER_SM_WIDE * near_sm_count()),
+                              256, smem1, s>>>(
+          op.n_near_leaves, near_prefetch_leaves(), int(maxnc), op.ncols_end16, op.nrow_ptr, op.ncol_ptr,
           op.nval_ptr, op.nrows, op.ncols, vals, xff + int64_t(r) * N, y + int64_t(r) * N, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();

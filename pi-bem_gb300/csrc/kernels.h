@@ -79,13 +79,8 @@ namespace pibem
     int64_t        n_rows = 0;
     const int32_t *row_leaf = nullptr, *nrows = nullptr, *ncols = nullptr;
     const int64_t *nrow_ptr = nullptr, *ncol_ptr = nullptr, *nval_ptr = nullptr;
-    // one-column SpMV work split: block b takes leaves near_part[b] ..
-    // near_part[b + 1] - 1 (about equal value bytes), NEAR_BLOCKS_PER_SM_F32
-    // blocks per SM for FP32 values, NEAR_BLOCKS_PER_SM_WIDE for 8-byte values
-    // (near_part_wide); ncols_end16 = bytes of the column-id array rounded down
-    // to 16 (the L2 prefetch stays inside it)
-    const int32_t *near_part = nullptr, *near_part_wide = nullptr;
-    int            near_nblk = 0, near_nblk_wide = 0;
+    // bytes of the column-id array rounded down to 16 (the one-column near
+    // SpMVs' L2 prefetch stays inside it)
     int64_t        ncols_end16 = 0;
     // p2m
     int            n_p2m_leaves = 0;

@@ -62,13 +62,17 @@ namespace pibem
     }
 
     // w[r][t] -= sum_i V[r][i][t] h[r][i]   (h on the device, layout [r][ldh])
+    //   (jctl non-null: ncols = jctl[0])
     __global__ void gemv_sub_kernel(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
                                     const double *__restrict__ V, const double *__restrict__ h,
-                                    int ldh, double *__restrict__ w, double sign)
+                                    int ldh, double *__restrict__ w, double sign,
+                                    const int *__restrict__ jctl)
     {
       int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * R)
         return;
+      if (jctl)
+        ncols = jctl[0];
       int64_t r = idx / n, t = idx % n;
       double  s = 0;
 #pragma unroll 8
@@ -89,13 +93,18 @@ namespace pibem
     // finish (a ticket taken after a fence) adds the nblk partials of each
     // output in the fixed order of dots_final and resets the ticket, so the
     // result does not depend on which block is last.
+    //   jctl (may be null): the Arnoldi step j is read from jctl[0] and the
+    //   pass takes ncols = j + 1 basis vectors (device-driven GMRES); out holds
+    //   ldo values per column r.
     template <int MODE>
     __global__ void __launch_bounds__(256)
       cgs_step_kernel(int64_t n, int ncols, int64_t ldv, int64_t ldr, const double *__restrict__ V,
                       const double *__restrict__ hin, int ldh, double *__restrict__ w, int nblk,
                       double *__restrict__ partial, int *__restrict__ ticket,
-                      double *__restrict__ out)
+                      double *__restrict__ out, const int *__restrict__ jctl, int ldo)
     {
+      if (jctl)
+        ncols = jctl[0] + 1;
       const int     r     = blockIdx.y;
       const int     blk   = blockIdx.x;
       const double *Vr    = V + int64_t(r) * ldr;
@@ -146,23 +155,144 @@ namespace pibem
           for (int o = 16; o > 0; o >>= 1)
             s += __shfl_xor_sync(0xffffffffu, s, o);
           if (lane == 0)
-            out[int64_t(r) * nout + i] = s;
+            out[int64_t(r) * ldo + i] = s;
         }
       if (threadIdx.x == 0)
         ticket[r] = 0;
     }
 
-    // V[r][j+1] = w[r] / hn[r]  (hn > 0), else 0
+    // V[r][j+1] = w[r] / hn[r]  (hn > 0), else 0; with jctl the output column
+    // is out + (jctl[0] + 1) * n; with z the value is also written to z[r]
     __global__ void normalize_kernel(int64_t n, int R, const double *__restrict__ w,
                                      const double *__restrict__ nrm, double *__restrict__ out,
-                                     int64_t ldr)
+                                     int64_t ldr, const int *__restrict__ jctl,
+                                     double *__restrict__ z)
     {
       int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * R)
         return;
       int64_t r = idx / n, t = idx % n;
       double  h = sqrt(nrm[r]);
-      out[r * ldr + t] = h > 0 ? w[idx] / h : 0.0;
+      const double v = h > 0 ? w[idx] / h : 0.0;
+      out[r * ldr + (jctl ? int64_t(jctl[0] + 1) * n : 0) + t] = v;
+      if (z)
+        z[idx] = v;
+    }
+
+    // ---- device-driven restart cycle of GMRES -------------------------------
+    // State per column r: Hessenberg H[r] ((m+1) x m, entry (i, j) at i m + j),
+    // Givens cosines / sines cs[r], sn[r] (m), g[r] (m+1), kdone[r] (-1: active;
+    // k >= 0: the column stopped after k steps of this cycle).  ctl: [0] step j
+    // of the cycle, [1] iterations so far, [2] iteration limit, [3] 1 while the
+    // cycle goes on.  hb: [h1 (R x L) | h2 (R x L) | |w|^2 (R)], L = m + 1, the
+    // two Gram-Schmidt passes' coefficients and the norm of step j.
+
+    // cycle start: g[r] = (beta_r, 0, ...), kdone[r] = 0 where beta_r / bn_r
+    // already meets tol_r, else -1; ctl[0] = 0, ctl[1] = its, ctl[3] = 1
+    __global__ void gmres_cycle_init_kernel(int R, int L, const double *__restrict__ nrm2,
+                                            const double *__restrict__ bn,
+                                            const double *__restrict__ tol, double *__restrict__ g,
+                                            int *__restrict__ kdone, int *__restrict__ ctl, int its,
+                                            int maxit)
+    {
+      for (int r = threadIdx.x; r < R; r += blockDim.x)
+        {
+          const double beta = sqrt(nrm2[r]);
+          g[int64_t(r) * L] = beta;
+          kdone[r]          = beta / bn[r] <= tol[r] ? 0 : -1;
+        }
+      if (threadIdx.x == 0)
+        {
+          ctl[0] = 0;
+          ctl[1] = its;
+          ctl[2] = maxit;
+          ctl[3] = 1;
+        }
+    }
+
+    // Step j's Hessenberg column, its Givens rotation and the stopping test
+    // (|g_{j+1}| / |b| <= tol or a zero subdiagonal), one thread per column;
+    // then j and the iteration count advance and ctl[3] (and, in a graph, the
+    // loop's condition) says whether the cycle goes on.
+    __global__ void gmres_givens_kernel(int R, int m, const double *__restrict__ hb,
+                                        double *__restrict__ H, double *__restrict__ cs,
+                                        double *__restrict__ sn, double *__restrict__ g,
+                                        int *__restrict__ kdone, const double *__restrict__ bn,
+                                        const double *__restrict__ tol, int *__restrict__ ctl,
+                                        cudaGraphConditionalHandle cond, int use_cond)
+    {
+      const int L = m + 1;
+      const int j = ctl[0];
+      __shared__ int all_done;
+      if (threadIdx.x == 0)
+        all_done = 1;
+      __syncthreads();
+      for (int r = threadIdx.x; r < R; r += blockDim.x)
+        {
+          if (kdone[r] >= 0)
+            continue;
+          double       *Hc = H + int64_t(r) * L * m;
+          const double *h1 = hb + int64_t(r) * L, *h2 = hb + int64_t(R) * L + int64_t(r) * L;
+          for (int i = 0; i <= j; ++i)
+            Hc[int64_t(i) * m + j] = h1[i] + h2[i];
+          Hc[int64_t(j + 1) * m + j] = sqrt(hb[2 * int64_t(R) * L + r]);
+          double *c = cs + int64_t(r) * m, *sv = sn + int64_t(r) * m, *gg = g + int64_t(r) * L;
+          for (int i = 0; i < j; ++i)
+            {
+              const double a0 = Hc[int64_t(i) * m + j], a1 = Hc[int64_t(i + 1) * m + j];
+              Hc[int64_t(i) * m + j]     = c[i] * a0 + sv[i] * a1;
+              Hc[int64_t(i + 1) * m + j] = -sv[i] * a0 + c[i] * a1;
+            }
+          const double a = Hc[int64_t(j) * m + j], bb = Hc[int64_t(j + 1) * m + j];
+          const double d = hypot(a, bb);
+          c[j]           = d > 0 ? a / d : 1.0;
+          sv[j]          = d > 0 ? bb / d : 0.0;
+          Hc[int64_t(j) * m + j]     = d;
+          Hc[int64_t(j + 1) * m + j] = 0;
+          gg[j + 1]                  = -sv[j] * gg[j];
+          gg[j]                      = c[j] * gg[j];
+          if (fabs(gg[j + 1]) / bn[r] <= tol[r] || bb == 0.0)
+            kdone[r] = j + 1;
+          else
+            all_done = 0;
+        }
+      __syncthreads();
+      if (threadIdx.x == 0)
+        {
+          const int its    = ctl[1] + 1;
+          const int active = !all_done && j + 1 < m && its < ctl[2];
+          ctl[0]           = j + 1;
+          ctl[1]           = its;
+          ctl[3]           = active;
+          if (use_cond && !active)
+            cudaGraphSetConditional(cond, 0);
+        }
+    }
+
+    // End of a cycle: y[r] solves the column's triangular system of its k steps
+    // (k = kdone[r] if it stopped, else the cycle's step count ctl[0]); y[r][i]
+    // = 0 for i >= k.
+    __global__ void gmres_lsq_kernel(int R, int m, const double *__restrict__ H,
+                                     const double *__restrict__ g, const int *__restrict__ kdone,
+                                     const int *__restrict__ ctl, double *__restrict__ y)
+    {
+      const int L = m + 1;
+      for (int r = threadIdx.x; r < R; r += blockDim.x)
+        {
+          const int     k  = kdone[r] < 0 ? ctl[0] : kdone[r];
+          const double *Hc = H + int64_t(r) * L * m;
+          const double *gg = g + int64_t(r) * L;
+          double       *yr = y + int64_t(r) * L;
+          for (int i = k; i < L; ++i)
+            yr[i] = 0.0;
+          for (int i = k - 1; i >= 0; --i)
+            {
+              double sum = gg[i];
+              for (int jj = i + 1; jj < k; ++jj)
+                sum -= Hc[int64_t(i) * m + jj] * yr[jj];
+              yr[i] = sum / Hc[int64_t(i) * m + i];
+            }
+        }
     }
 
     __global__ void axpby_kernel(int64_t n, double a, const double *__restrict__ x, double b,
@@ -285,6 +415,16 @@ namespace pibem
       x[idx] += shift[idx / n];
     }
 
+    // x[r] += -sqrt(nrm2[r])  (the pure-Neumann shift v - ||v||)
+    __global__ void sub_norm_kernel(int64_t n, int R, const double *__restrict__ nrm2,
+                                    double *__restrict__ x)
+    {
+      int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      x[idx] += -sqrt(nrm2[idx / n]);
+    }
+
     // z[node] = sum_c Pinv[leaf][r][c] v[rows_c]  (leaf-block Jacobi, right
     // preconditioner), in the precision P of the stored inverses: FP32 for the
     // mixed path's inner solves (GB300's FP64 rate is 1/58 of its FP32 rate),
@@ -300,9 +440,12 @@ namespace pibem
                          const int64_t *__restrict__ row_ptr, const int64_t *__restrict__ blk_ptr,
                          const int32_t *__restrict__ rows, const P *__restrict__ Pinv,
                          const double *__restrict__ v, double *__restrict__ z,
-                         const double *__restrict__ nrm2, double *__restrict__ vout, int64_t ldo)
+                         const double *__restrict__ nrm2, double *__restrict__ vout, int64_t ldo,
+                         const int *__restrict__ jctl)
     {
       extern __shared__ __align__(8) unsigned char sv_raw[];
+      if (jctl)
+        vout += int64_t(jctl[0] + 1) * n; // basis vector j + 1 of each column
       P        *sv_all = reinterpret_cast<P *>(sv_raw);
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int leaf = blockIdx.x * 8 + warp;
@@ -432,34 +575,64 @@ namespace pibem
 
   void launch_cgs_step(int mode, int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
                        const double *V, const double *hin, int ldh, double *w, int nblk,
-                       double *partial, int *ticket, double *out, cudaStream_t s)
+                       double *partial, int *ticket, double *out, cudaStream_t s, const int *jctl,
+                       int ldo)
   {
     dim3 grid(nblk, R);
+    if (ldo <= 0)
+      ldo = mode == 2 ? 1 : ncols;
     if (mode == 0)
       cgs_step_kernel<0><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
-                                                     ticket, out);
+                                                     ticket, out, jctl, ldo);
     else if (mode == 1)
       cgs_step_kernel<1><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
-                                                     ticket, out);
+                                                     ticket, out, jctl, ldo);
     else
       cgs_step_kernel<2><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
-                                                     ticket, out);
+                                                     ticket, out, jctl, ldo);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
   void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
-                       const double *h, int ldh, double *w, double sign, cudaStream_t s)
+                       const double *h, int ldh, double *w, double sign, cudaStream_t s,
+                       const int *jctl)
   {
-    gemv_sub_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, ncols, ldv, ldr, V, h, ldh, w, sign);
+    gemv_sub_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, ncols, ldv, ldr, V, h, ldh, w, sign, jctl);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
   void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
-                        int64_t ldr, cudaStream_t s)
+                        int64_t ldr, cudaStream_t s, const int *jctl, double *z)
   {
-    normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr);
+    normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr, jctl, z);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_gmres_cycle_init(int R, int m, const double *nrm2, const double *bn, const double *tol,
+                               double *g, int *kdone, int *ctl, int its, int maxit, cudaStream_t s)
+  {
+    gmres_cycle_init_kernel<<<1, 256, 0, s>>>(R, m + 1, nrm2, bn, tol, g, kdone, ctl, its, maxit);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_gmres_givens(int R, int m, const double *hb, double *H, double *cs, double *sn,
+                           double *g, int *kdone, const double *bn, const double *tol, int *ctl,
+                           cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s)
+  {
+    gmres_givens_kernel<<<1, 256, 0, s>>>(R, m, hb, H, cs, sn, g, kdone, bn, tol, ctl, cond,
+                                          use_cond ? 1 : 0);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_gmres_lsq(int R, int m, const double *H, const double *g, const int *kdone,
+                        const int *ctl, double *y, cudaStream_t s)
+  {
+    gmres_lsq_kernel<<<1, 256, 0, s>>>(R, m, H, g, kdone, ctl, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -552,6 +725,13 @@ namespace pibem
     note_launch();
   }
 
+  void launch_sub_norm(int64_t n, int R, const double *nrm2, double *x, cudaStream_t s)
+  {
+    sub_norm_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, nrm2, x);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
   void launch_add_scalar(int64_t n, int R, const double *shift, double *x, cudaStream_t s)
   {
     add_scalar_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, shift, x);
@@ -563,7 +743,7 @@ namespace pibem
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
                           const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,
                           const double *v, int64_t ldv, double *z, cudaStream_t s,
-                          const double *nrm2, double *vout, int64_t ldo)
+                          const double *nrm2, double *vout, int64_t ldo, const int *jctl)
   {
     if (n_leaves == 0)
       return;
@@ -573,16 +753,18 @@ namespace pibem
       raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel<P>), smem);
     block_apply_kernel<P><<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
                                                                 blk_ptr, rows, Pinv, v, z, nrm2,
-                                                                vout, ldo);
+                                                                vout, ldo, jctl);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
   template void launch_block_apply<float>(int, int, int, int64_t, const int64_t *, const int64_t *,
                                           const int32_t *, const float *, const double *, int64_t,
-                                          double *, cudaStream_t, const double *, double *, int64_t);
+                                          double *, cudaStream_t, const double *, double *, int64_t,
+                                          const int *);
   template void launch_block_apply<double>(int, int, int, int64_t, const int64_t *, const int64_t *,
                                            const int32_t *, const double *, const double *, int64_t,
-                                           double *, cudaStream_t, const double *, double *, int64_t);
+                                           double *, cudaStream_t, const double *, double *, int64_t,
+                                           const int *);
 
   template <typename T>
   void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,

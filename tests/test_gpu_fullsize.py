@@ -11,13 +11,14 @@
 Each operator of the library is compared with the oracle (the CPU restatement
 of source/bem_fma.cc multipole_matr_vect_products :2391-3072 and of
 source/bem_problem.cc compute_alpha / vmult / compute_rhs :1139-1260) on the
-same seeded inputs:
+same seeded inputs (measured on GB300: FP64 <= 6e-14, FP64-accurate <= 7e-14,
+FP32 <= 1e-7):
 
   octree boxes and the three lists                          identical
-  FP64 path: FMM matvec, alpha, vmult, rhs                  1e-10 relative (2-norm)
+  FP64 path: FMM matvec, alpha, vmult, rhs                  1e-12 relative (2-norm)
   FP64-accurate operator (float-float translations, the
-    tcgen05 BF16-digit M2L): vmult, rhs                      1e-11 relative
-  FP32 operator (tcgen05 3xTF32 M2L): vmult                 2e-5 relative
+    tcgen05 BF16-digit M2L): vmult, rhs                      1e-12 relative
+  FP32 operator (tcgen05 3xTF32 M2L): vmult                 1e-6 relative
 
 and the solves: the mixed path's reported residual at 1e-8 is the FP64 one
 (1e-3 relative), and its solution at residual 1e-10 is within 1e-7 of the FP64
@@ -101,14 +102,14 @@ def test_fp64_operators(big, pibem_mod):
     errs = dict(fmmN=rel(gN, oN), fmmD=rel(gD, oD), alpha=rel(g.alpha(), big["alpha"]),
                 vmult=rel(g.system_matvec(big["x"]), big["y_o"]), rhs=rel(g.rhs(big["tmp"]), big["b_o"]))
     print(big["name"], "fp64 vs oracle", errs)
-    assert max(errs.values()) < 1e-10, errs
+    assert max(errs.values()) < 1e-12, errs
 
 
 def test_fp64_accurate_operator(big, pibem_mod):
     g = big["handle"](pibem_mod.PRECISION_FLOAT_FLOAT)
     errs = dict(vmult=rel(g.system_matvec(big["x"]), big["y_o"]), rhs=rel(g.rhs(big["tmp"]), big["b_o"]))
     print(big["name"], "fp64-accurate vs oracle", errs)
-    assert max(errs.values()) < 1e-11, errs
+    assert max(errs.values()) < 1e-12, errs
 
 
 def test_fp32_tensor_core_operator(big, pibem_mod):
@@ -120,7 +121,7 @@ def test_fp32_tensor_core_operator(big, pibem_mod):
         os.environ.pop("PIBEM_MATVEC_FP32", None)
     e = rel(y, big["y_o"])
     print(big["name"], "fp32 tensor-core vs oracle", e)
-    assert e < 2e-5, e
+    assert e < 1e-6, e
 
 
 def test_solves(big, pibem_mod):

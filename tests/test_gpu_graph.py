@@ -66,3 +66,37 @@ def test_graph_is_rebuilt_after_new_mesh(pibem_mod, synthetic):
     np.testing.assert_array_equal(dp, dp2)
     g.close()
     ref.close()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_gmres_cycle_graph_matches_step_launches(pibem_mod, synthetic, mode):
+    """A GMRES restart cycle runs as one CUDA graph (a conditional while node
+    around one Arnoldi step, with the Givens rotation and the stopping test on
+    the device); with phase timing on the same launches are issued step by step.
+    Solutions, iteration counts, operator counts and launch counts agree, for
+    one column and for a batch of three."""
+    S = synthetic
+    mesh, mask, tmp, _, _ = S.spheroid_mixed_case(14, seed=2)
+    prec = pibem_mod.PRECISION_FP64 if mode == "fp64" else pibem_mod.PRECISION_MIXED
+    g = pibem_mod.BEMSolver(fma_truncation_order=6, max_nodes_per_childless_block=20,
+                            is_external_flow=1, precision_mode=prec, gmres_restart=8)
+    g.set_mesh(mesh.xyz, mesh.cells)
+    g.set_bc(mask)
+    for t in (tmp, np.stack([tmp, 0.5 * tmp + 0.1, -tmp])):
+        out = []
+        for prof in (True, False, False):
+            g.set_profiling(prof)
+            l0 = pibem_mod.launch_count()
+            p, d, st = g.solve(t)
+            out.append((p, d, st, pibem_mod.launch_count() - l0))
+        for p, d, st, nl in out[1:]:
+            np.testing.assert_array_equal(p, out[0][0])
+            np.testing.assert_array_equal(d, out[0][1])
+            for k in ("iterations", "fp32_matvecs", "fp64_matvecs", "refinement_steps"):
+                assert st[k] == out[0][2][k], k
+            assert nl == out[0][3]
+        assert out[0][2]["relative_residual"] <= 1e-8
+        # restarts (restart length 8) happened on the way
+        assert out[0][2]["iterations"] > 8
+    g.set_profiling(False)
+    g.close()
