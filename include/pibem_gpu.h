@@ -170,6 +170,12 @@ int pibem_solve_device(pibem_handle *h, int32_t nrhs, double *d_phi, double *d_d
 
 /* Introspection for parity tests and logging. */
 int pibem_tree_info_get(pibem_handle *h, pibem_tree_info *info);
+/* Wall time in seconds of the phases of the last pibem_set_mesh, in the order:
+ * mesh checks and quadrature points, octree and lists, operator plan, plan
+ * upload, near-field integrals, P2M / L2P tables, translation operators, the
+ * rest (the reference times its phases with Teuchos::TimeMonitor). */
+#define PIBEM_SETUP_PHASES 8
+int pibem_setup_phases(pibem_handle *h, double *seconds);
 /* Box table: level, parent, number of children, pmin[3], delta, nodes, quad points. */
 int pibem_tree_boxes(pibem_handle *h, int32_t *level, int32_t *parent, int32_t *nchild,
                      double *pmin, double *delta, int32_t *n_nodes, int32_t *n_quads);

@@ -152,6 +152,8 @@ struct pibem_handle
   Tree         tree;
   Plan         plan;
   double       setup_seconds = 0;
+  // wall time of the set-up phases of the last pibem_set_mesh (pibem_setup_phases)
+  double       setup_phase[PIBEM_SETUP_PHASES] = {};
   size_t       bytes_resident = 0;
   // mesh
   DBuf<double>  d_xyz, d_qpts, d_qnrm, d_qjxw, d_qshape, d_gpts, d_gw;
@@ -1232,7 +1234,6 @@ namespace
       op.nrow_ptr      = h->d_nrow_ptr.p;
       op.ncol_ptr      = h->d_ncol_ptr.p;
       op.nval_ptr      = h->d_nval_ptr.p;
-      op.ncols_end16   = int64_t(pl.ncols.size()) * 4 / 16 * 16;
       op.n_p2m_leaves  = int(pl.pleaf_box.size());
       op.prow_ptr      = h->d_prow_ptr.p;
       op.pleaf_box     = h->d_pleaf_box.p;
@@ -1458,6 +1459,13 @@ namespace
                      const int32_t *cells, const int32_t *doff, const int32_t *dids)
   {
     auto t0 = std::chrono::steady_clock::now();
+    auto tp = t0;
+    auto phase = [&](int i) {
+      const auto now     = std::chrono::steady_clock::now();
+      h->setup_phase[i]  = std::chrono::duration<double>(now - tp).count();
+      tp                 = now;
+    };
+    std::fill(h->setup_phase, h->setup_phase + PIBEM_SETUP_PHASES, 0.0);
     drop_graph(h); // its kernels carry the previous mesh's sizes
     h->d_con_nrm.release();
     if (n_nodes <= 0 || n_cells <= 0 || !xyz || !cells)
@@ -1531,9 +1539,12 @@ namespace
     std::vector<double> qpts(3 * Q);
     h->d_qpts.download(qpts.data(), qpts.size(), s);
     PIBEM_CUDA(cudaStreamSynchronize(s));
+    phase(0);
     // octree, lists and plan
     build_tree(m, qpts, h->nq, P.num_octree_levels, P.max_nodes_per_childless_block, h->tree);
+    phase(1);
     build_plan(m, h->tree, h->nq, P.fma_truncation_order, h->plan);
+    phase(2);
     const Tree &t  = h->tree;
     const Plan &pl = h->plan;
     const int   K  = pl.K;
@@ -1625,6 +1636,7 @@ namespace
       h->d_m2p_tnodes.upload(tnodes, s);
     }
     ensure_fmm_tables(P.device, s);
+    phase(3);
     // diagonal column of every row inside its leaf (block-Jacobi)
     {
       std::vector<int32_t> dc(pl.nrows.size());
@@ -1700,6 +1712,7 @@ namespace
       h->d_S.alloc(nval);
       h->d_S32.alloc(nval);
     }
+    phase(4);
     // P2M and L2P tables
     {
       const int64_t nrows_p = int64_t(pl.prow_dof.size());
@@ -1732,6 +1745,8 @@ namespace
           launch_convert_d2ff(npos * K4, h->d_W.p, h->d_Wff.p, s);
         }
     }
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    phase(5);
     // translation operators
     {
       std::vector<double> m2m, l2l, m2l;
@@ -1794,6 +1809,7 @@ namespace
       h->d_err.zero(s);
       PIBEM_CUDA(cudaStreamSynchronize(s));
     }
+    phase(6);
     fill_operator_views(h);
     // free setup-only buffers
     h->d_entries.release();
@@ -1812,6 +1828,7 @@ namespace
                            : 0);
     if (P.hbm_budget_gb > 0 && double(h->bytes_resident) > P.hbm_budget_gb * 1e9)
       throw Error(PIBEM_ENOMEM_HBM, "resident operator exceeds the HBM budget");
+    phase(7);
     h->mesh_ok       = true;
     h->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
@@ -2431,6 +2448,15 @@ extern "C"
       return PIBEM_EINVAL;
     *bytes = uint64_t(h->device_bytes());
     return PIBEM_OK;
+  }
+
+  int pibem_setup_phases(pibem_handle *h, double *seconds)
+  {
+    return guarded(h, [&] {
+      if (!seconds)
+        throw Error(PIBEM_EINVAL, "null output");
+      std::copy(h->setup_phase, h->setup_phase + PIBEM_SETUP_PHASES, seconds);
+    });
   }
 
   int pibem_tree_info_get(pibem_handle *h, pibem_tree_info *info)

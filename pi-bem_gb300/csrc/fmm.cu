@@ -174,55 +174,19 @@ namespace pibem
     __device__ inline void cp_async_x(float *dst, const float *src) { cp_async4(dst, src); }
     __device__ inline void cp_async_x(double *dst, const double *src) { cp_async8(dst, src); }
 
-    // L2 prefetch (a hint) of leaf l's value block, 16 KB per lane of the calling
-    // warp (the first 512 KB of a block), and of its column ids (lane 31, the
-    // ids rounded out to 16 bytes within the first ids_end16 bytes of the array,
-    // at most 16 KB).  Value blocks start on 16 bytes and are multiples of 16
-    // bytes long (rows of 4 values).
-    template <typename V>
-    __device__ inline void prefetch_leaf(int l, const int64_t *__restrict__ ncol_ptr,
-                                         const int64_t *__restrict__ nval_ptr,
-                                         const int32_t *__restrict__ ncols, const V *__restrict__ vals,
-                                         int64_t ids_end16, int lane)
-    {
-      const int64_t v0 = nval_ptr[l], vb = (nval_ptr[l + 1] - v0) * int64_t(sizeof(V));
-      const int64_t o  = int64_t(lane) * 16384;
-      if (o < vb)
-        {
-          const uint32_t n = uint32_t(vb - o < 16384 ? vb - o : 16384);
-          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
-                         reinterpret_cast<const char *>(vals + v0) + o),
-                       "r"(n)
-                       : "memory");
-        }
-      if (lane == 31)
-        {
-          const int64_t b0 = ncol_ptr[l] * 4 / 16 * 16;
-          int64_t       b1 = (ncol_ptr[l + 1] * 4 + 15) / 16 * 16;
-          b1               = b1 < ids_end16 ? b1 : ids_end16;
-          b1               = b1 < b0 + 16384 ? b1 : b0 + 16384;
-          if (b1 > b0)
-            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
-                           reinterpret_cast<const char *>(ncols) + b0),
-                         "r"(uint32_t(b1 - b0))
-                         : "memory");
-        }
-    }
-
     // Near-field SpMV for one column, software-pipelined: persistent blocks
     // take leaves L, L + gridDim.x, ... (the blocks of the grid stream one
-    // window of consecutive leaves at a time, which keeps the DRAM accesses of
-    // the whole grid close together); the last warp prefetches into L2
-    // (cp.async.bulk.prefetch) the value blocks and column ids of the block's
-    // leaves pf windows ahead, and while the warps stream the rows of a leaf,
-    // the x entries of the block's next leaf are gathered into the other half
-    // of a double buffer with cp.async.  A row is computed exactly as in
-    // near_leaf_kernel (same chunks per lane, same order, same butterfly).
-    // Shared memory: 2 x ld_max values.
+    // window of consecutive leaves at a time: measured faster on GB300 than
+    // contiguous leaf ranges of equal bytes per block, 80 against 125 us on the
+    // 98k spheroid; an L2 prefetch of the next windows with
+    // cp.async.bulk.prefetch made it slower, 89-92 us); while the warps stream
+    // the rows of a leaf, the x entries of the block's next leaf are gathered
+    // into the other half of a double buffer with cp.async.  A row is computed
+    // exactly as in near_leaf_kernel (same chunks per lane, same order, same
+    // butterfly).  Shared memory: 2 x ld_max values.
     template <typename T, int MINB>
     __global__ void __launch_bounds__(256, MINB)
-      near_leaf_pipe_kernel(int n_leaves, int pf, int ld_max, int64_t ids_end16,
-                            const int64_t *__restrict__ nrow_ptr,
+      near_leaf_pipe_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ nrow_ptr,
                             const int64_t *__restrict__ ncol_ptr,
                             const int64_t *__restrict__ nval_ptr, const int32_t *__restrict__ nrows,
                             const int32_t *__restrict__ ncols, const T *__restrict__ vals,
@@ -246,10 +210,6 @@ namespace pibem
       int leaf = blockIdx.x, buf = 0;
       if (leaf >= n_leaves)
         return;
-      if (pf > 0 && warp == nw - 1)
-        for (int k = 1; k <= pf; ++k)
-          if (leaf + k * gridDim.x < n_leaves)
-            prefetch_leaf(leaf + k * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
       gather(leaf, 0);
       for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
         {
@@ -258,9 +218,6 @@ namespace pibem
           const int next = leaf + gridDim.x;
           if (next < n_leaves)
             gather(next, buf ^ 1);
-          if (pf > 0 && warp == nw - 1 && leaf + (pf + 1) * gridDim.x < n_leaves)
-            prefetch_leaf(leaf + (pf + 1) * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16,
-                          lane);
           const T      *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -305,12 +262,11 @@ namespace pibem
     // product split exactly (TwoProduct) with its cross terms, the row sums
     // carried with TwoSum; about 11 FP32 instructions per value, so the kernel
     // streams at HBM speed where FP64 FMA (1/58 of the FP32 rate) could not.
-    // Same structure as near_leaf_pipe_kernel: persistent blocks with L2
-    // prefetch ahead, the next leaf's x gathered with cp.async while the warps
-    // stream two rows each.
+    // Same structure as near_leaf_pipe_kernel: persistent blocks, the next
+    // leaf's x gathered with cp.async while the warps stream two rows each.
     // y[row] = hi + lo in FP64 (acc: added).
     __global__ void __launch_bounds__(256, NEAR_BLOCKS_PER_SM_WIDE)
-      near_leaf_ff_kernel(int n_leaves, int pf, int ld_max, int64_t ids_end16,
+      near_leaf_ff_kernel(int n_leaves, int ld_max,
                           const int64_t *__restrict__ nrow_ptr,
                           const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
                           const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
@@ -334,10 +290,6 @@ namespace pibem
       int leaf = blockIdx.x, buf = 0;
       if (leaf >= n_leaves)
         return;
-      if (pf > 0 && warp == nw - 1)
-        for (int k = 1; k <= pf; ++k)
-          if (leaf + k * gridDim.x < n_leaves)
-            prefetch_leaf(leaf + k * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16, lane);
       gather(leaf, 0);
       for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
         {
@@ -346,9 +298,6 @@ namespace pibem
           const int next = leaf + gridDim.x;
           if (next < n_leaves)
             gather(next, buf ^ 1);
-          if (pf > 0 && warp == nw - 1 && leaf + (pf + 1) * gridDim.x < n_leaves)
-            prefetch_leaf(leaf + (pf + 1) * gridDim.x, ncol_ptr, nval_ptr, ncols, vals, ids_end16,
-                          lane);
           const float2 *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -1073,15 +1022,6 @@ namespace pibem
       return n_sm;
     }
 
-    // windows of L2 prefetch ahead in the one-column near SpMVs
-    int near_prefetch_leaves()
-    {
-      static const int pf = [] {
-        const char *e = std::getenv("PIBEM_NEAR_PREFETCH");
-        return e ? std::max(0, std::min(8, std::atoi(e))) : 2;
-      }();
-      return pf;
-    }
   } // namespace
 
   void launch_l2p_ff(const OperatorDev<double> &op, int R, int N, const float2 *Lff, double *y,
@@ -1117,9 +1057,8 @@ namespace pibem
         if (smem1 > 48 * 1024)
           raise_smem_limit(reinterpret_cast<const void *>(kern), smem1);
         const int grid = std::min(op.n_near_leaves, MINB * near_sm_count());
-        kern<<<grid, 256, smem1, s>>>(op.n_near_leaves, near_prefetch_leaves(), int(maxnc),
-                                      op.ncols_end16, op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows,
-                                      op.ncols, vals, x, y, accumulate);
+        kern<<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr, op.ncol_ptr,
+                                      op.nval_ptr, op.nrows, op.ncols, vals, x, y, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
         return;
@@ -1153,8 +1092,8 @@ namespace pibem
       {
         near_leaf_ff_kernel<<<std::min(op.n_near_leaves, NEAR_BLOCKS_PER_SM_WIDE * near_sm_count()),
                               256, smem1, s>>>(
-          op.n_near_leaves, near_prefetch_leaves(), int(maxnc), op.ncols_end16, op.nrow_ptr, op.ncol_ptr,
-          op.nval_ptr, op.nrows, op.ncols, vals, xff + int64_t(r) * N, y + int64_t(r) * N, accumulate);
+          op.n_near_leaves, int(maxnc), op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols, vals,
+          xff + int64_t(r) * N, y + int64_t(r) * N, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
       }

@@ -79,9 +79,6 @@ namespace pibem
     int64_t        n_rows = 0;
     const int32_t *row_leaf = nullptr, *nrows = nullptr, *ncols = nullptr;
     const int64_t *nrow_ptr = nullptr, *ncol_ptr = nullptr, *nval_ptr = nullptr;
-    // bytes of the column-id array rounded down to 16 (the one-column near
-    // SpMVs' L2 prefetch stays inside it)
-    int64_t        ncols_end16 = 0;
     // p2m
     int            n_p2m_leaves = 0;
     const int64_t *prow_ptr = nullptr;

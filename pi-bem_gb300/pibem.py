@@ -97,7 +97,7 @@ EXPORTS = [
     "pibem_launch_count", "pibem_fmm_matvec_noalloc", "pibem_device_bytes",
     "pibem_ucd_read", "pibem_mesh_io_error", "pibem_double_nodes",
     "pibem_dirichlet_mask_from_materials", "pibem_compute_normals",
-    "pibem_compute_surface_gradients", "pibem_compute_gradients",
+    "pibem_compute_surface_gradients", "pibem_compute_gradients", "pibem_setup_phases",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -157,6 +157,7 @@ def load():
     L.pibem_compute_normals.argtypes = [C.c_void_p, _dp]
     L.pibem_compute_surface_gradients.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
     L.pibem_compute_gradients.argtypes = [C.c_void_p, C.c_int32, _dp, _dp, _dp]
+    L.pibem_setup_phases.argtypes = [C.c_void_p, _dp]
     _lib = L
     return L
 
@@ -334,6 +335,15 @@ class BEMSolver:
         self._check(self.L.pibem_solve_device(self.h, nrhs, C.c_void_p(phi_ptr), C.c_void_p(dphi_ptr),
                                               C.c_void_p(tmp_ptr), C.byref(st)))
         return st.as_dict()
+
+    SETUP_PHASES = ("mesh_quadrature", "octree_lists", "plan", "plan_upload", "near_field",
+                    "p2m_l2p_tables", "translation_operators", "rest")
+
+    def setup_phases(self):
+        """Seconds of each phase of the last set_mesh (dict)."""
+        out = np.zeros(len(self.SETUP_PHASES))
+        self._check(self.L.pibem_setup_phases(self.h, _d(out)))
+        return dict(zip(self.SETUP_PHASES, out.tolist()))
 
     def tree_info(self):
         ti = TreeInfo()
