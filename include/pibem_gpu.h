@@ -30,6 +30,7 @@ extern "C" {
 #define PIBEM_ENOCONV 3     /* GMRES did not reach the tolerance within max steps */
 #define PIBEM_ETIMEDOUT 4   /* a bounded device wait gave up */
 #define PIBEM_ECUDA 5       /* CUDA runtime error */
+#define PIBEM_EAGAIN 6      /* request slots: no free slot / no finished request yet */
 
 /* Arithmetic of the solve. */
 #define PIBEM_PRECISION_FP64 0  /* plain path: every matvec in FP64 */
@@ -167,6 +168,38 @@ int pibem_solve(pibem_handle *h, int32_t nrhs, double *phi, double *dphi_dn,
 /* Same as pibem_solve with device pointers, stream-ordered. */
 int pibem_solve_device(pibem_handle *h, int32_t nrhs, double *d_phi, double *d_dphi_dn,
                        const double *d_tmp_rhs, pibem_solve_stats *stats);
+
+/* ---- request slots: continuous batching of solves on one mesh -------------
+ * The serving form of pibem_solve (BEMProblem::solve, bem_problem.cc:1352-1374,
+ * one solve per call there).  A handle opens max_slots slots; each submitted
+ * right-hand side (tmp_rhs as in pibem_solve, with a caller's request id) takes
+ * a free slot and runs the same algorithm as a column of pibem_solve.  Each
+ * pibem_slots_step advances every slot from event to event (right-hand side,
+ * residuals, refinement decisions: operator applications shared by the slots
+ * that need them at that moment) and runs the Arnoldi steps of all slots in a
+ * GMRES cycle on the device until one of them ends its cycle; right-hand sides
+ * submitted between steps join at the next step.  A slot's arithmetic does not
+ * depend on the other slots: its result equals what pibem_solve gives for that
+ * right-hand side alone.  Finished requests are collected in request-id order
+ * with the full phi / dphi_dn vectors (known entries from tmp_rhs) and their
+ * own statistics.  Host arrays of n_nodes doubles; the work is ordered on the
+ * handle's stream and every call returns after it.  pibem_solve is refused
+ * while slots are open.
+ *   pibem_slots_submit: PIBEM_EAGAIN when every slot is taken; *slot = the slot.
+ *   pibem_slots_step:   max_steps > 0 bounds the Arnoldi steps of this call
+ *                       (so that waiting submissions join soon: a slot in the
+ *                       middle of a GMRES cycle resumes it at the next call);
+ *                       *n_active = slots in progress, *n_done = finished ones
+ *                       waiting to be collected.
+ *   pibem_slots_collect: PIBEM_EAGAIN when none has finished; PIBEM_ENOCONV
+ *                       (the results are written) when it stopped on the step
+ *                       limit above the tolerance. */
+int pibem_slots_open(pibem_handle *h, int32_t max_slots);
+int pibem_slots_submit(pibem_handle *h, int64_t request_id, const double *tmp_rhs, int32_t *slot);
+int pibem_slots_step(pibem_handle *h, int32_t max_steps, int32_t *n_active, int32_t *n_done);
+int pibem_slots_collect(pibem_handle *h, int64_t *request_id, double *phi, double *dphi_dn,
+                        pibem_solve_stats *stats);
+int pibem_slots_close(pibem_handle *h);
 
 /* Introspection for parity tests and logging. */
 int pibem_tree_info_get(pibem_handle *h, pibem_tree_info *info);

@@ -11,6 +11,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -136,6 +137,63 @@ namespace
   }
 } // namespace
 
+namespace pibem
+{
+  // stage of one column (right-hand side) in the solve engine (capi.cu)
+  enum ColStage : uint8_t
+  {
+    ST_FREE,      // slot unused
+    ST_RHS,       // needs its right-hand side b = rhs(tmp)
+    ST_ASSESS,    // mixed: the refinement decision on |r|
+    ST_TRUERES,   // mixed: needs r = b - A64 x
+    ST_R32,       // mixed: needs r <- r - A32 d
+    ST_INNER,     // mixed: a restart of the correction's GMRES (w = r - A32 d)
+    ST_RES,       // plain: a restart of GMRES (w = b - A64 x)
+    ST_ARNOLDI,   // in a GMRES cycle on the device
+    ST_CYCLE_END, // its cycle ended: x (plain) or d (mixed) += P^-1 V y
+    ST_XUPD,      // mixed: x += d after a correction
+    ST_DONE       // solved; waiting to be collected
+  };
+
+  struct ColHost
+  {
+    ColStage st         = ST_FREE;
+    int64_t  rid        = -1;
+    bool     final_pass = false; // mixed: the exact residual after the refinement loop
+    bool     r_exact    = true;  // mixed: r is b - A64 x (not the A32-updated estimate)
+    bool     refine_inc = false; // mixed: the pending residual ends a refinement step
+    bool     ok         = false;
+    int      refine = 0, iters = 0, its_inner = 0, inner_maxit = 0;
+    int      c32 = 0, c64 = 0; // operator applications of this column
+    double   bn_outer = 1, bn_inner = 1, rel = 1, itol = 0;
+    std::chrono::steady_clock::time_point t0;
+    double   seconds = 0;
+  };
+
+  // One GMRES cycle graph (per active-column count and buffer set)
+  struct CycleGraph
+  {
+    std::array<uintptr_t, 48> key{};
+    cudaGraphExec_t           exec    = nullptr;
+    int64_t                   kernels = 0;
+    int                       c32 = 0, c64 = 0;
+  };
+
+  // Device state of the solve engine: S column slots, Krylov dimension m;
+  // vectors slot-strided (column k at k N), Krylov bases (m + 1) N apart
+  struct Engine
+  {
+    int                  S = 0, m = 0;
+    bool                 mixed = false, prec = false;
+    std::vector<ColHost> col;
+    DBuf<double>         V, z, w, u, b, x, r, d, tmp, cz, cw, hb, partial, H, cs, sn, g, y, bn, tol, nrm;
+    DBuf<int>            ticket, kdone, jvec, its, maxit, sel, act, ctl;
+    PinnedBuf<int>       ipin;
+    std::vector<double>  h_bn, h_tol;
+    std::vector<int>     h_its, h_maxit, h_jvec, h_ctl;
+  };
+} // namespace pibem
+
 struct pibem_handle
 {
   pibem_params prm;
@@ -187,6 +245,7 @@ struct pibem_handle
   DBuf<float2>  d_Wff;  // L2P rows as pairs (modes other than FP64)
   DBuf<double>  d_Tcr;  // P2M strengths of the right-hand side: dir ? T1 : -T2
   DBuf<int>     d_err;
+  DBuf<int>     d_near_queue; // leaf schedule of the one-column near SpMVs
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
   int                  max_leaf_rows = 0;
@@ -217,15 +276,7 @@ struct pibem_handle
   DBuf<uint16_t> d_ozimg, d_ozslc;
   DBuf<int16_t>  d_ozecol;
   DBuf<int>      d_ozerow;
-  DBuf<double> g_V, g_w, g_z, g_partial, g_h, g_y, g_nrm, g_u, g_bn;
-  DBuf<int>    g_ticket; // Arnoldi pass tickets (zero between launches)
-  // device state of a GMRES restart cycle (krylov.cu): Hessenberg matrices,
-  // rotations, right-hand sides g, tolerances, per-column step of stopping,
-  // control words [step, iterations, limit, go on]
-  DBuf<double> g_H, g_cs, g_sn, g_g, g_tol;
-  DBuf<int>    g_kdone, g_ctl;
   PinnedBuf<double> g_small; // small reads the host waits for (norms)
-  PinnedBuf<int>    g_ctlpin; // host copy of the cycle's control words
   DBuf<double> sh_part, sh_nrm; // pure-Neumann shift of the operator input / output
   // solve temporaries and host-pointer staging (grow-only: no cudaMalloc / cudaFree,
   // and so no device-wide synchronisation, once a handle has solved its largest batch)
@@ -236,14 +287,11 @@ struct pibem_handle
   cudaGraphExec_t g32_exec = nullptr;
   uintptr_t       g32_key[8] = {};
   int64_t         g32_kernels = 0;
-  // one GMRES restart cycle as a CUDA graph: a conditional while node around
-  // one Arnoldi step, captured for the key's buffers, column count, Krylov
-  // dimension, operator and preconditioner; per step: kernels and operator
-  // applications (FP32, FP64) it makes
-  cudaGraphExec_t gm_exec = nullptr;
-  uintptr_t       gm_key[32] = {};
-  int64_t         gm_kernels = 0;
-  int             gm_c32 = 0, gm_c64 = 0;
+  // the solve engine and its GMRES cycle graphs (a conditional while node
+  // around one Arnoldi step of the active columns)
+  Engine                  eng;
+  std::vector<CycleGraph> cycle_graphs;
+  bool                    slots_open = false; // pibem_slots_open
   // d_modes holds this mode for modes_R columns (-1: other contents)
   int             modes_R = -1;
   uint8_t         modes_val = 0;
@@ -280,12 +328,13 @@ struct pibem_handle
     add(d_con_row, d_con_col, d_con_p, d_con_q, d_con_kind, d_con_nrm, d_con_sg);
     add(d_Sff, d_Srff, d_xff, d_Wff, d_Tcr);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
-        d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
+        d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_near_queue, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
         d_y32, d_m2p32, d_Y32, d_Mff, d_Lff, d_ozimg, d_ozslc, d_ozecol, d_ozerow);
-    add(g_V, g_w, g_z, g_partial, g_h, g_y, g_nrm, g_u, g_bn, sv_b, sv_x, sv_r, sv_d, sv_w,
-        sv_part, sv_nrm);
-    add(g_H, g_cs, g_sn, g_g, g_tol, g_kdone, g_ctl, sh_part, sh_nrm);
+    add(sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm, sh_part, sh_nrm);
+    add(eng.V, eng.z, eng.w, eng.u, eng.b, eng.x, eng.r, eng.d, eng.tmp, eng.cz, eng.cw, eng.hb,
+        eng.partial, eng.H, eng.cs, eng.sn, eng.g, eng.y, eng.bn, eng.tol, eng.nrm);
+    add(eng.ticket, eng.kdone, eng.jvec, eng.its, eng.maxit, eng.sel, eng.act, eng.ctl);
     for (const auto &b : io_buf)
       t += b.bytes();
     return t;
@@ -656,9 +705,10 @@ namespace
     if (h->g32_exec)
       cudaGraphExecDestroy(h->g32_exec);
     h->g32_exec = nullptr;
-    if (h->gm_exec)
-      cudaGraphExecDestroy(h->gm_exec);
-    h->gm_exec = nullptr;
+    for (auto &c : h->cycle_graphs)
+      if (c.exec)
+        cudaGraphExecDestroy(c.exec);
+    h->cycle_graphs.clear();
   }
 
   // The FP32 operator is applied once per GMRES iteration with the same buffers,
@@ -767,29 +817,36 @@ namespace
     h->cnt32 += R;
   }
 
+  void compute_rhs_dev(pibem_handle *h, int R, const double *tmp, double *rhs);
+  void constrain_rhs(pibem_handle *h, int R, const double *tmp, double *b);
+
   // ---------------------------------------------------------------------
-  // Restarted GMRES(m) for R right-hand sides in lockstep, right leaf-block
-  // Jacobi preconditioning, CGS2 Arnoldi in FP64 on the device.  Stops column r
-  // at ||b - A x|| / ||b|| <= tol[r] (true residual at every restart); a column
-  // with tol[r] = +inf is left unchanged.  The columns share the operator
-  // applications but no arithmetic, so a column's iterates do not depend on the
-  // other columns of the batch.
-  //
-  // A restart cycle runs on the device without the host: each Arnoldi step is
-  // followed by gmres_givens_kernel (the Hessenberg column, its Givens rotation,
-  // the stopping test), and the cycle's least-squares solution and update of x
-  // are kernels too.  The cycle is one CUDA graph -- a conditional while node
-  // around one step, captured once per handle, column count, Krylov dimension,
-  // operator and buffer set -- so the host waits only at restarts.  While phase
-  // timing is on, or the caller's stream is itself being captured, the same
-  // launches are issued step by step with a read of the continue flag after
-  // each (the same arithmetic).
+  // The solve engine.  Every right-hand side ("column") of a solve -- the
+  // batch of pibem_solve, or the request slots of the pibem_slots_* entry
+  // points -- runs its own state machine:
+  //   plain FP64 path (BEMProblem::solve_system, bem_problem.cc:1267-1347):
+  //     b = rhs(tmp), x0 = b, restarted GMRES(m) on the FP64 operator with
+  //     right leaf-block Jacobi preconditioning, stopping at the relative true
+  //     residual ||b - A x|| / ||b|| <= tol, checked at every restart;
+  //   mixed path: FP64 iterative refinement from x0 = 0 around GMRES(m) on the
+  //     FP32 operator: each correction d solves A32 d = r to an inner tolerance;
+  //     the first residual after a correction is b - A64 x, later ones are
+  //     updated as r <- r - A32 d (|d| shrinks by the inner tolerance at each
+  //     step, so the update's rounding stays far below the target); an
+  //     estimate that meets the tolerance is confirmed with b - A64 x before the
+  //     column stops (A64: the FP64-accurate operator).
+  // The host advances the columns from event to event.  Each operator
+  // application is shared by the columns that need it at that moment (they are
+  // gathered into one contiguous batch), and the Arnoldi steps of every column
+  // inside a GMRES cycle run on the device -- CGS2 in FP64, the Hessenberg
+  // column's Givens rotation and the stopping test (gmres_givens_kernel) -- as
+  // one CUDA graph, a conditional while node around one step, until some column
+  // ends its cycle (it met its tolerance, took m steps or reached its iteration
+  // limit).  While phase timing is on, or the caller's stream is itself being
+  // captured, the same launches are issued step by step.  A column's arithmetic
+  // never depends on the other columns, so its result is the same alone, in a
+  // batch, or admitted while other columns are in the middle of their solves.
   // ---------------------------------------------------------------------
-  struct GmresResult
-  {
-    int                 iterations = 0;
-    std::vector<double> rel;
-  };
 
   // R columns of n doubles from src (column stride lds) to dst (column stride ldd)
   void copy_cols(double *dst, int64_t ldd, const double *src, int64_t lds, int64_t n, int R,
@@ -803,16 +860,16 @@ namespace
   // handle keeps them (GMRES on an FP64-accurate operator), else the FP32 ones
   void apply_block_jacobi(pibem_handle *h, int R, const double *v, int64_t ldv, double *z,
                           cudaStream_t s, const double *nrm2 = nullptr, double *vout = nullptr,
-                          int64_t ldo = 0, const int *jctl = nullptr)
+                          int64_t ldo = 0, const int *jvec = nullptr, const int *sel = nullptr)
   {
     const int     nl = int(h->blk_ptr.size()) - 1;
     const int64_t N  = h->N();
     if (h->d_Pinv64.p)
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
-                         h->d_Pinv64.p, v, ldv, z, s, nrm2, vout, ldo, jctl);
+                         h->d_Pinv64.p, v, ldv, z, s, nrm2, vout, ldo, jvec, sel);
     else
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
-                         h->d_Pinv.p, v, ldv, z, s, nrm2, vout, ldo, jctl);
+                         h->d_Pinv.p, v, ldv, z, s, nrm2, vout, ldo, jvec, sel);
   }
 
   // n values from the device into out, through the handle's page-locked buffer
@@ -825,44 +882,179 @@ namespace
     std::copy(h->g_small.p, h->g_small.p + n, out);
   }
 
-  // One Arnoldi step j (j read on the device from g_ctl[0]): z holds P^-1 V_j
-  // (V_j itself without preconditioner); w = A z; CGS2 coefficients into
-  // g_h; V_{j+1} = w / |w| and the next z; then the Givens step, which also
-  // advances j and decides whether the cycle goes on.
-  void gmres_step(pibem_handle *h, int R, int m, bool prec,
-                  const std::function<void(const double *, double *)> &A,
-                  cudaGraphConditionalHandle cond, bool use_cond)
+  constexpr int ENG_NBLK = 2 * 152; // partial-sum blocks of the GMRES norms and Gram-Schmidt passes
+  constexpr int ENG_NBLK_REFINE = 64; // of the refinement residual norms
+
+  // (re)size the engine for S columns and Krylov dimension m; keeps nothing
+  void engine_open(pibem_handle *h, int S, int m)
   {
-    const int64_t N    = h->N();
-    cudaStream_t  s    = h->stream;
-    const int     nblk = 2 * 152;
-    const int     L    = m + 1;
-    const int64_t ldr  = int64_t(L) * N;
-    const int    *jc   = h->g_ctl.p;
-    double       *h1 = h->g_h.p, *h2 = h1 + size_t(R) * L, *nr = h2 + size_t(R) * L;
-    A(h->g_z.p, h->g_w.p);
-    launch_cgs_step(0, N, R, 0, N, ldr, h->g_V.p, nullptr, 0, h->g_w.p, nblk, h->g_partial.p,
-                    h->g_ticket.p, h1, s, jc, L);
-    launch_cgs_step(1, N, R, 0, N, ldr, h->g_V.p, h1, L, h->g_w.p, nblk, h->g_partial.p,
-                    h->g_ticket.p, h2, s, jc, L);
-    launch_cgs_step(2, N, R, 0, N, ldr, h->g_V.p, h2, L, h->g_w.p, nblk, h->g_partial.p,
-                    h->g_ticket.p, nr, s, jc, 1);
-    if (prec) // V_{j+1} = w / |w| and the next step's z = P^-1 V_{j+1} in one pass
-      apply_block_jacobi(h, R, h->g_w.p, N, h->g_z.p, s, nr, h->g_V.p, ldr, jc);
-    else
-      launch_normalize(N, R, h->g_w.p, nr, h->g_V.p, ldr, s, jc, h->g_z.p);
-    launch_gmres_givens(R, m, h1, h->g_H.p, h->g_cs.p, h->g_sn.p, h->g_g.p, h->g_kdone.p,
-                        h->g_bn.p, h->g_tol.p, h->g_ctl.p, cond, use_cond, s);
+    Engine       &E = h->eng;
+    const int64_t N = h->N();
+    if (S < 1 || S > 1024)
+      throw Error(PIBEM_EINVAL, "between 1 and 1024 columns per solve / slots per handle");
+    if (m < 1)
+      throw Error(PIBEM_EINVAL, "GMRES restart length must be at least 1");
+    const int L = m + 1;
+    E.S         = S;
+    E.m         = m;
+    E.mixed     = h->prm.precision_mode == PIBEM_PRECISION_MIXED;
+    E.prec      = h->prm.preconditioner != 0;
+    E.col.assign(S, ColHost());
+    E.V.alloc(size_t(S) * L * N);
+    for (DBuf<double> *v : {&E.z, &E.w, &E.b, &E.x, &E.r, &E.d, &E.tmp, &E.cz, &E.cw, &E.u})
+      v->alloc(size_t(S) * N);
+    E.hb.alloc(size_t(S) * (2 * L + 1));
+    E.partial.alloc(size_t(S) * ENG_NBLK * L);
+    E.H.alloc(size_t(S) * L * m);
+    E.cs.alloc(size_t(S) * m);
+    E.sn.alloc(size_t(S) * m);
+    E.g.alloc(size_t(S) * L);
+    E.y.alloc(size_t(S) * L);
+    E.bn.alloc(S);
+    E.tol.alloc(S);
+    E.nrm.alloc(S);
+    E.ticket.alloc(S);
+    E.ticket.zero(h->stream);
+    for (DBuf<int> *v : {&E.kdone, &E.jvec, &E.its, &E.maxit, &E.sel, &E.act})
+      v->alloc(S);
+    std::vector<int> minus(S, -1);
+    E.jvec.upload(minus, h->stream);
+    E.ctl.alloc(3);
+    E.ipin.alloc(size_t(3) * S + 3);
+    E.h_bn.assign(S, 1.0);
+    E.h_tol.assign(S, 0.0);
+    E.h_its.assign(S, 0);
+    E.h_maxit.assign(S, 0);
+    E.h_jvec.assign(S, -1);
   }
 
-  // The restart cycle: steps until every column has stopped, the cycle has m
-  // steps or the iteration limit is reached (all decided on the device).
-  // Returns true when it ran as the cycle graph.
-  bool gmres_cycle(pibem_handle *h, int R, int m, bool prec, int op_tag,
-                   const std::function<void(const double *, double *)> &A)
+  std::vector<int> cols_in(const Engine &E, ColStage st)
   {
-    cudaStream_t s     = h->stream;
-    bool         graph = !h->timing;
+    std::vector<int> c;
+    for (int k = 0; k < E.S; ++k)
+      if (E.col[k].st == st)
+        c.push_back(k);
+    return c;
+  }
+
+  void upload_sel(pibem_handle *h, const std::vector<int> &cols)
+  {
+    Engine          &E = h->eng;
+    std::vector<int> sel(E.S, 0);
+    for (int c : cols)
+      sel[c] = 1;
+    E.sel.upload(sel, h->stream);
+  }
+
+  // squared 2-norms of the S slot columns of v (nblk partial blocks), into out
+  void eng_norms(pibem_handle *h, const double *v, int nblk, std::vector<double> &out)
+  {
+    Engine       &E = h->eng;
+    const int64_t N = h->N();
+    launch_dots(N, E.S, 1, N, N, v, v, E.partial.p, nblk, E.nrm.p, h->stream);
+    out.resize(E.S);
+    read_small(h, out.data(), E.nrm.p, E.S, h->stream);
+  }
+
+  enum EngOp
+  {
+    OP_A32,
+    OP_A64,
+    OP_RHS
+  };
+
+  // the operator (or the right-hand side) on the listed columns: in and out
+  // slot-strided (column k at k N), through the contiguous batch cz -> cw
+  void eng_apply(pibem_handle *h, EngOp op, const std::vector<int> &cols, const double *in,
+                 double *out)
+  {
+    Engine       &E = h->eng;
+    const int64_t N = h->N();
+    cudaStream_t  s = h->stream;
+    const int     R = int(cols.size());
+    if (R == 0)
+      return;
+    E.act.upload(cols, s);
+    launch_gather_cols(N, R, E.act.p, in, N, E.cz.p, s);
+    if (op == OP_A32)
+      system_apply32(h, R, E.cz.p, E.cw.p, true);
+    else if (op == OP_A64)
+      system_apply64(h, R, E.cz.p, E.cw.p, true);
+    else
+      {
+        compute_rhs_dev(h, R, E.cz.p, E.cw.p);
+        constrain_rhs(h, R, E.cz.p, E.cw.p);
+      }
+    launch_scatter_cols(N, R, E.act.p, E.cw.p, out, N, s);
+    for (int c : cols)
+      {
+        if (op == OP_A32)
+          E.col[c].c32++;
+        else
+          E.col[c].c64++;
+      }
+  }
+
+  void eng_copy(pibem_handle *h, double *dst, const double *src, const std::vector<int> &cols)
+  {
+    const int64_t N = h->N();
+    for (int c : cols)
+      PIBEM_CUDA(cudaMemcpyAsync(dst + int64_t(c) * N, src + int64_t(c) * N, sizeof(double) * N,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+  }
+  void eng_zero(pibem_handle *h, double *v, const std::vector<int> &cols)
+  {
+    const int64_t N = h->N();
+    for (int c : cols)
+      PIBEM_CUDA(cudaMemsetAsync(v + int64_t(c) * N, 0, sizeof(double) * N, h->stream));
+  }
+
+  // One Arnoldi step of every column in a cycle (E.act holds them, R' of them):
+  // w = A z (through the contiguous batch), CGS2 into hb, V_{j+1} = w / |w| and
+  // the next z, then the Givens step.
+  void eng_step(pibem_handle *h, int Ra, const std::function<void(const double *, double *, int)> &A,
+                cudaGraphConditionalHandle cond, bool use_cond)
+  {
+    Engine       &E   = h->eng;
+    const int64_t N   = h->N();
+    cudaStream_t  s   = h->stream;
+    const int     L   = E.m + 1;
+    const int64_t ldr = int64_t(L) * N;
+    double *h1 = E.hb.p, *h2 = h1 + size_t(E.S) * L, *nr = h2 + size_t(E.S) * L;
+    launch_gather_cols(N, Ra, E.act.p, E.z.p, N, E.cz.p, s);
+    A(E.cz.p, E.cw.p, Ra);
+    launch_scatter_cols(N, Ra, E.act.p, E.cw.p, E.w.p, N, s);
+    launch_cgs_step(0, N, E.S, 0, N, ldr, E.V.p, nullptr, 0, E.w.p, ENG_NBLK, E.partial.p,
+                    E.ticket.p, h1, s, E.jvec.p, L);
+    launch_cgs_step(1, N, E.S, 0, N, ldr, E.V.p, h1, L, E.w.p, ENG_NBLK, E.partial.p, E.ticket.p, h2,
+                    s, E.jvec.p, L);
+    launch_cgs_step(2, N, E.S, 0, N, ldr, E.V.p, h2, L, E.w.p, ENG_NBLK, E.partial.p, E.ticket.p, nr,
+                    s, E.jvec.p, 1);
+    if (E.prec) // V_{j+1} = w / |w| and the next step's z = P^-1 V_{j+1} in one pass
+      apply_block_jacobi(h, E.S, E.w.p, N, E.z.p, s, nr, E.V.p, ldr, E.jvec.p);
+    else
+      launch_normalize(N, E.S, E.w.p, nr, E.V.p, ldr, s, E.jvec.p, E.z.p);
+    launch_gmres_givens(E.S, E.m, h1, E.H.p, E.cs.p, E.sn.p, E.g.p, E.kdone.p, E.jvec.p, E.its.p,
+                        E.maxit.p, E.bn.p, E.tol.p, E.ctl.p, cond, use_cond, s);
+  }
+
+  // Runs the Arnoldi steps of the columns in a cycle until one of them ends its
+  // cycle or quantum steps have run; returns the steps run.
+  int eng_cycle(pibem_handle *h, const std::vector<int> &act, int quantum)
+  {
+    Engine      &E  = h->eng;
+    cudaStream_t s  = h->stream;
+    const int    Ra = int(act.size());
+    auto A = [h](const double *in, double *out, int R) {
+      if (h->eng.mixed)
+        system_apply32(h, R, in, out, true);
+      else
+        system_apply64(h, R, in, out, true);
+    };
+    E.act.upload(act, s);
+    E.h_ctl = {0, 0, quantum > 0 ? quantum : std::numeric_limits<int>::max()};
+    E.ctl.upload(E.h_ctl, s);
+    bool graph = !h->timing;
     if (graph)
       {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -871,38 +1063,68 @@ namespace
       }
     if (!graph)
       {
-        h->g_ctlpin.alloc(4);
+        int steps = 0;
         while (true)
           {
-            gmres_step(h, R, m, prec, A, 0, false);
-            PIBEM_CUDA(cudaMemcpyAsync(h->g_ctlpin.p, h->g_ctl.p, 4 * sizeof(int),
-                                       cudaMemcpyDeviceToHost, s));
+            eng_step(h, Ra, A, 0, false);
+            ++steps;
+            PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p, E.ctl.p, sizeof(int), cudaMemcpyDeviceToHost, s));
             PIBEM_CUDA(cudaStreamSynchronize(s));
-            if (!h->g_ctlpin.p[3])
+            if (!E.ipin.p[0])
               break;
           }
-        return false;
+        return steps;
       }
+    // the operator reads d_modes: COMBINED for the Ra columns (other calls
+    // may have left other modes there)
+    if (!E.mixed)
+      set_modes(h, Ra, MODE_COMBINED);
     // every buffer a step touches (a reallocation changes an address)
-    const void *bufs[] = {h->g_V.p,    h->g_w.p,     h->g_z.p,      h->g_h.p,      h->g_partial.p,
-                          h->g_ticket.p, h->g_H.p,   h->g_cs.p,     h->g_sn.p,     h->g_g.p,
-                          h->g_kdone.p, h->g_bn.p,   h->g_tol.p,    h->g_ctl.p,    h->d_x32.p,
-                          h->d_y32.p,  h->d_M32.p,   h->d_L32.p,    h->d_Y32.p,    h->d_m2p32.p,
-                          h->d_M64.p,  h->d_L64.p,   h->d_Y64.p,    h->d_m2p64.p,  h->d_t4.p,
-                          h->d_Mff.p,  h->d_Lff.p,   h->d_xff.p,    h->d_ozslc.p};
-    constexpr int nb = int(sizeof(bufs) / sizeof(bufs[0]));
-    static_assert(nb + 3 <= 32, "graph key");
-    uintptr_t key[32] = {};
-    key[0]            = uintptr_t(R) | (uintptr_t(m) << 16) | (uintptr_t(prec) << 40) |
-             (uintptr_t(op_tag) << 48);
+    auto bufs_now = [&](int i) -> const void * {
+      const void *b[] = {E.V.p,    E.z.p,     E.w.p,      E.hb.p,    E.partial.p, E.ticket.p,
+                         E.H.p,    E.cs.p,    E.sn.p,     E.g.p,     E.kdone.p,   E.jvec.p,
+                         E.its.p,  E.maxit.p, E.bn.p,     E.tol.p,   E.ctl.p,     E.act.p,
+                         E.cz.p,   E.cw.p,    h->d_x32.p, h->d_y32.p, h->d_M32.p, h->d_L32.p,
+                         h->d_Y32.p, h->d_m2p32.p, h->d_M64.p, h->d_L64.p, h->d_Y64.p,
+                         h->d_m2p64.p, h->d_t4.p, h->d_Mff.p, h->d_Lff.p, h->d_xff.p,
+                         h->d_ozslc.p, h->d_modes.p, h->d_modes32.p, h->sh_part.p};
+      return b[i];
+    };
+    constexpr int             nb = 38;
+    std::array<uintptr_t, 48> key{};
+    key[0] = uintptr_t(Ra) | (uintptr_t(E.S) << 16) | (uintptr_t(E.m) << 32) |
+             (uintptr_t(E.prec) << 48) | (uintptr_t(E.mixed) << 49);
     key[1] = uintptr_t(s);
     for (int i = 0; i < nb; ++i)
-      key[2 + i] = uintptr_t(bufs[i]);
-    if (!h->gm_exec || !std::equal(key, key + 32, h->gm_key))
+      key[2 + i] = uintptr_t(bufs_now(i));
+    CycleGraph *cg = nullptr;
+    for (auto &c : h->cycle_graphs)
+      if (c.exec && c.key == key)
+        cg = &c;
+    if (!cg)
       {
-        if (h->gm_exec)
-          cudaGraphExecDestroy(h->gm_exec);
-        h->gm_exec = nullptr;
+        // one uncaptured operator application on Ra columns first (its result
+        // is not used): it sizes the operator's work buffers for Ra columns, so
+        // nothing is allocated during the capture
+        {
+          PIBEM_CUDA(cudaMemsetAsync(E.cz.p, 0, sizeof(double) * Ra * h->N(), s));
+          const int64_t l0 = t_launches;
+          const int     c32 = h->cnt32, c64 = h->cnt64;
+          A(E.cz.p, E.cw.p, Ra);
+          const int64_t extra = t_launches - l0;
+          g_launches.fetch_sub(extra, std::memory_order_relaxed);
+          t_launches = l0;
+          h->cnt32   = c32;
+          h->cnt64   = c64;
+        }
+        for (int i = 0; i < nb; ++i)
+          key[2 + i] = uintptr_t(bufs_now(i));
+        // a graph per active-column count; the oldest goes when there are eight
+        if (h->cycle_graphs.size() >= 8)
+          {
+            cudaGraphExecDestroy(h->cycle_graphs.front().exec);
+            h->cycle_graphs.erase(h->cycle_graphs.begin());
+          }
         cudaGraph_t                g = nullptr;
         cudaGraphConditionalHandle cond{};
         PIBEM_CUDA(cudaGraphCreate(&g, 0));
@@ -930,7 +1152,7 @@ namespace
                                                  cudaStreamCaptureModeRelaxed));
         try
           {
-            gmres_step(h, R, m, prec, A, cond, true);
+            eng_step(h, Ra, A, cond, true);
           }
         catch (...)
           {
@@ -939,132 +1161,306 @@ namespace
             throw;
           }
         PIBEM_CUDA(cudaStreamEndCapture(s, &body));
+        CycleGraph c;
+        c.key = key;
         // the captured kernels did not run: they are counted per executed step
-        h->gm_kernels = t_launches - l0;
-        g_launches.fetch_sub(h->gm_kernels, std::memory_order_relaxed);
+        c.kernels = t_launches - l0;
+        g_launches.fetch_sub(c.kernels, std::memory_order_relaxed);
         t_launches = l0;
-        h->gm_c32  = h->cnt32 - c32;
-        h->gm_c64  = h->cnt64 - c64;
+        c.c32      = h->cnt32 - c32;
+        c.c64      = h->cnt64 - c64;
         h->cnt32   = c32;
         h->cnt64   = c64;
         const cudaError_t e =
-          cudaGraphInstantiateWithFlags(&h->gm_exec, g, cudaGraphInstantiateFlagUseNodePriority);
+          cudaGraphInstantiateWithFlags(&c.exec, g, cudaGraphInstantiateFlagUseNodePriority);
         if (e != cudaSuccess)
-          {
-            h->gm_exec = nullptr;
-            throw Error(PIBEM_ECUDA, std::string("GMRES cycle graph instantiation: ") +
-                                       cudaGetErrorString(e));
-          }
-        std::copy(key, key + 32, h->gm_key);
+          throw Error(PIBEM_ECUDA, std::string("GMRES cycle graph instantiation: ") +
+                                     cudaGetErrorString(e));
+        h->cycle_graphs.push_back(c);
+        cg = &h->cycle_graphs.back();
       }
-    PIBEM_CUDA(cudaGraphLaunch(h->gm_exec, s));
-    return true;
+    PIBEM_CUDA(cudaGraphLaunch(cg->exec, s));
+    PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p, E.ctl.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    const int steps = E.ipin.p[1];
+    note_launch(cg->kernels * steps);
+    h->cnt32 += cg->c32 * steps;
+    h->cnt64 += cg->c64 * steps;
+    return steps;
   }
 
-  GmresResult gmres(pibem_handle *h, int R, const double *b, double *x,
-                    const std::vector<double> &tol, int maxit, int m,
-                    const std::function<void(const double *, double *)> &A, bool prec, int op_tag)
+  // Advances every column from event to event until each has finished or waits
+  // in a GMRES cycle, then runs the cycle graph once (until some column ends
+  // its cycle, or for at most quantum steps when quantum > 0).  Returns the
+  // number of columns that finished.
+  int engine_advance(pibem_handle *h, int quantum = 0)
   {
-    const int64_t N    = h->N();
-    cudaStream_t  s    = h->stream;
-    const int     nblk = 2 * 152;
-    const int     L    = m + 1;
-    const int64_t ldr  = int64_t(L) * N;
-    if (m < 1)
-      throw Error(PIBEM_EINVAL, "GMRES restart length must be at least 1");
-    h->g_V.alloc(size_t(R) * L * N);
-    h->g_w.alloc(size_t(R) * N);
-    h->g_z.alloc(size_t(R) * N);
-    h->g_u.alloc(size_t(R) * N);
-    h->g_partial.alloc(size_t(R) * nblk * L);
-    h->g_h.alloc(size_t(R) * (2 * L + 1));
-    h->g_ticket.alloc(R);
-    h->g_ticket.zero(s);
-    h->g_nrm.alloc(R);
-    h->g_bn.alloc(R);
-    h->g_H.alloc(size_t(R) * L * m);
-    h->g_cs.alloc(size_t(R) * m);
-    h->g_sn.alloc(size_t(R) * m);
-    h->g_g.alloc(size_t(R) * L);
-    h->g_y.alloc(size_t(R) * L);
-    h->g_tol.alloc(R);
-    h->g_kdone.alloc(R);
-    h->g_ctl.alloc(4);
-    h->g_ctlpin.alloc(4);
-    h->g_tol.upload(tol, s);
-    GmresResult res;
-    res.rel.assign(R, 1.0);
-    std::vector<double> bn(R);
-    launch_dots(N, R, 1, N, N, b, b, h->g_partial.p, nblk, h->g_bn.p, s);
-    read_small(h, bn.data(), h->g_bn.p, R, s);
-    for (auto &v : bn)
-      v = v > 0 ? std::sqrt(v) : 1.0;
-    h->g_bn.upload(bn, s);
-    std::vector<double> b2(R);
-    int                 pending     = -1; // iterations before the cycle whose count is in g_ctlpin
-    bool                graph_cycle = false;
-    auto settle = [&] {
-      // the last cycle's control words have arrived (the stream was synchronised)
-      if (pending < 0)
-        return;
-      const int done = h->g_ctlpin.p[1] - pending;
-      res.iterations = h->g_ctlpin.p[1];
-      if (graph_cycle)
-        {
-          note_launch(h->gm_kernels * done);
-          h->cnt32 += h->gm_c32 * done;
-          h->cnt64 += h->gm_c64 * done;
-        }
-      pending = -1;
+    Engine             &E    = h->eng;
+    const int64_t       N    = h->N();
+    cudaStream_t        s    = h->stream;
+    const pibem_params &P    = h->prm;
+    const int           L    = E.m + 1;
+    const int64_t       ldr  = int64_t(L) * N;
+    const int           max_refine = 12;
+    int                 finished   = 0;
+    std::vector<double> nv;
+    auto finish = [&](int c) {
+      ColHost &C = E.col[c];
+      C.st       = ST_DONE;
+      C.seconds  = std::chrono::duration<double>(std::chrono::steady_clock::now() - C.t0).count();
+      ++finished;
     };
-    while (true)
+    bool progress = true;
+    while (progress)
       {
-        // true residual r = b - A x into V[:,0]
-        A(x, h->g_w.p);
-        launch_axpby(int64_t(R) * N, 1.0, b, -1.0, h->g_w.p, s);
-        copy_cols(h->g_V.p, ldr, h->g_w.p, N, N, R, s);
-        launch_dots(N, R, 1, N, N, h->g_w.p, h->g_w.p, h->g_partial.p, nblk, h->g_nrm.p, s);
-        read_small(h, b2.data(), h->g_nrm.p, R, s);
-        if (graph_cycle)
-          settle();
-        bool any = false;
-        for (int r = 0; r < R; ++r)
+        progress = false;
+        // right-hand sides of newly admitted columns
+        std::vector<int> cols = cols_in(E, ST_RHS);
+        if (!cols.empty())
           {
-            res.rel[r] = std::sqrt(b2[r]) / bn[r];
-            any        = any || !(res.rel[r] <= tol[r]);
+            progress = true;
+            eng_apply(h, OP_RHS, cols, E.tmp.p, E.b.p);
+            if (E.mixed)
+              {
+                eng_norms(h, E.b.p, ENG_NBLK_REFINE, nv);
+                eng_zero(h, E.x.p, cols);
+                eng_copy(h, E.r.p, E.b.p, cols);
+                for (int c : cols)
+                  {
+                    ColHost &C = E.col[c];
+                    C.bn_outer = nv[c] > 0 ? std::sqrt(nv[c]) : 1.0; // norms of b: sqrt, 0 -> 1
+                    C.r_exact  = true;
+                    C.refine   = 0;
+                    C.iters    = 0;
+                    C.st       = ST_ASSESS;
+                  }
+              }
+            else
+              {
+                eng_norms(h, E.b.p, ENG_NBLK, nv);
+                eng_copy(h, E.x.p, E.b.p, cols); // initial guess = rhs (bem_problem.cc:1295)
+                for (int c : cols)
+                  {
+                    ColHost &C = E.col[c];
+                    C.bn_inner = nv[c] > 0 ? std::sqrt(nv[c]) : 1.0;
+                    C.its_inner   = 0;
+                    C.inner_maxit = P.solver_max_steps;
+                    C.itol        = P.solver_tolerance;
+                    C.st          = ST_RES;
+                  }
+              }
           }
-        if (!any || res.iterations >= maxit)
-          break;
-        // V[r][0] = r_r / beta_r (and z = V_0 without preconditioner)
-        launch_normalize(N, R, h->g_w.p, h->g_nrm.p, h->g_V.p, ldr, s, nullptr,
-                         prec ? nullptr : h->g_z.p);
-        if (prec)
-          apply_block_jacobi(h, R, h->g_V.p, ldr, h->g_z.p, s);
-        launch_gmres_cycle_init(R, m, h->g_nrm.p, h->g_bn.p, h->g_tol.p, h->g_g.p, h->g_kdone.p,
-                                h->g_ctl.p, res.iterations, maxit, s);
-        graph_cycle = gmres_cycle(h, R, m, prec, op_tag, A);
-        // x += P^-1 V y, y from the cycle's triangular systems
-        launch_gmres_lsq(R, m, h->g_H.p, h->g_g.p, h->g_kdone.p, h->g_ctl.p, h->g_y.p, s);
-        PIBEM_CUDA(cudaMemsetAsync(h->g_u.p, 0, sizeof(double) * R * N, s));
-        launch_gemv_sub(N, R, 0, N, ldr, h->g_V.p, h->g_y.p, L, h->g_u.p, -1.0, s, h->g_ctl.p);
-        if (prec)
+        // end of a GMRES cycle: x (plain) or d (mixed) += P^-1 V y
+        cols = cols_in(E, ST_CYCLE_END);
+        if (!cols.empty())
           {
-            apply_block_jacobi(h, R, h->g_u.p, N, h->g_z.p, s);
-            launch_axpby(int64_t(R) * N, 1.0, h->g_z.p, 1.0, x, s);
+            progress = true;
+            upload_sel(h, cols);
+            launch_gmres_lsq(E.S, E.m, E.sel.p, E.H.p, E.g.p, E.kdone.p, E.jvec.p, E.y.p, s);
+            eng_zero(h, E.u.p, cols);
+            launch_gemv_sub(N, E.S, 0, N, ldr, E.V.p, E.y.p, L, E.u.p, -1.0, s, E.jvec.p, E.sel.p);
+            double *tgt = E.mixed ? E.d.p : E.x.p;
+            if (E.prec)
+              {
+                apply_block_jacobi(h, E.S, E.u.p, N, E.z.p, s, nullptr, nullptr, 0, nullptr, E.sel.p);
+                launch_axpby_sel(N, E.S, E.sel.p, 1.0, E.z.p, 1.0, tgt, s);
+              }
+            else
+              launch_axpby_sel(N, E.S, E.sel.p, 1.0, E.u.p, 1.0, tgt, s);
+            for (int c : cols)
+              {
+                E.h_jvec[c] = -1;
+                E.col[c].st = E.mixed ? ST_INNER : ST_RES;
+              }
+            E.jvec.upload(E.h_jvec, s);
           }
-        else
-          launch_axpby(int64_t(R) * N, 1.0, h->g_u.p, 1.0, x, s);
-        // the cycle's iteration count arrives with the next synchronisation
-        PIBEM_CUDA(cudaMemcpyAsync(h->g_ctlpin.p, h->g_ctl.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
-        pending = res.iterations;
-        if (!graph_cycle)
+        // mixed: r = b - A64 x
+        cols = cols_in(E, ST_TRUERES);
+        if (!cols.empty())
           {
-            PIBEM_CUDA(cudaStreamSynchronize(s));
-            res.iterations = h->g_ctlpin.p[1];
-            pending        = -1;
+            progress = true;
+            eng_apply(h, OP_A64, cols, E.x.p, E.w.p);
+            eng_copy(h, E.r.p, E.b.p, cols);
+            upload_sel(h, cols);
+            launch_axpby_sel(N, E.S, E.sel.p, -1.0, E.w.p, 1.0, E.r.p, s);
+            for (int c : cols)
+              {
+                ColHost &C = E.col[c];
+                C.r_exact  = true;
+                if (C.refine_inc)
+                  {
+                    C.refine++;
+                    C.refine_inc = false;
+                  }
+                C.st = ST_ASSESS;
+              }
+          }
+        // mixed: r <- r - A32 d
+        cols = cols_in(E, ST_R32);
+        if (!cols.empty())
+          {
+            progress = true;
+            eng_apply(h, OP_A32, cols, E.d.p, E.w.p);
+            upload_sel(h, cols);
+            launch_axpby_sel(N, E.S, E.sel.p, -1.0, E.w.p, 1.0, E.r.p, s);
+            for (int c : cols)
+              {
+                ColHost &C = E.col[c];
+                C.r_exact  = false;
+                C.refine++;
+                C.st = ST_ASSESS;
+              }
+          }
+        // mixed: the refinement decision on |r|
+        cols = cols_in(E, ST_ASSESS);
+        if (!cols.empty())
+          {
+            progress = true;
+            eng_norms(h, E.r.p, ENG_NBLK_REFINE, nv);
+            std::vector<int> start;
+            for (int c : cols)
+              {
+                ColHost &C = E.col[c];
+                C.rel      = std::sqrt(nv[c]) / C.bn_outer;
+                C.ok       = C.rel <= P.solver_tolerance;
+                C.itol     = C.ok ? std::numeric_limits<double>::infinity()
+                                  : std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / C.rel);
+                if (C.final_pass)
+                  finish(c);
+                else if (C.ok && !C.r_exact)
+                  C.st = ST_TRUERES; // confirm the estimate with the FP64-accurate operator
+                else if (C.ok || C.refine == max_refine || C.iters >= P.solver_max_steps)
+                  {
+                    if (!C.r_exact)
+                      {
+                        C.final_pass = true; // a stop on the step limits: the exact residual
+                        C.st         = ST_TRUERES;
+                      }
+                    else
+                      finish(c);
+                  }
+                else
+                  start.push_back(c);
+              }
+            if (!start.empty())
+              {
+                // a new correction: d = 0, the inner right-hand side is r
+                eng_zero(h, E.d.p, start);
+                eng_norms(h, E.r.p, ENG_NBLK, nv);
+                for (int c : start)
+                  {
+                    ColHost &C    = E.col[c];
+                    C.bn_inner    = nv[c] > 0 ? std::sqrt(nv[c]) : 1.0;
+                    C.its_inner   = 0;
+                    C.inner_maxit = P.solver_max_steps - C.iters;
+                    C.st          = ST_INNER;
+                  }
+              }
+          }
+        // a GMRES restart: w = rhs - A x, and the cycle start or the stop
+        const ColStage rst = E.mixed ? ST_INNER : ST_RES;
+        cols               = cols_in(E, rst);
+        if (!cols.empty())
+          {
+            progress = true;
+            // mixed: A32 on d against r; plain: A64 on x against b
+            eng_apply(h, E.mixed ? OP_A32 : OP_A64, cols, E.mixed ? E.d.p : E.x.p, E.w.p);
+            upload_sel(h, cols);
+            launch_axpby_sel(N, E.S, E.sel.p, 1.0, E.mixed ? E.r.p : E.b.p, -1.0, E.w.p, s);
+            eng_norms(h, E.w.p, ENG_NBLK, nv);
+            std::vector<int> cyc;
+            for (int c : cols)
+              {
+                ColHost     &C   = E.col[c];
+                const double rel = std::sqrt(nv[c]) / C.bn_inner;
+                if (rel <= C.itol || C.its_inner >= C.inner_maxit)
+                  {
+                    if (!E.mixed)
+                      {
+                        C.rel   = rel;
+                        C.iters = C.its_inner;
+                        finish(c);
+                        continue;
+                      }
+                    // the correction is done: x += d, then the new residual
+                    C.iters += C.its_inner;
+                    C.st = ST_XUPD;
+                    continue;
+                  }
+                cyc.push_back(c);
+              }
+            if (!cyc.empty())
+              {
+                upload_sel(h, cyc);
+                // V[c][0] = w / |w| (and z = V_0 without preconditioner)
+                launch_normalize(N, E.S, E.w.p, E.nrm.p, E.V.p, ldr, s, nullptr,
+                                 E.prec ? nullptr : E.z.p, E.sel.p);
+                if (E.prec)
+                  apply_block_jacobi(h, E.S, E.V.p, ldr, E.z.p, s, nullptr, nullptr, 0, nullptr, E.sel.p);
+                launch_gmres_cycle_init(E.S, E.m, E.sel.p, E.nrm.p, E.g.p, E.kdone.p, E.jvec.p, s);
+                for (int c : cyc)
+                  {
+                    ColHost &C   = E.col[c];
+                    E.h_bn[c]    = C.bn_inner;
+                    E.h_tol[c]   = C.itol;
+                    E.h_its[c]   = C.its_inner;
+                    E.h_maxit[c] = C.inner_maxit;
+                    E.h_jvec[c]  = 0;
+                    C.st         = ST_ARNOLDI;
+                  }
+                E.bn.upload(E.h_bn, s);
+                E.tol.upload(E.h_tol, s);
+                E.its.upload(E.h_its, s);
+                E.maxit.upload(E.h_maxit, s);
+              }
+          }
+        // mixed: x += d after a correction
+        cols = cols_in(E, ST_XUPD);
+        if (!cols.empty())
+          {
+            progress = true;
+            upload_sel(h, cols);
+            launch_axpby_sel(N, E.S, E.sel.p, 1.0, E.d.p, 1.0, E.x.p, s);
+            for (int c : cols)
+              {
+                ColHost &C = E.col[c];
+                if (C.refine == 0)
+                  {
+                    C.refine_inc = true;
+                    C.st         = ST_TRUERES;
+                  }
+                else
+                  C.st = ST_R32;
+              }
           }
       }
-    return res;
+    // the Arnoldi steps of the columns in a cycle
+    std::vector<int> act = cols_in(E, ST_ARNOLDI);
+    if (!act.empty())
+      {
+        eng_cycle(h, act, quantum);
+        const int S = E.S;
+        PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p, E.jvec.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
+        PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p + S, E.kdone.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
+        PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p + 2 * S, E.its.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
+        PIBEM_CUDA(cudaStreamSynchronize(s));
+        for (int c : act)
+          {
+            ColHost  &C   = E.col[c];
+            const int j   = E.ipin.p[c], kd = E.ipin.p[S + c], it = E.ipin.p[2 * S + c];
+            const int now = it - C.its_inner; // steps this column took
+            if (E.mixed)
+              C.c32 += now;
+            else
+              C.c64 += now;
+            C.its_inner  = it;
+            E.h_jvec[c]  = j;
+            E.h_its[c]   = it;
+            if (kd >= 0 || j >= E.m || it >= C.inner_maxit)
+              C.st = ST_CYCLE_END;
+          }
+      }
+    return finished;
   }
 
   // The double-node constraint lines of BEMProblem::compute_constraints
@@ -1234,6 +1630,7 @@ namespace
       op.nrow_ptr      = h->d_nrow_ptr.p;
       op.ncol_ptr      = h->d_ncol_ptr.p;
       op.nval_ptr      = h->d_nval_ptr.p;
+      op.near_queue    = h->d_near_queue.p;
       op.n_p2m_leaves  = int(pl.pleaf_box.size());
       op.prow_ptr      = h->d_prow_ptr.p;
       op.pleaf_box     = h->d_pleaf_box.p;
@@ -1807,6 +2204,8 @@ namespace
         }
       h->d_err.alloc(1);
       h->d_err.zero(s);
+      h->d_near_queue.alloc(2);
+      h->d_near_queue.zero(s);
       PIBEM_CUDA(cudaStreamSynchronize(s));
     }
     phase(6);
@@ -2037,141 +2436,71 @@ namespace
                           h->con_proj ? h->d_con_sg.p : nullptr, b, h->stream);
   }
 
+  // The mixed path forms its right-hand sides and FP64 residuals with the
+  // FP64-accurate float-float translations (FP64 near field and expansions):
+  // the handle's FP64 operator view takes them for the scope of this guard.
+  struct FfGuard
+  {
+    OperatorDev<double> &op;
+    const float2        *prev;
+    FfGuard(pibem_handle *h) : op(h->op64), prev(h->op64.ops_ff)
+    {
+      if (h->prm.precision_mode == PIBEM_PRECISION_MIXED)
+        op.ops_ff = h->d_opsff.p;
+    }
+    ~FfGuard() { op.ops_ff = prev; }
+  };
+
   void solve_dev(pibem_handle *h, int R, double *phi, double *dphi, const double *tmp,
                  pibem_solve_stats *st)
   {
     if (!h->bc_ok)
       throw Error(PIBEM_EINVAL, "pibem_solve before pibem_set_bc");
+    if (h->slots_open)
+      throw Error(PIBEM_EINVAL, "pibem_solve while request slots are open (pibem_slots_close first)");
     auto          t0 = std::chrono::steady_clock::now();
     const int64_t N  = h->N();
     cudaStream_t  s  = h->stream;
+    const pibem_params &P = h->prm;
     h->cnt64 = h->cnt32 = 0;
-    // The mixed path forms its right-hand side and FP64 residuals with the
-    // FP64-accurate float-float translations (FP64 near field and expansions).
-    struct FfGuard
-    {
-      OperatorDev<double> &op;
-      const float2        *prev;
-      ~FfGuard() { op.ops_ff = prev; }
-    } ff_guard{h->op64, h->op64.ops_ff};
-    if (h->prm.precision_mode == PIBEM_PRECISION_MIXED)
-      h->op64.ops_ff = h->d_opsff.p;
-    DBuf<double> &b = h->sv_b, &x = h->sv_x, &r = h->sv_r, &d = h->sv_d, &w = h->sv_w;
-    b.alloc(size_t(R) * N);
-    x.alloc(size_t(R) * N);
-    compute_rhs_dev(h, R, tmp, b.p);
-    constrain_rhs(h, R, tmp, b.p);
-    PIBEM_CUDA(cudaMemcpyAsync(x.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
-    const pibem_params &P    = h->prm;
-    const bool          prec = P.preconditioner != 0;
-    auto A64 = [h, R](const double *in, double *out) { system_apply64(h, R, in, out, true); };
-    auto A32 = [h, R](const double *in, double *out) { system_apply32(h, R, in, out, true); };
-    int                 iters = 0, refine = 0;
-    std::vector<double> rel;
-    if (P.precision_mode != PIBEM_PRECISION_MIXED)
+    FfGuard ff(h);
+    engine_open(h, R, P.gmres_restart);
+    Engine &E = h->eng;
+    PIBEM_CUDA(cudaMemcpyAsync(E.tmp.p, tmp, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
+    for (int c = 0; c < R; ++c)
       {
-        GmresResult gr = gmres(h, R, b.p, x.p, std::vector<double>(R, P.solver_tolerance),
-                               P.solver_max_steps, P.gmres_restart, A64, prec, 64);
-        iters          = gr.iterations;
-        rel            = gr.rel;
+        E.col[c].st = ST_RHS;
+        E.col[c].t0 = t0;
       }
-    else
+    for (int64_t rounds = 0;; ++rounds)
       {
-        // Mixed precision: FP64 iterative refinement around GMRES on the FP32
-        // operator, from x0 = 0 (r0 = b exactly).  The first correction carries
-        // the whole solution, so its residual is formed with the FP64 operator;
-        // every later correction d_k is small (|d_k| <= tol_inner^k |x|), so the
-        // residual is updated as r <- r - A32 d_k, whose rounding error
-        // eps32 * |A| |d_k| stays far below the target.  When the updated
-        // residuals of all columns meet the tolerance, b - A64 x is formed once
-        // more and the solve returns only if that exact residual meets it too, so
-        // the reported residual is always an FP64 one.  Each column has its own
-        // inner tolerance and stops refining once it meets the target (its later
-        // corrections are zero), so a column's solution is the same alone or in a
-        // batch.
-        r.alloc(size_t(R) * N);
-        d.alloc(size_t(R) * N);
-        w.alloc(size_t(R) * N);
-        h->sv_part.alloc(size_t(R) * 64);
-        h->sv_nrm.alloc(R);
-        const int max_refine = 12;
-        rel.assign(R, 1.0);
-        std::vector<double> bn(R), rn(R), itol(R);
-        auto norms = [&](const double *v, std::vector<double> &out) {
-          launch_dots(N, R, 1, N, N, v, v, h->sv_part.p, 64, h->sv_nrm.p, s);
-          read_small(h, out.data(), h->sv_nrm.p, R, s);
-          for (auto &v2 : out)
-            v2 = std::sqrt(v2);
-        };
-        norms(b.p, bn);
-        for (auto &v : bn)
-          v = v > 0 ? v : 1.0;
-        PIBEM_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * R * N, s));
-        PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
-        // r_exact: r holds b - A64 x (x0 = 0, or just recomputed) rather than
-        // the A32-updated estimate
-        bool r_exact = true;
-        auto true_residual = [&] {
-          A64(x.p, w.p);
-          PIBEM_CUDA(cudaMemcpyAsync(r.p, b.p, sizeof(double) * R * N, cudaMemcpyDeviceToDevice, s));
-          launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
-          r_exact = true;
-        };
-        bool ok = false;
-        auto assess = [&] {
-          norms(r.p, rn);
-          ok = true;
-          for (int c = 0; c < R; ++c)
-            {
-              rel[c]  = rn[c] / bn[c];
-              itol[c] = rel[c] <= P.solver_tolerance
-                          ? std::numeric_limits<double>::infinity()
-                          : std::max(P.inner_tolerance, 0.5 * P.solver_tolerance / rel[c]);
-              ok = ok && rel[c] <= P.solver_tolerance;
-            }
-        };
-        for (; refine <= max_refine; ++refine)
-          {
-            assess();
-            // the stopping test is an FP64 claim: an estimate that meets the
-            // tolerance is confirmed with the FP64-accurate operator, and
-            // refinement goes on from the exact residual if it does not hold
-            if (ok && !r_exact)
-              {
-                true_residual();
-                assess();
-              }
-            if (ok || refine == max_refine || iters >= P.solver_max_steps)
-              break;
-            PIBEM_CUDA(cudaMemsetAsync(d.p, 0, sizeof(double) * R * N, s));
-            GmresResult gr = gmres(h, R, r.p, d.p, itol, P.solver_max_steps - iters,
-                                   P.gmres_restart, A32, prec, 32);
-            iters += gr.iterations;
-            launch_axpby(int64_t(R) * N, 1.0, d.p, 1.0, x.p, s);
-            if (refine == 0)
-              true_residual(); // r = b - A64 x
-            else
-              {
-                A32(d.p, w.p); // r = r - A32 d
-                launch_axpby(int64_t(R) * N, -1.0, w.p, 1.0, r.p, s);
-                r_exact = false;
-              }
-          }
-        // a solve that stopped on its step limits also reports the exact residual
-        if (!r_exact)
-          {
-            true_residual();
-            assess();
-          }
+        bool all = true;
+        for (int c = 0; c < R; ++c)
+          all = all && E.col[c].st == ST_DONE;
+        if (all)
+          break;
+        // every round finishes a column, moves one on or runs at least one
+        // Arnoldi step, and each column takes at most about 13 (max_steps + 4)
+        // rounds; this bound only guards against an internal error
+        if (rounds > 64 * (int64_t(P.solver_max_steps) + 16) * R)
+          throw Error(PIBEM_ECUDA, "internal error: the solve engine does not advance");
+        engine_advance(h);
       }
-    launch_scatter(N, R, x.p, h->d_dir.p, phi, dphi, s);
+    launch_scatter(N, R, E.x.p, h->d_dir.p, phi, dphi, s);
     PIBEM_CUDA(cudaStreamSynchronize(s));
     check_device_error(h);
-    double worst = rel.empty() ? 0 : *std::max_element(rel.begin(), rel.end());
+    double worst = 0;
+    int    iters = 0, refine = 0;
+    for (int c = 0; c < R; ++c)
+      {
+        worst  = std::max(worst, E.col[c].rel);
+        iters  = std::max(iters, E.col[c].iters);
+        refine = std::max(refine, E.col[c].refine);
+      }
     if (st)
       {
         st->iterations        = iters;
-        st->refinement_steps  = refine;
+        st->refinement_steps  = E.mixed ? refine : 0;
         st->fp64_matvecs      = h->cnt64;
         st->fp32_matvecs      = h->cnt32;
         st->relative_residual = worst;
@@ -2406,6 +2735,126 @@ extern "C"
 
   // L2 projections (BEMProblem::compute_normals / compute_surface_gradients /
   // compute_gradients, source/bem_problem.cc:1747-2070)
+  // ---- request slots: continuous batching of solves on one mesh ----------
+  int pibem_slots_open(pibem_handle *h, int32_t max_slots)
+  {
+    return guarded(h, [&] {
+      if (!h->bc_ok)
+        throw Error(PIBEM_EINVAL, "pibem_slots_open before pibem_set_bc");
+      engine_open(h, max_slots, h->prm.gmres_restart);
+      h->slots_open = true;
+    });
+  }
+
+  int pibem_slots_close(pibem_handle *h)
+  {
+    return guarded(h, [&] {
+      h->slots_open = false;
+      h->eng.col.assign(h->eng.S, ColHost());
+    });
+  }
+
+  int pibem_slots_submit(pibem_handle *h, int64_t request_id, const double *tmp_rhs, int32_t *slot)
+  {
+    return guarded(h, [&] {
+      if (!h->slots_open)
+        throw Error(PIBEM_EINVAL, "pibem_slots_submit before pibem_slots_open");
+      if (!tmp_rhs)
+        throw Error(PIBEM_EINVAL, "null tmp_rhs");
+      Engine &E = h->eng;
+      int     c = 0;
+      while (c < E.S && E.col[c].st != ST_FREE)
+        ++c;
+      if (c == E.S)
+        throw Error(PIBEM_EAGAIN, "no free slot");
+      const int64_t N = h->N();
+      PIBEM_CUDA(cudaMemcpyAsync(E.tmp.p + int64_t(c) * N, tmp_rhs, sizeof(double) * N,
+                                 cudaMemcpyHostToDevice, h->stream));
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+      E.col[c]     = ColHost();
+      E.col[c].st  = ST_RHS;
+      E.col[c].rid = request_id;
+      E.col[c].t0  = std::chrono::steady_clock::now();
+      if (slot)
+        *slot = c;
+    });
+  }
+
+  int pibem_slots_step(pibem_handle *h, int32_t max_steps, int32_t *n_active, int32_t *n_done)
+  {
+    return guarded(h, [&] {
+      if (!h->slots_open)
+        throw Error(PIBEM_EINVAL, "pibem_slots_step before pibem_slots_open");
+      FfGuard ff(h);
+      Engine &E   = h->eng;
+      bool    any = false;
+      for (const auto &c : E.col)
+        any = any || (c.st != ST_FREE && c.st != ST_DONE);
+      if (any)
+        engine_advance(h, max_steps);
+      check_device_error(h);
+      int act = 0, done = 0;
+      for (const auto &c : E.col)
+        {
+          act += c.st != ST_FREE && c.st != ST_DONE;
+          done += c.st == ST_DONE;
+        }
+      if (n_active)
+        *n_active = act;
+      if (n_done)
+        *n_done = done;
+    });
+  }
+
+  int pibem_slots_collect(pibem_handle *h, int64_t *request_id, double *phi, double *dphi_dn,
+                          pibem_solve_stats *stats)
+  {
+    return guarded(h, [&] {
+      if (!h->slots_open)
+        throw Error(PIBEM_EINVAL, "pibem_slots_collect before pibem_slots_open");
+      Engine &E = h->eng;
+      int     c = -1;
+      for (int k = 0; k < E.S; ++k)
+        if (E.col[k].st == ST_DONE && (c < 0 || E.col[k].rid < E.col[c].rid))
+          c = k;
+      if (c < 0)
+        throw Error(PIBEM_EAGAIN, "no finished request");
+      const int64_t N = h->N();
+      cudaStream_t  s = h->stream;
+      HostIO        io{h};
+      double       *dp = io.scratch(size_t(N)), *dd = io.scratch(size_t(N));
+      // known entries from tmp_rhs, unknown ones from the solution
+      PIBEM_CUDA(cudaMemcpyAsync(dp, E.tmp.p + int64_t(c) * N, sizeof(double) * N,
+                                 cudaMemcpyDeviceToDevice, s));
+      PIBEM_CUDA(cudaMemcpyAsync(dd, E.tmp.p + int64_t(c) * N, sizeof(double) * N,
+                                 cudaMemcpyDeviceToDevice, s));
+      launch_scatter(N, 1, E.x.p + int64_t(c) * N, h->d_dir.p, dp, dd, s);
+      if (phi)
+        PIBEM_CUDA(cudaMemcpyAsync(phi, dp, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+      if (dphi_dn)
+        PIBEM_CUDA(cudaMemcpyAsync(dphi_dn, dd, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+      PIBEM_CUDA(cudaStreamSynchronize(s));
+      const ColHost &C = E.col[c];
+      if (request_id)
+        *request_id = C.rid;
+      if (stats)
+        {
+          stats->iterations        = C.iters;
+          stats->refinement_steps  = E.mixed ? C.refine : 0;
+          stats->fp64_matvecs      = C.c64;
+          stats->fp32_matvecs      = C.c32;
+          stats->relative_residual = C.rel;
+          stats->seconds           = C.seconds;
+        }
+      const bool conv = C.rel <= h->prm.solver_tolerance;
+      const double rel = C.rel;
+      E.col[c] = ColHost();
+      if (!conv)
+        throw Error(PIBEM_ENOCONV, "request did not reach the tolerance (relative residual " +
+                                     std::to_string(rel) + ")");
+    });
+  }
+
   static int projection(pibem_handle *h, int mode, int32_t R, const double *u, const double *dudn,
                         double *out)
   {

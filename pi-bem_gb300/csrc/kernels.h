@@ -68,7 +68,7 @@ namespace pibem
 
   // resident blocks per SM of the one-column near SpMVs (their launch bounds)
   constexpr int NEAR_BLOCKS_PER_SM_F32  = 6;
-  constexpr int NEAR_BLOCKS_PER_SM_WIDE = 4;
+  constexpr int NEAR_BLOCKS_PER_SM_WIDE = 5;
 
   template <typename T>
   struct OperatorDev
@@ -79,6 +79,9 @@ namespace pibem
     int64_t        n_rows = 0;
     const int32_t *row_leaf = nullptr, *nrows = nullptr, *ncols = nullptr;
     const int64_t *nrow_ptr = nullptr, *ncol_ptr = nullptr, *nval_ptr = nullptr;
+    // leaf schedule of the one-column near SpMVs (2 ints, zero between launches;
+    // one launch at a time per operator)
+    int           *near_queue = nullptr;
     // p2m
     int            n_p2m_leaves = 0;
     const int64_t *prow_ptr = nullptr;

@@ -62,18 +62,21 @@ namespace pibem
     }
 
     // w[r][t] -= sum_i V[r][i][t] h[r][i]   (h on the device, layout [r][ldh])
-    //   (jctl non-null: ncols = jctl[0])
+    //   (jvec non-null: column r takes ncols = jvec[r]; sel non-null: selected
+    //   columns only)
     __global__ void gemv_sub_kernel(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
                                     const double *__restrict__ V, const double *__restrict__ h,
                                     int ldh, double *__restrict__ w, double sign,
-                                    const int *__restrict__ jctl)
+                                    const int *__restrict__ jvec, const int *__restrict__ sel)
     {
       int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * R)
         return;
-      if (jctl)
-        ncols = jctl[0];
       int64_t r = idx / n, t = idx % n;
+      if (sel && !sel[r])
+        return;
+      if (jvec)
+        ncols = jvec[r];
       double  s = 0;
 #pragma unroll 8
       for (int i = 0; i < ncols; ++i)
@@ -93,18 +96,23 @@ namespace pibem
     // finish (a ticket taken after a fence) adds the nblk partials of each
     // output in the fixed order of dots_final and resets the ticket, so the
     // result does not depend on which block is last.
-    //   jctl (may be null): the Arnoldi step j is read from jctl[0] and the
-    //   pass takes ncols = j + 1 basis vectors (device-driven GMRES); out holds
-    //   ldo values per column r.
+    //   jvec (may be null): per-column Arnoldi step j = jvec[r] read on the
+    //   device (the pass takes ncols = j + 1 basis vectors; j < 0: the column
+    //   is idle and its blocks return); out holds ldo values per column r.
     template <int MODE>
     __global__ void __launch_bounds__(256)
       cgs_step_kernel(int64_t n, int ncols, int64_t ldv, int64_t ldr, const double *__restrict__ V,
                       const double *__restrict__ hin, int ldh, double *__restrict__ w, int nblk,
                       double *__restrict__ partial, int *__restrict__ ticket,
-                      double *__restrict__ out, const int *__restrict__ jctl, int ldo)
+                      double *__restrict__ out, const int *__restrict__ jvec, int ldo)
     {
-      if (jctl)
-        ncols = jctl[0] + 1;
+      if (jvec)
+        {
+          const int j = jvec[blockIdx.y];
+          if (j < 0)
+            return;
+          ncols = j + 1;
+        }
       const int     r     = blockIdx.y;
       const int     blk   = blockIdx.x;
       const double *Vr    = V + int64_t(r) * ldr;
@@ -161,76 +169,87 @@ namespace pibem
         ticket[r] = 0;
     }
 
-    // V[r][j+1] = w[r] / hn[r]  (hn > 0), else 0; with jctl the output column
-    // is out + (jctl[0] + 1) * n; with z the value is also written to z[r]
+    // V[r][j+1] = w[r] / hn[r]  (hn > 0), else 0; with jvec the output column
+    // is basis vector jvec[r] + 1 of out (jvec[r] < 0: column skipped); with sel
+    // only the columns with sel[r] != 0; with z the value is also written to z[r]
     __global__ void normalize_kernel(int64_t n, int R, const double *__restrict__ w,
                                      const double *__restrict__ nrm, double *__restrict__ out,
-                                     int64_t ldr, const int *__restrict__ jctl,
-                                     double *__restrict__ z)
+                                     int64_t ldr, const int *__restrict__ jvec,
+                                     double *__restrict__ z, const int *__restrict__ sel)
     {
       int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * R)
         return;
       int64_t r = idx / n, t = idx % n;
-      double  h = sqrt(nrm[r]);
+      if (sel && !sel[r])
+        return;
+      int64_t off = 0;
+      if (jvec)
+        {
+          if (jvec[r] < 0)
+            return;
+          off = int64_t(jvec[r] + 1) * n;
+        }
+      double       h = sqrt(nrm[r]);
       const double v = h > 0 ? w[idx] / h : 0.0;
-      out[r * ldr + (jctl ? int64_t(jctl[0] + 1) * n : 0) + t] = v;
+      out[r * ldr + off + t] = v;
       if (z)
         z[idx] = v;
     }
 
-    // ---- device-driven restart cycle of GMRES -------------------------------
-    // State per column r: Hessenberg H[r] ((m+1) x m, entry (i, j) at i m + j),
-    // Givens cosines / sines cs[r], sn[r] (m), g[r] (m+1), kdone[r] (-1: active;
-    // k >= 0: the column stopped after k steps of this cycle).  ctl: [0] step j
-    // of the cycle, [1] iterations so far, [2] iteration limit, [3] 1 while the
-    // cycle goes on.  hb: [h1 (R x L) | h2 (R x L) | |w|^2 (R)], L = m + 1, the
-    // two Gram-Schmidt passes' coefficients and the norm of step j.
+    // ---- device-driven GMRES cycles, one state per column (slot) -------------
+    // Per column r: Hessenberg H[r] ((m+1) x m, entry (i, j) at i m + j), Givens
+    // cosines / sines cs[r], sn[r] (m), g[r] (m+1), jvec[r] (the column's next
+    // Arnoldi step; -1: the column takes no part), kdone[r] (-1, or the step
+    // count after which the column met its tolerance), its[r] / maxit[r]
+    // (iterations so far / limit), bn[r], tol[r] (stopping test |g_{j+1}| /
+    // bn <= tol).  hb: [h1 (R x L) | h2 (R x L) | |w|^2 (R)], L = m + 1, the two
+    // Gram-Schmidt passes' coefficients and the norm of a step.  ctl[0]: 1 while
+    // the steps go on; ctl[1]: steps run; ctl[2]: most steps before the host
+    // is back (a quantum: the steps stop when a column ends its cycle or after
+    // that many).
 
-    // cycle start: g[r] = (beta_r, 0, ...), kdone[r] = 0 where beta_r / bn_r
-    // already meets tol_r, else -1; ctl[0] = 0, ctl[1] = its, ctl[3] = 1
-    __global__ void gmres_cycle_init_kernel(int R, int L, const double *__restrict__ nrm2,
-                                            const double *__restrict__ bn,
-                                            const double *__restrict__ tol, double *__restrict__ g,
-                                            int *__restrict__ kdone, int *__restrict__ ctl, int its,
-                                            int maxit)
+    // cycle start of the selected columns: g[r] = (beta_r, 0, ...) with beta_r =
+    // sqrt(nrm2[r]), jvec[r] = 0, kdone[r] = -1
+    __global__ void gmres_cycle_init_kernel(int R, int L, const int *__restrict__ sel,
+                                            const double *__restrict__ nrm2, double *__restrict__ g,
+                                            int *__restrict__ kdone, int *__restrict__ jvec)
     {
       for (int r = threadIdx.x; r < R; r += blockDim.x)
-        {
-          const double beta = sqrt(nrm2[r]);
-          g[int64_t(r) * L] = beta;
-          kdone[r]          = beta / bn[r] <= tol[r] ? 0 : -1;
-        }
-      if (threadIdx.x == 0)
-        {
-          ctl[0] = 0;
-          ctl[1] = its;
-          ctl[2] = maxit;
-          ctl[3] = 1;
-        }
+        if (sel[r])
+          {
+            g[int64_t(r) * L] = sqrt(nrm2[r]);
+            kdone[r]          = -1;
+            jvec[r]           = 0;
+          }
     }
 
-    // Step j's Hessenberg column, its Givens rotation and the stopping test
-    // (|g_{j+1}| / |b| <= tol or a zero subdiagonal), one thread per column;
-    // then j and the iteration count advance and ctl[3] (and, in a graph, the
-    // loop's condition) says whether the cycle goes on.
+    // Step j = jvec[r] of every active column: the Hessenberg column, its Givens
+    // rotation and the stopping test (|g_{j+1}| / bn <= tol, or a zero
+    // subdiagonal); then jvec and the iteration count advance.  A column ends its
+    // cycle when it meets its tolerance, after m steps or at its iteration
+    // limit; then, or after ctl[2] steps, ctl[0] = 0 and, in a graph, the
+    // loop's condition is cleared.
     __global__ void gmres_givens_kernel(int R, int m, const double *__restrict__ hb,
                                         double *__restrict__ H, double *__restrict__ cs,
                                         double *__restrict__ sn, double *__restrict__ g,
-                                        int *__restrict__ kdone, const double *__restrict__ bn,
+                                        int *__restrict__ kdone, int *__restrict__ jvec,
+                                        int *__restrict__ its, const int *__restrict__ maxit,
+                                        const double *__restrict__ bn,
                                         const double *__restrict__ tol, int *__restrict__ ctl,
                                         cudaGraphConditionalHandle cond, int use_cond)
     {
       const int L = m + 1;
-      const int j = ctl[0];
-      __shared__ int all_done;
+      __shared__ int ended, active;
       if (threadIdx.x == 0)
-        all_done = 1;
+        ended = active = 0;
       __syncthreads();
       for (int r = threadIdx.x; r < R; r += blockDim.x)
         {
-          if (kdone[r] >= 0)
+          const int j = jvec[r];
+          if (j < 0)
             continue;
+          active = 1;
           double       *Hc = H + int64_t(r) * L * m;
           const double *h1 = hb + int64_t(r) * L, *h2 = hb + int64_t(R) * L + int64_t(r) * L;
           for (int i = 0; i <= j; ++i)
@@ -251,35 +270,42 @@ namespace pibem
           Hc[int64_t(j + 1) * m + j] = 0;
           gg[j + 1]                  = -sv[j] * gg[j];
           gg[j]                      = c[j] * gg[j];
+          const int it               = its[r] + 1;
+          its[r]                     = it;
+          jvec[r]                    = j + 1;
           if (fabs(gg[j + 1]) / bn[r] <= tol[r] || bb == 0.0)
             kdone[r] = j + 1;
-          else
-            all_done = 0;
+          if (kdone[r] >= 0 || j + 1 >= m || it >= maxit[r])
+            ended = 1;
         }
       __syncthreads();
       if (threadIdx.x == 0)
         {
-          const int its    = ctl[1] + 1;
-          const int active = !all_done && j + 1 < m && its < ctl[2];
-          ctl[0]           = j + 1;
-          ctl[1]           = its;
-          ctl[3]           = active;
-          if (use_cond && !active)
+          const int steps = ctl[1] + 1; // steps run since the host set ctl
+          // (with no active column the steps stop at once; an active one ends
+          // its cycle within m steps)
+          const int stop = ended || !active || steps >= ctl[2];
+          ctl[0]          = !stop;
+          ctl[1]          = steps;
+          if (use_cond && stop)
             cudaGraphSetConditional(cond, 0);
         }
     }
 
-    // End of a cycle: y[r] solves the column's triangular system of its k steps
-    // (k = kdone[r] if it stopped, else the cycle's step count ctl[0]); y[r][i]
-    // = 0 for i >= k.
-    __global__ void gmres_lsq_kernel(int R, int m, const double *__restrict__ H,
-                                     const double *__restrict__ g, const int *__restrict__ kdone,
-                                     const int *__restrict__ ctl, double *__restrict__ y)
+    // End of a column's cycle: y[r] solves its triangular system of k steps (k =
+    // kdone[r] if it met its tolerance, else jvec[r]); y[r][i] = 0 for i >= k.
+    // Selected columns only.
+    __global__ void gmres_lsq_kernel(int R, int m, const int *__restrict__ sel,
+                                     const double *__restrict__ H, const double *__restrict__ g,
+                                     const int *__restrict__ kdone, const int *__restrict__ jvec,
+                                     double *__restrict__ y)
     {
       const int L = m + 1;
       for (int r = threadIdx.x; r < R; r += blockDim.x)
         {
-          const int     k  = kdone[r] < 0 ? ctl[0] : kdone[r];
+          if (!sel[r])
+            continue;
+          const int     k  = kdone[r] < 0 ? jvec[r] : kdone[r];
           const double *Hc = H + int64_t(r) * L * m;
           const double *gg = g + int64_t(r) * L;
           double       *yr = y + int64_t(r) * L;
@@ -293,6 +319,39 @@ namespace pibem
               yr[i] = sum / Hc[int64_t(i) * m + i];
             }
         }
+    }
+
+    // dst[k] = src[cols[k]] (n values a column; source column stride lds)
+    __global__ void gather_cols_kernel(int64_t n, int Rc, const int *__restrict__ cols,
+                                       const double *__restrict__ src, int64_t lds,
+                                       double *__restrict__ dst)
+    {
+      const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * Rc)
+        return;
+      const int64_t k = idx / n, t = idx - k * n;
+      dst[idx]        = src[int64_t(cols[k]) * lds + t];
+    }
+    // dst[cols[k]] = src[k]
+    __global__ void scatter_cols_kernel(int64_t n, int Rc, const int *__restrict__ cols,
+                                        const double *__restrict__ src, double *__restrict__ dst,
+                                        int64_t ldd)
+    {
+      const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * Rc)
+        return;
+      const int64_t k = idx / n, t = idx - k * n;
+      dst[int64_t(cols[k]) * ldd + t] = src[idx];
+    }
+
+    // y[r] = a x[r] + b y[r] for the selected columns
+    __global__ void axpby_sel_kernel(int64_t n, int R, const int *__restrict__ sel, double a,
+                                     const double *__restrict__ x, double b, double *__restrict__ y)
+    {
+      const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R || !sel[idx / n])
+        return;
+      y[idx] = a * x[idx] + b * y[idx];
     }
 
     __global__ void axpby_kernel(int64_t n, double a, const double *__restrict__ x, double b,
@@ -441,11 +500,9 @@ namespace pibem
                          const int32_t *__restrict__ rows, const P *__restrict__ Pinv,
                          const double *__restrict__ v, double *__restrict__ z,
                          const double *__restrict__ nrm2, double *__restrict__ vout, int64_t ldo,
-                         const int *__restrict__ jctl)
+                         const int *__restrict__ jvec, const int *__restrict__ sel)
     {
       extern __shared__ __align__(8) unsigned char sv_raw[];
-      if (jctl)
-        vout += int64_t(jctl[0] + 1) * n; // basis vector j + 1 of each column
       P        *sv_all = reinterpret_cast<P *>(sv_raw);
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       const int leaf = blockIdx.x * 8 + warp;
@@ -457,6 +514,15 @@ namespace pibem
       const P      *B  = Pinv + blk_ptr[leaf];
       for (int rr = 0; rr < R; ++rr)
         {
+          if (sel && !sel[rr])
+            continue;
+          int64_t vo = int64_t(rr) * ldo; // output column (basis vector jvec[rr] + 1 with jvec)
+          if (jvec)
+            {
+              if (jvec[rr] < 0)
+                continue;
+              vo += int64_t(jvec[rr] + 1) * n;
+            }
           if (nrm2)
             {
               // the Arnoldi normalisation fused in (as normalize_kernel):
@@ -466,8 +532,8 @@ namespace pibem
                 {
                   const int64_t row = rows[r0 + c];
                   const double  vn  = h > 0 ? v[int64_t(rr) * ldv + row] / h : 0.0;
-                  vout[int64_t(rr) * ldo + row] = vn;
-                  sv[c]                         = P(vn);
+                  vout[vo + row] = vn;
+                  sv[c]          = P(vn);
                 }
             }
           else
@@ -575,7 +641,7 @@ namespace pibem
 
   void launch_cgs_step(int mode, int64_t n, int R, int ncols, int64_t ldv, int64_t ldr,
                        const double *V, const double *hin, int ldh, double *w, int nblk,
-                       double *partial, int *ticket, double *out, cudaStream_t s, const int *jctl,
+                       double *partial, int *ticket, double *out, cudaStream_t s, const int *jvec,
                        int ldo)
   {
     dim3 grid(nblk, R);
@@ -583,56 +649,86 @@ namespace pibem
       ldo = mode == 2 ? 1 : ncols;
     if (mode == 0)
       cgs_step_kernel<0><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
-                                                     ticket, out, jctl, ldo);
+                                                     ticket, out, jvec, ldo);
     else if (mode == 1)
       cgs_step_kernel<1><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
-                                                     ticket, out, jctl, ldo);
+                                                     ticket, out, jvec, ldo);
     else
       cgs_step_kernel<2><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
-                                                     ticket, out, jctl, ldo);
+                                                     ticket, out, jvec, ldo);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
   void launch_gemv_sub(int64_t n, int R, int ncols, int64_t ldv, int64_t ldr, const double *V,
                        const double *h, int ldh, double *w, double sign, cudaStream_t s,
-                       const int *jctl)
+                       const int *jvec, const int *sel)
   {
-    gemv_sub_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, ncols, ldv, ldr, V, h, ldh, w, sign, jctl);
+    gemv_sub_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, ncols, ldv, ldr, V, h, ldh, w, sign, jvec,
+                                                   sel);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
   void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
-                        int64_t ldr, cudaStream_t s, const int *jctl, double *z)
+                        int64_t ldr, cudaStream_t s, const int *jvec, double *z, const int *sel)
   {
-    normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr, jctl, z);
+    normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr, jvec, z, sel);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
-  void launch_gmres_cycle_init(int R, int m, const double *nrm2, const double *bn, const double *tol,
-                               double *g, int *kdone, int *ctl, int its, int maxit, cudaStream_t s)
+  void launch_gmres_cycle_init(int R, int m, const int *sel, const double *nrm2, double *g, int *kdone,
+                               int *jvec, cudaStream_t s)
   {
-    gmres_cycle_init_kernel<<<1, 256, 0, s>>>(R, m + 1, nrm2, bn, tol, g, kdone, ctl, its, maxit);
+    gmres_cycle_init_kernel<<<1, 256, 0, s>>>(R, m + 1, sel, nrm2, g, kdone, jvec);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
   void launch_gmres_givens(int R, int m, const double *hb, double *H, double *cs, double *sn,
-                           double *g, int *kdone, const double *bn, const double *tol, int *ctl,
+                           double *g, int *kdone, int *jvec, int *its, const int *maxit,
+                           const double *bn, const double *tol, int *ctl,
                            cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s)
   {
-    gmres_givens_kernel<<<1, 256, 0, s>>>(R, m, hb, H, cs, sn, g, kdone, bn, tol, ctl, cond,
-                                          use_cond ? 1 : 0);
+    gmres_givens_kernel<<<1, 256, 0, s>>>(R, m, hb, H, cs, sn, g, kdone, jvec, its, maxit, bn, tol,
+                                          ctl, cond, use_cond ? 1 : 0);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
 
-  void launch_gmres_lsq(int R, int m, const double *H, const double *g, const int *kdone,
-                        const int *ctl, double *y, cudaStream_t s)
+  void launch_gmres_lsq(int R, int m, const int *sel, const double *H, const double *g,
+                        const int *kdone, const int *jvec, double *y, cudaStream_t s)
   {
-    gmres_lsq_kernel<<<1, 256, 0, s>>>(R, m, H, g, kdone, ctl, y);
+    gmres_lsq_kernel<<<1, 256, 0, s>>>(R, m, sel, H, g, kdone, jvec, y);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_gather_cols(int64_t n, int Rc, const int *cols, const double *src, int64_t lds,
+                          double *dst, cudaStream_t s)
+  {
+    if (Rc == 0)
+      return;
+    gather_cols_kernel<<<nblocks(n * Rc), 256, 0, s>>>(n, Rc, cols, src, lds, dst);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_scatter_cols(int64_t n, int Rc, const int *cols, const double *src, double *dst,
+                           int64_t ldd, cudaStream_t s)
+  {
+    if (Rc == 0)
+      return;
+    scatter_cols_kernel<<<nblocks(n * Rc), 256, 0, s>>>(n, Rc, cols, src, dst, ldd);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_axpby_sel(int64_t n, int R, const int *sel, double a, const double *x, double b,
+                        double *y, cudaStream_t s)
+  {
+    axpby_sel_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, sel, a, x, b, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -743,7 +839,8 @@ namespace pibem
   void launch_block_apply(int n_leaves, int max_rows, int R, int64_t n, const int64_t *row_ptr,
                           const int64_t *blk_ptr, const int32_t *rows, const P *Pinv,
                           const double *v, int64_t ldv, double *z, cudaStream_t s,
-                          const double *nrm2, double *vout, int64_t ldo, const int *jctl)
+                          const double *nrm2, double *vout, int64_t ldo, const int *jvec,
+                          const int *sel)
   {
     if (n_leaves == 0)
       return;
@@ -753,18 +850,18 @@ namespace pibem
       raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel<P>), smem);
     block_apply_kernel<P><<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
                                                                 blk_ptr, rows, Pinv, v, z, nrm2,
-                                                                vout, ldo, jctl);
+                                                                vout, ldo, jvec, sel);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
   template void launch_block_apply<float>(int, int, int, int64_t, const int64_t *, const int64_t *,
                                           const int32_t *, const float *, const double *, int64_t,
                                           double *, cudaStream_t, const double *, double *, int64_t,
-                                          const int *);
+                                          const int *, const int *);
   template void launch_block_apply<double>(int, int, int, int64_t, const int64_t *, const int64_t *,
                                            const int32_t *, const double *, const double *, int64_t,
                                            double *, cudaStream_t, const double *, double *, int64_t,
-                                           const int *);
+                                           const int *, const int *);
 
   template <typename T>
   void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,

@@ -251,25 +251,39 @@ namespace pibem
     // dipole layer (Ker1, MultipoleExpansion::AddNormDer multipole_expansion.cc:125-181)
     // and of the single layer (Ker2, MultipoleExpansion::Add multipole_expansion.cc:94-122)
     // of the dof's shape function over the leaf's quadrature points, strengths
-    // N_j JxW / (4 pi) (bem_fma.cc:1722-1734).  One thread per (row, k).
-    __global__ void p2m_table_kernel(int64_t n_rows, int K, int p, int n_leaves,
-                                     const int64_t *__restrict__ row_ptr,
-                                     const int32_t *__restrict__ leaf_box,
-                                     const int64_t *__restrict__ contrib_ptr,
-                                     const int32_t *__restrict__ contrib_q,
-                                     const double *__restrict__ box_center,
-                                     const double *__restrict__ box_delta,
-                                     const double *__restrict__ qpts,
-                                     const double *__restrict__ qnrm,
-                                     const double *__restrict__ qjxw,
-                                     const double *__restrict__ qshape, double *T1, double *T2)
+    // N_j JxW / (4 pi) (bem_fma.cc:1722-1734).  One block per row: the row's
+    // contributions are taken P2M_CHUNK at a time; per contribution its geometry
+    // (scaled offset, angles, normal derivatives of rho, alpha, beta), rho^n,
+    // cos / sin (m beta) and the Legendre values P~_n^m and dP~_n^m/dtheta are
+    // computed once into shared memory, then thread k adds the contributions'
+    // terms of coefficient k in contribution order.
+    constexpr int P2M_CHUNK = 32;
+    // doubles per contribution in shared memory for order p
+    __host__ __device__ inline int p2m_geo_stride(int p)
     {
-      int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (t >= n_rows * K)
+      const int npm = (p + 1) * (p + 2) / 2;
+      return 8 + 3 * (p + 1) + 2 * npm;
+    }
+    __global__ void __launch_bounds__(128)
+      p2m_table_kernel(int64_t n_rows, int K, int p, int n_leaves,
+                       const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ leaf_box,
+                       const int64_t *__restrict__ contrib_ptr,
+                       const int32_t *__restrict__ contrib_q,
+                       const double *__restrict__ box_center,
+                       const double *__restrict__ box_delta, const double *__restrict__ qpts,
+                       const double *__restrict__ qnrm, const double *__restrict__ qjxw,
+                       const double *__restrict__ qshape, double *T1, double *T2)
+    {
+      extern __shared__ double geo[]; // [P2M_CHUNK][stride]
+      const int64_t row = blockIdx.x;
+      if (row >= n_rows)
         return;
-      const int64_t row = t / K;
-      const int     k   = int(t % K);
-      int           lo = 0, hi = n_leaves - 1;
+      const int stride = p2m_geo_stride(p);
+      const int npm    = (p + 1) * (p + 2) / 2;
+      // layout of one contribution: 0 w, 1 ws, 2 rho, 3 dRhodN, 4 dBetadN,
+      // 5 dAlphadN, 6 ca, 7 sa, then rn[p+1], cos(m beta)[p+1], sin(m beta)[p+1],
+      // P[npm], dS[npm] (pair (n, m) at n (n+1) / 2 + m)
+      int lo = 0, hi = n_leaves - 1;
       while (lo < hi)
         {
           int mid = (lo + hi + 1) >> 1;
@@ -282,68 +296,117 @@ namespace pibem
       const double h   = box_delta[box];
       const double cx = box_center[3 * box], cy = box_center[3 * box + 1],
                    cz = box_center[3 * box + 2];
-      int n, m, part;
-      real_index(k, n, m, part);
-      double a1 = 0, a2 = 0;
-      for (int64_t ci = contrib_ptr[row]; ci < contrib_ptr[row + 1]; ++ci)
+      const int k = threadIdx.x;
+      int       n = 0, m = 0, part = 0;
+      if (k < K)
+        real_index(k, n, m, part);
+      double        a1 = 0, a2 = 0;
+      const int64_t c0 = contrib_ptr[row], c1 = contrib_ptr[row + 1];
+      for (int64_t cb0 = c0; cb0 < c1; cb0 += P2M_CHUNK)
         {
-          const int32_t qj = contrib_q[ci];
-          const int64_t q  = qj >> 2;
-          const int     j  = qj & 3;
-          const double  w  = qshape[4 * q + j] * qjxw[q] / 4 / kPi;
-          const double  rx = (qpts[3 * q] - cx) / h, ry = (qpts[3 * q + 1] - cy) / h,
-                       rz = (qpts[3 * q + 2] - cz) / h;
-          const double rho  = sqrt(rx * rx + ry * ry + rz * rz);
-          const double ca   = rz / rho;
-          const double sa   = sqrt(fmax(0.0, 1.0 - ca * ca));
-          const double beta = atan2(ry, rx);
-          double       sb, cb;
-          sincos(m * beta, &sb, &cb);
-          const double P  = legendre_nm<double>(n, m, ca, sa);
-          double       rn = 1.0;
-          for (int i = 0; i < n; ++i)
-            rn *= rho;
-          // monopole: w P rho^n e^{-i m beta}
-          const double mono = w * P * rn;
-          a2 += part == 0 ? mono * cb : -mono * sb;
-          // dipole (scaled coordinates, strength w / h)
-          double nn_ = sqrt(qnrm[3 * q] * qnrm[3 * q] + qnrm[3 * q + 1] * qnrm[3 * q + 1] +
-                            qnrm[3 * q + 2] * qnrm[3 * q + 2]);
-          double nx = qnrm[3 * q] / nn_, ny = qnrm[3 * q + 1] / nn_, nz = qnrm[3 * q + 2] / nn_;
-          double dRhodN   = (rx / rho) * nx + (ry / rho) * ny + (rz / rho) * nz;
-          double rxy2     = rx * rx + ry * ry;
-          double dBetadN  = (-ry / rxy2) * nx + (rx / rxy2) * ny;
-          double dAlphadN = (ca * cos(beta) / rho) * nx + (ca * sin(beta) / rho) * ny +
-                            (-sa / rho) * nz;
-          double dS       = legendre_dsin<double>(n, m, ca, sa);
-          double rnm1     = n > 0 ? rn / rho : 0.0;
-          double A        = double(n) * rnm1 * P * dRhodN - rn * dS * dAlphadN;
-          double B        = -double(m) * rn * P * dBetadN;
-          double ws       = w / h;
-          // e^{-i m beta} (A + i B)
-          a1 += ws * (part == 0 ? (cb * A + sb * B) : (cb * B - sb * A));
+          const int nc = int(c1 - cb0 < P2M_CHUNK ? c1 - cb0 : int64_t(P2M_CHUNK));
+          __syncthreads(); // the previous chunk's values are used up
+          if (threadIdx.x < nc)
+            {
+              double       *gq = geo + threadIdx.x * stride;
+              const int32_t qj = contrib_q[cb0 + threadIdx.x];
+              const int64_t q  = qj >> 2;
+              const int     j  = qj & 3;
+              const double  w  = qshape[4 * q + j] * qjxw[q] / 4 / kPi;
+              const double  rx = (qpts[3 * q] - cx) / h, ry = (qpts[3 * q + 1] - cy) / h,
+                           rz = (qpts[3 * q + 2] - cz) / h;
+              const double rho  = sqrt(rx * rx + ry * ry + rz * rz);
+              const double ca   = rz / rho;
+              const double sa   = sqrt(fmax(0.0, 1.0 - ca * ca));
+              const double beta = atan2(ry, rx);
+              double nn_ = sqrt(qnrm[3 * q] * qnrm[3 * q] + qnrm[3 * q + 1] * qnrm[3 * q + 1] +
+                                qnrm[3 * q + 2] * qnrm[3 * q + 2]);
+              double nx = qnrm[3 * q] / nn_, ny = qnrm[3 * q + 1] / nn_, nz = qnrm[3 * q + 2] / nn_;
+              double rxy2 = rx * rx + ry * ry;
+              gq[0]       = w;
+              gq[1]       = w / h;
+              gq[2]       = rho;
+              gq[3]       = (rx / rho) * nx + (ry / rho) * ny + (rz / rho) * nz;
+              gq[4]       = (-ry / rxy2) * nx + (rx / rxy2) * ny;
+              gq[5] = (ca * cos(beta) / rho) * nx + (ca * sin(beta) / rho) * ny + (-sa / rho) * nz;
+              gq[6] = ca;
+              gq[7] = sa;
+              double rn = 1.0;
+              for (int i = 0; i <= p; ++i)
+                {
+                  gq[8 + i] = rn;
+                  rn *= rho;
+                }
+              for (int mm = 0; mm <= p; ++mm)
+                {
+                  double sb, cb;
+                  sincos(mm * beta, &sb, &cb);
+                  gq[8 + (p + 1) + mm]     = cb;
+                  gq[8 + 2 * (p + 1) + mm] = sb;
+                }
+            }
+          __syncthreads();
+          // Legendre values of every (contribution, n, m)
+          for (int it = threadIdx.x; it < nc * npm; it += blockDim.x)
+            {
+              const int cq = it / npm, pm = it - cq * npm;
+              int       nn = 0;
+              while ((nn + 1) * (nn + 2) / 2 <= pm)
+                ++nn;
+              const int mm = pm - nn * (nn + 1) / 2;
+              double   *gq = geo + cq * stride;
+              gq[8 + 3 * (p + 1) + pm]       = legendre_nm<double>(nn, mm, gq[6], gq[7]);
+              gq[8 + 3 * (p + 1) + npm + pm] = legendre_dsin<double>(nn, mm, gq[6], gq[7]);
+            }
+          __syncthreads();
+          if (k < K)
+            for (int cq = 0; cq < nc; ++cq)
+              {
+                const double *gq  = geo + cq * stride;
+                const int     pmi = n * (n + 1) / 2 + m;
+                const double  cb = gq[8 + (p + 1) + m], sb = gq[8 + 2 * (p + 1) + m];
+                const double  P  = gq[8 + 3 * (p + 1) + pmi];
+                const double  rn = gq[8 + n];
+                // monopole: w P rho^n e^{-i m beta}
+                const double mono = gq[0] * P * rn;
+                a2 += part == 0 ? mono * cb : -mono * sb;
+                // dipole (scaled coordinates, strength w / h)
+                const double dS   = gq[8 + 3 * (p + 1) + npm + pmi];
+                const double rho  = gq[2];
+                const double rnm1 = n > 0 ? rn / rho : 0.0;
+                const double A    = double(n) * rnm1 * P * gq[3] - rn * dS * gq[5];
+                const double B    = -double(m) * rn * P * gq[4];
+                // e^{-i m beta} (A + i B)
+                a1 += gq[1] * (part == 0 ? (cb * A + sb * B) : (cb * B - sb * A));
+              }
         }
-      const int K4    = (K + 3) / 4 * 4; // padded row stride (16-byte vector loads)
-      T1[row * K4 + k] = a1;
-      T2[row * K4 + k] = a2;
+      if (k < K)
+        {
+          const int K4    = (K + 3) / 4 * 4; // padded row stride (16-byte vector loads)
+          T1[row * K4 + k] = a1;
+          T2[row * K4 + k] = a2;
+        }
     }
 
     // L2P tables: W[pos][k] such that the field at node rows[pos] of its leaf is
     // sum_k W[pos][k] L^[leaf][k] (LocalExpansion::Evaluate local_expansion.cc:252-287).
-    __global__ void l2p_table_kernel(int64_t n_pos, int K, int ldw, int n_leaves,
-                                     const int64_t *__restrict__ pos_ptr,
-                                     const int32_t *__restrict__ leaf_box,
-                                     const int32_t *__restrict__ nodes,
-                                     const double *__restrict__ xyz,
-                                     const double *__restrict__ box_center,
-                                     const double *__restrict__ box_delta, double *W)
+    // One warp per position: lane 0 forms the geometry, the lanes the Legendre
+    // values of every (n, m) and then the K coefficients.
+    __global__ void __launch_bounds__(256)
+      l2p_table_kernel(int64_t n_pos, int K, int p, int ldw, int n_leaves,
+                       const int64_t *__restrict__ pos_ptr, const int32_t *__restrict__ leaf_box,
+                       const int32_t *__restrict__ nodes, const double *__restrict__ xyz,
+                       const double *__restrict__ box_center,
+                       const double *__restrict__ box_delta, double *W)
     {
-      int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (t >= n_pos * K)
+      extern __shared__ double lgeo[]; // per warp: [rho, ca, sa, beta, h | rn[p+1] | cos[p+1] | sin[p+1] | P[npm]]
+      const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      const int64_t pos  = int64_t(blockIdx.x) * (blockDim.x >> 5) + warp;
+      const int     npm  = (p + 1) * (p + 2) / 2;
+      double       *g    = lgeo + warp * (5 + 3 * (p + 1) + npm);
+      if (pos >= n_pos)
         return;
-      const int64_t pos = t / K;
-      const int     k   = int(t % K);
-      int           lo = 0, hi = n_leaves - 1;
+      int lo = 0, hi = n_leaves - 1;
       while (lo < hi)
         {
           int mid = (lo + hi + 1) >> 1;
@@ -355,32 +418,67 @@ namespace pibem
       const int    box  = leaf_box[lo];
       const double h    = box_delta[box];
       const int    node = nodes[pos];
-      const double rx = (xyz[3 * int64_t(node)] - box_center[3 * box]) / h;
-      const double ry = (xyz[3 * int64_t(node) + 1] - box_center[3 * box + 1]) / h;
-      const double rz = (xyz[3 * int64_t(node) + 2] - box_center[3 * box + 2]) / h;
-      int n, m, part;
-      real_index(k, n, m, part);
-      const double rho  = sqrt(rx * rx + ry * ry + rz * rz);
-      double       val  = 0.0;
+      if (lane == 0)
+        {
+          const double rx  = (xyz[3 * int64_t(node)] - box_center[3 * box]) / h;
+          const double ry  = (xyz[3 * int64_t(node) + 1] - box_center[3 * box + 1]) / h;
+          const double rz  = (xyz[3 * int64_t(node) + 2] - box_center[3 * box + 2]) / h;
+          const double rho = sqrt(rx * rx + ry * ry + rz * rz);
+          g[0]             = rho;
+          if (rho > 0)
+            {
+              const double ca   = rz / rho;
+              const double sa   = sqrt(fmax(0.0, 1.0 - ca * ca));
+              const double beta = atan2(ry, rx);
+              g[1]              = ca;
+              g[2]              = sa;
+              g[3]              = beta;
+              double rn         = 1.0;
+              for (int i = 0; i <= p; ++i)
+                {
+                  g[5 + i] = rn;
+                  rn *= rho;
+                }
+            }
+        }
+      __syncwarp();
+      const double rho = g[0];
       if (rho > 0)
         {
-          const double ca   = rz / rho;
-          const double sa   = sqrt(fmax(0.0, 1.0 - ca * ca));
-          const double beta = atan2(ry, rx);
-          double       sb, cb;
-          sincos(m * beta, &sb, &cb);
-          double rn = 1.0;
-          for (int i = 0; i < n; ++i)
-            rn *= rho;
-          const double P = legendre_nm<double>(n, m, ca, sa) * rn;
-          if (m == 0)
-            val = P;
-          else
-            val = part == 0 ? 2.0 * P * cb : -2.0 * P * sb;
+          for (int mm = lane; mm <= p; mm += 32)
+            {
+              double sb, cb;
+              sincos(mm * g[3], &sb, &cb);
+              g[5 + (p + 1) + mm]     = cb;
+              g[5 + 2 * (p + 1) + mm] = sb;
+            }
+          for (int pm = lane; pm < npm; pm += 32)
+            {
+              int nn = 0;
+              while ((nn + 1) * (nn + 2) / 2 <= pm)
+                ++nn;
+              g[5 + 3 * (p + 1) + pm] = legendre_nm<double>(nn, pm - nn * (nn + 1) / 2, g[1], g[2]);
+            }
         }
-      else if (k == 0)
-        val = 1.0;
-      W[pos * ldw + k] = val / h;
+      __syncwarp();
+      for (int k = lane; k < K; k += 32)
+        {
+          int n, m, part;
+          real_index(k, n, m, part);
+          double val = 0.0;
+          if (rho > 0)
+            {
+              const double cb = g[5 + (p + 1) + m], sb = g[5 + 2 * (p + 1) + m];
+              const double P  = g[5 + 3 * (p + 1) + n * (n + 1) / 2 + m] * g[5 + n];
+              if (m == 0)
+                val = P;
+              else
+                val = part == 0 ? 2.0 * P * cb : -2.0 * P * sb;
+            }
+          else if (k == 0)
+            val = 1.0;
+          W[pos * ldw + k] = val / h;
+        }
     }
   } // namespace
 
@@ -487,7 +585,12 @@ namespace pibem
     int64_t n = n_rows * K;
     if (n == 0)
       return;
-    p2m_table_kernel<<<unsigned((n + 127) / 128), 128, 0, s>>>(
+    if (K > 128)
+      throw Error(PIBEM_EINVAL, "P2M tables: more than 128 coefficients");
+    const size_t smem = size_t(P2M_CHUNK) * p2m_geo_stride(p) * sizeof(double);
+    if (smem > 48 * 1024)
+      raise_smem_limit(reinterpret_cast<const void *>(p2m_table_kernel), smem);
+    p2m_table_kernel<<<unsigned(n_rows), 128, smem, s>>>(
       n_rows, K, p, n_leaves, row_ptr, leaf_box, contrib_ptr, contrib_q, box_center, box_delta,
       qpts, qnrm, qjxw, qshape, T1, T2);
     PIBEM_CUDA(cudaGetLastError());
@@ -499,12 +602,15 @@ namespace pibem
                          const double *box_center, const double *box_delta, double *W,
                          cudaStream_t s)
   {
-    int64_t n = n_pos * K;
-    if (n == 0)
+    if (n_pos == 0)
       return;
-    l2p_table_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n_pos, K, ldw, n_leaves, pos_ptr,
-                                                               leaf_box, nodes, xyz, box_center,
-                                                               box_delta, W);
+    int p = 0;
+    while ((p + 1) * (p + 1) < K)
+      ++p;
+    const size_t smem = size_t(8) * (5 + 3 * (p + 1) + (p + 1) * (p + 2) / 2) * sizeof(double);
+    l2p_table_kernel<<<unsigned((n_pos + 7) / 8), 256, smem, s>>>(n_pos, K, p, ldw, n_leaves,
+                                                                  pos_ptr, leaf_box, nodes, xyz,
+                                                                  box_center, box_delta, W);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpibem_gb300.so")
 
-OK, EINVAL, ENOMEM_HBM, ENOCONV, ETIMEDOUT, ECUDA = 0, 1, 2, 3, 4, 5
+OK, EINVAL, ENOMEM_HBM, ENOCONV, ETIMEDOUT, ECUDA, EAGAIN = 0, 1, 2, 3, 4, 5, 6
 PRECISION_FP64, PRECISION_MIXED, PRECISION_FLOAT_FLOAT = 0, 1, 2
 M2L_TENSOR_CORE, M2L_CUDA_CORE = 0, 1
 
@@ -98,6 +98,8 @@ EXPORTS = [
     "pibem_ucd_read", "pibem_mesh_io_error", "pibem_double_nodes",
     "pibem_dirichlet_mask_from_materials", "pibem_compute_normals",
     "pibem_compute_surface_gradients", "pibem_compute_gradients", "pibem_setup_phases",
+    "pibem_slots_open", "pibem_slots_submit", "pibem_slots_step", "pibem_slots_collect",
+    "pibem_slots_close",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -158,6 +160,12 @@ def load():
     L.pibem_compute_surface_gradients.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
     L.pibem_compute_gradients.argtypes = [C.c_void_p, C.c_int32, _dp, _dp, _dp]
     L.pibem_setup_phases.argtypes = [C.c_void_p, _dp]
+    L.pibem_slots_open.argtypes = [C.c_void_p, C.c_int32]
+    L.pibem_slots_submit.argtypes = [C.c_void_p, C.c_int64, _dp, C.POINTER(C.c_int32)]
+    L.pibem_slots_step.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.pibem_slots_collect.argtypes = [C.c_void_p, C.POINTER(C.c_int64), _dp, _dp,
+                                      C.POINTER(SolveStats)]
+    L.pibem_slots_close.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -329,6 +337,47 @@ class BEMSolver:
             return phi, dphi, st.as_dict()
         self._check(rc)
         return phi, dphi, st.as_dict()
+
+    # -- request slots (continuous batching, pibem_slots_*) --------------------
+    def slots_open(self, max_slots: int):
+        self._check(self.L.pibem_slots_open(self.h, int(max_slots)))
+
+    def slots_close(self):
+        self._check(self.L.pibem_slots_close(self.h))
+
+    def slots_submit(self, request_id: int, tmp_rhs):
+        """Queue one right-hand side (n values); returns its slot, or None when
+        every slot is taken."""
+        t = np.ascontiguousarray(tmp_rhs, np.float64).reshape(-1)
+        slot = C.c_int32(-1)
+        rc = self.L.pibem_slots_submit(self.h, int(request_id), _d(t), C.byref(slot))
+        if rc == EAGAIN:
+            return None
+        self._check(rc)
+        return int(slot.value)
+
+    def slots_step(self, max_steps: int = 0):
+        """Advance the slots; returns (slots in progress, finished slots)."""
+        a, d = C.c_int32(0), C.c_int32(0)
+        self._check(self.L.pibem_slots_step(self.h, int(max_steps), C.byref(a), C.byref(d)))
+        return int(a.value), int(d.value)
+
+    def slots_collect(self):
+        """The finished request with the smallest id as (request_id, phi,
+        dphi_dn, stats), or None; stats["converged"] is False when it stopped on
+        the step limit above the tolerance."""
+        rid = C.c_int64(-1)
+        phi = np.empty(self.n)
+        dphi = np.empty(self.n)
+        st = SolveStats()
+        rc = self.L.pibem_slots_collect(self.h, C.byref(rid), _d(phi), _d(dphi), C.byref(st))
+        if rc == EAGAIN:
+            return None
+        if rc not in (OK, ENOCONV):
+            self._check(rc)
+        d = st.as_dict()
+        d["converged"] = rc == OK
+        return int(rid.value), phi, dphi, d
 
     def solve_device(self, nrhs, phi_ptr, dphi_ptr, tmp_ptr):
         st = SolveStats()

@@ -3,16 +3,22 @@
 `BEMServer` answers solve requests (a mesh id and 1..n right-hand sides of
 `tmp_rhs` data) with the FMM-GMRES solve of `pibem.BEMSolver`.  It keeps the
 meshes it has seen resident on the device -- octree, near field, P2M/L2P tables
-and Krylov space of one handle per mesh -- inside an HBM budget, evicting the
-least recently used idle mesh when a new one would not fit.
+and the Krylov spaces of one handle per mesh -- inside an HBM budget, evicting
+the least recently used idle mesh when a new one would not fit.
 
-Requests are taken in arrival order.  A worker that takes a request also takes
-every request for the same mesh that is waiting at that moment (up to
-`max_batch_rhs` columns) and solves them as one multi-RHS solve (continuous
-batching): the operator applications are shared, the arithmetic of each column
-is not, so every request gets the solution it would get alone.  Workers run on
-their own threads; each handle owns a CUDA stream, so solves of different
-meshes overlap on the GPU.  A handle is used by one worker at a time.
+Continuous batching: a worker serving a mesh keeps its handle's request slots
+(`pibem_slots_*`, `max_batch_rhs` of them) busy.  Between steps of the solve
+engine it admits the waiting requests of that mesh, oldest first, into free
+slots (a request's columns may be admitted as slots free up); a column that
+joins shares every operator application with the columns already in flight
+from its next step on, and leaves as soon as it has converged, while the
+others go on.  While slots are free, a step returns after at most
+`quantum_steps` Arnoldi steps, so that a request arriving in the middle of
+other requests' solves starts within a few milliseconds.  Every column's
+arithmetic is independent of the others', so each request gets the solution
+it would get alone.  Workers run on their own threads; each handle owns a CUDA
+stream, so different meshes overlap on the GPU.  A handle is served by one
+worker at a time.
 
 The reference solves one mesh per process (BEMProblem::solve,
 source/bem_problem.cc:1352-1374); this loop is the serving layer around that
@@ -55,8 +61,11 @@ class Request:
         self.phi = None
         self.dphi_dn = None
         self.stats = None
-        self.batch_rhs = 0
+        self.batch_rhs = 0      # most columns in flight with this request's columns
         self.error = None
+        self._next = 0          # columns admitted so far
+        self._ndone = 0         # columns finished
+        self._col_stats = []
         self._done = threading.Event()
 
     def wait(self, timeout: float | None = None) -> bool:
@@ -94,17 +103,20 @@ class BEMServer:
 
     hbm_budget_gb   device memory the resident meshes may hold together
     workers         threads issuing solves (each on its mesh's own stream)
-    max_batch_rhs   most columns of one coalesced solve
-    solver_factory  callable(**params) -> solver with set_mesh / set_bc / solve /
+    max_batch_rhs   request slots per mesh (columns in flight together)
+    quantum_steps   Arnoldi steps per engine step while slots are free
+    solver_factory  callable(**params) -> solver with set_mesh / set_bc /
+                    slots_open / slots_submit / slots_step / slots_collect /
                     device_bytes / close (default pibem.BEMSolver)
     defaults        pibem_params fields applied to every mesh (per-mesh fields
                     given to add_mesh override them)
     """
 
     def __init__(self, hbm_budget_gb: float = 150.0, workers: int = 4, max_batch_rhs: int = 16,
-                 solver_factory=None, start: bool = True, **defaults):
+                 solver_factory=None, start: bool = True, quantum_steps: int = 8, **defaults):
         self.budget = float(hbm_budget_gb) * 1e9
         self.max_batch_rhs = int(max_batch_rhs)
+        self.quantum_steps = int(quantum_steps)
         self.defaults = dict(defaults)
         self._factory = solver_factory or pibem.BEMSolver
         self._cv = threading.Condition()
@@ -113,7 +125,8 @@ class BEMServer:
         self._resident = 0
         self._next_id = 0
         self._stop = False
-        self.counters = dict(setups=0, evictions=0, solves=0, columns=0, batches=0)
+        self.counters = dict(setups=0, evictions=0, solves=0, columns=0, steps=0, admissions=0,
+                             joined_in_flight=0)
         self._threads = [threading.Thread(target=self._worker, name=f"pibem-serve-{i}", daemon=True)
                          for i in range(int(workers))]
         self._started = False
@@ -239,6 +252,7 @@ class BEMServer:
             h = self._factory(**m.params)
             h.set_mesh(m.xyz, m.cells)
             h.set_bc(m.mask)
+            h.slots_open(self.max_batch_rhs)
             actual = int(h.device_bytes())
         except Exception:
             with self._cv:
@@ -251,25 +265,13 @@ class BEMServer:
             m.bytes = actual
             self.counters["setups"] += 1
 
-    def _take_batch(self):
-        """Oldest waiting request whose mesh is free, plus the mesh's other
-        waiting requests (arrival order, <= max_batch_rhs columns)."""
+    def _next_mesh(self):
+        """Mesh of the oldest waiting request that no worker is serving."""
         for r in self._pending:
             m = self._meshes[r.mesh_id]
-            if m.busy:
-                continue
-            batch, cols = [], 0
-            for q in list(self._pending):
-                if q.mesh_id != r.mesh_id:
-                    continue
-                if batch and cols + q.nrhs > self.max_batch_rhs:
-                    break
-                batch.append(q)
-                cols += q.nrhs
-            for q in batch:
-                self._pending.remove(q)
-            return m, batch
-        return None, None
+            if not m.busy:
+                return m
+        return None
 
     def _worker(self):
         while True:
@@ -277,7 +279,7 @@ class BEMServer:
                 while True:
                     if self._stop:
                         return
-                    m, batch = self._take_batch()
+                    m = self._next_mesh()
                     if m is not None:
                         break
                     self._cv.wait()
@@ -287,19 +289,35 @@ class BEMServer:
                     need = self._reserve(m)
                 except Exception as e:  # budget or shutdown
                     need, err = False, e
-            t0 = time.perf_counter()
+            flight = {}
             try:
                 if err is not None:
                     raise err
                 if need:
                     self._setup(m)
-                self._solve(m, batch, t0)
+                self._serve(m, flight)
             except Exception as e:
-                for q in batch:
+                t = time.perf_counter()
+                with self._cv:
+                    # the mesh's requests in flight and, if the mesh failed
+                    # before serving, its waiting ones
+                    failed = list(flight)
+                    if not flight:
+                        failed = [q for q in self._pending if q.mesh_id == m.mesh_id]
+                        for q in failed:
+                            self._pending.remove(q)
+                for q in failed:
                     q.error = e
-                    q.start = t0
-                    q.end = time.perf_counter()
+                    q.start = q.start if q.start is not None else t
+                    q.end = t
                     q._done.set()
+                if m.handle is not None and flight:
+                    # the slots' state is unknown after a failure: a fresh set
+                    try:
+                        m.handle.slots_close()
+                        m.handle.slots_open(self.max_batch_rhs)
+                    except Exception:
+                        pass
             finally:
                 with self._cv:
                     if m.handle is not None:
@@ -310,23 +328,84 @@ class BEMServer:
                     m.last_used = time.perf_counter()
                     self._cv.notify_all()
 
-    def _solve(self, m: _Mesh, batch, t0):
-        tmp = np.concatenate([q.tmp for q in batch], axis=0)
-        phi, dphi, st = m.handle.solve(tmp.reshape(-1))
-        phi = phi.reshape(tmp.shape)
-        dphi = dphi.reshape(tmp.shape)
-        t1 = time.perf_counter()
-        c = 0
-        for q in batch:
-            q.phi = phi[c:c + q.nrhs].copy()
-            q.dphi_dn = dphi[c:c + q.nrhs].copy()
-            q.stats = st
-            q.batch_rhs = tmp.shape[0]
-            q.start = t0
-            q.end = t1
-            c += q.nrhs
-            q._done.set()
-        with self._cv:
-            self.counters["solves"] += len(batch)
-            self.counters["columns"] += tmp.shape[0]
-            self.counters["batches"] += 1
+    def _serve(self, m: _Mesh, flight: dict):
+        """Keep the mesh's slots busy until no request of it is in flight or
+        waiting (no lock held)."""
+        h = m.handle
+        cap = self.max_batch_rhs
+        cols = {}      # column id -> (request, column)
+        used = 0
+        cid = 0
+        while True:
+            admitted = []
+            with self._cv:
+                for q in list(self._pending):
+                    if q.mesh_id != m.mesh_id:
+                        continue
+                    if used >= cap:
+                        break
+                    k = min(q.nrhs - q._next, cap - used)
+                    admitted.append((q, q._next, k))
+                    q._next += k
+                    used += k
+                    if q._next == q.nrhs:
+                        self._pending.remove(q)
+                    else:
+                        break  # arrival order: the rest of q before any later request
+                if admitted:
+                    self.counters["admissions"] += 1
+                    if flight:
+                        self.counters["joined_in_flight"] += 1
+            if not flight and not admitted:
+                return
+            t = time.perf_counter()
+            for q, c0, k in admitted:
+                if q not in flight:
+                    flight[q] = True
+                    q.start = t
+                    q.phi = np.empty_like(q.tmp)
+                    q.dphi_dn = np.empty_like(q.tmp)
+                    q._col_stats = [None] * q.nrhs
+                for c in range(c0, c0 + k):
+                    cols[cid] = (q, c)
+                    if h.slots_submit(cid, q.tmp[c]) is None:
+                        raise RuntimeError("no free request slot")
+                    cid += 1
+            for q in flight:
+                q.batch_rhs = max(q.batch_rhs, used)
+            h.slots_step(self.quantum_steps if used < cap else 0)
+            with self._cv:
+                self.counters["steps"] += 1
+            while True:
+                res = h.slots_collect()
+                if res is None:
+                    break
+                rid, phi, dphi, st = res
+                q, c = cols.pop(rid)
+                used -= 1
+                q.phi[c] = phi
+                q.dphi_dn[c] = dphi
+                q._col_stats[c] = st
+                q._ndone += 1
+                if not st.get("converged", True) and q.error is None:
+                    q.error = pibem.PibemError(pibem.ENOCONV, "request did not reach the tolerance")
+                if q._ndone == q.nrhs:
+                    q.end = time.perf_counter()
+                    q.stats = _merge_stats(q._col_stats)
+                    flight.pop(q)
+                    with self._cv:
+                        self.counters["solves"] += 1
+                        self.counters["columns"] += q.nrhs
+                    q._done.set()
+
+
+def _merge_stats(cols):
+    """A request's statistics from its columns': the worst residual, the most
+    iterations and refinement steps, the operator applications summed."""
+    out = {"iterations": max(c["iterations"] for c in cols),
+           "refinement_steps": max(c["refinement_steps"] for c in cols),
+           "fp64_matvecs": sum(c["fp64_matvecs"] for c in cols),
+           "fp32_matvecs": sum(c["fp32_matvecs"] for c in cols),
+           "relative_residual": max(c["relative_residual"] for c in cols),
+           "seconds": max(c["seconds"] for c in cols)}
+    return out

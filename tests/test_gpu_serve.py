@@ -88,3 +88,52 @@ def test_eviction_under_small_budget_keeps_results(pibem_mod, synthetic):
             assert srv.resident_bytes() <= budget
     assert srv.counters["evictions"] >= 3 and srv.counters["setups"] >= 4
     srv.close()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_slots_request_joining_mid_solve_equals_alone(mode, pibem_mod, synthetic):
+    """Request slots (pibem_slots_*): a right-hand side submitted while another
+    is in the middle of its GMRES cycle joins the batch at the next step (a few
+    Arnoldi steps per engine step) and both results are bitwise those of
+    pibem_solve alone, with their own statistics."""
+    S = synthetic
+    prm = dict(PARAMS, precision_mode=pibem_mod.PRECISION_MIXED if mode == "mixed"
+               else pibem_mod.PRECISION_FP64)
+    mesh, mask, where = _cases(S)["wigley"]
+    ta = _rhs(S, mesh, mask, where, 41, 1)[0]
+    tb = _rhs(S, mesh, mask, where, 42, 1)[0]
+    g = pibem_mod.BEMSolver(**prm)
+    g.set_mesh(mesh.xyz, mesh.cells)
+    g.set_bc(mask)
+    alone = {k: g.solve(t) for k, t in (("a", ta), ("b", tb))}
+    g.slots_open(4)
+    assert g.slots_submit(7, ta) is not None
+    steps_before_b = 0
+    for _ in range(3):
+        act, done = g.slots_step(max_steps=2)
+        steps_before_b += 1
+        assert act == 1 and done == 0  # a is still in flight
+    assert g.slots_submit(3, tb) is not None
+    got = {}
+    for _ in range(10000):
+        act, done = g.slots_step(max_steps=2)
+        while True:
+            res = g.slots_collect()
+            if res is None:
+                break
+            got[res[0]] = res
+        if len(got) == 2:
+            break
+    assert sorted(got) == [3, 7]
+    for rid, key in ((7, "a"), (3, "b")):
+        _, phi, dphi, st = got[rid]
+        p0, d0, s0 = alone[key]
+        np.testing.assert_array_equal(phi, p0)
+        np.testing.assert_array_equal(dphi, d0)
+        assert st["converged"] and st["relative_residual"] == s0["relative_residual"]
+        assert st["iterations"] == s0["iterations"]
+    # the solve entry point is refused while slots are open
+    with pytest.raises(pibem_mod.PibemError):
+        g.solve(ta)
+    g.slots_close()
+    g.close()

@@ -1,5 +1,6 @@
 """Host logic of the request loop (pi-bem_gb300/serve.py) with a fake solver:
-coalescing of waiting requests per mesh, the column cap, LRU eviction under
+admission of waiting requests per mesh into the request slots, the slot cap,
+requests joining a batch in flight (continuous batching), LRU eviction under
 the HBM budget, refusal of a mesh larger than the budget, error propagation and
 overlap of different meshes on different workers.  No GPU."""
 import threading
@@ -12,16 +13,21 @@ import serve
 
 
 class FakeSolver:
-    """Stands in for pibem.BEMSolver: phi = 2 tmp + column index of the request
-    data (so results depend on the column only), dphi = -tmp."""
+    """Stands in for pibem.BEMSolver's request slots: phi = 2 tmp, dphi = -tmp;
+    a column finishes after `steps` engine steps (each takes `delay` seconds).
+    Every step is logged as (solver, columns in flight, start, end)."""
     log = []
     lock = threading.Lock()
 
-    def __init__(self, fake_bytes=10**9, delay=0.0, fail=False, **_):
+    def __init__(self, fake_bytes=10**9, delay=0.0, fail=False, steps=1, **_):
         self.bytes = fake_bytes
         self.delay = delay
         self.fail = fail
+        self.steps = steps
         self.closed = False
+        self.cap = 0
+        self.cols = {}   # rid -> [tmp, steps left]
+        self.done = {}
 
     def set_mesh(self, xyz, cells):
         self.n = np.asarray(xyz).reshape(-1, 3).shape[0]
@@ -32,16 +38,42 @@ class FakeSolver:
     def device_bytes(self):
         return self.bytes
 
-    def solve(self, tmp):
+    def slots_open(self, cap):
+        self.cap = cap
+        self.cols.clear()
+        self.done.clear()
+
+    def slots_close(self):
+        self.cap = 0
+
+    def slots_submit(self, rid, tmp):
+        if len(self.cols) + len(self.done) >= self.cap:
+            return None
+        self.cols[rid] = [np.array(tmp), self.steps]
+        return len(self.cols) - 1
+
+    def slots_step(self, max_steps=0):
         t0 = time.perf_counter()
         if self.delay:
             time.sleep(self.delay)
         if self.fail:
             raise RuntimeError("solver failed")
-        R = tmp.size // self.n
         with FakeSolver.lock:
-            FakeSolver.log.append((id(self), R, t0, time.perf_counter()))
-        return 2 * tmp, -tmp, {"iterations": 1}
+            FakeSolver.log.append((id(self), len(self.cols), t0, time.perf_counter()))
+        for rid in list(self.cols):
+            self.cols[rid][1] -= 1
+            if self.cols[rid][1] <= 0:
+                self.done[rid] = self.cols.pop(rid)[0]
+        return len(self.cols), len(self.done)
+
+    def slots_collect(self):
+        if not self.done:
+            return None
+        rid = min(self.done)
+        t = self.done.pop(rid)
+        return rid, 2 * t, -t, {"iterations": 1, "refinement_steps": 0, "fp64_matvecs": 1,
+                                "fp32_matvecs": 0, "relative_residual": 0.0, "seconds": 0.0,
+                                "converged": True}
 
     def close(self):
         self.closed = True
@@ -73,7 +105,8 @@ def test_waiting_requests_for_one_mesh_are_coalesced():
     for r in reqs + [rb]:
         np.testing.assert_array_equal(r.phi, 2 * r.tmp)
         np.testing.assert_array_equal(r.dphi_dn, -r.tmp)
-    assert s.counters["batches"] == 2 and s.counters["columns"] == 8
+    assert sorted(R for _, R, _, _ in FakeSolver.log) == [2, 6]
+    assert s.counters["admissions"] == 2 and s.counters["columns"] == 8
     s.close()
 
 
@@ -125,6 +158,26 @@ def test_solver_error_reaches_the_request():
     assert r.wait(10) and isinstance(r.error, RuntimeError)
     r2 = s.submit("good", np.ones(10))
     assert r2.wait(10) and r2.error is None
+    s.close()
+
+
+def test_request_arriving_mid_solve_joins_the_batch_in_flight():
+    """A request submitted while another of the same mesh is in flight starts
+    before that one ends (it joins at the next engine step) and gets its own
+    result."""
+    s = serve.BEMServer(hbm_budget_gb=100, workers=1, solver_factory=FakeSolver)
+    s.add_mesh("A", *_mesh(), delay=0.05, steps=6)
+    s.preload("A")
+    ra = s.submit("A", np.full((1, 10), 1.0))
+    while ra.start is None:
+        time.sleep(0.005)
+    time.sleep(0.08)  # ra is a step or two into its solve
+    rb = s.submit("A", np.full((2, 10), 3.0))
+    assert ra.wait(10) and rb.wait(10) and ra.error is None and rb.error is None
+    assert rb.start < ra.end and ra.start < rb.start
+    assert ra.batch_rhs == 3 and rb.batch_rhs == 3
+    assert s.counters["joined_in_flight"] == 1
+    np.testing.assert_array_equal(rb.phi, 2 * rb.tmp)
     s.close()
 
 
