@@ -58,9 +58,10 @@ WORKLOADS = {
                             "(z > -T/2 Dirichlet), exterior, 1 RHS to 1e-8"),
     "batched": dict(kind="batched",
                     desc="one step = the 98,306-node spheroid (p=8, leaf<=40) x 64 RHS (seeds "
-                         "100..163) in one lockstep solve, concurrently with 32 perturbed spheres "
-                         "(n ~ log-U[12,100], 866..60,002 nodes, p in {6,8,10}, leaf and M2L "
-                         "engine by the autotuner), each handle on its own stream; 96 solves"),
+                         "100..163) in one solve, concurrently with 32 perturbed spheres "
+                         "(n ~ log-U[12,100], 866..60,002 nodes; per size tercile p in {6,8,10}, "
+                         "leaf, M2L engine and M2L tiles by the autotuner), each handle on its own "
+                         "stream; 96 solves"),
     "served": dict(kind="served",
                    desc="request loop: Poisson arrivals over 12 meshes (perturbed spheres and "
                         "Wigley hulls, N ~ log-U[2k,200k], D/N split by a seeded random plane), "
@@ -439,32 +440,39 @@ def run_batched(args, w, rank, world, local):
     meshA, maskA, _, _, _ = S.spheroid_mixed_case(128, seed=2)
     tmpA = np.stack([S.spheroid_mixed_case(0, seed=sd, mesh=meshA)[2] for sd in range(100, 164)])
     prmA = dict(base, fma_truncation_order=8, max_nodes_per_childless_block=40)
-    # part B: 32 perturbed spheres
+    # part B: 32 perturbed spheres, in three size classes (terciles of n)
     rng = np.random.Generator(np.random.PCG64(4))
     partB = []
     for i in range(32):
         n = int(round(np.exp(rng.uniform(np.log(12), np.log(100)))))
-        p = int(rng.choice([6, 8, 10]))
         m = S.perturbed_sphere(n, seed=200 + i)
         mask = S.mixed_bc_by_cell_centroid(m)
         r2 = np.random.Generator(np.random.PCG64(300 + i))
         q = r2.uniform(-1, 1, 8)
         tmp = S.point_source_data(m, mask, S.sources_in_ball(r2, 8), q)[0]
-        partB.append((m, mask, tmp, p))
-    # autotuner: leaf size and translation engine per order, on the median mesh of each order
+        partB.append([m, mask, tmp, None])
+    order = sorted(range(len(partB)), key=lambda i: partB[i][0].n_nodes)
+    classes = [order[:11], order[11:22], order[22:]]
+    # autotuner per class, on its median mesh: the order p in {6, 8, 10} under an
+    # accuracy target (FMM truncation error <= 1e-5 against p = 10), then the
+    # leaf size, the translation engine and the tensor-core M2L tiles
     tuned, t0 = {}, time.perf_counter()
-    for p in (6, 8, 10):
-        cls = sorted([x for x in partB if x[3] == p], key=lambda x: x[0].n_nodes)
-        if not cls:
-            continue
-        m, mask, tmp, _ = cls[len(cls) // 2]
-        best, table = autotune.autotune(m.xyz, m.cells, mask, tmp, leaves=(20, 30, 40, 60),
-                                        repeats=1, precision_mode=pibem.PRECISION_MIXED,
-                                        fma_truncation_order=p, **base)
-        tuned[p] = {"leaf": best["max_nodes_per_childless_block"],
-                    "m2l_engine": ["tensor cores", "CUDA cores"][best["m2l_engine"]],
-                    "params": best, "trials_s": [(lf, e, round(t, 4)) for lf, e, t in table],
-                    "tuned_on_nodes": m.n_nodes}
+    for ci, cls in enumerate(classes):
+        m, mask, tmp, _ = partB[cls[len(cls) // 2]]
+        best, info = autotune.autotune(m.xyz, m.cells, mask, tmp, orders=(6, 8, 10), accuracy=1e-5,
+                                       leaves=(20, 30, 40, 60), repeats=1,
+                                       precision_mode=pibem.PRECISION_MIXED, **base)
+        for i in cls:
+            partB[i][3] = ci
+        tuned[ci] = {"nodes": [int(partB[i][0].n_nodes) for i in (cls[0], cls[-1])],
+                     "p": best["fma_truncation_order"],
+                     "leaf": best["max_nodes_per_childless_block"],
+                     "m2l_engine": ["tensor cores", "CUDA cores"][best["m2l_engine"]],
+                     "m2l_chunk_pairs": best["m2l_chunk_pairs"], "m2l_stages": best["m2l_stages"],
+                     "truncation_error": info["errors"], "params": best,
+                     "trials_s": [(pp, lf, e, c, st, round(t, 4))
+                                  for pp, lf, e, c, st, t in info["trials"]],
+                     "tuned_on_nodes": int(m.n_nodes)}
     autotune_s = time.perf_counter() - t0
 
     def make(mode):
@@ -473,8 +481,8 @@ def run_batched(args, w, rank, world, local):
         hA.set_mesh(meshA.xyz, meshA.cells)
         hA.set_bc(maskA)
         hB = []
-        for m, mask, tmp, p in partB:
-            g = pibem.BEMSolver(**dict(tuned[p]["params"], precision_mode=mode))
+        for m, mask, tmp, ci in partB:
+            g = pibem.BEMSolver(**dict(tuned[ci]["params"], precision_mode=mode))
             g.set_mesh(m.xyz, m.cells)
             g.set_bc(mask)
             hB.append(g)
@@ -570,7 +578,8 @@ def run_batched(args, w, rank, world, local):
                       "f32 operator + f64 refinement/Arnoldi",
                       {"nodes_A": meshA.n_nodes, "nrhs_A": 64, "meshes_B": len(partB),
                        "nodes_B_min_max": [min(nB), max(nB)],
-                       "orders_B": {str(p): sum(1 for x in partB if x[3] == p) for p in (6, 8, 10)},
+                       "orders_B": {str(p): sum(1 for x in partB if tuned[x[3]]["p"] == p)
+                                    for p in (6, 8, 10)},
                        "concurrency": f"{workers} host threads, one CUDA stream per handle",
                        "timing": "host clock around synchronised concurrent solves (inputs device-resident)",
                        "l2": "working set > L2 (spheroid near field 230 MB FP32 + 461 MB FP64)"})

@@ -85,6 +85,12 @@ typedef struct pibem_params
   /* "Continuos gradient across edges" (bem_problem.cc:277, default 1): the
    * constraint lines of Dirichlet-Dirichlet double nodes (see pibem_solve). */
   int32_t continuous_gradient;
+  /* Tiles of the tensor-core FP32 M2L (tuning only; results do not change):
+   * the most M2L pairs of one operator in a tile chunk (0 = 128; 16..128) and
+   * the pipeline depth of the tile stages (0 = the deepest that fits in shared
+   * memory; 2 or 3). */
+  int32_t m2l_chunk_pairs;
+  int32_t m2l_stages;
 } pibem_params;
 
 typedef struct pibem_solve_stats

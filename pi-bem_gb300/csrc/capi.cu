@@ -245,7 +245,6 @@ struct pibem_handle
   DBuf<float2>  d_Wff;  // L2P rows as pairs (modes other than FP64)
   DBuf<double>  d_Tcr;  // P2M strengths of the right-hand side: dir ? T1 : -T2
   DBuf<int>     d_err;
-  DBuf<int>     d_near_queue; // leaf schedule of the one-column near SpMVs
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
   int                  max_leaf_rows = 0;
@@ -328,7 +327,7 @@ struct pibem_handle
     add(d_con_row, d_con_col, d_con_p, d_con_q, d_con_kind, d_con_nrm, d_con_sg);
     add(d_Sff, d_Srff, d_xff, d_Wff, d_Tcr);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
-        d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_near_queue, d_dir, d_modes, d_modes32, d_alpha);
+        d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
     add(d_M64, d_L64, d_x64, d_y64, d_t1, d_t2, d_t3, d_t4, d_m2p64, d_Y64, d_M32, d_L32, d_x32,
         d_y32, d_m2p32, d_Y32, d_Mff, d_Lff, d_ozimg, d_ozslc, d_ozecol, d_ozerow);
     add(sv_b, sv_x, sv_r, sv_d, sv_w, sv_part, sv_nrm, sh_part, sh_nrm);
@@ -1630,7 +1629,6 @@ namespace
       op.nrow_ptr      = h->d_nrow_ptr.p;
       op.ncol_ptr      = h->d_ncol_ptr.p;
       op.nval_ptr      = h->d_nval_ptr.p;
-      op.near_queue    = h->d_near_queue.p;
       op.n_p2m_leaves  = int(pl.pleaf_box.size());
       op.prow_ptr      = h->d_prow_ptr.p;
       op.pleaf_box     = h->d_pleaf_box.p;
@@ -1701,6 +1699,7 @@ namespace
     h->op32.lv_ops  = h->d_lvopsf.p;
     h->op32.dev_err = h->d_err.p;
     h->op32.tc_images = h->d_tcimg.n ? h->d_tcimg.p : nullptr;
+    h->op32.tc_stages = h->prm.m2l_stages;
     h->op32.tc_err    = h->d_err.p;
     TreeDev &td               = h->td;
     td.nb                     = h->tree.nb;
@@ -1940,7 +1939,8 @@ namespace
     // octree, lists and plan
     build_tree(m, qpts, h->nq, P.num_octree_levels, P.max_nodes_per_childless_block, h->tree);
     phase(1);
-    build_plan(m, h->tree, h->nq, P.fma_truncation_order, h->plan);
+    build_plan(m, h->tree, h->nq, P.fma_truncation_order, h->plan,
+               P.m2l_chunk_pairs > 0 ? P.m2l_chunk_pairs : 128);
     phase(2);
     const Tree &t  = h->tree;
     const Plan &pl = h->plan;
@@ -2204,8 +2204,6 @@ namespace
         }
       h->d_err.alloc(1);
       h->d_err.zero(s);
-      h->d_near_queue.alloc(2);
-      h->d_near_queue.zero(s);
       PIBEM_CUDA(cudaStreamSynchronize(s));
     }
     phase(6);
@@ -2546,7 +2544,9 @@ extern "C"
         P.singular_quadrature_order > 12 || P.gmres_restart < 1 || P.solver_max_steps < 1 ||
         !(P.solver_tolerance > 0) || P.precision_mode < PIBEM_PRECISION_FP64 ||
         P.precision_mode > PIBEM_PRECISION_FLOAT_FLOAT || P.m2l_engine < PIBEM_M2L_TENSOR_CORE ||
-        P.m2l_engine > PIBEM_M2L_CUDA_CORE)
+        P.m2l_engine > PIBEM_M2L_CUDA_CORE ||
+        (P.m2l_chunk_pairs != 0 && (P.m2l_chunk_pairs < 16 || P.m2l_chunk_pairs > 128)) ||
+        (P.m2l_stages != 0 && P.m2l_stages != 2 && P.m2l_stages != 3))
       return PIBEM_EINVAL;
     pibem_handle *h = new (std::nothrow) pibem_handle();
     if (!h)

@@ -174,47 +174,24 @@ namespace pibem
     __device__ inline void cp_async_x(float *dst, const float *src) { cp_async4(dst, src); }
     __device__ inline void cp_async_x(double *dst, const double *src) { cp_async8(dst, src); }
 
-    // Dynamic leaf schedule of the persistent one-column near SpMVs: blocks take
-    // the next unprocessed leaf from a counter (ctl[0]), so the leaves are
-    // worked through in ascending order by the whole grid (the DRAM accesses of
-    // the grid stay close together) and a block that drew small leaves takes
-    // more.  The last block to finish (ticket ctl[1], taken after a fence) sets
-    // both words back to zero for the next launch.
-    __device__ inline void leaf_queue_done(int *ctl)
-    {
-      __syncthreads();
-      if (threadIdx.x == 0)
-        {
-          __threadfence();
-          if (atomicAdd(ctl + 1, 1) == int(gridDim.x) - 1)
-            {
-              ctl[0] = 0;
-              ctl[1] = 0;
-              __threadfence();
-            }
-        }
-    }
-
     // Near-field SpMV for one column, software-pipelined: persistent blocks
-    // draw leaves from the dynamic schedule above (the grid works through the
-    // leaves in ascending order: measured faster on GB300 than contiguous leaf
-    // ranges of equal bytes per block, 80 against 125 us on the 98k spheroid;
-    // an L2 prefetch of the leaves ahead with cp.async.bulk.prefetch made it
-    // slower, 89-92 us); while the warps stream the rows of a leaf, the x
-    // entries of the block's next leaf are gathered into the other half of a
-    // double buffer with cp.async, and thread 0 draws the leaf after that.  A
-    // row is computed exactly as in near_leaf_kernel (same chunks per lane,
-    // same order, same butterfly).  Shared memory: 2 x ld_max values.
+    // take leaves L, L + gridDim.x, ... (the grid works through the leaves in
+    // ascending windows.  Measured on GB300, 98k spheroid: 80 us; contiguous
+    // leaf ranges of equal bytes per block 125 us; an L2 prefetch of the leaves
+    // ahead with cp.async.bulk.prefetch 89-92 us; a dynamic schedule drawing
+    // leaves from an atomic counter 89 us); while the warps stream the rows of a
+    // leaf, the x entries of the block's next leaf are gathered into the other
+    // half of a double buffer with cp.async.  A row is computed exactly as in
+    // near_leaf_kernel (same chunks per lane, same order, same butterfly).
+    // Shared memory: 2 x ld_max values.
     template <typename T>
     __global__ void __launch_bounds__(256)
       near_leaf_pipe_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ nrow_ptr,
                             const int64_t *__restrict__ ncol_ptr,
                             const int64_t *__restrict__ nval_ptr, const int32_t *__restrict__ nrows,
                             const int32_t *__restrict__ ncols, const T *__restrict__ vals,
-                            const T *__restrict__ x, T *__restrict__ y, bool acc,
-                            int *__restrict__ qctl)
+                            const T *__restrict__ x, T *__restrict__ y, bool acc)
     {
-      __shared__ int qidx[3]; // [0], [1]: drawn leaves (alternating), [2]: the first leaf
       extern __shared__ __align__(16) unsigned char smem_raw[];
       T        *sxb  = reinterpret_cast<T *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -230,24 +207,17 @@ namespace pibem
             sx[c] = T(0);
         asm volatile("cp.async.commit_group;" ::: "memory");
       };
-      if (threadIdx.x == 0)
-        {
-          qidx[2] = atomicAdd(qctl, 1);
-          qidx[0] = atomicAdd(qctl, 1);
-        }
-      __syncthreads();
-      int leaf = qidx[2], buf = 0, k = 0;
-      if (leaf < n_leaves)
-        gather(leaf, 0);
-      for (; leaf < n_leaves; buf ^= 1, ++k)
+      int leaf = blockIdx.x, buf = 0;
+      if (leaf >= n_leaves)
+        return;
+      gather(leaf, 0);
+      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncthreads(); // this leaf's x is in place; the other buffer is free
-          const int next = qidx[k & 1];
+          const int next = leaf + gridDim.x;
           if (next < n_leaves)
             gather(next, buf ^ 1);
-          if (threadIdx.x == 0 && next < n_leaves)
-            qidx[(k + 1) & 1] = atomicAdd(qctl, 1);
           const T      *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -283,10 +253,8 @@ namespace pibem
                     }
                 }
             }
-          leaf = next;
         }
       asm volatile("cp.async.wait_group 0;" ::: "memory");
-      leaf_queue_done(qctl);
     }
 
     // FP64-accurate near-field SpMV for one column on the FP32 pipes: the
@@ -303,9 +271,8 @@ namespace pibem
                           const int64_t *__restrict__ ncol_ptr, const int64_t *__restrict__ nval_ptr,
                           const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
                           const float2 *__restrict__ vals, const float2 *__restrict__ x,
-                          double *__restrict__ y, bool acc, int *__restrict__ qctl)
+                          double *__restrict__ y, bool acc)
     {
-      __shared__ int qidx[3];
       extern __shared__ __align__(16) unsigned char smem_raw[];
       float2   *sxb  = reinterpret_cast<float2 *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -320,24 +287,17 @@ namespace pibem
             sx[c] = make_float2(0.f, 0.f);
         asm volatile("cp.async.commit_group;" ::: "memory");
       };
-      if (threadIdx.x == 0)
-        {
-          qidx[2] = atomicAdd(qctl, 1);
-          qidx[0] = atomicAdd(qctl, 1);
-        }
-      __syncthreads();
-      int leaf = qidx[2], buf = 0, k = 0;
-      if (leaf < n_leaves)
-        gather(leaf, 0);
-      for (; leaf < n_leaves; buf ^= 1, ++k)
+      int leaf = blockIdx.x, buf = 0;
+      if (leaf >= n_leaves)
+        return;
+      gather(leaf, 0);
+      for (; leaf < n_leaves; leaf += gridDim.x, buf ^= 1)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncthreads();
-          const int next = qidx[k & 1];
+          const int next = leaf + gridDim.x;
           if (next < n_leaves)
             gather(next, buf ^ 1);
-          if (threadIdx.x == 0 && next < n_leaves)
-            qidx[(k + 1) & 1] = atomicAdd(qctl, 1);
           const float2 *sx = sxb + int64_t(buf) * ld_max;
           const int64_t c0 = ncol_ptr[leaf], nc = ncol_ptr[leaf + 1] - c0;
           const int64_t ld = (nc + 3) / 4 * 4;
@@ -386,10 +346,8 @@ namespace pibem
                     }
                 }
             }
-          leaf = next;
         }
       asm volatile("cp.async.wait_group 0;" ::: "memory");
-      leaf_queue_done(qctl);
     }
 
     // P2M apply: M^[leaf][r][k] = sum_rows w(row, r) T[row][k] x_r[dof(row)],
@@ -1099,8 +1057,7 @@ namespace pibem
           raise_smem_limit(reinterpret_cast<const void *>(kern), smem1);
         const int grid = std::min(op.n_near_leaves, MINB * near_sm_count());
         kern<<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr, op.ncol_ptr,
-                                      op.nval_ptr, op.nrows, op.ncols, vals, x, y, accumulate,
-                                      op.near_queue);
+                                      op.nval_ptr, op.nrows, op.ncols, vals, x, y, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
         return;
@@ -1135,7 +1092,7 @@ namespace pibem
         near_leaf_ff_kernel<<<std::min(op.n_near_leaves, NEAR_BLOCKS_PER_SM_WIDE * near_sm_count()),
                               256, smem1, s>>>(
           op.n_near_leaves, int(maxnc), op.nrow_ptr, op.ncol_ptr, op.nval_ptr, op.nrows, op.ncols, vals,
-          xff + int64_t(r) * N, y + int64_t(r) * N, accumulate, op.near_queue);
+          xff + int64_t(r) * N, y + int64_t(r) * N, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
       }

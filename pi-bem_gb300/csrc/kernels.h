@@ -79,9 +79,6 @@ namespace pibem
     int64_t        n_rows = 0;
     const int32_t *row_leaf = nullptr, *nrows = nullptr, *ncols = nullptr;
     const int64_t *nrow_ptr = nullptr, *ncol_ptr = nullptr, *nval_ptr = nullptr;
-    // leaf schedule of the one-column near SpMVs (2 ints, zero between launches;
-    // one launch at a time per operator)
-    int           *near_queue = nullptr;
     // p2m
     int            n_p2m_leaves = 0;
     const int64_t *prow_ptr = nullptr;
@@ -121,6 +118,7 @@ namespace pibem
     int64_t        max_near_cols = 0;
     // tensor-core path of the FP32 translations (null: CUDA-core GEMM)
     const float   *tc_images = nullptr;
+    int            tc_stages = 0; // pipeline stages of the tensor-core kernel (0: by fit)
     // FP64-accurate operator only: BF16 digit images of the operators and
     // their row exponents for the tensor-core FP64-accurate GEMM (ozaki_tc.cu)
     const uint16_t *oz_images = nullptr;

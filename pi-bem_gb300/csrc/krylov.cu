@@ -134,6 +134,10 @@ namespace pibem
           __syncthreads(); // the block's w rows are updated (visible to the block)
         }
       const int nout = MODE == 2 ? 1 : ncols;
+      // partial sums of column r: per block pstride values (with jvec the
+      // columns have different output counts, so a fixed stride, ldo, keeps
+      // their regions apart)
+      const int pstride = jvec ? ldo : nout;
       for (int i = warp; i < nout; i += nw)
         {
           const double *v = MODE == 2 ? wr : Vr + int64_t(i) * ldv;
@@ -144,7 +148,7 @@ namespace pibem
           for (int o = 16; o > 0; o >>= 1)
             s += __shfl_xor_sync(0xffffffffu, s, o);
           if (lane == 0)
-            partial[(int64_t(r) * nblk + blk) * nout + i] = s;
+            partial[(int64_t(r) * nblk + blk) * pstride + i] = s;
         }
       __threadfence();
       __syncthreads();
@@ -159,7 +163,7 @@ namespace pibem
         {
           double s = 0;
           for (int b = lane; b < nblk; b += 32)
-            s += __ldcg(partial + (int64_t(r) * nblk + b) * nout + i);
+            s += __ldcg(partial + (int64_t(r) * nblk + b) * pstride + i);
           for (int o = 16; o > 0; o >>= 1)
             s += __shfl_xor_sync(0xffffffffu, s, o);
           if (lane == 0)

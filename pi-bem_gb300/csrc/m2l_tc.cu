@@ -593,8 +593,15 @@ namespace pibem
     int dev = 0, n_sm = 0;
     PIBEM_CUDA(cudaGetDevice(&dev));
     PIBEM_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-    const TcGeometry g   = tc_geometry(op.K);
-    const int        nch = c1 - c0;
+    TcGeometry g = tc_geometry(op.K);
+    if (op.tc_stages == 2 && g.stages == 3)
+      {
+        // two stages asked for (a tuning choice): the smaller layout
+        const TcLayout lay(g.Np, op.K, 2);
+        g.stages = 2;
+        g.smem   = size_t(lay.total) + 1024;
+      }
+    const int nch = c1 - c0;
     if (int64_t(op.n_boxes) * R * op.K >= (int64_t(1) << 31))
       throw Error(PIBEM_EINVAL, "too many right-hand sides for the tensor-core translations "
                                 "(expansion offsets exceed 32 bits); use the CUDA-core engine");

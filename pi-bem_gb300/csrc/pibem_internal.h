@@ -248,7 +248,9 @@ namespace pibem
     int64_t               n_m2l = 0, n_m2p = 0;
   };
 
-  void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &plan);
+  // chunk_pairs: the most M2L pairs of one operator in a tensor-core chunk
+  void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &plan,
+                  int chunk_pairs = 128);
 
   // Real-form translation operators (scaled expansions), row-major K x K.
   void build_m2m_ops(int p, std::vector<double> &ops8);

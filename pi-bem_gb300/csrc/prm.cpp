@@ -58,6 +58,8 @@ extern "C" int pibem_params_default(pibem_params *p)
   p->double_body                   = 0;
   p->symmetry_plane_z_level        = 0.0;
   p->continuous_gradient           = 1;
+  p->m2l_chunk_pairs               = 0;
+  p->m2l_stages                    = 0;
   return PIBEM_OK;
 }
 
@@ -142,6 +144,10 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
             p->m2l_engine = (val == "CUDA cores" || val == "cuda" || val == "1")
                               ? PIBEM_M2L_CUDA_CORE
                               : PIBEM_M2L_TENSOR_CORE;
+          else if (key == "M2L chunk pairs")
+            p->m2l_chunk_pairs = std::atoi(v);
+          else if (key == "M2L stages")
+            p->m2l_stages = std::atoi(v);
         }
     }
   return PIBEM_OK;

@@ -252,11 +252,52 @@ namespace pibem
     // and of the single layer (Ker2, MultipoleExpansion::Add multipole_expansion.cc:94-122)
     // of the dof's shape function over the leaf's quadrature points, strengths
     // N_j JxW / (4 pi) (bem_fma.cc:1722-1734).  One block per row: the row's
-    // contributions are taken P2M_CHUNK at a time; per contribution its geometry
-    // (scaled offset, angles, normal derivatives of rho, alpha, beta), rho^n,
-    // cos / sin (m beta) and the Legendre values P~_n^m and dP~_n^m/dtheta are
-    // computed once into shared memory, then thread k adds the contributions'
+    // contributions are taken P2M_CHUNK at a time; per contribution one thread
+    // computes its geometry (scaled offset, angles, normal derivatives of rho,
+    // alpha, beta), rho^n, cos / sin (m beta) and the tables of P~_n^m and
+    // dP~_n^m/dtheta into shared memory, then thread k adds the contributions'
     // terms of coefficient k in contribution order.
+    // P~_n^m(x) of every n <= p, m <= n into P[n (n + 1) / 2 + m] and, with dS,
+    // legendre_dsin(n, m) into dS[...]: the recurrences of legendre_nm and
+    // legendre_dsin (devmath.cuh) with the same operations in the same order,
+    // so the values are theirs bit for bit, at O(p^2) instead of O(p^3).
+    __device__ inline void legendre_table(int p, double x, double s, double *P, double *dS)
+    {
+      double pmm = 1.0;
+      for (int m = 0; m <= p; ++m)
+        {
+          if (m > 0)
+            pmm *= -sqrt(double(2 * m - 1) / double(2 * m)) * s;
+          P[m * (m + 1) / 2 + m] = pmm;
+          if (m + 1 > p)
+            continue;
+          double p1 = x * sqrt(double(2 * m + 1)) * pmm, p0 = pmm;
+          P[(m + 1) * (m + 2) / 2 + m] = p1;
+          for (int n = m + 2; n <= p; ++n)
+            {
+              const double p2 = (double(2 * n - 1) * x * p1 - sqrt(double((n - 1) * (n - 1) - m * m)) * p0) /
+                                sqrt(double(n * n - m * m));
+              p0                      = p1;
+              p1                      = p2;
+              P[n * (n + 1) / 2 + m] = p2;
+            }
+        }
+      if (!dS)
+        return;
+      for (int n = 0; n <= p; ++n)
+        for (int m = 0; m <= n; ++m)
+          {
+            auto   pv = [&](int mm) { return mm >= 0 && mm <= n ? P[n * (n + 1) / 2 + mm] : 0.0; };
+            double dth;
+            if (m == 0)
+              dth = n > 0 ? sqrt(double(n) * double(n + 1)) * pv(1) : 0.0;
+            else
+              dth = 0.5 * (sqrt(double(n - m) * double(n + m + 1)) * pv(m + 1) -
+                           sqrt(double(n + m) * double(n - m + 1)) * pv(m - 1));
+            dS[n * (n + 1) / 2 + m] = -dth;
+          }
+    }
+
     constexpr int P2M_CHUNK = 32;
     // doubles per contribution in shared memory for order p
     __host__ __device__ inline int p2m_geo_stride(int p)
@@ -344,19 +385,7 @@ namespace pibem
                   gq[8 + (p + 1) + mm]     = cb;
                   gq[8 + 2 * (p + 1) + mm] = sb;
                 }
-            }
-          __syncthreads();
-          // Legendre values of every (contribution, n, m)
-          for (int it = threadIdx.x; it < nc * npm; it += blockDim.x)
-            {
-              const int cq = it / npm, pm = it - cq * npm;
-              int       nn = 0;
-              while ((nn + 1) * (nn + 2) / 2 <= pm)
-                ++nn;
-              const int mm = pm - nn * (nn + 1) / 2;
-              double   *gq = geo + cq * stride;
-              gq[8 + 3 * (p + 1) + pm]       = legendre_nm<double>(nn, mm, gq[6], gq[7]);
-              gq[8 + 3 * (p + 1) + npm + pm] = legendre_dsin<double>(nn, mm, gq[6], gq[7]);
+              legendre_table(p, ca, sa, gq + 8 + 3 * (p + 1), gq + 8 + 3 * (p + 1) + npm);
             }
           __syncthreads();
           if (k < K)
@@ -390,8 +419,8 @@ namespace pibem
 
     // L2P tables: W[pos][k] such that the field at node rows[pos] of its leaf is
     // sum_k W[pos][k] L^[leaf][k] (LocalExpansion::Evaluate local_expansion.cc:252-287).
-    // One warp per position: lane 0 forms the geometry, the lanes the Legendre
-    // values of every (n, m) and then the K coefficients.
+    // One warp per position: lane 0 forms the geometry and the Legendre table,
+    // the lanes cos / sin (m beta) and then the K coefficients.
     __global__ void __launch_bounds__(256)
       l2p_table_kernel(int64_t n_pos, int K, int p, int ldw, int n_leaves,
                        const int64_t *__restrict__ pos_ptr, const int32_t *__restrict__ leaf_box,
@@ -452,13 +481,8 @@ namespace pibem
               g[5 + (p + 1) + mm]     = cb;
               g[5 + 2 * (p + 1) + mm] = sb;
             }
-          for (int pm = lane; pm < npm; pm += 32)
-            {
-              int nn = 0;
-              while ((nn + 1) * (nn + 2) / 2 <= pm)
-                ++nn;
-              g[5 + 3 * (p + 1) + pm] = legendre_nm<double>(nn, pm - nn * (nn + 1) / 2, g[1], g[2]);
-            }
+          if (lane == 0)
+            legendre_table(p, g[1], g[2], g + 5 + 3 * (p + 1), nullptr);
         }
       __syncwarp();
       for (int k = lane; k < K; k += 32)

@@ -393,7 +393,7 @@ namespace pibem
       }
   }
 
-  void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &pl)
+  void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &pl, int chunk_pairs)
   {
     pl     = Plan();
     pl.p   = p;
@@ -655,7 +655,7 @@ namespace pibem
         while (i < b)
           {
             int64_t j = i;
-            while (j < b && pl.q_op[j] == pl.q_op[i] && j - i < 128)
+            while (j < b && pl.q_op[j] == pl.q_op[i] && j - i < chunk_pairs)
               ++j;
             pl.ch_start.push_back(int32_t(i));
             pl.ch_cnt.push_back(int32_t(j - i));

@@ -46,6 +46,8 @@ class Params(C.Structure):
         ("double_body", C.c_int32),
         ("symmetry_plane_z_level", C.c_double),
         ("continuous_gradient", C.c_int32),
+        ("m2l_chunk_pairs", C.c_int32),
+        ("m2l_stages", C.c_int32),
     ]
 
 
