@@ -111,6 +111,8 @@ typedef struct pibem_tree_info
   int64_t n_m2l_pairs, n_m2p_pairs, near_nnz, p2m_rows, n_quad_points;
   int32_t n_m2l_offsets;
   double  setup_seconds;
+  int32_t octree_on_device; /* 1: octree and lists built on the device, 0: on the host
+                               (a list beyond the device builder's capacity) */
 } pibem_tree_info;
 
 /* Defaults of the reference parameter file. */

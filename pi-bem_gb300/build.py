@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpibem_gb300.so")
-SOURCES = ["setup.cu", "fmm.cu", "m2l_tc.cu", "ozaki_tc.cu", "levels.cu", "krylov.cu", "capi.cu", "projection.cu", "tree.cpp",
+SOURCES = ["setup.cu", "fmm.cu", "m2l_tc.cu", "ozaki_tc.cu", "levels.cu", "krylov.cu", "capi.cu", "projection.cu", "octree.cu", "tree.cpp",
            "prm.cpp", "mesh_io.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -210,6 +210,7 @@ struct pibem_handle
   Tree         tree;
   Plan         plan;
   double       setup_seconds = 0;
+  bool         tree_on_host  = false; // the octree came from the host builder (capacity)
   // wall time of the set-up phases of the last pibem_set_mesh (pibem_setup_phases)
   double       setup_phase[PIBEM_SETUP_PHASES] = {};
   size_t       bytes_resident = 0;
@@ -900,8 +901,13 @@ namespace
     E.prec      = h->prm.preconditioner != 0;
     E.col.assign(S, ColHost());
     E.V.alloc(size_t(S) * L * N);
-    for (DBuf<double> *v : {&E.z, &E.w, &E.b, &E.x, &E.r, &E.d, &E.tmp, &E.cz, &E.cw, &E.u})
+    for (DBuf<double> *v : {&E.b, &E.x, &E.r, &E.d, &E.tmp, &E.u})
       v->alloc(size_t(S) * N);
+    // z, w and the contiguous batch also hold the idle padding columns of the
+    // cycle graphs (S .. bucket(S) - 1, at most S of them); their z is zero
+    for (DBuf<double> *v : {&E.z, &E.w, &E.cz, &E.cw})
+      v->alloc(size_t(2 * S) * N);
+    PIBEM_CUDA(cudaMemsetAsync(E.z.p + size_t(S) * N, 0, sizeof(double) * size_t(S) * N, h->stream));
     E.hb.alloc(size_t(S) * (2 * L + 1));
     E.partial.alloc(size_t(S) * ENG_NBLK * L);
     E.H.alloc(size_t(S) * L * m);
@@ -914,12 +920,13 @@ namespace
     E.nrm.alloc(S);
     E.ticket.alloc(S);
     E.ticket.zero(h->stream);
-    for (DBuf<int> *v : {&E.kdone, &E.jvec, &E.its, &E.maxit, &E.sel, &E.act})
+    for (DBuf<int> *v : {&E.kdone, &E.jvec, &E.its, &E.maxit, &E.sel})
       v->alloc(S);
+    E.act.alloc(2 * S);
     std::vector<int> minus(S, -1);
     E.jvec.upload(minus, h->stream);
-    E.ctl.alloc(3);
-    E.ipin.alloc(size_t(3) * S + 3);
+    E.ctl.alloc(4);
+    E.ipin.alloc(size_t(3) * S + 4);
     E.h_bn.assign(S, 1.0);
     E.h_tol.assign(S, 0.0);
     E.h_its.assign(S, 0);
@@ -1008,6 +1015,17 @@ namespace
       PIBEM_CUDA(cudaMemsetAsync(v + int64_t(c) * N, 0, sizeof(double) * N, h->stream));
   }
 
+  // Operator batch sizes of the cycle graphs (one graph each): the active
+  // column count rounded up to 1, 2, 3, 4, 6, 8, 12, 16, ... (at most half
+  // again), so that a changing count reuses a few graphs
+  int eng_bucket(int n)
+  {
+    int b = 1;
+    while (b < n)
+      b = (b & (b - 1)) == 0 && b >= 2 ? b + b / 2 : (b == 1 ? 2 : (b / 3) * 4);
+    return b;
+  }
+
   // One Arnoldi step of every column in a cycle (E.act holds them, R' of them):
   // w = A z (through the contiguous batch), CGS2 into hb, V_{j+1} = w / |w| and
   // the next z, then the Givens step.
@@ -1043,15 +1061,23 @@ namespace
   {
     Engine      &E  = h->eng;
     cudaStream_t s  = h->stream;
-    const int    Ra = int(act.size());
+    const int    Ra = eng_bucket(int(act.size())); // operator batch of the graph
     auto A = [h](const double *in, double *out, int R) {
       if (h->eng.mixed)
         system_apply32(h, R, in, out, true);
       else
         system_apply64(h, R, in, out, true);
     };
-    E.act.upload(act, s);
-    E.h_ctl = {0, 0, quantum > 0 ? quantum : std::numeric_limits<int>::max()};
+    // the active columns, padded to a bucket of the graph cache with idle
+    // columns beyond S (zero input, output not used)
+    const int Rb = eng_bucket(int(act.size()));
+    std::vector<int> actp(act);
+    for (int k = 0; int(actp.size()) < Rb; ++k)
+      actp.push_back(E.S + k);
+    E.act.upload(actp, s);
+    // a quantum (serving) stops at the first column that ends its cycle, so
+    // that it leaves soon; otherwise the steps go on until every column ended
+    E.h_ctl = {0, 0, quantum > 0 ? quantum : std::numeric_limits<int>::max(), quantum > 0 ? 1 : 0};
     E.ctl.upload(E.h_ctl, s);
     bool graph = !h->timing;
     if (graph)
@@ -1443,21 +1469,30 @@ namespace
         PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p + S, E.kdone.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
         PIBEM_CUDA(cudaMemcpyAsync(E.ipin.p + 2 * S, E.its.p, sizeof(int) * S, cudaMemcpyDeviceToHost, s));
         PIBEM_CUDA(cudaStreamSynchronize(s));
+        bool ended = false;
         for (int c : act)
           {
             ColHost  &C   = E.col[c];
-            const int j   = E.ipin.p[c], kd = E.ipin.p[S + c], it = E.ipin.p[2 * S + c];
+            const int jv  = E.ipin.p[c], it = E.ipin.p[2 * S + c];
             const int now = it - C.its_inner; // steps this column took
             if (E.mixed)
               C.c32 += now;
             else
               C.c64 += now;
-            C.its_inner  = it;
-            E.h_jvec[c]  = j;
-            E.h_its[c]   = it;
-            if (kd >= 0 || j >= E.m || it >= C.inner_maxit)
-              C.st = ST_CYCLE_END;
+            C.its_inner = it;
+            E.h_its[c]  = it;
+            if (jv <= -2)
+              {
+                // ended its cycle after -2 - jv steps (the count lsq takes)
+                E.h_jvec[c] = -2 - jv;
+                C.st        = ST_CYCLE_END;
+                ended       = true;
+              }
+            else
+              E.h_jvec[c] = jv;
           }
+        if (ended)
+          E.jvec.upload(E.h_jvec, s);
       }
     return finished;
   }
@@ -1932,12 +1967,22 @@ namespace
     h->d_qshape.alloc(4 * Q);
     launch_quad_data(n_cells, h->nq, h->d_xyz.p, h->d_cells.p, h->d_gpts.p, h->d_gw.p,
                      h->d_qpts.p, h->d_qnrm.p, h->d_qjxw.p, h->d_qshape.p, s);
-    std::vector<double> qpts(3 * Q);
-    h->d_qpts.download(qpts.data(), qpts.size(), s);
     PIBEM_CUDA(cudaStreamSynchronize(s));
     phase(0);
-    // octree, lists and plan
-    build_tree(m, qpts, h->nq, P.num_octree_levels, P.max_nodes_per_childless_block, h->tree);
+    // octree and lists on the device; on the host when a list exceeds the
+    // device builder's capacity (the same tree either way)
+    if (!build_tree_device(m, h->d_xyz.p, h->d_qpts.p, h->nq, P.num_octree_levels,
+                           P.max_nodes_per_childless_block, h->d_dbl_off.p, h->d_dbl_ids.p,
+                           h->d_elem_off.p, h->d_elem_ids.p, h->tree, s))
+      {
+        std::vector<double> qpts(3 * Q);
+        h->d_qpts.download(qpts.data(), qpts.size(), s);
+        PIBEM_CUDA(cudaStreamSynchronize(s));
+        build_tree(m, qpts, h->nq, P.num_octree_levels, P.max_nodes_per_childless_block, h->tree);
+        h->tree_on_host = true;
+      }
+    else
+      h->tree_on_host = false;
     phase(1);
     build_plan(m, h->tree, h->nq, P.fma_truncation_order, h->plan,
                P.m2l_chunk_pairs > 0 ? P.m2l_chunk_pairs : 128);
@@ -2923,6 +2968,7 @@ extern "C"
       info->n_quad_points = h->mesh.n_cells * h->nq;
       info->n_m2l_offsets = int(h->plan.offsets.size() / 3);
       info->setup_seconds = h->setup_seconds;
+      info->octree_on_device = h->tree_on_host ? 0 : 1;
     });
   }
 

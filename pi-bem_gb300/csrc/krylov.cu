@@ -209,9 +209,9 @@ namespace pibem
     // (iterations so far / limit), bn[r], tol[r] (stopping test |g_{j+1}| /
     // bn <= tol).  hb: [h1 (R x L) | h2 (R x L) | |w|^2 (R)], L = m + 1, the two
     // Gram-Schmidt passes' coefficients and the norm of a step.  ctl[0]: 1 while
-    // the steps go on; ctl[1]: steps run; ctl[2]: most steps before the host
-    // is back (a quantum: the steps stop when a column ends its cycle or after
-    // that many).
+    // the steps go on; ctl[1]: steps run; ctl[2]: most steps before the host is
+    // back (a quantum); ctl[3]: 1 to stop at the first column that ends its
+    // cycle, 0 to go on until every column has ended its cycle.
 
     // cycle start of the selected columns: g[r] = (beta_r, 0, ...) with beta_r =
     // sqrt(nrm2[r]), jvec[r] = 0, kdone[r] = -1
@@ -232,8 +232,8 @@ namespace pibem
     // rotation and the stopping test (|g_{j+1}| / bn <= tol, or a zero
     // subdiagonal); then jvec and the iteration count advance.  A column ends its
     // cycle when it meets its tolerance, after m steps or at its iteration
-    // limit; then, or after ctl[2] steps, ctl[0] = 0 and, in a graph, the
-    // loop's condition is cleared.
+    // limit (jvec = -2 - steps: no more steps); when the steps stop (see ctl),
+    // ctl[0] = 0 and, in a graph, the loop's condition is cleared.
     __global__ void gmres_givens_kernel(int R, int m, const double *__restrict__ hb,
                                         double *__restrict__ H, double *__restrict__ cs,
                                         double *__restrict__ sn, double *__restrict__ g,
@@ -244,9 +244,9 @@ namespace pibem
                                         cudaGraphConditionalHandle cond, int use_cond)
     {
       const int L = m + 1;
-      __shared__ int ended, active;
+      __shared__ int ended, active, alive;
       if (threadIdx.x == 0)
-        ended = active = 0;
+        ended = active = alive = 0;
       __syncthreads();
       for (int r = threadIdx.x; r < R; r += blockDim.x)
         {
@@ -276,19 +276,29 @@ namespace pibem
           gg[j]                      = c[j] * gg[j];
           const int it               = its[r] + 1;
           its[r]                     = it;
-          jvec[r]                    = j + 1;
           if (fabs(gg[j + 1]) / bn[r] <= tol[r] || bb == 0.0)
             kdone[r] = j + 1;
           if (kdone[r] >= 0 || j + 1 >= m || it >= maxit[r])
-            ended = 1;
+            {
+              // the column ends its cycle: it takes no more steps (jvec
+              // -2 - steps until the host has used it)
+              jvec[r] = -2 - (j + 1);
+              ended   = 1;
+            }
+          else
+            {
+              jvec[r] = j + 1;
+              alive   = 1;
+            }
         }
       __syncthreads();
       if (threadIdx.x == 0)
         {
           const int steps = ctl[1] + 1; // steps run since the host set ctl
-          // (with no active column the steps stop at once; an active one ends
-          // its cycle within m steps)
-          const int stop = ended || !active || steps >= ctl[2];
+          // the steps go on while some column is in its cycle, for at most
+          // ctl[2] steps, and with ctl[3] set only until the first column ends
+          // its cycle (every active column ends its cycle within m steps)
+          const int stop = !alive || (ended && ctl[3]) || steps >= ctl[2];
           ctl[0]          = !stop;
           ctl[1]          = steps;
           if (use_cond && stop)

@@ -248,6 +248,14 @@ namespace pibem
     int64_t               n_m2l = 0, n_m2p = 0;
   };
 
+  // The same tree built on the device (octree.cu) from the device copies of the
+  // coordinates, quadrature points, double-node sets and node -> cells CSR;
+  // false when a list does not fit its capacity (the caller then uses
+  // build_tree).
+  bool build_tree_device(const MeshHost &mesh, const double *d_xyz, const double *d_qpts, int nq,
+                         int L, int max_nodes, const int32_t *d_dbl_off, const int32_t *d_dbl_ids,
+                         const int32_t *d_elem_off, const int32_t *d_elem_ids, Tree &t,
+                         cudaStream_t s);
   // chunk_pairs: the most M2L pairs of one operator in a tensor-core chunk
   void build_plan(const MeshHost &mesh, const Tree &t, int nq, int p, Plan &plan,
                   int chunk_pairs = 128);

@@ -77,6 +77,7 @@ class TreeInfo(C.Structure):
         ("n_quad_points", C.c_int64),
         ("n_m2l_offsets", C.c_int32),
         ("setup_seconds", C.c_double),
+        ("octree_on_device", C.c_int32),
     ]
 
     def as_dict(self):

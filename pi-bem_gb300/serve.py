@@ -13,8 +13,11 @@ slots (a request's columns may be admitted as slots free up); a column that
 joins shares every operator application with the columns already in flight
 from its next step on, and leaves as soon as it has converged, while the
 others go on.  While slots are free, a step returns after at most
-`quantum_steps` Arnoldi steps, so that a request arriving in the middle of
-other requests' solves starts within a few milliseconds.  Every column's
+`quantum_steps` Arnoldi steps (or as soon as a column ends its GMRES cycle),
+so that a request arriving in the middle of other requests' solves starts
+within a few milliseconds.  A mesh admits new requests only while no older
+request of another mesh is waiting for a worker (all workers busy): the
+worker then finishes what it has in flight and moves on in arrival order.  Every column's
 arithmetic is independent of the others', so each request gets the solution
 it would get alone.  Workers run on their own threads; each handle owns a CUDA
 stream, so different meshes overlap on the GPU.  A handle is served by one
@@ -113,7 +116,7 @@ class BEMServer:
     """
 
     def __init__(self, hbm_budget_gb: float = 150.0, workers: int = 4, max_batch_rhs: int = 16,
-                 solver_factory=None, start: bool = True, quantum_steps: int = 8, **defaults):
+                 solver_factory=None, start: bool = True, quantum_steps: int = 16, **defaults):
         self.budget = float(hbm_budget_gb) * 1e9
         self.max_batch_rhs = int(max_batch_rhs)
         self.quantum_steps = int(quantum_steps)
@@ -130,6 +133,7 @@ class BEMServer:
         self._threads = [threading.Thread(target=self._worker, name=f"pibem-serve-{i}", daemon=True)
                          for i in range(int(workers))]
         self._started = False
+        self._idle = 0   # workers waiting for work
         if start:
             self.start()
 
@@ -282,7 +286,9 @@ class BEMServer:
                     m = self._next_mesh()
                     if m is not None:
                         break
+                    self._idle += 1
                     self._cv.wait()
+                    self._idle -= 1
                 m.busy = True
                 err = None
                 try:
@@ -341,6 +347,12 @@ class BEMServer:
             with self._cv:
                 for q in list(self._pending):
                     if q.mesh_id != m.mesh_id:
+                        # an older request of a mesh no worker serves, and no
+                        # idle worker to take it: this mesh admits nothing
+                        # newer until its work in flight is done (the worker then
+                        # moves on in arrival order)
+                        if not self._meshes[q.mesh_id].busy and self._idle == 0:
+                            break
                         continue
                     if used >= cap:
                         break

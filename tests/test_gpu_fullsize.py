@@ -14,7 +14,7 @@ source/bem_problem.cc compute_alpha / vmult / compute_rhs :1139-1260) on the
 same seeded inputs (measured on GB300: FP64 <= 6e-14, FP64-accurate <= 7e-14,
 FP32 <= 1e-7):
 
-  octree boxes and the three lists                          identical
+  octree boxes and the three lists (built on the device)    identical
   FP64 path: FMM matvec, alpha, vmult, rhs                  1e-12 relative (2-norm)
   FP64-accurate operator (float-float translations, the
     tcgen05 BF16-digit M2L): vmult, rhs                      1e-12 relative
@@ -83,6 +83,7 @@ def big(request, synthetic, oracle_mod, pibem_mod):
 
 
 def test_tree_and_lists(big, pibem_mod):
+    assert big["handle"](pibem_mod.PRECISION_FP64).tree_info()["octree_on_device"] == 1
     to = big["oracle"].tree()
     tg = big["handle"](pibem_mod.PRECISION_FP64).tree()
     for k in ("level", "parent", "nchild", "n_nodes", "n_quads"):

@@ -72,7 +72,10 @@ def test_quadrature_points_bitwise(case):
 
 
 def test_octree_and_lists_match_reference_semantics(case):
+    """Boxes and all three lists of the device-built octree equal the oracle's
+    restatement of generate_octree_blocking (bem_fma.cc:3615-4801)."""
     o, g = case["oracle"], case["gpu"]
+    assert g.tree_info()["octree_on_device"] == 1
     to, tg = o.tree(), g.tree()
     assert len(to["level"]) == len(tg["level"])
     for k in ("level", "parent", "nchild", "n_nodes", "n_quads"):
