@@ -202,10 +202,12 @@ class Oracle:
         return b
 
     def solve(self, tmp, tol=1e-8, max_steps=1000, restart=100, dense=False, phi=None, dphi=None,
-              block_jacobi=False):
+              block_jacobi=False, ilu=False):
         """GMRES(restart) from x0 = rhs to relative true residual tol; with
-        block_jacobi, right-preconditioned by the leaf-block Jacobi inverses."""
-        self.L.orc_set_preconditioner(self.h, int(block_jacobi))
+        block_jacobi, right-preconditioned by the leaf-block Jacobi inverses;
+        with ilu, by the ILU(0) of the near-field system matrix
+        (BEMFMA::FMA_preconditioner)."""
+        self.L.orc_set_preconditioner(self.h, 2 if ilu else int(block_jacobi))
         tmp = np.ascontiguousarray(tmp, np.float64)
         phi = np.where(self.mask == 1, tmp, 0.0) if phi is None else phi.copy()
         dphi = np.where(self.mask == 0, tmp, 0.0) if dphi is None else dphi.copy()

@@ -565,9 +565,13 @@ struct orc_handle
   // constraint lines of the solve: x[row] - (col >= 0 ? x[col] : 0) = g
   std::vector<int>               con_row, con_col;
   std::vector<double>            con_g;
-  // preconditioner of orc_solve: 0 none, 1 leaf-block Jacobi (right)
+  // preconditioner of orc_solve: 0 none, 1 leaf-block Jacobi (right), 2 ILU(0)
+  // of the near-field system matrix (BEMFMA::FMA_preconditioner)
   int                            prec = 0;
   std::vector<std::vector<double>> blk_inv; // per childless block, row-major m x m
+  std::vector<int64_t>           ilu_ptr;   // CSR of the ILU(0) factors (L unit lower, U)
+  std::vector<int>               ilu_col, ilu_diag;
+  std::vector<double>            ilu_val;
   // Telles rules per singular vertex, Gauss rule
   std::vector<double>            gpts, gw;
   std::vector<double>            tpts[4], tw[4];
@@ -1463,6 +1467,105 @@ extern "C"
       }
   }
 
+  // BEMFMA::FMA_preconditioner (bem_fma.cc:3080-3411): the matrix on the
+  // sparsity pattern of the near field (init_prec_sparsity_pattern), N on
+  // Neumann and -D on Dirichlet columns (init_preconditioner, :952-962), alpha
+  // added on the diagonal of unconstrained Neumann rows (:3293-3308); a
+  // constrained row holds 1 on its diagonal and each constraint entry's weight
+  // as it is stored (:3190-3201, set(i, entry.first, entry.second): +1 for a
+  // double-node line x_d = x_i).  Then TrilinosWrappers::PreconditionILU with
+  // its default parameters (:3408): ILU(0), no fill, no diagonal
+  // perturbation (Ifpack's classical IKJ factorisation on the matrix pattern).
+  static void build_ilu(orc_handle *h, const double *alpha)
+  {
+    const int        n = h->n_nodes;
+    std::vector<int> con(n, -2); // -2: unconstrained, else the line's column (-1: none)
+    for (size_t k = 0; k < h->con_row.size(); ++k)
+      con[h->con_row[k]] = h->con_col[k];
+    h->ilu_ptr.assign(n + 1, 0);
+    h->ilu_col.clear();
+    h->ilu_val.clear();
+    for (int i = 0; i < n; ++i)
+      {
+        if (con[i] != -2)
+          {
+            std::vector<std::pair<int, double>> e = {{i, 1.0}};
+            if (con[i] >= 0 && con[i] != i)
+              e.push_back({con[i], 1.0});
+            std::sort(e.begin(), e.end());
+            for (auto &p : e)
+              {
+                h->ilu_col.push_back(p.first);
+                h->ilu_val.push_back(p.second);
+              }
+          }
+        else
+          {
+            const Row &row = h->near[i];
+            for (size_t k = 0; k < row.cols.size(); ++k)
+              {
+                const int j = row.cols[k];
+                double    v = h->dir[j] ? -row.D[k] : row.N[k];
+                if (j == i && !h->dir[i])
+                  v += alpha[i];
+                h->ilu_col.push_back(j);
+                h->ilu_val.push_back(v);
+              }
+          }
+        h->ilu_ptr[i + 1] = int64_t(h->ilu_col.size());
+      }
+    h->ilu_diag.assign(n, -1);
+    for (int i = 0; i < n; ++i)
+      for (int64_t e = h->ilu_ptr[i]; e < h->ilu_ptr[i + 1]; ++e)
+        if (h->ilu_col[e] == i)
+          h->ilu_diag[i] = int(e);
+    // IKJ ILU(0): for each row i, for its columns k < i in ascending order,
+    // a_ik /= a_kk, then a_ij -= a_ik a_kj for the columns j > k of row k that
+    // row i also holds
+    std::vector<int64_t> pos(n, -1);
+    for (int i = 0; i < n; ++i)
+      {
+        for (int64_t e = h->ilu_ptr[i]; e < h->ilu_ptr[i + 1]; ++e)
+          pos[h->ilu_col[e]] = e;
+        for (int64_t e = h->ilu_ptr[i]; e < h->ilu_ptr[i + 1] && h->ilu_col[e] < i; ++e)
+          {
+            const int k = h->ilu_col[e];
+            h->ilu_val[e] /= h->ilu_val[h->ilu_diag[k]];
+            const double lik = h->ilu_val[e];
+            for (int64_t f = h->ilu_diag[k] + 1; f < h->ilu_ptr[k + 1]; ++f)
+              {
+                const int64_t q = pos[h->ilu_col[f]];
+                if (q >= 0)
+                  h->ilu_val[q] -= lik * h->ilu_val[f];
+              }
+          }
+        for (int64_t e = h->ilu_ptr[i]; e < h->ilu_ptr[i + 1]; ++e)
+          pos[h->ilu_col[e]] = -1;
+      }
+  }
+
+  // z = (L U)^-1 v
+  static void apply_ilu(const orc_handle *h, const double *v, double *z)
+  {
+    const int n = h->n_nodes;
+    for (int i = 0; i < n; ++i)
+      {
+        double s = v[i];
+        for (int64_t e = h->ilu_ptr[i]; e < h->ilu_diag[i]; ++e)
+          s -= h->ilu_val[e] * z[h->ilu_col[e]];
+        z[i] = s;
+      }
+    for (int i = n - 1; i >= 0; --i)
+      {
+        double s = z[i];
+        for (int64_t e = h->ilu_diag[i] + 1; e < h->ilu_ptr[i + 1]; ++e)
+          s -= h->ilu_val[e] * z[h->ilu_col[e]];
+        z[i] = s / h->ilu_val[h->ilu_diag[i]];
+      }
+  }
+
+  static void apply_preconditioner(const orc_handle *h, const double *v, double *z);
+
   static void apply_block_jacobi(const orc_handle *h, const double *v, double *z)
   {
     const int nc = int(h->childless.size());
@@ -1482,6 +1585,14 @@ extern "C"
       }
   }
 
+  static void apply_preconditioner(const orc_handle *h, const double *v, double *z)
+  {
+    if (h->prec == 2)
+      apply_ilu(h, v, z);
+    else
+      apply_block_jacobi(h, v, z);
+  }
+
   void orc_set_preconditioner(orc_handle *h, int kind) { h->prec = kind; }
 
   int orc_solve(orc_handle *h, int dense, double *phi, double *dphi, const double *tmp, double tol,
@@ -1491,8 +1602,10 @@ extern "C"
     std::vector<double> alpha(n), b(n), x(n), r(n), w(n);
     orc_compute_alpha(h, dense, alpha.data());
     orc_compute_rhs(h, dense, alpha.data(), tmp, b.data());
-    if (h->prec)
+    if (h->prec == 1)
       build_block_jacobi(h, alpha.data());
+    else if (h->prec == 2)
+      build_ilu(h, alpha.data());
     // ConstrainedOperator::distribute_rhs (include/constrained_matrix.h:172-181)
     for (size_t k = 0; k < h->con_row.size(); ++k)
       b[h->con_row[k]] = h->con_g[k];
@@ -1524,7 +1637,7 @@ extern "C"
             ++its;
             if (h->prec)
               {
-                apply_block_jacobi(h, V[k].data(), z.data());
+                apply_preconditioner(h, V[k].data(), z.data());
                 constrained_matvec(h, dense, alpha.data(), z.data(), w.data());
               }
             else
@@ -1574,7 +1687,7 @@ extern "C"
             u[t] += y[i] * V[i][t];
         if (h->prec)
           {
-            apply_block_jacobi(h, u.data(), z.data());
+            apply_preconditioner(h, u.data(), z.data());
             u.swap(z);
           }
         for (size_t t = 0; t < n; ++t)

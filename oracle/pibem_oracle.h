@@ -52,7 +52,8 @@ void orc_compute_rhs(orc_handle *h, int use_dense, const double *alpha, const do
 /* BEMProblem::solve_system semantics with an own GMRES(restart); returns iterations. */
 /* Preconditioner of orc_solve: 0 none (default), 1 right leaf-block Jacobi
  * (dense inverses of the near-field system matrix on each childless block's
- * own nodes, the GPU library's preconditioner). */
+ * own nodes, the GPU library's default), 2 right ILU(0) of the near-field
+ * system matrix (BEMFMA::FMA_preconditioner, bem_fma.cc:3080-3411). */
 void orc_set_preconditioner(orc_handle *h, int kind);
 int orc_solve(orc_handle *h, int use_dense, double *phi, double *dphi_dn, const double *tmp_rhs,
               double tol, int max_steps, int restart, double *final_rel_res);

@@ -1075,9 +1075,11 @@ namespace
     for (int k = 0; int(actp.size()) < Rb; ++k)
       actp.push_back(E.S + k);
     E.act.upload(actp, s);
-    // a quantum (serving) stops at the first column that ends its cycle, so
-    // that it leaves soon; otherwise the steps go on until every column ended
-    E.h_ctl = {0, 0, quantum > 0 ? quantum : std::numeric_limits<int>::max(), quantum > 0 ? 1 : 0};
+    // the steps go on until every column ended its cycle (a column that ended
+    // waits, frozen, and the columns' next operator applications stay
+    // batched) or for at most a quantum of steps (serving: new submissions
+    // join, and finished columns leave, at the next call)
+    E.h_ctl = {0, 0, quantum > 0 ? quantum : std::numeric_limits<int>::max(), 0};
     E.ctl.upload(E.h_ctl, s);
     bool graph = !h->timing;
     if (graph)

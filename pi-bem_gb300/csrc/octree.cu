@@ -13,9 +13,10 @@
 //   * near neighbours (TOLL touch test), intList (near neighbours plus the
 //     boxes of the quadrature points of the cells around a box's nodes and
 //     their doubles) and nonIntList, one block per box and level, each list
-//     sorted in shared memory.
-// A list that does not fit the shared-memory capacity (an unusual mesh) is
-// reported, and the caller builds the tree on the host instead.
+//     gathered into a bitmap of box ids in shared memory and read out in
+//     ascending order.
+// A tree whose box-id bitmap or lists exceed the builder's capacities (an
+// unusual mesh) is reported, and the caller builds the tree on the host.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -299,110 +300,90 @@ namespace pibem
     };
 
     constexpr int OT_THREADS = 256;
-    constexpr int OT_SMEM    = 8192; // ids a block gathers and sorts at once
 
-    // sorts the n (<= OT_SMEM) ids of s ascending (bitonic, padded with
-    // INT32_MAX to a power of two) and returns the count without repeats,
-    // the distinct ids first
-    __device__ int sort_unique(int32_t *s, int n)
+    // A set of box ids as a bitmap in shared memory (nwords 32-bit words):
+    // insertion by atomicOr, extraction in ascending order (sorted, unique)
+    __device__ inline void bm_clear(uint32_t *bm, int nwords)
     {
-      int m = 1;
-      while (m < n)
-        m <<= 1;
-      for (int i = n + int(threadIdx.x); i < m; i += blockDim.x)
-        s[i] = INT32_MAX;
-      __syncthreads();
-      for (int k = 2; k <= m; k <<= 1)
-        for (int j = k >> 1; j > 0; j >>= 1)
-          {
-            for (int i = threadIdx.x; i < m; i += blockDim.x)
-              {
-                const int ij = i ^ j;
-                if (ij > i)
-                  {
-                    const bool up = (i & k) == 0;
-                    const int32_t a = s[i], b = s[ij];
-                    if ((a > b) == up)
-                      {
-                        s[i]  = b;
-                        s[ij] = a;
-                      }
-                  }
-              }
-            __syncthreads();
-          }
-      // compaction of the distinct values: one thread (lists are short)
-      __shared__ int cntu;
-      if (threadIdx.x == 0)
-        {
-          int u = 0;
-          for (int i = 0; i < n; ++i)
-            if (i == 0 || s[i] != s[i - 1])
-              s[u++] = s[i];
-          cntu = u;
-        }
-      __syncthreads();
-      return cntu;
+      for (int w = threadIdx.x; w < nwords; w += blockDim.x)
+        bm[w] = 0;
     }
+    __device__ inline void bm_add(uint32_t *bm, int v) { atomicOr(&bm[v >> 5], 1u << (v & 31)); }
+    __device__ inline bool bm_has(const uint32_t *bm, int v) { return (bm[v >> 5] >> (v & 31)) & 1u; }
 
-    __device__ inline void list_write(const ListStore &L, int li, const int32_t *s, int n, int *err)
+    // writes the ids of bm in ascending order into list li of L (count into
+    // L.cnt[li]; more than L.cap: error)
+    __device__ void bm_extract(const uint32_t *bm, int nwords, const ListStore &L, int li, int *err)
     {
-      if (n > L.cap)
+      __shared__ int part[OT_THREADS + 1];
+      const int      per = (nwords + blockDim.x - 1) / blockDim.x;
+      const int      w0 = threadIdx.x * per, w1 = min(nwords, w0 + per);
+      int            c  = 0;
+      for (int w = w0; w < w1; ++w)
+        c += __popc(bm[w]);
+      part[threadIdx.x + 1] = c;
+      if (threadIdx.x == 0)
+        part[0] = 0;
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int t = 1; t <= int(blockDim.x); ++t)
+          part[t] += part[t - 1];
+      __syncthreads();
+      const int total = part[blockDim.x];
+      if (total > L.cap)
         {
           if (threadIdx.x == 0)
             atomicExch(err, 1);
-          n = L.cap;
         }
-      for (int i = threadIdx.x; i < n; i += blockDim.x)
-        L.ids[int64_t(li) * L.cap + i] = s[i];
-      if (threadIdx.x == 0)
-        L.cnt[li] = n;
-    }
-
-    // appends v to the shared gather buffer (overflow: error, value dropped)
-    __device__ inline void gadd(int32_t *s, int *n, int32_t v, int *err)
-    {
-      const int k = atomicAdd(n, 1);
-      if (k < OT_SMEM)
-        s[k] = v;
       else
-        atomicExch(err, 1);
+        {
+          int o = part[threadIdx.x];
+          for (int w = w0; w < w1; ++w)
+            {
+              uint32_t x = bm[w];
+              while (x)
+                {
+                  const int bit = __ffs(x) - 1;
+                  x &= x - 1;
+                  L.ids[int64_t(li) * L.cap + o++] = w * 32 + bit;
+                }
+            }
+        }
+      if (threadIdx.x == 0)
+        L.cnt[li] = total > L.cap ? 0 : total;
+      __syncthreads();
     }
 
     // near neighbours of the boxes of one level (bem_fma.cc:4269-4580)
     __global__ void __launch_bounds__(OT_THREADS)
-      nn_kernel(int box0, int nbx, int L, int level, BoxDev B, const int32_t *__restrict__ lbase,
-                ListStore NN, int *err)
+      nn_kernel(int box0, int nbx, int L, int level, int nwords, BoxDev B,
+                const int32_t *__restrict__ lbase, ListStore NN, int *err)
     {
-      __shared__ int32_t s[OT_SMEM];
-      __shared__ int     n;
-      const int          b = box0 + blockIdx.x;
+      extern __shared__ uint32_t bm[];
+      const int b = box0 + blockIdx.x;
       if (blockIdx.x >= nbx)
         return;
       const int ns = B.nchild[b] == 0 ? L - level + 1 : 1;
       for (int sub = 0; sub < ns; ++sub)
         {
-          if (threadIdx.x == 0)
-            n = 0;
+          bm_clear(bm, nwords);
           __syncthreads();
           // source list: the parent's sublevel-0 list, or this box's previous sublevel
           const int src = sub == 0 ? lbase[B.parent[b]] : lbase[b] + sub - 1;
           const int cn  = NN.cnt[src];
           if (sub == 0 && threadIdx.x == 0)
-            gadd(s, &n, b, err);
+            bm_add(bm, b);
           for (int e = threadIdx.x; e < cn; e += blockDim.x)
             {
               const int pos = NN.ids[int64_t(src) * NN.cap + e];
               if (B.nchild[pos] == 0 && (sub > 0 || touches(B, b, pos)))
-                gadd(s, &n, pos, err);
+                bm_add(bm, pos);
               for (int c = 0; c < B.nchild[pos]; ++c)
                 if (touches(B, b, B.child_first[pos] + c))
-                  gadd(s, &n, B.child_first[pos] + c, err);
+                  bm_add(bm, B.child_first[pos] + c);
             }
           __syncthreads();
-          const int u = sort_unique(s, min(n, OT_SMEM));
-          list_write(NN, lbase[b] + sub, s, u, err);
-          __syncthreads();
+          bm_extract(bm, nwords, NN, lbase[b] + sub, err);
         }
     }
 
@@ -410,63 +391,42 @@ namespace pibem
     // list's level, of the quadrature points of the cells around the box's nodes
     // and their doubles
     __global__ void __launch_bounds__(OT_THREADS)
-      il_kernel(int box0, int nbx, int L, int level, BoxDev B, const int32_t *__restrict__ lbase,
-                const int32_t *__restrict__ node_sorted, const int32_t *__restrict__ dbl_off,
-                const int32_t *__restrict__ dbl_ids, const int32_t *__restrict__ elem_off,
-                const int32_t *__restrict__ elem_ids, int nq, int64_t Q,
-                const int32_t *__restrict__ qbox, ListStore NN, ListStore IL, int *err)
+      il_kernel(int box0, int nbx, int L, int level, int nwords, BoxDev B,
+                const int32_t *__restrict__ lbase, const int32_t *__restrict__ node_sorted,
+                const int32_t *__restrict__ dbl_off, const int32_t *__restrict__ dbl_ids,
+                const int32_t *__restrict__ elem_off, const int32_t *__restrict__ elem_ids, int nq,
+                int64_t Q, const int32_t *__restrict__ qbox, ListStore NN, ListStore IL, int *err)
     {
-      __shared__ int32_t s[OT_SMEM];
-      __shared__ int32_t cells[OT_SMEM / 4];
-      __shared__ int     n, nc;
-      const int          b = box0 + blockIdx.x;
+      extern __shared__ uint32_t bm[];
+      const int b = box0 + blockIdx.x;
       if (blockIdx.x >= nbx)
         return;
-      if (threadIdx.x == 0)
-        n = 0;
-      __syncthreads();
-      for (int k = B.nbeg[b] + int(threadIdx.x); k < B.nend[b]; k += blockDim.x)
-        {
-          const int node = node_sorted[k];
-          for (int a = dbl_off[node]; a < dbl_off[node + 1]; ++a)
-            {
-              const int dn = dbl_ids[a];
-              for (int e = elem_off[dn]; e < elem_off[dn + 1]; ++e)
-                gadd(s, &n, elem_ids[e], err);
-            }
-        }
-      __syncthreads();
-      {
-        const int u = sort_unique(s, min(n, OT_SMEM));
-        if (u > OT_SMEM / 4)
-          {
-            if (threadIdx.x == 0)
-              atomicExch(err, 1);
-            return;
-          }
-        for (int i = threadIdx.x; i < u; i += blockDim.x)
-          cells[i] = s[i];
-        if (threadIdx.x == 0)
-          nc = u;
-        __syncthreads();
-      }
       const int ns = B.nchild[b] == 0 ? L - level + 1 : 1;
       for (int sub = 0; sub < ns; ++sub)
         {
-          if (threadIdx.x == 0)
-            n = 0;
+          bm_clear(bm, nwords);
           __syncthreads();
           const int li = lbase[b] + sub;
           const int cn = NN.cnt[li];
           for (int e = threadIdx.x; e < cn; e += blockDim.x)
-            gadd(s, &n, NN.ids[int64_t(li) * NN.cap + e], err);
+            bm_add(bm, NN.ids[int64_t(li) * NN.cap + e]);
           const int32_t *qb = qbox + int64_t(level + sub) * Q;
-          for (int e = threadIdx.x; e < nc * nq; e += blockDim.x)
-            gadd(s, &n, qb[int64_t(cells[e / nq]) * nq + e % nq], err);
+          for (int k = B.nbeg[b] + int(threadIdx.x); k < B.nend[b]; k += blockDim.x)
+            {
+              const int node = node_sorted[k];
+              for (int a = dbl_off[node]; a < dbl_off[node + 1]; ++a)
+                {
+                  const int dn = dbl_ids[a];
+                  for (int e = elem_off[dn]; e < elem_off[dn + 1]; ++e)
+                    {
+                      const int64_t c = elem_ids[e];
+                      for (int q = 0; q < nq; ++q)
+                        bm_add(bm, qb[c * nq + q]);
+                    }
+                }
+            }
           __syncthreads();
-          const int u = sort_unique(s, min(n, OT_SMEM));
-          list_write(IL, li, s, u, err);
-          __syncthreads();
+          bm_extract(bm, nwords, IL, li, err);
         }
     }
 
@@ -474,35 +434,24 @@ namespace pibem
     // the box's previous sublevel's, childless entries not in the box's own
     // intList and the children not in it
     __global__ void __launch_bounds__(OT_THREADS)
-      nil_kernel(int box0, int nbx, int L, int level, BoxDev B, const int32_t *__restrict__ lbase,
-                 ListStore IL, ListStore NIL, int *err)
+      nil_kernel(int box0, int nbx, int L, int level, int nwords, BoxDev B,
+                 const int32_t *__restrict__ lbase, ListStore IL, ListStore NIL, int *err)
     {
-      __shared__ int32_t s[OT_SMEM];
-      __shared__ int     n;
-      const int          b = box0 + blockIdx.x;
+      extern __shared__ uint32_t bm[];
+      uint32_t *own = bm + nwords; // the box's intList
+      const int b   = box0 + blockIdx.x;
       if (blockIdx.x >= nbx)
         return;
       const int ns = B.nchild[b] == 0 ? L - level + 1 : 1;
       for (int sub = 0; sub < ns; ++sub)
         {
-          if (threadIdx.x == 0)
-            n = 0;
+          bm_clear(bm, 2 * nwords);
           __syncthreads();
-          const int      li  = lbase[b] + sub;
-          const int32_t *il  = IL.ids + int64_t(li) * IL.cap;
-          const int      nil = IL.cnt[li];
-          auto           in  = [&](int v) {
-            int lo = 0, hi = nil;
-            while (lo < hi)
-              {
-                const int mid = (lo + hi) >> 1;
-                if (il[mid] < v)
-                  lo = mid + 1;
-                else
-                  hi = mid;
-              }
-            return lo < nil && il[lo] == v;
-          };
+          const int li  = lbase[b] + sub;
+          const int nil = IL.cnt[li];
+          for (int e = threadIdx.x; e < nil; e += blockDim.x)
+            bm_add(own, IL.ids[int64_t(li) * IL.cap + e]);
+          __syncthreads();
           const int src = sub == 0 ? lbase[B.parent[b]] : li - 1;
           const int cn  = IL.cnt[src];
           for (int e = threadIdx.x; e < cn; e += blockDim.x)
@@ -510,18 +459,16 @@ namespace pibem
               const int pos = IL.ids[int64_t(src) * IL.cap + e];
               if (B.nchild[pos] == 0)
                 {
-                  if (!in(pos))
-                    gadd(s, &n, pos, err);
+                  if (!bm_has(own, pos))
+                    bm_add(bm, pos);
                 }
               else
                 for (int c = 0; c < B.nchild[pos]; ++c)
-                  if (!in(B.child_first[pos] + c))
-                    gadd(s, &n, B.child_first[pos] + c, err);
+                  if (!bm_has(own, B.child_first[pos] + c))
+                    bm_add(bm, B.child_first[pos] + c);
             }
           __syncthreads();
-          const int u = sort_unique(s, min(n, OT_SMEM));
-          list_write(NIL, li, s, u, err);
-          __syncthreads();
+          bm_extract(bm, nwords, NIL, li, err);
         }
     }
   } // namespace
@@ -847,6 +794,17 @@ namespace pibem
         }
       PIBEM_CUDA(cudaStreamSynchronize(s)); // the host staging above goes out of scope
     }
+    // box-id bitmaps of the list kernels in shared memory (two for nonIntList)
+    const int    nwords   = (nbt + 31) / 32;
+    const size_t bm_bytes = size_t(nwords) * sizeof(uint32_t);
+    if (2 * bm_bytes > 200 * 1024)
+      return false;
+    if (2 * bm_bytes > 48 * 1024)
+      {
+        raise_smem_limit(reinterpret_cast<const void *>(nil_kernel), 2 * bm_bytes);
+        raise_smem_limit(reinterpret_cast<const void *>(il_kernel), bm_bytes);
+        raise_smem_limit(reinterpret_cast<const void *>(nn_kernel), bm_bytes);
+      }
     BoxDev B{d_pmin.p, d_delta.p, d_nchild.p, d_cfirst.p, d_parent.p, d_nbeg.p, d_nend.p};
     ListStore NN{d_nn.p, c_nn.p, CAP_NN}, IL{d_il.p, c_il.p, CAP_IL}, NIL{d_nil.p, c_nil.p, CAP_NIL};
     for (int l = 2; l <= L; ++l)
@@ -854,11 +812,12 @@ namespace pibem
         const int b0 = t.startLevel[l], nbx = t.endLevel[l] - b0 + 1;
         if (nbx <= 0)
           continue;
-        nn_kernel<<<nbx, OT_THREADS, 0, s>>>(b0, nbx, L, l, B, d_lbase.p, NN, d_err.p);
-        il_kernel<<<nbx, OT_THREADS, 0, s>>>(b0, nbx, L, l, B, d_lbase.p, nv[nc].p, d_dbl_off,
-                                             d_dbl_ids, d_elem_off, d_elem_ids, nq, Q, dqbox.p, NN,
-                                             IL, d_err.p);
-        nil_kernel<<<nbx, OT_THREADS, 0, s>>>(b0, nbx, L, l, B, d_lbase.p, IL, NIL, d_err.p);
+        nn_kernel<<<nbx, OT_THREADS, bm_bytes, s>>>(b0, nbx, L, l, nwords, B, d_lbase.p, NN, d_err.p);
+        il_kernel<<<nbx, OT_THREADS, bm_bytes, s>>>(b0, nbx, L, l, nwords, B, d_lbase.p, nv[nc].p,
+                                                    d_dbl_off, d_dbl_ids, d_elem_off, d_elem_ids, nq,
+                                                    Q, dqbox.p, NN, IL, d_err.p);
+        nil_kernel<<<nbx, OT_THREADS, 2 * bm_bytes, s>>>(b0, nbx, L, l, nwords, B, d_lbase.p, IL, NIL,
+                                                         d_err.p);
         PIBEM_CUDA(cudaGetLastError());
         note_launch(3);
       }
