@@ -70,7 +70,9 @@ typedef struct pibem_params
   int32_t gmres_restart;                 /* Krylov dimension (reference: 100) */
   int32_t is_external_flow;              /* 0 interior (alpha=-N1), 1 exterior (alpha=-1-N1) */
   int32_t precision_mode;                /* PIBEM_PRECISION_* */
-  int32_t preconditioner;                /* 0 none, 1 leaf-block Jacobi (right) */
+  int32_t preconditioner;                /* 0 none, 1 leaf-block Jacobi (right), 2 ILU(0) of
+                                            the near-field system matrix (right; the
+                                            reference's FMA_preconditioner, bem_fma.cc:3080) */
   int32_t device;                        /* CUDA device ordinal */
   double  inner_tolerance;               /* mixed mode: inner FP32 GMRES tolerance */
   double  hbm_budget_gb;                 /* 0 = unlimited */
@@ -153,6 +155,14 @@ int pibem_compute_alpha(pibem_handle *h, double *alpha);
 
 /* BEMProblem::vmult (bem_problem.cc:1165): y = N(x.neu) - D(x.dir) + alpha.x.neu. */
 int pibem_system_matvec(pibem_handle *h, int32_t nrhs, const double *x, double *y);
+
+/* PreconditionILU::vmult on BEMFMA::FMA_preconditioner's matrix
+ * (bem_fma.cc:3080-3411, applied in bem_problem.cc:1302-1318): z = P^-1 v for
+ * nrhs vectors with the handle's preconditioner -- the ILU(0) of the near-field
+ * system matrix (preconditioner 2), the leaf-block Jacobi inverses
+ * (preconditioner 1; FP32 inverses in PRECISION_MIXED, FP64 otherwise), or
+ * z = v (0).  Built by pibem_set_bc. */
+int pibem_apply_preconditioner(pibem_handle *h, int32_t nrhs, const double *v, double *z);
 
 /* BEMProblem::compute_rhs (bem_problem.cc:1220). */
 int pibem_compute_rhs(pibem_handle *h, int32_t nrhs, const double *tmp_rhs, double *rhs);

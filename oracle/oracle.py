@@ -61,6 +61,10 @@ def lib():
         L.orc_solve.restype = C.c_int
         L.orc_solve.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, _dp]
         L.orc_set_preconditioner.argtypes = [C.c_void_p, C.c_int]
+        L.orc_preconditioner_build.restype = C.c_int64
+        L.orc_preconditioner_build.argtypes = [C.c_void_p, C.c_int]
+        L.orc_preconditioner_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.orc_ilu_factors.argtypes = [C.c_void_p, C.POINTER(C.c_int64), _ip, _dp]
         L.orc_num_blocks.argtypes = [C.c_void_p]
         L.orc_num_levels.argtypes = [C.c_void_p]
         L.orc_level_range.argtypes = [C.c_void_p, _ip, _ip]
@@ -215,6 +219,27 @@ class Oracle:
         its = self.L.orc_solve(self.h, int(dense), _d(phi), _d(dphi), _d(tmp), tol, max_steps,
                                restart, _d(res))
         return phi, dphi, its, float(res[0])
+
+    def preconditioner(self, kind):
+        """Builds the preconditioner `kind` (0 none, 1 leaf-block Jacobi, 2
+        ILU(0) of the near-field system matrix); returns a function v -> P^-1 v
+        and, for the ILU, its factors (ptr, col, val) in place in the CSR."""
+        nnz = self.L.orc_preconditioner_build(self.h, int(kind))
+        factors = None
+        if kind == 2:
+            ptr = np.zeros(self.n + 1, np.int64)
+            col = np.zeros(nnz, np.int32)
+            val = np.zeros(nnz)
+            self.L.orc_ilu_factors(self.h, ptr.ctypes.data_as(C.POINTER(C.c_int64)), _i(col), _d(val))
+            factors = (ptr, col, val)
+
+        def apply(v):
+            v = np.ascontiguousarray(v, np.float64)
+            z = np.zeros(self.n)
+            self.L.orc_preconditioner_apply(self.h, _d(v), _d(z))
+            return z
+
+        return apply, factors
 
     # -- tree export --------------------------------------------------------
     def tree(self):

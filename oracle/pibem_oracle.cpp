@@ -1595,6 +1595,36 @@ extern "C"
 
   void orc_set_preconditioner(orc_handle *h, int kind) { h->prec = kind; }
 
+  int64_t orc_preconditioner_build(orc_handle *h, int kind)
+  {
+    std::vector<double> alpha(h->n_nodes);
+    orc_compute_alpha(h, 0, alpha.data());
+    h->prec = kind;
+    if (kind == 1)
+      build_block_jacobi(h, alpha.data());
+    else if (kind == 2)
+      {
+        build_ilu(h, alpha.data());
+        return int64_t(h->ilu_col.size());
+      }
+    return 0;
+  }
+
+  void orc_preconditioner_apply(orc_handle *h, const double *v, double *z)
+  {
+    if (h->prec == 0)
+      std::copy(v, v + h->n_nodes, z);
+    else
+      apply_preconditioner(h, v, z);
+  }
+
+  void orc_ilu_factors(orc_handle *h, int64_t *ptr, int32_t *col, double *val)
+  {
+    std::copy(h->ilu_ptr.begin(), h->ilu_ptr.end(), ptr);
+    std::copy(h->ilu_col.begin(), h->ilu_col.end(), col);
+    std::copy(h->ilu_val.begin(), h->ilu_val.end(), val);
+  }
+
   int orc_solve(orc_handle *h, int dense, double *phi, double *dphi, const double *tmp, double tol,
                 int max_steps, int restart, double *final_res)
   {

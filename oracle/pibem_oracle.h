@@ -10,6 +10,8 @@
 #ifndef PIBEM_ORACLE_H
 #define PIBEM_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -55,6 +57,15 @@ void orc_compute_rhs(orc_handle *h, int use_dense, const double *alpha, const do
  * own nodes, the GPU library's default), 2 right ILU(0) of the near-field
  * system matrix (BEMFMA::FMA_preconditioner, bem_fma.cc:3080-3411). */
 void orc_set_preconditioner(orc_handle *h, int kind);
+/* Builds the preconditioner `kind` (as above) with the FMM alpha and makes it
+ * the handle's; returns the ILU's number of stored entries (0 otherwise). */
+int64_t orc_preconditioner_build(orc_handle *h, int kind);
+/* z = P^-1 v with the handle's preconditioner (v for none). */
+void orc_preconditioner_apply(orc_handle *h, const double *v, double *z);
+/* The ILU(0) factors in place in the CSR of the near-field system matrix:
+ * ptr (n + 1), col, val (L below the diagonal with unit diagonal implied, U
+ * from the diagonal on). */
+void orc_ilu_factors(orc_handle *h, int64_t *ptr, int32_t *col, double *val);
 int orc_solve(orc_handle *h, int use_dense, double *phi, double *dphi_dn, const double *tmp_rhs,
               double tol, int max_steps, int restart, double *final_rel_res);
 

@@ -246,6 +246,16 @@ struct pibem_handle
   DBuf<float2>  d_Wff;  // L2P rows as pairs (modes other than FP64)
   DBuf<double>  d_Tcr;  // P2M strengths of the right-hand side: dir ? T1 : -T2
   DBuf<int>     d_err;
+  // ILU(0) of the near-field system matrix (preconditioner 2): CSR in node
+  // order (values: L below the diagonal, unit diagonal implied; U from it),
+  // the position of each row's diagonal, and the rows by level of the lower
+  // and of the upper triangle (the rows of a level depend on earlier levels
+  // only); level bounds on the host
+  DBuf<int64_t> d_ilu_ptr, d_ilu_diag;
+  DBuf<int32_t> d_ilu_col, d_ilu_rows_lo, d_ilu_rows_up;
+  DBuf<double>  d_ilu_val;
+  std::vector<int64_t> ilu_lptr_lo, ilu_lptr_up;
+  bool          ilu_on = false;
   bool          use_tc = true;
   std::vector<int64_t> blk_ptr;
   int                  max_leaf_rows = 0;
@@ -326,6 +336,7 @@ struct pibem_handle
         d_up_box, d_down_box, d_up_q, d_down_q, d_up_child8, d_down_par, d_down_oct,
         d_m2p_item_pair, d_m2l_yslot, d_down_m2l_beg, d_down_m2l_end, d_m2p_tnodes);
     add(d_con_row, d_con_col, d_con_p, d_con_q, d_con_kind, d_con_nrm, d_con_sg);
+    add(d_ilu_ptr, d_ilu_diag, d_ilu_col, d_ilu_rows_lo, d_ilu_rows_up, d_ilu_val);
     add(d_Sff, d_Srff, d_xff, d_Wff, d_Tcr);
     add(d_entries, d_N, d_D, d_S, d_T1, d_T2, d_W, d_ops, d_Pinv, d_Pinv64, d_Tc, d_Tcf, d_S32, d_T1f, d_T2f, d_Wf,
         d_opsf, d_opsff, d_tcimg, d_lvopsf, d_err, d_dir, d_modes, d_modes32, d_alpha);
@@ -856,14 +867,28 @@ namespace
                                  size_t(n) * sizeof(double), size_t(R), cudaMemcpyDeviceToDevice, s));
   }
 
-  // z = P^-1 v for R columns (v column stride ldv): the FP64 inverses where the
-  // handle keeps them (GMRES on an FP64-accurate operator), else the FP32 ones
-  void apply_block_jacobi(pibem_handle *h, int R, const double *v, int64_t ldv, double *z,
-                          cudaStream_t s, const double *nrm2 = nullptr, double *vout = nullptr,
-                          int64_t ldo = 0, const int *jvec = nullptr, const int *sel = nullptr)
+  // z = P^-1 v for R columns (v column stride ldv).  Leaf-block Jacobi: the
+  // FP64 inverses where the handle keeps them (GMRES on an FP64-accurate
+  // operator), else the FP32 ones.  ILU(0): z = v, then the level-scheduled
+  // forward and backward substitutions in place (FP64).  With nrm2, v / |v|
+  // is also written to vout (column stride ldo, at column jvec[r] + 1).
+  void apply_prec(pibem_handle *h, int R, const double *v, int64_t ldv, double *z, cudaStream_t s,
+                  const double *nrm2 = nullptr, double *vout = nullptr, int64_t ldo = 0,
+                  const int *jvec = nullptr, const int *sel = nullptr)
   {
-    const int     nl = int(h->blk_ptr.size()) - 1;
-    const int64_t N  = h->N();
+    const int64_t N = h->N();
+    if (h->ilu_on)
+      {
+        if (nrm2)
+          launch_normalize(N, R, v, nrm2, vout, ldo, s, jvec, z, sel);
+        else
+          launch_copy_sel(N, R, v, ldv, z, sel, s);
+        launch_ilu_apply(h->ilu_lptr_lo, h->d_ilu_rows_lo.p, h->ilu_lptr_up, h->d_ilu_rows_up.p, R, N,
+                         h->d_ilu_ptr.p, h->d_ilu_col.p, h->d_ilu_val.p, h->d_ilu_diag.p, z, sel,
+                         jvec, s);
+        return;
+      }
+    const int nl = int(h->blk_ptr.size()) - 1;
     if (h->d_Pinv64.p)
       launch_block_apply(nl, h->max_leaf_rows, R, N, h->d_nrow_ptr.p, h->d_blk_ptr.p, h->d_nrows.p,
                          h->d_Pinv64.p, v, ldv, z, s, nrm2, vout, ldo, jvec, sel);
@@ -1048,7 +1073,7 @@ namespace
     launch_cgs_step(2, N, E.S, 0, N, ldr, E.V.p, h2, L, E.w.p, ENG_NBLK, E.partial.p, E.ticket.p, nr,
                     s, E.jvec.p, 1);
     if (E.prec) // V_{j+1} = w / |w| and the next step's z = P^-1 V_{j+1} in one pass
-      apply_block_jacobi(h, E.S, E.w.p, N, E.z.p, s, nr, E.V.p, ldr, E.jvec.p);
+      apply_prec(h, E.S, E.w.p, N, E.z.p, s, nr, E.V.p, ldr, E.jvec.p);
     else
       launch_normalize(N, E.S, E.w.p, nr, E.V.p, ldr, s, E.jvec.p, E.z.p);
     launch_gmres_givens(E.S, E.m, h1, E.H.p, E.cs.p, E.sn.p, E.g.p, E.kdone.p, E.jvec.p, E.its.p,
@@ -1114,13 +1139,15 @@ namespace
                          E.cz.p,   E.cw.p,    h->d_x32.p, h->d_y32.p, h->d_M32.p, h->d_L32.p,
                          h->d_Y32.p, h->d_m2p32.p, h->d_M64.p, h->d_L64.p, h->d_Y64.p,
                          h->d_m2p64.p, h->d_t4.p, h->d_Mff.p, h->d_Lff.p, h->d_xff.p,
-                         h->d_ozslc.p, h->d_modes.p, h->d_modes32.p, h->sh_part.p};
+                         h->d_ozslc.p, h->d_modes.p, h->d_modes32.p, h->sh_part.p,
+                         h->d_ilu_val.p, h->d_ilu_col.p, h->d_ilu_ptr.p, h->d_ilu_diag.p,
+                         h->d_ilu_rows_lo.p, h->d_ilu_rows_up.p};
       return b[i];
     };
-    constexpr int             nb = 38;
+    constexpr int             nb = 44;
     std::array<uintptr_t, 48> key{};
     key[0] = uintptr_t(Ra) | (uintptr_t(E.S) << 16) | (uintptr_t(E.m) << 32) |
-             (uintptr_t(E.prec) << 48) | (uintptr_t(E.mixed) << 49);
+             (uintptr_t(E.prec) << 48) | (uintptr_t(E.mixed) << 49) | (uintptr_t(h->ilu_on) << 50);
     key[1] = uintptr_t(s);
     for (int i = 0; i < nb; ++i)
       key[2 + i] = uintptr_t(bufs_now(i));
@@ -1289,7 +1316,7 @@ namespace
             double *tgt = E.mixed ? E.d.p : E.x.p;
             if (E.prec)
               {
-                apply_block_jacobi(h, E.S, E.u.p, N, E.z.p, s, nullptr, nullptr, 0, nullptr, E.sel.p);
+                apply_prec(h, E.S, E.u.p, N, E.z.p, s, nullptr, nullptr, 0, nullptr, E.sel.p);
                 launch_axpby_sel(N, E.S, E.sel.p, 1.0, E.z.p, 1.0, tgt, s);
               }
             else
@@ -1423,7 +1450,7 @@ namespace
                 launch_normalize(N, E.S, E.w.p, E.nrm.p, E.V.p, ldr, s, nullptr,
                                  E.prec ? nullptr : E.z.p, E.sel.p);
                 if (E.prec)
-                  apply_block_jacobi(h, E.S, E.V.p, ldr, E.z.p, s, nullptr, nullptr, 0, nullptr, E.sel.p);
+                  apply_prec(h, E.S, E.V.p, ldr, E.z.p, s, nullptr, nullptr, 0, nullptr, E.sel.p);
                 launch_gmres_cycle_init(E.S, E.m, E.sel.p, E.nrm.p, E.g.p, E.kdone.p, E.jvec.p, s);
                 for (int c : cyc)
                   {
@@ -1650,6 +1677,109 @@ namespace
     h->d_Pinv64.release();
     if (h->prm.precision_mode != PIBEM_PRECISION_MIXED) // solves on an FP64-accurate operator
       h->d_Pinv64.upload(inv, s);
+  }
+
+  // ILU(0) of the near-field system matrix, the preconditioner the reference
+  // builds in BEMFMA::FMA_preconditioner (bem_fma.cc:3080-3411) and factors
+  // with Trilinos' PreconditionILU at its defaults (no fill, no diagonal
+  // shift; bem_problem.cc:1302): the pattern is each row's near field (the
+  // row's leaf columns), the values S = N (Neumann columns) or -D (Dirichlet
+  // columns) with alpha on the diagonal of unconstrained Neumann rows, and a
+  // constrained row is its constraint line {i: 1, c: +1} as the constraint
+  // matrix stores it (:3190-3201).  The factorisation and the triangular
+  // substitutions run level by level on the device.
+  void build_ilu(pibem_handle *h)
+  {
+    const Plan   &pl = h->plan;
+    const int64_t n  = h->N();
+    cudaStream_t  s  = h->stream;
+    std::vector<int32_t> pos(n, -1), con(n, -2);
+    for (size_t r = 0; r < pl.nrows.size(); ++r)
+      pos[pl.nrows[r]] = int32_t(r);
+    for (size_t k = 0; k < h->con_row.size(); ++k)
+      con[h->con_row[k]] = h->con_col[k];
+    // the sorted columns of row i: a view of its leaf's columns, or the line
+    auto cols_of = [&](int64_t i, int32_t *pair, const int32_t *&c, int64_t &nc) {
+      if (con[i] != -2)
+        {
+          const int32_t j = con[i];
+          nc              = (j >= 0 && j != i) ? 2 : 1;
+          pair[0]         = nc == 2 ? std::min<int32_t>(j, int32_t(i)) : int32_t(i);
+          pair[1]         = nc == 2 ? std::max<int32_t>(j, int32_t(i)) : int32_t(i);
+          c               = pair;
+          return;
+        }
+      if (pos[i] < 0)
+        throw Error(PIBEM_EINVAL, "ILU: a node without a near-field row");
+      const int lf = pl.row_leaf[pos[i]];
+      c            = pl.ncols.data() + pl.ncol_ptr[lf];
+      nc           = pl.ncol_ptr[lf + 1] - pl.ncol_ptr[lf];
+    };
+    std::vector<int64_t> ptr(n + 1, 0), diag(n);
+    std::vector<int32_t> lev_lo(n, 0), lev_up(n, 0);
+    int64_t              max_row = 0;
+    int32_t              pair[2];
+    for (int64_t i = 0; i < n; ++i)
+      {
+        const int32_t *c;
+        int64_t        nc;
+        cols_of(i, pair, c, nc);
+        const int64_t d = std::lower_bound(c, c + nc, int32_t(i)) - c;
+        if (d == nc || c[d] != i)
+          throw Error(PIBEM_EINVAL, "ILU: a near-field row without its diagonal");
+        ptr[i + 1] = ptr[i] + nc;
+        diag[i]    = ptr[i] + d;
+        max_row    = std::max(max_row, nc);
+        int32_t l  = 0;
+        for (int64_t k = 0; k < d; ++k)
+          l = std::max(l, lev_lo[c[k]] + 1);
+        lev_lo[i] = l;
+      }
+    for (int64_t i = n - 1; i >= 0; --i)
+      {
+        const int32_t *c;
+        int64_t        nc;
+        cols_of(i, pair, c, nc);
+        int32_t l = 0;
+        for (int64_t k = diag[i] - ptr[i] + 1; k < nc; ++k)
+          l = std::max(l, lev_up[c[k]] + 1);
+        lev_up[i] = l;
+      }
+    if (max_row * int64_t(sizeof(double) + sizeof(int32_t)) > 200 * 1024)
+      throw Error(PIBEM_EINVAL, "ILU: a near-field row longer than the factorisation's shared memory");
+    // rows grouped by level (ascending row order within a level)
+    auto group = [n](const std::vector<int32_t> &lev, std::vector<int64_t> &lptr,
+                     std::vector<int32_t> &rows) {
+      const int32_t nlev = n ? *std::max_element(lev.begin(), lev.end()) + 1 : 0;
+      lptr.assign(size_t(nlev) + 1, 0);
+      for (int64_t i = 0; i < n; ++i)
+        ++lptr[lev[i] + 1];
+      for (int32_t l = 0; l < nlev; ++l)
+        lptr[l + 1] += lptr[l];
+      rows.resize(n);
+      std::vector<int64_t> at(lptr.begin(), lptr.end() - 1);
+      for (int64_t i = 0; i < n; ++i)
+        rows[at[lev[i]]++] = int32_t(i);
+    };
+    std::vector<int32_t> rows_lo, rows_up;
+    group(lev_lo, h->ilu_lptr_lo, rows_lo);
+    group(lev_up, h->ilu_lptr_up, rows_up);
+    h->d_ilu_ptr.upload(ptr, s);
+    h->d_ilu_diag.upload(diag, s);
+    h->d_ilu_rows_lo.upload(rows_lo, s);
+    h->d_ilu_rows_up.upload(rows_up, s);
+    h->d_ilu_col.alloc(std::max<int64_t>(1, ptr[n]));
+    h->d_ilu_val.alloc(std::max<int64_t>(1, ptr[n]));
+    DBuf<int32_t> d_pos, d_con;
+    d_pos.upload(pos, s);
+    d_con.upload(con, s);
+    launch_ilu_fill(n, h->d_ilu_ptr.p, d_pos.p, h->d_row_leaf.p, h->d_nrow_ptr.p, h->d_ncol_ptr.p,
+                    h->d_nval_ptr.p, h->d_ncols.p, h->d_S.p, d_con.p, h->d_ilu_col.p, h->d_ilu_val.p,
+                    s);
+    launch_ilu_factor(h->ilu_lptr_lo, h->d_ilu_rows_lo.p, h->d_ilu_ptr.p, h->d_ilu_col.p,
+                      h->d_ilu_val.p, h->d_ilu_diag.p, max_row, s);
+    PIBEM_CUDA(cudaStreamSynchronize(s));
+    h->ilu_on = true;
   }
 
   void fill_operator_views(pibem_handle *h)
@@ -2357,8 +2487,11 @@ namespace
       h->op32.Tc = h->d_Tcf.p;
     }
     build_constraints(h);
-    if (h->prm.preconditioner)
+    h->ilu_on = false;
+    if (h->prm.preconditioner == 1)
       build_preconditioner(h);
+    else if (h->prm.preconditioner == 2)
+      build_ilu(h);
     PIBEM_CUDA(cudaStreamSynchronize(s));
     h->bc_ok = true;
   }
@@ -2593,7 +2726,8 @@ extern "C"
         P.precision_mode > PIBEM_PRECISION_FLOAT_FLOAT || P.m2l_engine < PIBEM_M2L_TENSOR_CORE ||
         P.m2l_engine > PIBEM_M2L_CUDA_CORE ||
         (P.m2l_chunk_pairs != 0 && (P.m2l_chunk_pairs < 16 || P.m2l_chunk_pairs > 128)) ||
-        (P.m2l_stages != 0 && P.m2l_stages != 2 && P.m2l_stages != 3))
+        (P.m2l_stages != 0 && P.m2l_stages != 2 && P.m2l_stages != 3) || P.preconditioner < 0 ||
+        P.preconditioner > 2)
       return PIBEM_EINVAL;
     pibem_handle *h = new (std::nothrow) pibem_handle();
     if (!h)
@@ -2701,6 +2835,26 @@ extern "C"
       if (!h->bc_ok)
         throw Error(PIBEM_EINVAL, "pibem_compute_alpha before pibem_set_bc");
       h->d_alpha.download(alpha, h->N(), h->stream);
+      PIBEM_CUDA(cudaStreamSynchronize(h->stream));
+    });
+  }
+
+  int pibem_apply_preconditioner(pibem_handle *h, int32_t R, const double *v, double *z)
+  {
+    return guarded(h, [&] {
+      if (!h->bc_ok)
+        throw Error(PIBEM_EINVAL, "pibem_apply_preconditioner before pibem_set_bc");
+      if (R < 1 || !v || !z)
+        throw Error(PIBEM_EINVAL, "bad arguments");
+      const int64_t N  = h->N();
+      const size_t  n  = size_t(R) * N;
+      HostIO        io{h};
+      double       *dv = io.in(v, n), *dz = io.scratch(n);
+      if (h->prm.preconditioner == 0)
+        PIBEM_CUDA(cudaMemcpyAsync(dz, dv, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      else
+        apply_prec(h, R, dv, N, dz, h->stream);
+      PIBEM_CUDA(cudaMemcpyAsync(z, dz, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
       PIBEM_CUDA(cudaStreamSynchronize(h->stream));
     });
   }

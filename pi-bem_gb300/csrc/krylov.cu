@@ -579,6 +579,150 @@ namespace pibem
         }
     }
 
+    // ---- ILU(0) of the near-field system matrix (preconditioner 2) ----------
+    // CSR in node order: ptr, col (ascending), val, diag (position of the
+    // diagonal).  Level sets: the rows of a level depend only on rows of
+    // earlier levels (lower part for the factorisation and the forward
+    // substitution, upper part for the backward one).
+
+    // one row of the near field (or a constraint line) into the CSR: warp per node
+    __global__ void ilu_fill_kernel(int64_t n, const int64_t *__restrict__ ptr,
+                                    const int32_t *__restrict__ pos, const int32_t *__restrict__ row_leaf,
+                                    const int64_t *__restrict__ nrow_ptr, const int64_t *__restrict__ ncol_ptr,
+                                    const int64_t *__restrict__ nval_ptr, const int32_t *__restrict__ ncols,
+                                    const double *__restrict__ S, const int32_t *__restrict__ con,
+                                    int32_t *__restrict__ col, double *__restrict__ val)
+    {
+      const int64_t i    = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+      const int     lane = threadIdx.x & 31;
+      if (i >= n)
+        return;
+      const int64_t o = ptr[i];
+      if (con[i] != -2)
+        {
+          // a constrained row: 1 on the diagonal and +1 at the line's column
+          // (bem_fma.cc:3190-3201 stores the constraint entries as they are)
+          if (lane == 0)
+            {
+              const int c = con[i];
+              if (c >= 0 && c != int(i))
+                {
+                  const bool lo = c < int(i);
+                  col[o]        = lo ? c : int32_t(i);
+                  col[o + 1]    = lo ? int32_t(i) : c;
+                  val[o]        = 1.0;
+                  val[o + 1]    = 1.0;
+                }
+              else
+                {
+                  col[o] = int32_t(i);
+                  val[o] = 1.0;
+                }
+            }
+          return;
+        }
+      const int     r  = pos[i];
+      const int     lf = row_leaf[r];
+      const int64_t c0 = ncol_ptr[lf], nc = ncol_ptr[lf + 1] - c0;
+      const int64_t ld = (nc + 3) / 4 * 4;
+      const double *v  = S + nval_ptr[lf] + (r - nrow_ptr[lf]) * ld;
+      for (int64_t k = lane; k < nc; k += 32)
+        {
+          col[o + k] = ncols[c0 + k];
+          val[o + k] = v[k];
+        }
+    }
+
+    // IKJ ILU(0) of the rows of one level, a block per row with the row in
+    // shared memory: for the row's columns k < i in ascending order,
+    // a_ik /= a_kk, then a_ij -= a_ik a_kj for the columns j > k of row k that
+    // row i holds (threads take row k's entries, a binary search finds j in
+    // the row's sorted columns); row k is final (an earlier level)
+    __global__ void ilu_factor_kernel(const int32_t *__restrict__ rows, const int64_t *__restrict__ ptr,
+                                      const int32_t *__restrict__ col, double *__restrict__ val,
+                                      const int64_t *__restrict__ diag)
+    {
+      extern __shared__ __align__(16) unsigned char ilu_smem[];
+      const int     i  = rows[blockIdx.x];
+      const int64_t a0 = ptr[i], n = ptr[i + 1] - a0, nd = diag[i] - a0;
+      double       *sv = reinterpret_cast<double *>(ilu_smem);
+      int32_t      *sc = reinterpret_cast<int32_t *>(sv + n);
+      for (int64_t e = threadIdx.x; e < n; e += blockDim.x)
+        {
+          sv[e] = val[a0 + e];
+          sc[e] = col[a0 + e];
+        }
+      __syncthreads();
+      for (int64_t e = 0; e < nd; ++e)
+        {
+          const int     k   = sc[e];
+          const int64_t dk  = diag[k], k1 = ptr[k + 1];
+          const double  lik = sv[e] / val[dk];
+          for (int64_t f = dk + 1 + threadIdx.x; f < k1; f += blockDim.x)
+            {
+              const int j  = col[f];
+              int64_t   lo = e + 1, hi = n;
+              while (lo < hi)
+                {
+                  const int64_t m = (lo + hi) >> 1;
+                  if (sc[m] < j)
+                    lo = m + 1;
+                  else
+                    hi = m;
+                }
+              if (lo < n && sc[lo] == j)
+                sv[lo] -= lik * val[f];
+            }
+          __syncthreads();
+          if (threadIdx.x == 0)
+            sv[e] = lik;
+        }
+      __syncthreads();
+      for (int64_t e = threadIdx.x; e < n; e += blockDim.x)
+        val[a0 + e] = sv[e];
+    }
+
+    // z[r] = v[r] for the columns with sel[r] (v column stride ldv, z stride n)
+    __global__ void copy_sel_kernel(int64_t n, int R, const double *__restrict__ v, int64_t ldv,
+                                    double *__restrict__ z, const int *__restrict__ sel)
+    {
+      const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * R)
+        return;
+      const int64_t r = idx / n, t = idx - r * n;
+      if (sel && !sel[r])
+        return;
+      z[idx] = v[r * ldv + t];
+    }
+
+    // forward (lower, unit diagonal) or backward (upper) substitution for the
+    // rows of one level, in place on the selected columns of z (stride n):
+    // warp per (row, column), lanes over the row's entries, fixed butterfly
+    template <bool FWD>
+    __global__ void ilu_solve_kernel(int nrows, const int32_t *__restrict__ rows, int R, int64_t n,
+                                     const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                     const double *__restrict__ val, const int64_t *__restrict__ diag,
+                                     double *__restrict__ z, const int *__restrict__ sel,
+                                     const int *__restrict__ jvec)
+    {
+      const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+      const int lane = threadIdx.x & 31;
+      if (w >= nrows * R)
+        return;
+      const int r = w / nrows, i = rows[w - r * nrows];
+      if ((sel && !sel[r]) || (jvec && jvec[r] < 0))
+        return;
+      double       *zr = z + int64_t(r) * n;
+      const int64_t a0 = FWD ? ptr[i] : diag[i] + 1, a1 = FWD ? diag[i] : ptr[i + 1];
+      double        s  = 0;
+      for (int64_t e = a0 + lane; e < a1; e += 32)
+        s += val[e] * zr[col[e]];
+      for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0)
+        zr[i] = FWD ? zr[i] - s : (zr[i] - s) / val[diag[i]];
+    }
+
     template <typename T>
     __global__ void combine_p2m_kernel(int64_t n, int K4, const int32_t *__restrict__ prow_dof,
                                        const uint8_t *__restrict__ dir, const T *__restrict__ T1,
@@ -876,6 +1020,75 @@ namespace pibem
                                            const int32_t *, const double *, const double *, int64_t,
                                            double *, cudaStream_t, const double *, double *, int64_t,
                                            const int *, const int *);
+
+  void launch_ilu_fill(int64_t n, const int64_t *ptr, const int32_t *pos, const int32_t *row_leaf,
+                       const int64_t *nrow_ptr, const int64_t *ncol_ptr, const int64_t *nval_ptr,
+                       const int32_t *ncols, const double *S, const int32_t *con, int32_t *col,
+                       double *val, cudaStream_t s)
+  {
+    if (n == 0)
+      return;
+    ilu_fill_kernel<<<nblocks(n * 32), 256, 0, s>>>(n, ptr, pos, row_leaf, nrow_ptr, ncol_ptr, nval_ptr,
+                                                    ncols, S, con, col, val);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_ilu_factor(const std::vector<int64_t> &lptr, const int32_t *rows, const int64_t *ptr,
+                         const int32_t *col, double *val, const int64_t *diag, int64_t max_row,
+                         cudaStream_t s)
+  {
+    const size_t smem = size_t(max_row) * (sizeof(double) + sizeof(int32_t));
+    if (smem > 48 * 1024)
+      PIBEM_CUDA(cudaFuncSetAttribute(ilu_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(smem)));
+    for (size_t l = 0; l + 1 < lptr.size(); ++l)
+      {
+        const int64_t nr = lptr[l + 1] - lptr[l];
+        if (nr == 0)
+          continue;
+        ilu_factor_kernel<<<unsigned(nr), 256, smem, s>>>(rows + lptr[l], ptr, col, val, diag);
+        note_launch();
+      }
+    PIBEM_CUDA(cudaGetLastError());
+  }
+
+  void launch_copy_sel(int64_t n, int R, const double *v, int64_t ldv, double *z, const int *sel,
+                       cudaStream_t s)
+  {
+    if (n * R == 0)
+      return;
+    copy_sel_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, v, ldv, z, sel);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_ilu_apply(const std::vector<int64_t> &lptr_lo, const int32_t *rows_lo,
+                        const std::vector<int64_t> &lptr_up, const int32_t *rows_up, int R, int64_t n,
+                        const int64_t *ptr, const int32_t *col, const double *val,
+                        const int64_t *diag, double *z, const int *sel, const int *jvec,
+                        cudaStream_t s)
+  {
+    for (size_t l = 0; l + 1 < lptr_lo.size(); ++l)
+      {
+        const int nr = int(lptr_lo[l + 1] - lptr_lo[l]);
+        if (nr == 0)
+          continue;
+        ilu_solve_kernel<true><<<nblocks(int64_t(nr) * R * 32), 256, 0, s>>>(
+          nr, rows_lo + lptr_lo[l], R, n, ptr, col, val, diag, z, sel, jvec);
+        note_launch();
+      }
+    for (size_t l = 0; l + 1 < lptr_up.size(); ++l)
+      {
+        const int nr = int(lptr_up[l + 1] - lptr_up[l]);
+        if (nr == 0)
+          continue;
+        ilu_solve_kernel<false><<<nblocks(int64_t(nr) * R * 32), 256, 0, s>>>(
+          nr, rows_up + lptr_up[l], R, n, ptr, col, val, diag, z, sel, jvec);
+        note_launch();
+      }
+    PIBEM_CUDA(cudaGetLastError());
+  }
 
   template <typename T>
   void launch_combine_p2m(int64_t n_rows, int K4, const int32_t *prow_dof, const uint8_t *dir,

@@ -1,6 +1,8 @@
 // Launchers of the vector kernels (krylov.cu).
 #pragma once
 
+#include <vector>
+
 #include "kernels.h"
 
 namespace pibem
@@ -46,6 +48,26 @@ namespace pibem
                         double *y, cudaStream_t s);
   // x[r] -= sqrt(nrm2[r])
   void launch_sub_norm(int64_t n, int R, const double *nrm2, double *x, cudaStream_t s);
+  // ILU(0) of the near-field system matrix: the CSR rows (node order) from the
+  // leaf blocks (con[i] != -2: a constraint line with column con[i]); the
+  // factorisation level by level (lptr over rows, max_row the longest row);
+  // and z = (L U)^-1 z in place on the columns r < R with sel[r] (if sel) and
+  // jvec[r] >= 0 (if jvec)
+  void launch_ilu_fill(int64_t n, const int64_t *ptr, const int32_t *pos, const int32_t *row_leaf,
+                       const int64_t *nrow_ptr, const int64_t *ncol_ptr, const int64_t *nval_ptr,
+                       const int32_t *ncols, const double *S, const int32_t *con, int32_t *col,
+                       double *val, cudaStream_t s);
+  void launch_ilu_factor(const std::vector<int64_t> &lptr, const int32_t *rows, const int64_t *ptr,
+                         const int32_t *col, double *val, const int64_t *diag, int64_t max_row,
+                         cudaStream_t s);
+  void launch_ilu_apply(const std::vector<int64_t> &lptr_lo, const int32_t *rows_lo,
+                        const std::vector<int64_t> &lptr_up, const int32_t *rows_up, int R, int64_t n,
+                        const int64_t *ptr, const int32_t *col, const double *val,
+                        const int64_t *diag, double *z, const int *sel, const int *jvec,
+                        cudaStream_t s);
+  // z[r] = v[r] (column strides ldv, n) for the columns r with sel[r] (all if !sel)
+  void launch_copy_sel(int64_t n, int R, const double *v, int64_t ldv, double *z, const int *sel,
+                       cudaStream_t s);
   void launch_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s);
   void launch_rhs_combine(int64_t n, int R, const double *tmp, const uint8_t *dir,
                           const double *alpha, const double *oN, const double *oD, double *rhs,

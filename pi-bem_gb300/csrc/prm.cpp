@@ -129,7 +129,9 @@ extern "C" int pibem_params_from_prm(pibem_params *p, const char *text)
                                       ? PIBEM_PRECISION_FLOAT_FLOAT
                                       : PIBEM_PRECISION_FP64;
           else if (key == "Preconditioner")
-            p->preconditioner = (val == "none" || val == "None" || val == "0") ? 0 : 1;
+            p->preconditioner = (val == "none" || val == "None" || val == "0")  ? 0
+                                : (val == "ILU" || val == "ilu" || val == "2") ? 2
+                                                                              : 1;
           else if (key == "GMRES restart")
             p->gmres_restart = std::atoi(v);
           else if (key == "Inner tolerance")

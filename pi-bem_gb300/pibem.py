@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "libpibem_gb300.so")
 OK, EINVAL, ENOMEM_HBM, ENOCONV, ETIMEDOUT, ECUDA, EAGAIN = 0, 1, 2, 3, 4, 5, 6
 PRECISION_FP64, PRECISION_MIXED, PRECISION_FLOAT_FLOAT = 0, 1, 2
 M2L_TENSOR_CORE, M2L_CUDA_CORE = 0, 1
+PREC_NONE, PREC_BLOCK_JACOBI, PREC_ILU = 0, 1, 2
 
 
 class Params(C.Structure):
@@ -102,7 +103,7 @@ EXPORTS = [
     "pibem_dirichlet_mask_from_materials", "pibem_compute_normals",
     "pibem_compute_surface_gradients", "pibem_compute_gradients", "pibem_setup_phases",
     "pibem_slots_open", "pibem_slots_submit", "pibem_slots_step", "pibem_slots_collect",
-    "pibem_slots_close",
+    "pibem_slots_close", "pibem_apply_preconditioner",
 ]
 
 _dp = C.POINTER(C.c_double)
@@ -131,6 +132,7 @@ def load():
     L.pibem_fmm_matvec.argtypes = [C.c_void_p, C.c_int32, _dp, _dp, _dp, _dp]
     L.pibem_compute_alpha.argtypes = [C.c_void_p, _dp]
     L.pibem_system_matvec.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
+    L.pibem_apply_preconditioner.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
     L.pibem_compute_rhs.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
     L.pibem_solve.argtypes = [C.c_void_p, C.c_int32, _dp, _dp, _dp, C.POINTER(SolveStats)]
     L.pibem_solve_device.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -320,6 +322,14 @@ class BEMSolver:
         y = np.zeros_like(x)
         self._check(self.L.pibem_system_matvec(self.h, x.size // self.n, _d(x), _d(y)))
         return y
+
+    def apply_preconditioner(self, v):
+        """z = P^-1 v with the handle's preconditioner (PreconditionILU::vmult
+        for preconditioner 2)."""
+        v = np.ascontiguousarray(v, np.float64)
+        z = np.zeros_like(v)
+        self._check(self.L.pibem_apply_preconditioner(self.h, v.size // self.n, _d(v), _d(z)))
+        return z
 
     def rhs(self, tmp_rhs):
         t = np.ascontiguousarray(tmp_rhs, np.float64)
