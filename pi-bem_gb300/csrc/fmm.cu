@@ -16,6 +16,7 @@
 #include "devmath.cuh"
 #include "ffmath.cuh"
 #include "kernels.h"
+#include "pdl.cuh"
 
 namespace pibem
 {
@@ -85,6 +86,7 @@ namespace pibem
                        const T *__restrict__ vals, const T *__restrict__ x, T *__restrict__ y,
                        bool acc)
     {
+      pdl_entry();
       extern __shared__ __align__(16) unsigned char smem_raw[];
       T            *sx   = reinterpret_cast<T *>(smem_raw); // [rb][ld]
       const int     leaf = blockIdx.x;
@@ -192,6 +194,7 @@ namespace pibem
                             const int32_t *__restrict__ ncols, const T *__restrict__ vals,
                             const T *__restrict__ x, T *__restrict__ y, bool acc)
     {
+      pdl_entry();
       extern __shared__ __align__(16) unsigned char smem_raw[];
       T        *sxb  = reinterpret_cast<T *>(smem_raw); // [2][ld_max]
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -368,6 +371,7 @@ namespace pibem
                        const uint8_t *__restrict__ dir, const uint8_t *__restrict__ modes,
                        const T *__restrict__ x, T *__restrict__ M)
     {
+      pdl_entry();
       const int leaf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
       if (leaf >= n_leaves)
         return;
@@ -721,6 +725,7 @@ namespace pibem
                                     const double *__restrict__ delta, const T *__restrict__ M,
                                     T *__restrict__ scratch)
     {
+      pdl_entry();
       const int64_t it = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (it >= n_items)
         return;
@@ -856,6 +861,7 @@ namespace pibem
                      const int64_t *__restrict__ item_ptr, const int32_t *__restrict__ tnodes,
                      const T *__restrict__ scratch, T *__restrict__ y)
     {
+      pdl_entry();
       const int ti = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
       if (ti >= n_tgt)
         return;
@@ -899,6 +905,7 @@ namespace pibem
                  const int32_t *__restrict__ lleaf_box, const int32_t *__restrict__ nrows,
                  const T *__restrict__ W, const T *__restrict__ Lx, T *__restrict__ y)
     {
+      pdl_entry();
       const int leaf = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
       if (leaf >= n_leaves)
         return;
@@ -1056,7 +1063,7 @@ namespace pibem
         if (smem1 > 48 * 1024)
           raise_smem_limit(reinterpret_cast<const void *>(kern), smem1);
         const int grid = std::min(op.n_near_leaves, MINB * near_sm_count());
-        kern<<<grid, 256, smem1, s>>>(op.n_near_leaves, int(maxnc), op.nrow_ptr, op.ncol_ptr,
+        launch_pdl(kern, grid, 256, smem1, s, op.n_near_leaves, int(maxnc), op.nrow_ptr, op.ncol_ptr,
                                       op.nval_ptr, op.nrows, op.ncols, vals, x, y, accumulate);
         PIBEM_CUDA(cudaGetLastError());
         note_launch();
@@ -1065,7 +1072,7 @@ namespace pibem
     auto kern = near_leaf_kernel<T, false>;
     if (smem > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
-    kern<<<op.n_near_leaves, 256, smem, s>>>(R, rb, N, op.nrow_ptr, op.ncol_ptr, op.nval_ptr,
+    launch_pdl(kern, op.n_near_leaves, 256, smem, s, R, rb, N, op.nrow_ptr, op.ncol_ptr, op.nval_ptr,
                                              op.nrows, op.ncols, vals, x, y, accumulate);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
@@ -1107,7 +1114,7 @@ namespace pibem
     const unsigned grid = unsigned((op.n_p2m_leaves + 7) / 8);
     const bool     comb = combined && op.Tc;
     auto launch = [&](auto kern) {
-      kern<<<grid, 256, 0, s>>>(op.n_p2m_leaves, R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof,
+      launch_pdl(kern, grid, 256, 0, s, op.n_p2m_leaves, R, op.K, N, op.prow_ptr, op.pleaf_box, op.prow_dof,
                                 comb ? op.Tc : op.T1, op.T2, dir, modes, x, M);
     };
     if (comb)
@@ -1337,13 +1344,13 @@ namespace pibem
   {
     if (op.n_m2p_tgt == 0)
       return;
-    m2p_eval_kernel<T><<<unsigned((op.n_m2p_items + 127) / 128), 128, 0, s>>>(
+    launch_pdl(m2p_eval_kernel<T>, unsigned((op.n_m2p_items + 127) / 128), 128, 0, s, 
       op.n_m2p_items, R, op.K, op.p, op.m2p_item_ptr, op.m2p_item_pair, op.m2p_pair_tgt,
       op.m2p_tgt, op.m2p_src, op.m2p_tnode_ptr, op.m2p_tnodes, td.xyz, td.center, td.delta, M,
       op.m2p_scratch);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
-    m2p_sum_kernel<T><<<unsigned((op.n_m2p_tgt + 7) / 8), 256, 0, s>>>(
+    launch_pdl(m2p_sum_kernel<T>, unsigned((op.n_m2p_tgt + 7) / 8), 256, 0, s, 
       op.n_m2p_tgt, R, N, op.n_m2p_items, op.m2p_tnode_ptr, op.m2p_tgt, op.m2p_src_ptr,
       op.m2p_item_ptr, op.m2p_tnodes, op.m2p_scratch, y);
     PIBEM_CUDA(cudaGetLastError());
@@ -1386,7 +1393,7 @@ namespace pibem
   {
     if (op.n_rows == 0 || op.n_near_leaves == 0)
       return;
-    l2p_kernel<T><<<unsigned((op.n_near_leaves + 7) / 8), 256, 0, s>>>(
+    launch_pdl(l2p_kernel<T>, unsigned((op.n_near_leaves + 7) / 8), 256, 0, s, 
       op.n_near_leaves, R, op.K, N, op.nrow_ptr, op.lleaf_box, op.nrows, op.W, Lx, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();

@@ -5,6 +5,7 @@
 #include <algorithm>
 
 #include "krylov.h"
+#include "pdl.cuh"
 
 namespace pibem
 {
@@ -106,6 +107,7 @@ namespace pibem
                       double *__restrict__ partial, int *__restrict__ ticket,
                       double *__restrict__ out, const int *__restrict__ jvec, int ldo)
     {
+      pdl_entry();
       if (jvec)
         {
           const int j = jvec[blockIdx.y];
@@ -181,6 +183,7 @@ namespace pibem
                                      int64_t ldr, const int *__restrict__ jvec,
                                      double *__restrict__ z, const int *__restrict__ sel)
     {
+      pdl_entry();
       int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * R)
         return;
@@ -243,6 +246,7 @@ namespace pibem
                                         const double *__restrict__ tol, int *__restrict__ ctl,
                                         cudaGraphConditionalHandle cond, int use_cond)
     {
+      pdl_entry();
       const int L = m + 1;
       __shared__ int ended, active, alive;
       if (threadIdx.x == 0)
@@ -340,6 +344,7 @@ namespace pibem
                                        const double *__restrict__ src, int64_t lds,
                                        double *__restrict__ dst)
     {
+      pdl_entry();
       const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * Rc)
         return;
@@ -351,6 +356,7 @@ namespace pibem
                                         const double *__restrict__ src, double *__restrict__ dst,
                                         int64_t ldd)
     {
+      pdl_entry();
       const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (idx >= n * Rc)
         return;
@@ -378,12 +384,14 @@ namespace pibem
 
     __global__ void d2f_kernel(int64_t n, const double *__restrict__ a, float *__restrict__ b)
     {
+      pdl_entry();
       int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (i < n)
         b[i] = float(a[i]);
     }
     __global__ void f2d_kernel(int64_t n, const float *__restrict__ a, double *__restrict__ b)
     {
+      pdl_entry();
       int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (i < n)
         b[i] = double(a[i]);
@@ -516,6 +524,7 @@ namespace pibem
                          const double *__restrict__ nrm2, double *__restrict__ vout, int64_t ldo,
                          const int *__restrict__ jvec, const int *__restrict__ sel)
     {
+      pdl_entry();
       extern __shared__ __align__(8) unsigned char sv_raw[];
       P        *sv_all = reinterpret_cast<P *>(sv_raw);
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -743,6 +752,7 @@ namespace pibem
                                           const int32_t *__restrict__ cols,
                                           const double *__restrict__ x, double *__restrict__ y)
     {
+      pdl_entry();
       const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
       if (t >= int64_t(n_con) * R)
         return;
@@ -806,13 +816,13 @@ namespace pibem
     if (ldo <= 0)
       ldo = mode == 2 ? 1 : ncols;
     if (mode == 0)
-      cgs_step_kernel<0><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
+      launch_pdl(cgs_step_kernel<0>, grid, kDotBlock, 0, s, n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
                                                      ticket, out, jvec, ldo);
     else if (mode == 1)
-      cgs_step_kernel<1><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
+      launch_pdl(cgs_step_kernel<1>, grid, kDotBlock, 0, s, n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
                                                      ticket, out, jvec, ldo);
     else
-      cgs_step_kernel<2><<<grid, kDotBlock, 0, s>>>(n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
+      launch_pdl(cgs_step_kernel<2>, grid, kDotBlock, 0, s, n, ncols, ldv, ldr, V, hin, ldh, w, nblk, partial,
                                                      ticket, out, jvec, ldo);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
@@ -831,7 +841,7 @@ namespace pibem
   void launch_normalize(int64_t n, int R, const double *w, const double *nrm2, double *out,
                         int64_t ldr, cudaStream_t s, const int *jvec, double *z, const int *sel)
   {
-    normalize_kernel<<<nblocks(n * R), 256, 0, s>>>(n, R, w, nrm2, out, ldr, jvec, z, sel);
+    launch_pdl(normalize_kernel, nblocks(n * R), 256, 0, s, n, R, w, nrm2, out, ldr, jvec, z, sel);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -849,7 +859,7 @@ namespace pibem
                            const double *bn, const double *tol, int *ctl,
                            cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s)
   {
-    gmres_givens_kernel<<<1, 256, 0, s>>>(R, m, hb, H, cs, sn, g, kdone, jvec, its, maxit, bn, tol,
+    launch_pdl(gmres_givens_kernel, 1, 256, 0, s, R, m, hb, H, cs, sn, g, kdone, jvec, its, maxit, bn, tol,
                                           ctl, cond, use_cond ? 1 : 0);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
@@ -868,7 +878,7 @@ namespace pibem
   {
     if (Rc == 0)
       return;
-    gather_cols_kernel<<<nblocks(n * Rc), 256, 0, s>>>(n, Rc, cols, src, lds, dst);
+    launch_pdl(gather_cols_kernel, nblocks(n * Rc), 256, 0, s, n, Rc, cols, src, lds, dst);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -878,7 +888,7 @@ namespace pibem
   {
     if (Rc == 0)
       return;
-    scatter_cols_kernel<<<nblocks(n * Rc), 256, 0, s>>>(n, Rc, cols, src, dst, ldd);
+    launch_pdl(scatter_cols_kernel, nblocks(n * Rc), 256, 0, s, n, Rc, cols, src, dst, ldd);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -904,7 +914,7 @@ namespace pibem
   {
     if (n == 0)
       return;
-    d2f_kernel<<<nblocks(n), 256, 0, s>>>(n, a, b);
+    launch_pdl(d2f_kernel, nblocks(n), 256, 0, s, n, a, b);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -912,7 +922,7 @@ namespace pibem
   {
     if (n == 0)
       return;
-    f2d_kernel<<<nblocks(n), 256, 0, s>>>(n, a, b);
+    launch_pdl(f2d_kernel, nblocks(n), 256, 0, s, n, a, b);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -962,7 +972,7 @@ namespace pibem
   {
     if (n_con == 0 || R == 0)
       return;
-    constrain_rows_kernel<<<nblocks(int64_t(n_con) * R), 256, 0, s>>>(n_con, R, n, rows, cols, x, y);
+    launch_pdl(constrain_rows_kernel, nblocks(int64_t(n_con) * R), 256, 0, s, n_con, R, n, rows, cols, x, y);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }
@@ -1006,7 +1016,7 @@ namespace pibem
     const size_t smem = size_t(8) * mr * sizeof(P);
     if (smem > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(block_apply_kernel<P>), smem);
-    block_apply_kernel<P><<<(n_leaves + 7) / 8, 256, smem, s>>>(n_leaves, mr, R, n, ldv, row_ptr,
+    launch_pdl(block_apply_kernel<P>, (n_leaves + 7) / 8, 256, smem, s, n_leaves, mr, R, n, ldv, row_ptr,
                                                                 blk_ptr, rows, Pinv, v, z, nrm2,
                                                                 vout, ldo, jvec, sel);
     PIBEM_CUDA(cudaGetLastError());

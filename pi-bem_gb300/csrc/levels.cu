@@ -29,6 +29,7 @@
 
 #include "async_copy.cuh"
 #include "kernels.h"
+#include "pdl.cuh"
 
 namespace pibem
 {
@@ -136,6 +137,7 @@ namespace pibem
                      const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
                      const float *__restrict__ Y, float *__restrict__ Lx)
     {
+      pdl_entry();
       const int64_t col = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
       if (col >= ncols)
         return;
@@ -298,6 +300,7 @@ namespace pibem
                             const int32_t *__restrict__ child8, const float *__restrict__ lvops,
                             float *__restrict__ M, int *__restrict__ err)
     {
+      pdl_entry();
       extern __shared__ __align__(16) float lv_sm[];
       __shared__ uint64_t ops_bar;
       const int Kx = lv_kx(K), KK = lv_kk(K);
@@ -400,6 +403,7 @@ namespace pibem
                             const float *__restrict__ lvops, float *__restrict__ Lx,
                             int *__restrict__ err)
     {
+      pdl_entry();
       extern __shared__ __align__(16) float lv_sm[];
       __shared__ uint64_t ops_bar;
       const int Kx = lv_kx(K), KK = lv_kk(K);
@@ -517,9 +521,8 @@ namespace pibem
         const dim3   grid(unsigned(std::min<int64_t>(lv_n_sm(), (ncols + cpb - 1) / cpb)));
         auto launch = [&](auto kern) {
           raise_smem_limit(reinterpret_cast<const void *>(kern), smem);
-          kern<<<grid, 8 * lv_kt(K), smem, s>>>(R, K, ncols, op.up_box + a,
-                                                op.up_child8 + size_t(8) * a, op.lv_ops, M,
-                                                op.dev_err);
+          launch_pdl(kern, grid, 8 * lv_kt(K), smem, s, R, K, ncols, op.up_box + a,
+                     op.up_child8 + size_t(8) * a, op.lv_ops, M, op.dev_err);
         };
         switch (cpb)
           {
@@ -557,7 +560,7 @@ namespace pibem
     if (b <= a)
       return;
     const int64_t ncols = int64_t(b - a) * R;
-    m2l_sum_kernel<<<unsigned((ncols + 7) / 8), 256, 0, s>>>(
+    launch_pdl(m2l_sum_kernel, unsigned((ncols + 7) / 8), 256, 0, s,
       R, op.K, ncols, op.down_box + a, op.down_m2l_beg + a, op.down_m2l_end + a, Y, Lx);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
@@ -575,7 +578,7 @@ namespace pibem
       {
         const size_t smem = lv_smem_bytes(K);
         raise_smem_limit(reinterpret_cast<const void *>(l2l_level_smem_kernel), smem);
-        l2l_level_smem_kernel<<<unsigned(std::min(lv_n_sm(), ncols)), 8 * lv_kt(K), smem, s>>>(
+        launch_pdl(l2l_level_smem_kernel, unsigned(std::min(lv_n_sm(), ncols)), 8 * lv_kt(K), smem, s,
           R, K, ncols, op.down_box + a, op.down_par + a, op.down_oct + a,
           op.lv_ops + size_t(8) * lv_kk(K), Lx, op.dev_err);
         PIBEM_CUDA(cudaGetLastError());

@@ -41,6 +41,7 @@
 #include "async_copy.cuh"
 #include "tcgen05.cuh"
 #include "kernels.h"
+#include "pdl.cuh"
 
 namespace pibem
 {
@@ -154,6 +155,7 @@ namespace pibem
                      float *__restrict__ Y, const int32_t *__restrict__ yslot, int ldy,
                      int *__restrict__ err)
     {
+      pdl_entry();
       extern __shared__ uint8_t smem_raw[];
       __shared__ uint32_t       tmem_slot;
       __shared__ volatile int   abort_flag;
@@ -609,7 +611,7 @@ namespace pibem
     auto       fn  = g.stages == 3 ? (all ? tc_gemm_kernel<true, 3> : tc_gemm_kernel<false, 3>)
                                    : (all ? tc_gemm_kernel<true, 2> : tc_gemm_kernel<false, 2>);
     raise_smem_limit(reinterpret_cast<const void *>(fn), g.smem);
-    fn<<<std::min(nch, std::max(n_sm, 1)), TC_THREADS, g.smem, s>>>(
+    launch_pdl(fn, std::min(nch, std::max(n_sm, 1)), TC_THREADS, g.smem, s,
       R, op.K, g.Np, g.Kp / TC_KC, c0, nch, op.ch_start, op.ch_cnt, op.ch_op, op.q_src,
       op.tc_images, E, Y, yslot, ldy, err);
     PIBEM_CUDA(cudaGetLastError());
