@@ -380,10 +380,27 @@ def run_ours(args, w, rank, world, local):
         for prec, (pt, c) in (("fp32", ph32[0]), ("fp64", ph32[1]))}
     if rank == 0 and world == 1 and not args.no_cpu_baseline and w.get("cpu", True):
         line["cpu_baseline"] = cpu_baseline(w, mesh, mask, st64[-1]["fp64_matvecs"])
-    if rank == 0:
-        print(json.dumps(line))
     g32.close()
     g64.close()
+    if world == 1 and args.workload == "spheroid98k" and not args.no_served:
+        # the request stream of --workload served, shortened (36 requests, 24
+        # timed), so that the default run also reports the served figures
+        try:
+            summary, config, _, clocks = served_stream(local, 36)
+            keep = ("value", "unit", "p50_ms", "p99_ms", "slowdown_p50", "slowdown_p99", "slowdown",
+                    "mean_alone_service_ms_8rhs", "offered_solves_per_s", "worst_relative_residual",
+                    "server")
+            line["served"] = {k: summary[k] for k in keep} | {
+                "config": {k: config[k] for k in ("requests_timed", "offered_load", "workers",
+                                                  "max_batch_rhs")}
+                | {"meshes": len(config["meshes"]),
+                   "nodes_min_max": [min(n for _, n in config["meshes"]),
+                                     max(n for _, n in config["meshes"])]},
+                "clocks": clocks}
+        except Exception as e:  # the headline line stands without it
+            line["served"] = {"error": f"{type(e).__name__}: {e}"}
+    if rank == 0:
+        print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
 
@@ -607,17 +624,15 @@ def run_batched(args, w, rank, world, local):
     _done_dist(world)
 
 
-def run_served(args, w, rank, world, local):
-    """Poisson request stream over a pool of meshes through serve.BEMServer."""
-    import threading as th
-
+def served_stream(local, n_req, n_warm=12, load=0.8, workers=4, max_batch_rhs=16, **server_kw):
+    """Poisson request stream over a pool of 12 meshes through serve.BEMServer;
+    returns (summary dict, config dict, launches, clocks)."""
     import torch
 
     import pibem
     import serve
     import synthetic as S
 
-    dev = _init_dist(world, local)
     rng = np.random.Generator(np.random.PCG64(5))
     pool = []
     for i in range(12):
@@ -640,25 +655,32 @@ def run_served(args, w, rank, world, local):
             cols.append(S.point_source_data(mesh, mask, src, r.uniform(-1, 1, 8))[0])
         return np.stack(cols)
 
-    srv = serve.BEMServer(hbm_budget_gb=150.0, workers=4, max_batch_rhs=16, **prm)
+    srv = serve.BEMServer(hbm_budget_gb=150.0, workers=workers, max_batch_rhs=max_batch_rhs,
+                          **server_kw, **prm)
     t0 = time.perf_counter()
     for mid, mesh, mask, _ in pool:
         srv.add_mesh(mid, mesh.xyz, mesh.cells, mask)
         srv.preload(mid)
     setup_s = time.perf_counter() - t0
-    # service time of one mean-sized request (8 RHS) per mesh, alone: sets the arrival rate
-    svc = []
-    for j, (mid, mesh, mask, kind) in enumerate(pool):
-        for _ in range(2):
-            r = srv.submit(mid, rhs(mesh, mask, kind, 9000 + j, 8))
-            r.wait()
-            if r.error:
-                raise r.error
-        svc.append(r.end - r.start)
-    mean_svc = float(np.mean(svc))
-    lam = 0.8 / mean_svc  # offered load 0.8 of one-at-a-time capacity
-    n_req = 24 + 12 * args.steps
-    n_warm = 12
+
+    def alone(j, R, seed):
+        mid, mesh, mask, kind = pool[j]
+        r = srv.submit(mid, rhs(mesh, mask, kind, seed, R))
+        r.wait()
+        if r.error:
+            raise r.error
+        return r.end - r.start
+
+    # service time alone of each mesh at 1, 8 and 16 RHS (the second of two
+    # runs); 8 RHS sets the arrival rate, and a request's slowdown is its
+    # latency over its service time alone (interpolated linearly in the RHS count)
+    t_alone = {}
+    for j in range(len(pool)):
+        for R in (1, 8, 16):
+            alone(j, R, 9000 + j)
+            t_alone[(j, R)] = alone(j, R, 9000 + j)
+    mean_svc = float(np.mean([t_alone[(j, 8)] for j in range(len(pool))]))
+    lam = load / mean_svc
     gaps = rng.exponential(1.0 / lam, n_req)
     picks = rng.integers(0, len(pool), n_req)
     nrhs = rng.integers(1, 17, n_req)
@@ -682,32 +704,53 @@ def run_served(args, w, rank, world, local):
         torch.cuda.synchronize()
     launches = pibem.launch_count() - l0
     timed = reqs[n_warm:]
+    tk = picks[n_warm:]
     lat = np.array([r.latency for r in timed]) * 1e3
+
+    def t_est(j, R):
+        t1, t16 = t_alone[(j, 1)], t_alone[(j, 16)]
+        return t1 + (t16 - t1) * (R - 1) / 15.0
+
+    slow = np.array([r.latency / t_est(int(j), r.nrhs) for r, j in zip(timed, tk)])
     span = max(r.end for r in timed) - min(r.arrival for r in timed)
     cols = sum(r.nrhs for r in timed)
-    value = cols / span
     worst = max(r.stats["relative_residual"] for r in reqs)
     resident = srv.resident_bytes()
     counters = dict(srv.counters)
     srv.close()
     h2d = sum(3 * r.nrhs * r.tmp.shape[1] * 8 for r in timed) / len(timed)
-    line = _base_line(w, args, world, value, "solves/s", float(np.mean(lat)),
-                      "f32 operator + f64 refinement/Arnoldi",
-                      {"meshes": [(mid, m.n_nodes) for mid, m, _, _ in pool],
-                       "requests_timed": len(timed), "requests_warmup": n_warm,
-                       "rhs_per_request": "U{1..16}", "arrival_rate_per_s": lam,
-                       "offered_load": "0.8 x 1 / mean alone service time of an 8-RHS request",
-                       "workers": 4, "max_batch_rhs": 16, "hbm_budget_gb": 150.0,
-                       "p": 8, "leaf": 40,
-                       "timing": "host clock from each request's arrival to its completion"})
-    line.update({
+    summary = {
+        "value": cols / span, "unit": "solves/s", "mean_ms": float(np.mean(lat)),
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "slowdown_p50": float(np.percentile(slow, 50)), "slowdown_p99": float(np.percentile(slow, 99)),
+        "slowdown": "latency over the request's service time alone on an idle server (same mesh, "
+                    "RHS count interpolated between 1 and 16)",
+        "alone_ms": {pool[j][0]: [round(t_alone[(j, R)] * 1e3, 1) for R in (1, 8, 16)]
+                     for j in range(len(pool))},
         "mean_alone_service_ms_8rhs": mean_svc * 1e3,
+        "offered_solves_per_s": lam * float(np.mean(nrhs)),
         "worst_relative_residual": worst, "resident_gb": resident / 1e9,
         "server": counters, "setup_s": setup_s,
-        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(h2d * 2 / 3)},
-        "clocks": clk.summary(), "gpu_launches": launches})
+        "e2e": {"value": cols / span, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(h2d * 2 / 3)}}
+    config = {"meshes": [(mid, m.n_nodes) for mid, m, _, _ in pool],
+              "requests_timed": len(timed), "requests_warmup": n_warm,
+              "rhs_per_request": "U{1..16}", "arrival_rate_per_s": lam,
+              "offered_load": f"{load} x 1 / mean alone service time of an 8-RHS request",
+              "workers": workers, "max_batch_rhs": max_batch_rhs, "hbm_budget_gb": 150.0,
+              "p": 8, "leaf": 40,
+              "timing": "host clock from each request's arrival to its completion"}
+    return summary, config, launches, clk.summary()
+
+
+def run_served(args, w, rank, world, local):
+    """Poisson request stream over a pool of meshes through serve.BEMServer."""
+    _init_dist(world, local)
+    summary, config, launches, clocks = served_stream(local, 24 + 12 * args.steps)
+    line = _base_line(w, args, world, summary["value"], "solves/s", summary["mean_ms"],
+                      "f32 operator + f64 refinement/Arnoldi", config)
+    line.update({k: v for k, v in summary.items() if k not in ("value", "unit")})
+    line.update({"clocks": clocks, "gpu_launches": launches})
     if rank == 0:
         print(json.dumps(line))
     _done_dist(world)
@@ -864,6 +907,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="spheroid98k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true",
+                    help="skip the short request-stream measurement of the default run")
     ap.add_argument("--mode", choices=["bench", "profile"], default="bench",
                     help="profile: only the mixed-path solves (for an ncu launch list)")
     args = ap.parse_args()

@@ -108,6 +108,9 @@ class BEMServer:
     workers         threads issuing solves (each on its mesh's own stream)
     max_batch_rhs   request slots per mesh (columns in flight together)
     quantum_steps   Arnoldi steps per engine step while slots are free
+    join_in_flight  admit a mesh's waiting requests while its solves are in
+                    flight (False: only when the mesh has nothing in flight, the
+                    waiting requests of the mesh then start together)
     solver_factory  callable(**params) -> solver with set_mesh / set_bc /
                     slots_open / slots_submit / slots_step / slots_collect /
                     device_bytes / close (default pibem.BEMSolver)
@@ -116,10 +119,12 @@ class BEMServer:
     """
 
     def __init__(self, hbm_budget_gb: float = 150.0, workers: int = 4, max_batch_rhs: int = 16,
-                 solver_factory=None, start: bool = True, quantum_steps: int = 16, **defaults):
+                 solver_factory=None, start: bool = True, quantum_steps: int = 16,
+                 join_in_flight: bool = True, **defaults):
         self.budget = float(hbm_budget_gb) * 1e9
         self.max_batch_rhs = int(max_batch_rhs)
         self.quantum_steps = int(quantum_steps)
+        self.join_in_flight = bool(join_in_flight)
         self.defaults = dict(defaults)
         self._factory = solver_factory or pibem.BEMSolver
         self._cv = threading.Condition()
@@ -354,7 +359,7 @@ class BEMServer:
                         if not self._meshes[q.mesh_id].busy and self._idle == 0:
                             break
                         continue
-                    if used >= cap:
+                    if used >= cap or (flight and not self.join_in_flight and q not in flight):
                         break
                     k = min(q.nrhs - q._next, cap - used)
                     admitted.append((q, q._next, k))
@@ -368,6 +373,9 @@ class BEMServer:
                     self.counters["admissions"] += 1
                     if flight:
                         self.counters["joined_in_flight"] += 1
+                # requests of this mesh still waiting (slots full, or held
+                # back): only then does a step return early to admit them
+                waiting = any(q.mesh_id == m.mesh_id for q in self._pending)
             if not flight and not admitted:
                 return
             t = time.perf_counter()
@@ -385,7 +393,10 @@ class BEMServer:
                     cid += 1
             for q in flight:
                 q.batch_rhs = max(q.batch_rhs, used)
-            h.slots_step(self.quantum_steps if used < cap else 0)
+            # with nobody waiting the step runs until every column has ended its
+            # GMRES cycle, so that the columns' FP64-accurate residuals and
+            # corrections are taken together (one operator application for all)
+            h.slots_step(self.quantum_steps if (used < cap and waiting) else 0)
             with self._cv:
                 self.counters["steps"] += 1
             while True:
