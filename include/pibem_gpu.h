@@ -195,8 +195,9 @@ int pibem_solve_device(pibem_handle *h, int32_t nrhs, double *d_phi, double *d_d
  * pibem_slots_step advances every slot from event to event (right-hand side,
  * residuals, refinement decisions: operator applications shared by the slots
  * that need them at that moment) and runs the Arnoldi steps of all slots in a
- * GMRES cycle on the device until one of them ends its cycle; right-hand sides
- * submitted between steps join at the next step.  A slot's arithmetic does not
+ * GMRES cycle on the device (one CUDA graph with a device-side loop condition)
+ * until every one of them has ended its cycle, or for max_steps steps;
+ * right-hand sides submitted between steps join at the next step.  A slot's arithmetic does not
  * depend on the other slots: its result equals what pibem_solve gives for that
  * right-hand side alone.  Finished requests are collected in request-id order
  * with the full phi / dphi_dn vectors (known entries from tmp_rhs) and their
