@@ -113,6 +113,15 @@ namespace pibem
       dst.resize(tmp_rhs.size());
       check(pibem_compute_rhs(h_, 1, tmp_rhs.data(), dst.data()));
     }
+    // PreconditionILU::vmult on the matrix of BEMFMA::FMA_preconditioner
+    // (bem_fma.cc:3080-3411) when the parameters ask for preconditioner 2 (the
+    // leaf-block Jacobi for 1, a copy for 0): dst = P^-1 src.
+    void preconditioner_vmult(std::vector<double> &dst, const std::vector<double> &src)
+    {
+      build();
+      dst.resize(src.size());
+      check(pibem_apply_preconditioner(h_, 1, src.data(), dst.data()));
+    }
     pibem_solve_stats solve_system(std::vector<double> &phi, std::vector<double> &dphi_dn,
                                    const std::vector<double> &tmp_rhs)
     {
