@@ -27,6 +27,7 @@
 
 #include "kernels.h"
 #include "krylov.h"
+#include "pdl.cuh"
 #include "pibem_internal.h"
 
 using namespace pibem;
@@ -558,6 +559,7 @@ namespace
   {
     const int    N = int(h->N());
     cudaStream_t s = h->stream;
+    PdlScope     pdl_scope(R == 1);
     if (h->timing || !h->side)
       {
         record(h, 0);

@@ -33,6 +33,21 @@ namespace pibem
     return on;
   }
 
+  // Launches of this host thread may use the attribute (cleared around the
+  // operator applications of several columns: there the near field and the
+  // tree passes run on two streams with multi-wave kernels, and a dependent
+  // grid waiting on SMs for its predecessor holds slots the other stream's
+  // kernels need -- measured 8 % slower at 16 columns, 0.3 % faster at one).
+  inline thread_local bool t_pdl_allowed = true;
+  struct PdlScope
+  {
+    bool prev;
+    explicit PdlScope(bool on) : prev(t_pdl_allowed) { t_pdl_allowed = on && prev; }
+    ~PdlScope() { t_pdl_allowed = prev; }
+    PdlScope(const PdlScope &)            = delete;
+    PdlScope &operator=(const PdlScope &) = delete;
+  };
+
   template <typename... P, typename... A>
   inline void launch_pdl(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                          A &&...args)
@@ -46,7 +61,7 @@ namespace pibem
     at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs                                        = at;
-    cfg.numAttrs                                     = pdl_on() ? 1 : 0;
+    cfg.numAttrs                                     = (pdl_on() && t_pdl_allowed) ? 1 : 0;
     PIBEM_CUDA(cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...));
   }
 } // namespace pibem
