@@ -412,16 +412,36 @@ namespace pibem
           tfill[l].push_back(b);
 
     // cell -> quad mask of a set of boxes
-    auto collect = [&](const std::vector<int> &boxes, std::vector<std::pair<int, uint64_t>> &out) {
-      std::unordered_map<int, uint64_t> m;
+    // cell -> quad mask of a set of boxes, sorted by cell: a dense per-thread
+    // mask array over the cells (zero between calls) and the list of the
+    // cells it touched
+    const int64_t n_qcells = nq > 0 ? int64_t(t.quad_sorted.size()) / nq : 0;
+    struct CollectScratch
+    {
+      std::vector<uint64_t> mask;
+      std::vector<int>      touched;
+    };
+    auto collect = [&](const std::vector<int> &boxes, std::vector<std::pair<int, uint64_t>> &out,
+                       CollectScratch &sc) {
+      if (int64_t(sc.mask.size()) < n_qcells)
+        sc.mask.assign(n_qcells, 0);
+      sc.touched.clear();
       for (int bx : boxes)
         for (int k = t.qbeg[bx]; k < t.qend[bx]; ++k)
           {
-            int qid = t.quad_sorted[k];
-            m[qid / nq] |= (uint64_t(1) << (qid % nq));
+            const int qid = t.quad_sorted[k], c = qid / nq;
+            if (!sc.mask[c])
+              sc.touched.push_back(c);
+            sc.mask[c] |= uint64_t(1) << (qid % nq);
           }
-      out.assign(m.begin(), m.end());
-      std::sort(out.begin(), out.end());
+      std::sort(sc.touched.begin(), sc.touched.end());
+      out.clear();
+      out.reserve(sc.touched.size());
+      for (int c : sc.touched)
+        {
+          out.push_back({c, sc.mask[c]});
+          sc.mask[c] = 0;
+        }
     };
 
     // coarse non-interaction boxes (direct integration, bem_fma.cc:997-1153)
@@ -429,19 +449,23 @@ namespace pibem
     for (int l = 1; l <= t.L; ++l)
       {
         const std::vector<int> &fl = tfill[l];
-#pragma omp parallel for schedule(dynamic, 16)
-        for (int k = 0; k < int(fl.size()); ++k)
-          {
-            int              b = fl[k];
-            std::vector<int> boxes;
-            for (size_t sub = 0; sub < t.nn[b].size(); ++sub)
-              for (int pos : t.nil[b][sub])
-                if (pos < t.startLevel[l])
-                  boxes.push_back(pos);
-            sort_unique(boxes);
-            if (!boxes.empty())
-              collect(boxes, coarse[b]);
-          }
+#pragma omp parallel
+        {
+          CollectScratch sc;
+#pragma omp for schedule(dynamic, 16)
+          for (int k = 0; k < int(fl.size()); ++k)
+            {
+              int              b = fl[k];
+              std::vector<int> boxes;
+              for (size_t sub = 0; sub < t.nn[b].size(); ++sub)
+                for (int pos : t.nil[b][sub])
+                  if (pos < t.startLevel[l])
+                    boxes.push_back(pos);
+              sort_unique(boxes);
+              if (!boxes.empty())
+                collect(boxes, coarse[b], sc);
+            }
+        }
       }
 
     // ---- near field per childless box with nodes
@@ -453,12 +477,15 @@ namespace pibem
     std::vector<std::vector<int>>       rows(nl), cols(nl);
     std::vector<std::vector<NearEntry>> ents(nl);
     std::vector<std::vector<int>>       gptr(nl), gids(nl);
-#pragma omp parallel for schedule(dynamic, 8)
+#pragma omp parallel
+    {
+    CollectScratch sc;
+#pragma omp for schedule(dynamic, 8)
     for (int k = 0; k < nl; ++k)
       {
         int                                    b = nleaves[k];
         std::vector<std::pair<int, uint64_t>> e1;
-        collect(t.il[b].back(), e1);
+        collect(t.il[b].back(), e1, sc);
         std::vector<NearEntry> E;
         for (auto &cm : e1)
           E.push_back(NearEntry{cm.first, 1, cm.second, {0, 0, 0, 0}});
@@ -481,27 +508,32 @@ namespace pibem
             e.lcol[j] = int(std::lower_bound(c.begin(), c.end(),
                                              mesh.dof(mesh.cells[4 * size_t(e.cell) + j])) -
                             c.begin());
-        std::vector<std::vector<int>> g(c.size());
+        // per column, the (entry, vertex) ids e * 4 + j touching it, in
+        // ascending order (a counting sort over the columns)
+        std::vector<int> gp(c.size() + 1, 0), gi(E.size() * 4);
         for (size_t ei = 0; ei < E.size(); ++ei)
           for (int j = 0; j < 4; ++j)
-            g[E[ei].lcol[j]].push_back(int(ei) * 4 + j);
-        std::vector<int> gp(1, 0), gi;
-        for (auto &v : g)
-          {
-            gi.insert(gi.end(), v.begin(), v.end());
-            gp.push_back(int(gi.size()));
-          }
+            ++gp[E[ei].lcol[j] + 1];
+        for (size_t q = 0; q < c.size(); ++q)
+          gp[q + 1] += gp[q];
+        {
+          std::vector<int> at(gp.begin(), gp.end() - 1);
+          for (size_t ei = 0; ei < E.size(); ++ei)
+            for (int j = 0; j < 4; ++j)
+              gi[at[E[ei].lcol[j]]++] = int(ei) * 4 + j;
+        }
         std::vector<int> r;
         for (int s = t.nbeg[b]; s < t.nend[b]; ++s)
           if (t.node_sorted[s] < mesh.n_dofs)
             r.push_back(t.node_sorted[s]);
         std::sort(r.begin(), r.end());
-        rows[k] = r;
-        cols[k] = c;
-        ents[k] = E;
-        gptr[k] = gp;
-        gids[k] = gi;
+        rows[k] = std::move(r);
+        cols[k] = std::move(c);
+        ents[k] = std::move(E);
+        gptr[k] = std::move(gp);
+        gids[k] = std::move(gi);
       }
+    }
     pl.nleaf_box = nleaves;
     pl.nrow_ptr.assign(nl + 1, 0);
     pl.ncol_ptr.assign(nl + 1, 0);
@@ -515,21 +547,30 @@ namespace pibem
         // rows padded to a multiple of 4 values (16-byte vector loads)
         pl.nval_ptr[k + 1] = pl.nval_ptr[k] + int64_t(rows[k].size()) * ((int64_t(cols[k].size()) + 3) / 4 * 4);
       }
-    pl.gather_ptr.reserve(pl.ncol_ptr[nl] + nl);
+    // the leaves' pieces concatenated in leaf order (offsets first, then the
+    // copies in parallel); gather_ptr per column (global column position),
+    // gather ids local to the leaf
+    std::vector<int64_t> gid_ptr(nl + 1, 0);
+    for (int k = 0; k < nl; ++k)
+      gid_ptr[k + 1] = gid_ptr[k] + int64_t(gids[k].size());
+    pl.nrows.resize(pl.nrow_ptr[nl]);
+    pl.row_leaf.resize(pl.nrow_ptr[nl]);
+    pl.ncols.resize(pl.ncol_ptr[nl]);
+    pl.entries.resize(pl.nent_ptr[nl]);
+    pl.gather_ptr.resize(pl.ncol_ptr[nl] + 1);
+    pl.gather_ids.resize(gid_ptr[nl]);
+#pragma omp parallel for schedule(dynamic, 64)
     for (int k = 0; k < nl; ++k)
       {
-        pl.nrows.insert(pl.nrows.end(), rows[k].begin(), rows[k].end());
-        pl.ncols.insert(pl.ncols.end(), cols[k].begin(), cols[k].end());
-        pl.entries.insert(pl.entries.end(), ents[k].begin(), ents[k].end());
-        // gather_ptr per column (global column position); ids local to the leaf
-        int base = int(pl.gather_ids.size());
+        std::copy(rows[k].begin(), rows[k].end(), pl.nrows.begin() + pl.nrow_ptr[k]);
+        std::fill(pl.row_leaf.begin() + pl.nrow_ptr[k], pl.row_leaf.begin() + pl.nrow_ptr[k + 1], k);
+        std::copy(cols[k].begin(), cols[k].end(), pl.ncols.begin() + pl.ncol_ptr[k]);
+        std::copy(ents[k].begin(), ents[k].end(), pl.entries.begin() + pl.nent_ptr[k]);
         for (size_t c = 0; c < cols[k].size(); ++c)
-          pl.gather_ptr.push_back(base + gptr[k][c]);
-        pl.gather_ids.insert(pl.gather_ids.end(), gids[k].begin(), gids[k].end());
-        for (size_t r = 0; r < rows[k].size(); ++r)
-          pl.row_leaf.push_back(k);
+          pl.gather_ptr[pl.ncol_ptr[k] + int64_t(c)] = int(gid_ptr[k]) + gptr[k][c];
+        std::copy(gids[k].begin(), gids[k].end(), pl.gather_ids.begin() + gid_ptr[k]);
       }
-    pl.gather_ptr.push_back(int(pl.gather_ids.size()));
+    pl.gather_ptr[pl.ncol_ptr[nl]] = int(gid_ptr[nl]);
 
     // ---- P2M tables per childless box with quadrature points
     std::vector<int> pleaves;
@@ -563,21 +604,29 @@ namespace pibem
             cq.push_back(dq[i].second);
           }
         cp.push_back(int(cq.size()));
-        prow[k] = rws;
-        pcp[k]  = cp;
-        pcq[k]  = cq;
+        prow[k] = std::move(rws);
+        pcp[k]  = std::move(cp);
+        pcq[k]  = std::move(cq);
       }
     pl.pleaf_box = pleaves;
     pl.prow_ptr.assign(np + 1, 0);
-    pl.pcontrib_ptr.push_back(0);
+    std::vector<int64_t> pq_ptr(np + 1, 0);
     for (int k = 0; k < np; ++k)
       {
         pl.prow_ptr[k + 1] = pl.prow_ptr[k] + int64_t(prow[k].size());
-        pl.prow_dof.insert(pl.prow_dof.end(), prow[k].begin(), prow[k].end());
-        int64_t base = int64_t(pl.pcontrib_q.size());
+        pq_ptr[k + 1]      = pq_ptr[k] + int64_t(pcq[k].size());
+      }
+    pl.prow_dof.resize(pl.prow_ptr[np]);
+    pl.pcontrib_ptr.resize(pl.prow_ptr[np] + 1);
+    pl.pcontrib_q.resize(pq_ptr[np]);
+    pl.pcontrib_ptr[0] = 0;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int k = 0; k < np; ++k)
+      {
+        std::copy(prow[k].begin(), prow[k].end(), pl.prow_dof.begin() + pl.prow_ptr[k]);
         for (size_t r = 0; r < prow[k].size(); ++r)
-          pl.pcontrib_ptr.push_back(base + pcp[k][r + 1]);
-        pl.pcontrib_q.insert(pl.pcontrib_q.end(), pcq[k].begin(), pcq[k].end());
+          pl.pcontrib_ptr[pl.prow_ptr[k] + int64_t(r) + 1] = pq_ptr[k] + pcp[k][r + 1];
+        std::copy(pcq[k].begin(), pcq[k].end(), pl.pcontrib_q.begin() + pq_ptr[k]);
       }
 
     // ---- L2P per childless box with nodes (same leaves as the near field)
