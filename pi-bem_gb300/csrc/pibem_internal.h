@@ -88,7 +88,7 @@ namespace pibem
   };
 
   // Page-locked host buffer (grow-only): small device -> host reads that the
-  // host waits for (the Arnoldi step's Hessenberg column) skip the driver's
+  // host waits for (the Arnoldi step's Hessenberg column) skip the CUDA runtime's
   // staging copy of pageable memory.
   template <typename T>
   struct PinnedBuf

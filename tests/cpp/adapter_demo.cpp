@@ -2,7 +2,7 @@
 // BEMProblem would: init_fma, octree / near field / multipole integrals, an
 // FMM matvec, alpha, and a solve, on a cube-sphere read from a text file
 // (n, xyz..., c, cells..., dirichlet flags..., tmp_rhs...).  Prints the solve
-// statistics and the first unknowns.  Test driver only.
+// statistics and the first unknowns.  A test program only.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
