@@ -3,7 +3,7 @@ expansion classes (_ref/libpibem_ref.so, present only where the reference
 checkout was available at build time).
 
 Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, always as the checker.
+CPU-baseline leg of bench.py, only to check or time against it.
 """
 from __future__ import annotations
 

@@ -3,7 +3,7 @@
 // ONE_BODY assemble_system) and the solve around them (source/bem_problem.cc
 // compute_alpha / vmult / compute_rhs / solve_system).
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker against which the GPU
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle against which the GPU
 // implementation is compared; the product never links, loads or calls it.
 //
 // The data structures deliberately mirror the reference (std::set interaction

@@ -1,7 +1,7 @@
 /* Oracle (test infrastructure only): a CPU restatement of pi-BEM's
  * FMM-accelerated collocation BEM operator, its dense collocation operator and
  * the solve around them.  Only tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline leg may load it, and only as a checker.
+ * CPU-baseline leg may load it, and only to compare or time against it.
  *
  * Index conventions follow the reference: nodes are DoFs of FE_Q(1) on a
  * quadrilateral surface mesh, cell vertices in deal.II lexicographic order
