@@ -3,7 +3,9 @@ restatement of BEMFMA::FMA_preconditioner (source/bem_fma.cc:3080-3411) with
 Trilinos' ILU(0) (source/bem_problem.cc:1302), whose factors the CPU tests pin
 to the defining property (L U)_ij = A_ij on the pattern.
 
-  z = P^-1 v (pibem_apply_preconditioner) vs the oracle's   1e-10 relative
+  z = P^-1 v (pibem_apply_preconditioner) vs the oracle's   1e-10 relative (ILU(0); the
+                                                            leaf-block Jacobi too, 1e-5
+                                                            with its FP32 inverses)
   FP64 solves at 1e-10 vs the oracle's ILU solve            1e-7 (spheroid),
                                                             1e-6 (sharp cube,
                                                             the constraint lines'
@@ -78,6 +80,22 @@ def test_apply_matches_oracle(case, pibem_mod):
         e = rel(Z[r], apply(V[r]))
         assert e < 1e-10, (r, e)
     g.close()
+
+
+def test_block_jacobi_apply_matches_oracle(case, pibem_mod):
+    """The default preconditioner through the same entry point: the leaf-block
+    Jacobi inverses (FP64 on the FP64 path, FP32 in the mixed path's inner
+    solves) against the oracle's Gauss-Jordan inverses of the same blocks."""
+    apply, _ = case["o"].preconditioner(1)
+    rng = np.random.Generator(np.random.PCG64(6))
+    V = rng.normal(size=(2, case["mesh"].n_nodes))
+    for mode, tol in ((pibem_mod.PRECISION_FP64, 1e-10), (pibem_mod.PRECISION_MIXED, 1e-5)):
+        g = _gpu(pibem_mod, case, prec=1, mode=mode)
+        Z = g.apply_preconditioner(V)
+        for r in range(2):
+            e = rel(Z[r], apply(V[r]))
+            assert e < tol, (mode, r, e)
+        g.close()
 
 
 def test_solve_matches_oracle(case, pibem_mod):
