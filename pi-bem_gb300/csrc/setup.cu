@@ -87,12 +87,16 @@ namespace pibem
 
     // LaplaceKernel::kernels (include/laplace_kernel.h:55-74) contracted with
     // the normal: returns D.n with D = R/(-4 pi r^3), s = 1/(4 pi r).
+    // s = 1 / (4 pi r), dn = -(R . n) / (4 pi r^3) from one reciprocal square
+    // root (FP64 division and square root are multi-instruction sequences on
+    // the FP64 pipe, which bounds this kernel)
     __device__ inline void kernel_pair(const double *R, const double *n, double &dn, double &s)
     {
-      double r = sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
-      s        = 1. / (r * 4 * kPi);
-      double f = -4 * kPi * r * r * r;
-      dn       = (R[0] / f) * n[0] + (R[1] / f) * n[1] + (R[2] / f) * n[2];
+      constexpr double c4pi = 1.0 / (4 * kPi);
+      const double     r2   = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+      const double     rinv = rsqrt(r2);
+      s                     = rinv * c4pi;
+      dn                    = -(R[0] * n[0] + R[1] * n[1] + R[2] * n[2]) * (rinv * rinv * rinv) * c4pi;
     }
 
     // One (leaf row, entry) integral: 4 N values and 4 D values.
