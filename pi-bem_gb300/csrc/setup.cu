@@ -5,7 +5,9 @@
 //     singular cells;
 //   P2M operator tables (BEMFMA::multipole_integrals, bem_fma.cc:1609-1840);
 //   L2P evaluation tables.
+#include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "devmath.cuh"
 #include "kernels.h"
@@ -20,6 +22,16 @@ namespace pibem
     __constant__ double c_tel_pts[4][2 * 144];
     __constant__ double c_tel_w[4][144];
     __constant__ int    c_tel_n;
+
+    // Coefficients of the normalised Legendre recurrences for n, m <= 10,
+    // indexed n (n + 1) / 2 + m where two-dimensional: the square roots and the
+    // reciprocal the set-up tables would otherwise evaluate per point in FP64.
+    constexpr int       LEG_PMAX = 10, LEG_NPM = (LEG_PMAX + 1) * (LEG_PMAX + 2) / 2;
+    __constant__ double c_leg_pm[LEG_PMAX + 1];              // -sqrt((2m - 1) / (2m))
+    __constant__ double c_leg_p1[LEG_PMAX + 1];              // sqrt(2m + 1)
+    __constant__ double c_leg_sq[LEG_NPM], c_leg_isq[LEG_NPM]; // sqrt((n-1)^2 - m^2), 1 / sqrt(n^2 - m^2)
+    __constant__ double c_leg_d1[LEG_PMAX + 1];              // sqrt(n (n + 1))
+    __constant__ double c_leg_d2[LEG_NPM], c_leg_d3[LEG_NPM]; // sqrt((n-m)(n+m+1)), sqrt((n+m)(n-m+1))
 
     struct Geo
     {
@@ -263,27 +275,29 @@ namespace pibem
     // terms of coefficient k in contribution order.
     // P~_n^m(x) of every n <= p, m <= n into P[n (n + 1) / 2 + m] and, with dS,
     // legendre_dsin(n, m) into dS[...]: the recurrences of legendre_nm and
-    // legendre_dsin (devmath.cuh) with the same operations in the same order,
-    // so the values are theirs bit for bit, at O(p^2) instead of O(p^3).
+    // legendre_dsin (devmath.cuh) at O(p^2), their square-root factors from
+    // the constant tables (the same values) and the division of the
+    // three-term recurrence as a product with the reciprocal (the values agree
+    // with theirs to a few ulp).
     __device__ inline void legendre_table(int p, double x, double s, double *P, double *dS)
     {
       double pmm = 1.0;
       for (int m = 0; m <= p; ++m)
         {
           if (m > 0)
-            pmm *= -sqrt(double(2 * m - 1) / double(2 * m)) * s;
+            pmm *= c_leg_pm[m] * s;
           P[m * (m + 1) / 2 + m] = pmm;
           if (m + 1 > p)
             continue;
-          double p1 = x * sqrt(double(2 * m + 1)) * pmm, p0 = pmm;
+          double p1 = x * c_leg_p1[m] * pmm, p0 = pmm;
           P[(m + 1) * (m + 2) / 2 + m] = p1;
           for (int n = m + 2; n <= p; ++n)
             {
-              const double p2 = (double(2 * n - 1) * x * p1 - sqrt(double((n - 1) * (n - 1) - m * m)) * p0) /
-                                sqrt(double(n * n - m * m));
-              p0                      = p1;
-              p1                      = p2;
-              P[n * (n + 1) / 2 + m] = p2;
+              const int    nm = n * (n + 1) / 2 + m;
+              const double p2 = (double(2 * n - 1) * x * p1 - c_leg_sq[nm] * p0) * c_leg_isq[nm];
+              p0              = p1;
+              p1              = p2;
+              P[nm]           = p2;
             }
         }
       if (!dS)
@@ -292,13 +306,13 @@ namespace pibem
         for (int m = 0; m <= n; ++m)
           {
             auto   pv = [&](int mm) { return mm >= 0 && mm <= n ? P[n * (n + 1) / 2 + mm] : 0.0; };
+            const int nm = n * (n + 1) / 2 + m;
             double dth;
             if (m == 0)
-              dth = n > 0 ? sqrt(double(n) * double(n + 1)) * pv(1) : 0.0;
+              dth = n > 0 ? c_leg_d1[n] * pv(1) : 0.0;
             else
-              dth = 0.5 * (sqrt(double(n - m) * double(n + m + 1)) * pv(m + 1) -
-                           sqrt(double(n + m) * double(n - m + 1)) * pv(m - 1));
-            dS[n * (n + 1) / 2 + m] = -dth;
+              dth = 0.5 * (c_leg_d2[nm] * pv(m + 1) - c_leg_d3[nm] * pv(m - 1));
+            dS[nm] = -dth;
           }
     }
 
@@ -603,6 +617,48 @@ namespace pibem
       }
   }
 
+  // The Legendre coefficient tables in constant memory, once per device.
+  static void set_legendre_coeffs(cudaStream_t s)
+  {
+    static std::mutex mu;
+    static bool       done[64] = {};
+    int               dev      = 0;
+    PIBEM_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 64 && done[dev])
+      return;
+    double pm[LEG_PMAX + 1] = {}, p1[LEG_PMAX + 1] = {}, d1[LEG_PMAX + 1] = {};
+    double sq[LEG_NPM] = {}, isq[LEG_NPM] = {}, d2[LEG_NPM] = {}, d3[LEG_NPM] = {};
+    for (int m = 0; m <= LEG_PMAX; ++m)
+      {
+        pm[m] = m > 0 ? -std::sqrt(double(2 * m - 1) / double(2 * m)) : 0.0;
+        p1[m] = std::sqrt(double(2 * m + 1));
+        d1[m] = std::sqrt(double(m) * double(m + 1));
+      }
+    for (int n = 0; n <= LEG_PMAX; ++n)
+      for (int m = 0; m <= n; ++m)
+        {
+          const int nm = n * (n + 1) / 2 + m;
+          if (n >= m + 2)
+            {
+              sq[nm]  = std::sqrt(double((n - 1) * (n - 1) - m * m));
+              isq[nm] = 1.0 / std::sqrt(double(n * n - m * m));
+            }
+          d2[nm] = std::sqrt(double(n - m) * double(n + m + 1));
+          d3[nm] = std::sqrt(double(n + m) * double(n - m + 1));
+        }
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_pm, pm, sizeof(pm), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_p1, p1, sizeof(p1), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_d1, d1, sizeof(d1), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_sq, sq, sizeof(sq), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_isq, isq, sizeof(isq), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_d2, d2, sizeof(d2), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaMemcpyToSymbolAsync(c_leg_d3, d3, sizeof(d3), 0, cudaMemcpyHostToDevice, s));
+    PIBEM_CUDA(cudaStreamSynchronize(s)); // the host arrays go out of scope
+    if (dev < 64)
+      done[dev] = true;
+  }
+
   void launch_p2m_tables(int64_t n_rows, int K, int p, int n_leaves, const int64_t *row_ptr,
                          const int32_t *leaf_box, const int64_t *contrib_ptr,
                          const int32_t *contrib_q, const double *box_center,
@@ -613,8 +669,9 @@ namespace pibem
     int64_t n = n_rows * K;
     if (n == 0)
       return;
-    if (K > 128)
+    if (K > 128 || p > LEG_PMAX)
       throw Error(PIBEM_EINVAL, "P2M tables: more than 128 coefficients");
+    set_legendre_coeffs(s);
     const size_t smem = size_t(P2M_CHUNK) * p2m_geo_stride(p) * sizeof(double);
     if (smem > 48 * 1024)
       raise_smem_limit(reinterpret_cast<const void *>(p2m_table_kernel), smem);
@@ -635,6 +692,9 @@ namespace pibem
     int p = 0;
     while ((p + 1) * (p + 1) < K)
       ++p;
+    if (p > LEG_PMAX)
+      throw Error(PIBEM_EINVAL, "L2P tables: order above 10");
+    set_legendre_coeffs(s);
     const size_t smem = size_t(8) * (5 + 3 * (p + 1) + (p + 1) * (p + 2) / 2) * sizeof(double);
     l2p_table_kernel<<<unsigned((n_pos + 7) / 8), 256, smem, s>>>(n_pos, K, p, ldw, n_leaves,
                                                                   pos_ptr, leaf_box, nodes, xyz,
