@@ -2247,6 +2247,10 @@ namespace
         maxrow = std::max<int64_t>(maxrow, pl.nent_ptr[k + 1] - pl.nent_ptr[k]);
       st_items = std::max(st_items, maxrow);
       staging.alloc(8 * std::max<int64_t>(st_items, 1));
+      DBuf<int64_t>            sing_list;
+      DBuf<unsigned long long> sing_count;
+      sing_list.alloc(std::max<int64_t>(st_items, 1));
+      sing_count.alloc(1);
       NearAssemblyArgs a;
       a.n_items       = item_ptr[nl];
       a.n_leaves      = nl;
@@ -2273,6 +2277,8 @@ namespace
       a.gather_ids    = h->d_gather_ids.p;
       a.staging       = staging.p;
       a.staging_items = st_items;
+      a.sing_list     = sing_list.p;
+      a.sing_count    = sing_count.p;
       a.Nval          = h->d_N.p;
       a.Dval          = h->d_D.p;
       if (nl > 0)

@@ -27,6 +27,8 @@ namespace pibem
     const int32_t   *gather_ptr = nullptr, *gather_ids = nullptr;
     double          *staging = nullptr;
     int64_t          staging_items = 0;
+    int64_t         *sing_list = nullptr;     // staging_items entries: singular items of a batch
+    unsigned long long *sing_count = nullptr; // their number
     double          *Nval = nullptr, *Dval = nullptr;
   };
 

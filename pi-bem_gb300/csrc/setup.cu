@@ -98,10 +98,9 @@ namespace pibem
     }
 
     // LaplaceKernel::kernels (include/laplace_kernel.h:55-74) contracted with
-    // the normal: returns D.n with D = R/(-4 pi r^3), s = 1/(4 pi r).
-    // s = 1 / (4 pi r), dn = -(R . n) / (4 pi r^3) from one reciprocal square
-    // root (FP64 division and square root are multi-instruction sequences on
-    // the FP64 pipe, which bounds this kernel)
+    // the normal: s = 1 / (4 pi r), dn = D.n with D = R / (-4 pi r^3), from one
+    // reciprocal square root (FP64 division and square root are
+    // multi-instruction sequences on the FP64 pipe, which bounds this kernel)
     __device__ inline void kernel_pair(const double *R, const double *n, double &dn, double &s)
     {
       constexpr double c4pi = 1.0 / (4 * kPi);
@@ -111,7 +110,13 @@ namespace pibem
       dn                    = -(R[0] * n[0] + R[1] * n[1] + R[2] * n[2]) * (rinv * rinv * rinv) * c4pi;
     }
 
-    // One (leaf row, entry) integral: 4 N values and 4 D values.
+    // One (leaf row, entry) integral: 4 N values and 4 D values.  PASS 0 takes
+    // the items of a batch, integrates the regular ones (Gauss points) and
+    // lists the singular ones (the cell holds the row's node or a double of
+    // it); PASS 1 integrates the listed items (Telles rule), so that a warp's
+    // threads run the same rule (a singular item costs several times a regular
+    // one).  Every item's values depend on the item alone.
+    template <int PASS>
     __global__ void near_entries_kernel(int64_t n_items, int n_leaves,
                                         const int64_t *__restrict__ item_ptr,
                                         const int64_t *__restrict__ row_ptr,
@@ -126,90 +131,108 @@ namespace pibem
                                         const double *__restrict__ qnrm,
                                         const double *__restrict__ qjxw,
                                         const double *__restrict__ qshape, int64_t item_base,
-                                        double *__restrict__ staging)
+                                        double *__restrict__ staging,
+                                        int64_t *__restrict__ sing_list,
+                                        unsigned long long *__restrict__ sing_count)
     {
-      int64_t it = item_base + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-      if (it >= n_items)
-        return;
-      // leaf by binary search over item_ptr
-      int lo = 0, hi = n_leaves - 1;
-      while (lo < hi)
-        {
-          int mid = (lo + hi + 1) >> 1;
-          if (item_ptr[mid] <= it)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-      const int     leaf = lo;
-      const int64_t loc  = it - item_ptr[leaf];
-      const int64_t ne   = ent_ptr[leaf + 1] - ent_ptr[leaf];
-      const int64_t r    = loc / ne;
-      const int64_t e    = loc % ne;
-      const int     node = rows[row_ptr[leaf] + r];
-      const NearEntry E  = ents[ent_ptr[leaf] + e];
-      const int64_t   c  = E.cell;
-      double xi[3] = {xyz[3 * int64_t(node)], xyz[3 * int64_t(node) + 1], xyz[3 * int64_t(node) + 2]};
-      double Nv[4] = {0, 0, 0, 0}, Dv[4] = {0, 0, 0, 0};
-      int    sv = -1;
-      if (E.singular_ok)
-        for (int j = 0; j < 4 && sv < 0; ++j)
+      auto item = [&](int64_t it) {
+        // leaf by binary search over item_ptr
+        int lo = 0, hi = n_leaves - 1;
+        while (lo < hi)
           {
-            int d = cells[4 * c + j];
-            for (int a = dbl_off[node]; a < dbl_off[node + 1]; ++a)
-              if (dbl_ids[a] == d)
-                {
-                  sv = j;
-                  break;
-                }
+            int mid = (lo + hi + 1) >> 1;
+            if (item_ptr[mid] <= it)
+              lo = mid;
+            else
+              hi = mid - 1;
           }
-      if (sv < 0)
-        {
-          uint64_t mask = E.qmask;
-          while (mask)
+        const int     leaf = lo;
+        const int64_t loc  = it - item_ptr[leaf];
+        const int64_t ne   = ent_ptr[leaf + 1] - ent_ptr[leaf];
+        const int64_t r    = loc / ne;
+        const int64_t e    = loc % ne;
+        const int     node = rows[row_ptr[leaf] + r];
+        const NearEntry E  = ents[ent_ptr[leaf] + e];
+        const int64_t   c  = E.cell;
+        double xi[3] = {xyz[3 * int64_t(node)], xyz[3 * int64_t(node) + 1], xyz[3 * int64_t(node) + 2]};
+        double Nv[4] = {0, 0, 0, 0}, Dv[4] = {0, 0, 0, 0};
+        int    sv = -1;
+        if (E.singular_ok)
+          for (int j = 0; j < 4 && sv < 0; ++j)
             {
-              int q = __ffsll((long long)mask) - 1;
-              mask &= mask - 1;
-              int64_t k = c * nq + q;
-              double  R[3] = {qpts[3 * k] - xi[0], qpts[3 * k + 1] - xi[1], qpts[3 * k + 2] - xi[2]};
-              double  n[3] = {qnrm[3 * k], qnrm[3 * k + 1], qnrm[3 * k + 2]};
-              double  dn, s;
-              kernel_pair(R, n, dn, s);
-              double w = qjxw[k];
-              for (int j = 0; j < 4; ++j)
-                {
-                  Nv[j] += dn * qshape[4 * k + j] * w;
-                  Dv[j] += s * qshape[4 * k + j] * w;
-                }
+              int d = cells[4 * c + j];
+              for (int a = dbl_off[node]; a < dbl_off[node + 1]; ++a)
+                if (dbl_ids[a] == d)
+                  {
+                    sv = j;
+                    break;
+                  }
             }
+        if (PASS == 0 && sv >= 0)
+          {
+            sing_list[atomicAdd(sing_count, 1ull)] = it;
+            return;
+          }
+        if (sv < 0)
+          {
+            uint64_t mask = E.qmask;
+            while (mask)
+              {
+                int q = __ffsll((long long)mask) - 1;
+                mask &= mask - 1;
+                int64_t k = c * nq + q;
+                double  R[3] = {qpts[3 * k] - xi[0], qpts[3 * k + 1] - xi[1], qpts[3 * k + 2] - xi[2]};
+                double  n[3] = {qnrm[3 * k], qnrm[3 * k + 1], qnrm[3 * k + 2]};
+                double  dn, s;
+                kernel_pair(R, n, dn, s);
+                double w = qjxw[k];
+                for (int j = 0; j < 4; ++j)
+                  {
+                    Nv[j] += dn * qshape[4 * k + j] * w;
+                    Dv[j] += s * qshape[4 * k + j] * w;
+                  }
+              }
+          }
+        else
+          {
+            double v[12];
+            for (int j = 0; j < 4; ++j)
+              for (int k = 0; k < 3; ++k)
+                v[3 * j + k] = xyz[3 * int64_t(cells[4 * c + j]) + k];
+            const int nt = c_tel_n;
+            for (int q = 0; q < nt; ++q)
+              {
+                Geo g;
+                cell_geo(v, c_tel_pts[sv][2 * q], c_tel_pts[sv][2 * q + 1], g);
+                double R[3] = {g.x[0] - xi[0], g.x[1] - xi[1], g.x[2] - xi[2]};
+                double dn, s;
+                kernel_pair(R, g.n, dn, s);
+                double w = g.J * c_tel_w[sv][q];
+                for (int j = 0; j < 4; ++j)
+                  {
+                    Nv[j] += dn * g.N[j] * w;
+                    Dv[j] += s * g.N[j] * w;
+                  }
+              }
+          }
+        double *o = staging + (it - item_base) * 8;
+        for (int j = 0; j < 4; ++j)
+          {
+            o[j]     = Nv[j];
+            o[4 + j] = Dv[j];
+          }
+      };
+      const int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (PASS == 0)
+        {
+          if (item_base + g < n_items)
+            item(item_base + g);
         }
       else
         {
-          double v[12];
-          for (int j = 0; j < 4; ++j)
-            for (int k = 0; k < 3; ++k)
-              v[3 * j + k] = xyz[3 * int64_t(cells[4 * c + j]) + k];
-          const int nt = c_tel_n;
-          for (int q = 0; q < nt; ++q)
-            {
-              Geo g;
-              cell_geo(v, c_tel_pts[sv][2 * q], c_tel_pts[sv][2 * q + 1], g);
-              double R[3] = {g.x[0] - xi[0], g.x[1] - xi[1], g.x[2] - xi[2]};
-              double dn, s;
-              kernel_pair(R, g.n, dn, s);
-              double w = g.J * c_tel_w[sv][q];
-              for (int j = 0; j < 4; ++j)
-                {
-                  Nv[j] += dn * g.N[j] * w;
-                  Dv[j] += s * g.N[j] * w;
-                }
-            }
-        }
-      double *o = staging + (it - item_base) * 8;
-      for (int j = 0; j < 4; ++j)
-        {
-          o[j]     = Nv[j];
-          o[4 + j] = Dv[j];
+          const int64_t cnt = int64_t(*sing_count);
+          for (int64_t q = g; q < cnt; q += int64_t(gridDim.x) * blockDim.x)
+            item(sing_list[q]);
         }
     }
 
@@ -581,11 +604,20 @@ namespace pibem
             end = rb;
           }
         int64_t cnt = end - start;
-        near_entries_kernel<<<unsigned((cnt + 127) / 128), 128, 0, s>>>(
+        PIBEM_CUDA(cudaMemsetAsync(a.sing_count, 0, sizeof(unsigned long long), s));
+        near_entries_kernel<0><<<unsigned((cnt + 127) / 128), 128, 0, s>>>(
           end, a.n_leaves, a.item_ptr, a.row_ptr, a.ent_ptr, a.rows, a.ents, a.xyz, a.cells,
-          a.dbl_off, a.dbl_ids, a.nq, a.qpts, a.qnrm, a.qjxw, a.qshape, start, a.staging);
+          a.dbl_off, a.dbl_ids, a.nq, a.qpts, a.qnrm, a.qjxw, a.qshape, start, a.staging,
+          a.sing_list, a.sing_count);
         PIBEM_CUDA(cudaGetLastError());
-    note_launch();
+        note_launch();
+        // the singular items of the batch (a grid-stride loop over the list)
+        near_entries_kernel<1><<<unsigned(std::min<int64_t>((cnt + 127) / 128, 4096)), 128, 0, s>>>(
+          end, a.n_leaves, a.item_ptr, a.row_ptr, a.ent_ptr, a.rows, a.ents, a.xyz, a.cells,
+          a.dbl_off, a.dbl_ids, a.nq, a.qpts, a.qnrm, a.qjxw, a.qshape, start, a.staging,
+          a.sing_list, a.sing_count);
+        PIBEM_CUDA(cudaGetLastError());
+        note_launch();
         // gather: all values whose row lies in [start, end)
         // value range: leaves covering the batch
         int l0 = 0, hi = a.n_leaves - 1;
