@@ -1065,9 +1065,24 @@ namespace
     const int     L   = E.m + 1;
     const int64_t ldr = int64_t(L) * N;
     double *h1 = E.hb.p, *h2 = h1 + size_t(E.S) * L, *nr = h2 + size_t(E.S) * L;
-    launch_gather_cols(N, Ra, E.act.p, E.z.p, N, E.cz.p, s);
-    A(E.cz.p, E.cw.p, Ra);
-    launch_scatter_cols(N, Ra, E.act.p, E.cw.p, E.w.p, N, s);
+    if (E.mixed && h->have_dirichlet && h->con_row.empty())
+      {
+        // the FP32 operator straight on the gathered columns: gather + FP32
+        // conversion and FP64 conversion + scatter fused (as system_apply32)
+        h->d_x32.alloc(size_t(Ra) * N);
+        h->d_y32.alloc(size_t(Ra) * N);
+        launch_gather_d2f(N, Ra, E.act.p, E.z.p, h->d_x32.p, s);
+        operator32(h, Ra);
+        finish_timing(h, 1);
+        launch_f2d_scatter(N, Ra, E.act.p, h->d_y32.p, E.w.p, s);
+        h->cnt32 += Ra;
+      }
+    else
+      {
+        launch_gather_cols(N, Ra, E.act.p, E.z.p, N, E.cz.p, s);
+        A(E.cz.p, E.cw.p, Ra);
+        launch_scatter_cols(N, Ra, E.act.p, E.cw.p, E.w.p, N, s);
+      }
     launch_cgs_step(0, N, E.S, 0, N, ldr, E.V.p, nullptr, 0, E.w.p, ENG_NBLK, E.partial.p,
                     E.ticket.p, h1, s, E.jvec.p, L);
     launch_cgs_step(1, N, E.S, 0, N, ldr, E.V.p, h1, L, E.w.p, ENG_NBLK, E.partial.p, E.ticket.p, h2,

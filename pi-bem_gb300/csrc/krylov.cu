@@ -364,6 +364,30 @@ namespace pibem
       dst[int64_t(cols[k]) * ldd + t] = src[idx];
     }
 
+    // dst[k] = float(src[cols[k]]) and dst[cols[k]] = double(src[k]): the
+    // gather / scatter of the active columns fused with the FP32 operator's
+    // input and output conversions
+    __global__ void gather_d2f_kernel(int64_t n, int Rc, const int *__restrict__ cols,
+                                      const double *__restrict__ src, float *__restrict__ dst)
+    {
+      pdl_entry();
+      const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * Rc)
+        return;
+      const int64_t k = idx / n, t = idx - k * n;
+      dst[idx]        = float(src[int64_t(cols[k]) * n + t]);
+    }
+    __global__ void f2d_scatter_kernel(int64_t n, int Rc, const int *__restrict__ cols,
+                                       const float *__restrict__ src, double *__restrict__ dst)
+    {
+      pdl_entry();
+      const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+      if (idx >= n * Rc)
+        return;
+      const int64_t k = idx / n, t = idx - k * n;
+      dst[int64_t(cols[k]) * n + t] = double(src[idx]);
+    }
+
     // y[r] = a x[r] + b y[r] for the selected columns
     __global__ void axpby_sel_kernel(int64_t n, int R, const int *__restrict__ sel, double a,
                                      const double *__restrict__ x, double b, double *__restrict__ y)
@@ -889,6 +913,26 @@ namespace pibem
     if (Rc == 0)
       return;
     launch_pdl(scatter_cols_kernel, nblocks(n * Rc), 256, 0, s, n, Rc, cols, src, dst, ldd);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_gather_d2f(int64_t n, int Rc, const int *cols, const double *src, float *dst,
+                         cudaStream_t s)
+  {
+    if (Rc == 0)
+      return;
+    launch_pdl(gather_d2f_kernel, nblocks(n * Rc), 256, 0, s, n, Rc, cols, src, dst);
+    PIBEM_CUDA(cudaGetLastError());
+    note_launch();
+  }
+
+  void launch_f2d_scatter(int64_t n, int Rc, const int *cols, const float *src, double *dst,
+                          cudaStream_t s)
+  {
+    if (Rc == 0)
+      return;
+    launch_pdl(f2d_scatter_kernel, nblocks(n * Rc), 256, 0, s, n, Rc, cols, src, dst);
     PIBEM_CUDA(cudaGetLastError());
     note_launch();
   }

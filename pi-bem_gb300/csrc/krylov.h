@@ -41,6 +41,11 @@ namespace pibem
   // compaction of selected columns for the operator: dst[k] = src[cols[k]] and back
   void launch_gather_cols(int64_t n, int Rc, const int *cols, const double *src, int64_t lds,
                           double *dst, cudaStream_t s);
+  // x32[k] = float(src[cols[k]]) / dst[cols[k]] = double(y32[k]) (column stride n)
+  void launch_gather_d2f(int64_t n, int Rc, const int *cols, const double *src, float *dst,
+                         cudaStream_t s);
+  void launch_f2d_scatter(int64_t n, int Rc, const int *cols, const float *src, double *dst,
+                          cudaStream_t s);
   void launch_scatter_cols(int64_t n, int Rc, const int *cols, const double *src, double *dst,
                            int64_t ldd, cudaStream_t s);
   // y[r] = a x[r] + b y[r] on the selected columns
