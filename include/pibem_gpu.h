@@ -246,8 +246,11 @@ int pibem_quad_points(pibem_handle *h, double *pts);
  * (L2L and the sums of each box's products, all levels), m2p, l2p (7 values);
  * needs profiling on. */
 int pibem_last_phase_ms(pibem_handle *h, double *ms7);
-/* Turns CUDA-event timing of the operator phases on or off (off by default;
- * on adds event records and one stream synchronisation per application). */
+/* CUDA-event timing of the operator phases: 0 off (default), 1 on (event
+ * records and one stream synchronisation per application), 2 on with a hold:
+ * each application starts behind a 0.4 ms single-thread kernel, so that the
+ * host has enqueued it before the GPU reaches the first phase event and the
+ * phase times are GPU execution times without host launch gaps. */
 int pibem_set_profiling(pibem_handle *h, int32_t on);
 /* Phase times (ms, same order as pibem_last_phase_ms) summed over the operator
  * applications of the given precision (PIBEM_PRECISION_FP64: FP64 operator,

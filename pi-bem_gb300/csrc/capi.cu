@@ -225,7 +225,7 @@ struct pibem_handle
   // plan
   DBuf<int64_t> d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr,
     d_m2l_src_ptr, d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr,
-    d_up_q_ptr, d_down_q_ptr;
+    d_up_q_ptr, d_down_q_ptr, d_near_sched;
   DBuf<int32_t> d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
     d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src, d_l2l_box,
     d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op, d_up_box,
@@ -306,8 +306,10 @@ struct pibem_handle
   // d_modes holds this mode for modes_R columns (-1: other contents)
   int             modes_R = -1;
   uint8_t         modes_val = 0;
-  // timing
+  // timing (timing_hold_ns: the stream is held this long before the first
+  // phase event of each application, pibem_set_profiling(h, 2))
   bool        timing = false;
+  int64_t     timing_hold_ns = 0;
   cudaEvent_t ev[8] = {};
   double      phase_ms[7] = {0, 0, 0, 0, 0, 0, 0};
   double      phase_tot[2][7] = {};
@@ -330,7 +332,7 @@ struct pibem_handle
         d_delta);
     add(d_nrow_ptr, d_ncol_ptr, d_nval_ptr, d_nent_ptr, d_prow_ptr, d_pcontrib_ptr, d_m2l_src_ptr,
         d_m2p_src_ptr, d_item_ptr, d_blk_ptr, d_m2p_item_ptr, d_m2p_tnode_ptr, d_up_q_ptr,
-        d_down_q_ptr);
+        d_down_q_ptr, d_near_sched);
     add(d_row_leaf, d_nrows, d_ncols, d_pleaf_box, d_prow_dof, d_pcontrib_q, d_lleaf_box,
         d_gather_ptr, d_gather_ids, d_m2l_tgt, d_m2l_src, d_m2l_off, d_m2p_tgt, d_m2p_src,
         d_l2l_box, d_parents, d_diag_col, d_m2p_pair_tgt, d_q_src, d_ch_start, d_ch_cnt, d_ch_op,
@@ -389,10 +391,36 @@ namespace
       }
   }
 
+  // Holds one thread for about ns nanoseconds (the global timer, at most
+  // 200,000 sleeps of 1 us), so that the host can enqueue an operator
+  // application behind it before the GPU reaches its first phase event.
+  __global__ void hold_stream_kernel(int64_t ns)
+  {
+    uint64_t t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (int i = 0; i < 200000; ++i)
+      {
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (int64_t(t - t0) >= ns)
+          break;
+        __nanosleep(1000);
+      }
+  }
+
+  // Phase event i.  With a hold set, the first event of an application comes
+  // after a short kernel that keeps the stream busy while the host enqueues
+  // the application, so that the phase times are GPU execution times and not
+  // host launch latency (the GPU would otherwise wait idle between events).
   void record(pibem_handle *h, int i)
   {
-    if (h->timing)
-      PIBEM_CUDA(cudaEventRecord(h->ev[i], h->stream));
+    if (!h->timing)
+      return;
+    if (i == 0 && h->timing_hold_ns > 0)
+      {
+        hold_stream_kernel<<<1, 1, 0, h->stream>>>(h->timing_hold_ns);
+        PIBEM_CUDA(cudaGetLastError());
+      }
+    PIBEM_CUDA(cudaEventRecord(h->ev[i], h->stream));
   }
 
   // ---------------------------------------------------------------------
@@ -1813,6 +1841,7 @@ namespace
       op.nrow_ptr      = h->d_nrow_ptr.p;
       op.ncol_ptr      = h->d_ncol_ptr.p;
       op.nval_ptr      = h->d_nval_ptr.p;
+      op.near_sched    = h->d_near_sched.p;
       op.n_p2m_leaves  = int(pl.pleaf_box.size());
       op.prow_ptr      = h->d_prow_ptr.p;
       op.pleaf_box     = h->d_pleaf_box.p;
@@ -2157,6 +2186,27 @@ namespace
     h->d_nrow_ptr.upload(pl.nrow_ptr, s);
     h->d_ncol_ptr.upload(pl.ncol_ptr, s);
     h->d_nval_ptr.upload(pl.nval_ptr, s);
+    {
+      // one-column near SpMV schedule: the leaves by value bytes, largest first
+      const int        nl = int(pl.nleaf_box.size());
+      std::vector<int> order(nl);
+      for (int k = 0; k < nl; ++k)
+        order[k] = k;
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return pl.nval_ptr[a + 1] - pl.nval_ptr[a] > pl.nval_ptr[b + 1] - pl.nval_ptr[b];
+      });
+      std::vector<int64_t> sched(4 * size_t(nl));
+      for (int i = 0; i < nl; ++i)
+        {
+          const int     k  = order[i];
+          const int64_t nr = pl.nrow_ptr[k + 1] - pl.nrow_ptr[k], nc = pl.ncol_ptr[k + 1] - pl.ncol_ptr[k];
+          sched[4 * size_t(i) + 0] = pl.nval_ptr[k];
+          sched[4 * size_t(i) + 1] = pl.ncol_ptr[k];
+          sched[4 * size_t(i) + 2] = pl.nrow_ptr[k];
+          sched[4 * size_t(i) + 3] = int64_t(uint64_t(nr) | (uint64_t(nc) << 32));
+        }
+      h->d_near_sched.upload(sched, s);
+    }
     h->d_nent_ptr.upload(pl.nent_ptr, s);
     h->d_row_leaf.upload(pl.row_leaf, s);
     h->d_nrows.upload(pl.nrows, s);
@@ -3253,7 +3303,12 @@ extern "C"
 
   int pibem_set_profiling(pibem_handle *h, int32_t on)
   {
-    return guarded(h, [&] { h->timing = on != 0; });
+    return guarded(h, [&] {
+      if (on < 0 || on > 2)
+        throw Error(PIBEM_EINVAL, "profiling mode must be 0, 1 or 2");
+      h->timing         = on != 0;
+      h->timing_hold_ns = on == 2 ? 400000 : 0;
+    });
   }
 
   int pibem_phase_totals(pibem_handle *h, int32_t precision, double *ms7, int64_t *applications,

@@ -176,7 +176,9 @@ namespace pibem
     __device__ inline void cp_async_x(float *dst, const float *src) { cp_async4(dst, src); }
     __device__ inline void cp_async_x(double *dst, const double *src) { cp_async8(dst, src); }
 
-    // Near-field SpMV for one column, software-pipelined: persistent blocks
+    // Near-field SpMV for one column where near_leaf_sched_kernel's shared
+    // memory would not fit (more than about 14,000 columns in a leaf; FP32),
+    // software-pipelined: persistent blocks
     // take leaves L, L + gridDim.x, ... (the grid works through the leaves in
     // ascending windows.  Measured on GB300, 98k spheroid: 80 us; contiguous
     // leaf ranges of equal bytes per block 125 us; an L2 prefetch of the leaves
@@ -253,6 +255,176 @@ namespace pibem
                     {
                       T &o1 = y[nrows[r0 + row + nw]];
                       o1    = acc ? o1 + t1 : t1;
+                    }
+                }
+            }
+        }
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+
+    __device__ inline void cp_async16(void *dst, const void *src)
+    {
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+                   "l"(src)
+                   : "memory");
+    }
+
+    // Position of round t of block b in the leaf schedule: snake order over the
+    // G blocks (b, 2G-1-b, 2G+b, ...), so that with the leaves sorted by bytes
+    // every block streams about the same amount.
+    __device__ __forceinline__ int64_t near_sched_pos(int b, int t, int G)
+    {
+      return int64_t(t) * G + ((t & 1) ? G - 1 - b : b);
+    }
+
+    // 16-byte streaming loads that do not allocate in L1
+    __device__ inline void load4_na(const float *p, float (&v)[4])
+    {
+      asm("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+          : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+          : "l"(p));
+    }
+    __device__ inline void load4_na(const double *p, double (&v)[4])
+    {
+      asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "l"(p));
+      asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v[2]), "=d"(v[3]) : "l"(p + 2));
+    }
+    template <bool NA, typename T>
+    __device__ __forceinline__ void load4v(const T *p, T (&v)[4])
+    {
+      if constexpr (NA)
+        load4_na(p, v);
+      else
+        load4(p, v);
+    }
+
+    // Near-field SpMV for one column: persistent blocks over a schedule of the
+    // leaves sorted by value bytes (record per leaf: value offset, column
+    // offset, row offset, rows | columns << 32), three stages deep.  While the
+    // warps stream the rows of round t, the block has one cp.async group in
+    // flight holding the x entries of round t+1 (gathered through the column
+    // ids already in shared memory), the column ids of round t+2 and the
+    // schedule record of round t+3, so that inside a round only the row values
+    // are waited for.  Rows: two per warp at a time, the 16-byte loads of NB
+    // chunks per lane and row issued before any is used (NA: loads that do not
+    // allocate in L1).  A row is computed exactly as in near_leaf_kernel (same
+    // chunks per lane, same order, same butterfly), so the leaf order and the
+    // block shape do not change a bit of y.
+    // Shared memory: 128 bytes of records, 2 x ld_max column ids, 2 x ld_max x.
+    template <typename T, int NB, int BS, bool NA>
+    __global__ void __launch_bounds__(BS)
+      near_leaf_sched_kernel(int n_leaves, int ld_max, const int64_t *__restrict__ sched,
+                             const int32_t *__restrict__ nrows, const int32_t *__restrict__ ncols,
+                             const T *__restrict__ vals, const T *__restrict__ x,
+                             T *__restrict__ y, bool acc)
+    {
+      pdl_entry();
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      int64_t  *srec = reinterpret_cast<int64_t *>(smem_raw);       // [4][4]
+      int32_t  *sid  = reinterpret_cast<int32_t *>(smem_raw + 128); // [2][ld_max]
+      T        *sxb  = reinterpret_cast<T *>(smem_raw + 128 + size_t(8) * ld_max); // [2][ld_max]
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      const int G = gridDim.x, b = blockIdx.x;
+      auto valid = [&](int t) { return near_sched_pos(b, t, G) < n_leaves; };
+      auto rec   = [&](int t) { return srec + 4 * (t & 3); };
+      // schedule record of round t (threads 0 and 1, 16 bytes each)
+      auto fetch_rec = [&](int t) {
+        if (threadIdx.x < 2 && valid(t))
+          cp_async16(rec(t) + 2 * threadIdx.x, sched + 4 * near_sched_pos(b, t, G) + 2 * threadIdx.x);
+      };
+      // column ids of round t (its record in place)
+      auto fetch_ids = [&](int t) {
+        const int64_t c0 = rec(t)[1];
+        const int     nc = int(uint64_t(rec(t)[3]) >> 32);
+        int32_t      *d  = sid + (t & 1) * ld_max;
+        for (int c = threadIdx.x; c < nc; c += blockDim.x)
+          cp_async4(d + c, ncols + c0 + c);
+      };
+      // x entries of round t (its column ids in place), zeros in the padding
+      auto gather_x = [&](int t) {
+        const int      nc = int(uint64_t(rec(t)[3]) >> 32), ld = (nc + 3) & ~3;
+        const int32_t *si = sid + (t & 1) * ld_max;
+        T             *d  = sxb + (t & 1) * ld_max;
+        for (int c = threadIdx.x; c < ld; c += blockDim.x)
+          if (c < nc)
+            cp_async_x(d + c, x + si[c]);
+          else
+            d[c] = T(0);
+      };
+      if (!valid(0))
+        return;
+      fetch_rec(0);
+      fetch_rec(1);
+      fetch_rec(2);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      __syncthreads();
+      fetch_ids(0);
+      if (valid(1))
+        fetch_ids(1);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+      __syncthreads();
+      gather_x(0);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+      for (int t = 0; valid(t); ++t)
+        {
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
+          __syncthreads(); // round t's x, round t+1's ids, records t..t+2 in place
+          if (valid(t + 1))
+            gather_x(t + 1);
+          if (valid(t + 2))
+            fetch_ids(t + 2);
+          fetch_rec(t + 3);
+          asm volatile("cp.async.commit_group;" ::: "memory");
+          const int64_t *r  = rec(t);
+          const T       *V  = vals + r[0];
+          const int64_t  r0 = r[2];
+          const int      nr = int(uint32_t(uint64_t(r[3]))), nc = int(uint64_t(r[3]) >> 32);
+          const int      ld = (nc + 3) & ~3, n4 = ld >> 2;
+          const T       *sx = sxb + (t & 1) * ld_max;
+          for (int row = warp; row < nr; row += 2 * nw)
+            {
+              const bool two = row + nw < nr;
+              int        o0 = 0, o1 = 0;
+              if (lane == 0)
+                {
+                  o0 = nrows[r0 + row];
+                  o1 = two ? nrows[r0 + row + nw] : o0;
+                }
+              const T *v0 = V + int64_t(row) * ld;
+              const T *v1 = V + int64_t(two ? row + nw : row) * ld;
+              T        s0 = T(0), s1 = T(0);
+              for (int jb = lane; jb < n4; jb += 32 * NB)
+                {
+                  T a0[NB][4], a1[NB][4];
+#pragma unroll
+                  for (int k = 0; k < NB; ++k)
+                    if (jb + 32 * k < n4)
+                      {
+                        load4v<NA>(v0 + 4 * (jb + 32 * k), a0[k]);
+                        if (two)
+                          load4v<NA>(v1 + 4 * (jb + 32 * k), a1[k]);
+                      }
+#pragma unroll
+                  for (int k = 0; k < NB; ++k)
+                    if (jb + 32 * k < n4)
+                      {
+                        s0 = dot4_acc(s0, a0[k], sx + 4 * (jb + 32 * k));
+                        if (two)
+                          s1 = dot4_acc(s1, a1[k], sx + 4 * (jb + 32 * k));
+                      }
+                }
+              const T t0 = warp_sum(s0), t1 = warp_sum(s1);
+              if (lane == 0)
+                {
+                  T &y0 = y[o0];
+                  y0    = acc ? y0 + t0 : t0;
+                  if (two)
+                    {
+                      T &y1 = y[o1];
+                      y1    = acc ? y1 + t1 : t1;
                     }
                 }
             }
@@ -1052,6 +1224,34 @@ namespace pibem
     int           rb    = int(std::max<int64_t>(1, (96 * 1024) / (maxnc * int64_t(sizeof(T)))));
     rb                  = std::min(rb, R);
     const size_t smem   = size_t(rb) * maxnc * sizeof(T);
+    const size_t smem_s = 128 + size_t(2) * maxnc * (4 + sizeof(T));
+    if (R == 1 && op.near_sched && smem_s <= 227 * 1024)
+      {
+        // one column: the scheduled three-stage kernel.  FP32: 4 warps a
+        // block, three 16-byte chunks per lane and row in flight, loads that
+        // do not allocate in L1; FP64: 8 warps, two chunks.  Measured on GB300
+        // (98k spheroid, CUDA events): FP32 79.5 -> 55.6 us, FP64 328 -> 265 us
+        // against near_leaf_pipe_kernel; 8 warps with two chunks 62 us, 4
+        // warps with two / four / five chunks 67 / 58 / 64 us, one row per
+        // warp with six chunks 62 us, a shared-memory carveout of 100 % 66 us.
+        constexpr int bs   = sizeof(T) == 4 ? 128 : 256;
+        auto          kern = [] {
+          if constexpr (sizeof(T) == 4)
+            return near_leaf_sched_kernel<T, 3, 128, true>;
+          else
+            return near_leaf_sched_kernel<T, 2, 256, false>;
+        }();
+        if (smem_s > 48 * 1024)
+          raise_smem_limit(reinterpret_cast<const void *>(kern), smem_s);
+        int per_sm = 0;
+        PIBEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, bs, smem_s));
+        const int grid = std::min(op.n_near_leaves, std::max(per_sm, 1) * near_sm_count());
+        launch_pdl(kern, grid, bs, smem_s, s, op.n_near_leaves, int(maxnc), op.near_sched,
+                   op.nrows, op.ncols, vals, x, y, accumulate);
+        PIBEM_CUDA(cudaGetLastError());
+        note_launch();
+        return;
+      }
     if (R == 1)
       {
         // one column: the software-pipelined persistent kernel (a row is

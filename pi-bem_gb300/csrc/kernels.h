@@ -81,6 +81,9 @@ namespace pibem
     int64_t        n_rows = 0;
     const int32_t *row_leaf = nullptr, *nrows = nullptr, *ncols = nullptr;
     const int64_t *nrow_ptr = nullptr, *ncol_ptr = nullptr, *nval_ptr = nullptr;
+    // the leaves sorted by value bytes, 4 int64 per leaf: value offset, column
+    // offset, row offset, rows | columns << 32 (one-column near SpMV)
+    const int64_t *near_sched = nullptr;
     // p2m
     int            n_p2m_leaves = 0;
     const int64_t *prow_ptr = nullptr;

@@ -488,8 +488,10 @@ class BEMSolver:
         self._check(self.L.pibem_device_bytes(self.h, C.byref(b)))
         return int(b.value)
 
-    def set_profiling(self, on: bool):
-        self._check(self.L.pibem_set_profiling(self.h, int(bool(on))))
+    def set_profiling(self, on):
+        """0 / False off, 1 / True phase timing, 2 phase timing behind a hold
+        kernel (GPU execution times without host launch gaps)."""
+        self._check(self.L.pibem_set_profiling(self.h, int(on)))
 
     def phase_totals(self, precision: int, reset: bool = False):
         """(dict phase -> total ms, number of operator applications)."""

@@ -72,7 +72,8 @@ def test_graph_is_rebuilt_after_new_mesh(pibem_mod, synthetic):
 def test_gmres_cycle_graph_matches_step_launches(pibem_mod, synthetic, mode):
     """A GMRES restart cycle runs as one CUDA graph (a conditional while node
     around one Arnoldi step, with the Givens rotation and the stopping test on
-    the device); with phase timing on the same launches are issued step by step.
+    the device); with phase timing on (with and without the hold kernel before
+    each operator application) the same launches are issued step by step.
     Solutions, iteration counts, operator counts and launch counts agree, for
     one column and for a batch of three."""
     S = synthetic
@@ -84,7 +85,7 @@ def test_gmres_cycle_graph_matches_step_launches(pibem_mod, synthetic, mode):
     g.set_bc(mask)
     for t in (tmp, np.stack([tmp, 0.5 * tmp + 0.1, -tmp])):
         out = []
-        for prof in (True, False, False):
+        for prof in (True, 2, False, False):
             g.set_profiling(prof)
             l0 = pibem_mod.launch_count()
             p, d, st = g.solve(t)
