@@ -177,7 +177,8 @@ namespace pibem
     __device__ inline void cp_async_x(double *dst, const double *src) { cp_async8(dst, src); }
 
     // Near-field SpMV for one column where near_leaf_sched_kernel's shared
-    // memory would not fit (more than about 14,000 columns in a leaf; FP32),
+    // memory would not fit (more than about 14,500 columns in a leaf in FP32,
+    // 9,600 in FP64),
     // software-pipelined: persistent blocks
     // take leaves L, L + gridDim.x, ... (the grid works through the leaves in
     // ascending windows.  Measured on GB300, 98k spheroid: 80 us; contiguous
@@ -1227,20 +1228,16 @@ namespace pibem
     const size_t smem_s = 128 + size_t(2) * maxnc * (4 + sizeof(T));
     if (R == 1 && op.near_sched && smem_s <= 227 * 1024)
       {
-        // one column: the scheduled three-stage kernel.  FP32: 4 warps a
-        // block, three 16-byte chunks per lane and row in flight, loads that
-        // do not allocate in L1; FP64: 8 warps, two chunks.  Measured on GB300
-        // (98k spheroid, CUDA events): FP32 79.5 -> 55.6 us, FP64 328 -> 265 us
-        // against near_leaf_pipe_kernel; 8 warps with two chunks 62 us, 4
-        // warps with two / four / five chunks 67 / 58 / 64 us, one row per
-        // warp with six chunks 62 us, a shared-memory carveout of 100 % 66 us.
-        constexpr int bs   = sizeof(T) == 4 ? 128 : 256;
-        auto          kern = [] {
-          if constexpr (sizeof(T) == 4)
-            return near_leaf_sched_kernel<T, 3, 128, true>;
-          else
-            return near_leaf_sched_kernel<T, 2, 256, false>;
-        }();
+        // one column: the scheduled three-stage kernel, 4 warps a block, three
+        // 4-value chunks per lane and row in flight, loads that do not
+        // allocate in L1.  Measured on GB300 (98k spheroid, CUDA events)
+        // against near_leaf_pipe_kernel: FP32 79.5 -> 55.6 us (8 warps with two
+        // chunks 62 us; 4 warps with two / four / five chunks 67 / 58 / 64 us;
+        // one row per warp with six chunks 62 us; a shared-memory carveout of
+        // 100 % 66 us), FP64 328 -> 229 us (8 warps with two chunks 265 us; 4
+        // warps with one / two chunks 269 / 233 us).
+        constexpr int bs   = 128;
+        auto          kern = near_leaf_sched_kernel<T, 3, 128, true>;
         if (smem_s > 48 * 1024)
           raise_smem_limit(reinterpret_cast<const void *>(kern), smem_s);
         int per_sm = 0;
