@@ -271,8 +271,8 @@ namespace pibem
                    : "memory");
     }
 
-    // Position of round t of block b in the leaf schedule: snake order over the
-    // G blocks (b, 2G-1-b, 2G+b, ...), so that with the leaves sorted by bytes
+    // Schedule position of the t-th leaf of block b: snake order over the G
+    // blocks (b, 2G-1-b, 2G+b, ...), so that with the leaves sorted by bytes
     // every block streams about the same amount.
     __device__ __forceinline__ int64_t near_sched_pos(int b, int t, int G)
     {
@@ -303,11 +303,11 @@ namespace pibem
     // Near-field SpMV for one column: persistent blocks over a schedule of the
     // leaves sorted by value bytes (record per leaf: value offset, column
     // offset, row offset, rows | columns << 32), three stages deep.  While the
-    // warps stream the rows of round t, the block has one cp.async group in
-    // flight holding the x entries of round t+1 (gathered through the column
-    // ids already in shared memory), the column ids of round t+2 and the
-    // schedule record of round t+3, so that inside a round only the row values
-    // are waited for.  Rows: two per warp at a time, the 16-byte loads of NB
+    // warps stream the rows of the block's leaf t, the block has one cp.async
+    // group in flight holding the x entries of its leaf t+1 (gathered through
+    // the column ids already in shared memory), the column ids of leaf t+2 and
+    // the schedule record of leaf t+3, so that inside a leaf only the row
+    // values are waited for.  Rows: two per warp at a time, the 16-byte loads of NB
     // chunks per lane and row issued before any is used (NA: loads that do not
     // allocate in L1).  A row is computed exactly as in near_leaf_kernel (same
     // chunks per lane, same order, same butterfly), so the leaf order and the
@@ -329,12 +329,12 @@ namespace pibem
       const int G = gridDim.x, b = blockIdx.x;
       auto valid = [&](int t) { return near_sched_pos(b, t, G) < n_leaves; };
       auto rec   = [&](int t) { return srec + 4 * (t & 3); };
-      // schedule record of round t (threads 0 and 1, 16 bytes each)
+      // schedule record of leaf t (threads 0 and 1, 16 bytes each)
       auto fetch_rec = [&](int t) {
         if (threadIdx.x < 2 && valid(t))
           cp_async16(rec(t) + 2 * threadIdx.x, sched + 4 * near_sched_pos(b, t, G) + 2 * threadIdx.x);
       };
-      // column ids of round t (its record in place)
+      // column ids of leaf t (its record in place)
       auto fetch_ids = [&](int t) {
         const int64_t c0 = rec(t)[1];
         const int     nc = int(uint64_t(rec(t)[3]) >> 32);
@@ -342,7 +342,7 @@ namespace pibem
         for (int c = threadIdx.x; c < nc; c += blockDim.x)
           cp_async4(d + c, ncols + c0 + c);
       };
-      // x entries of round t (its column ids in place), zeros in the padding
+      // x entries of leaf t (its column ids in place), zeros in the padding
       auto gather_x = [&](int t) {
         const int      nc = int(uint64_t(rec(t)[3]) >> 32), ld = (nc + 3) & ~3;
         const int32_t *si = sid + (t & 1) * ld_max;
@@ -372,7 +372,7 @@ namespace pibem
       for (int t = 0; valid(t); ++t)
         {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
-          __syncthreads(); // round t's x, round t+1's ids, records t..t+2 in place
+          __syncthreads(); // leaf t's x, leaf t+1's ids, records t..t+2 in place
           if (valid(t + 1))
             gather_x(t + 1);
           if (valid(t + 2))
